@@ -1,0 +1,921 @@
+// Host side of the C ABI (include/dgx.h): mesh connectivity with dgfem's semantics,
+// reference-element operators, per-element geometry records, the device-resident
+// context and the stream-ordered entry points.
+#include "../../include/dgx.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <string>
+#include <unordered_set>
+#include <vector>
+
+#include "dgx_internal.h"
+#include "quad_tables.inc"
+
+using namespace dgx;
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CUDA_OK(x)                                                                    \
+    do {                                                                              \
+        cudaError_t e_ = (x);                                                         \
+        if (e_ != cudaSuccess)                                                        \
+            return fail(DGX_ERR_CUDA, std::string(#x ": ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+extern "C" const char* dgx_last_error(void) { return g_err.c_str(); }
+extern "C" const char* dgx_version(void) { return "dgx 0.1 (sm_103a)"; }
+
+// ------------------------------------------------------------------ bases
+// MonomialBasisTriangle (src/basis/monomial.cpp:30-72): x^i y^j ordered by total degree,
+// then i ascending.
+static double ipow(double x, int n) { return n == 0 ? 1.0 : std::pow(x, (double)n); }
+
+static void monomial(int p, double x, double y, double* phi, double* grad) {
+    int k = 0;
+    for (int td = 0; td <= p; ++td)
+        for (int i = 0; i <= td; ++i, ++k) {
+            const int j = td - i;
+            if (phi) phi[k] = ipow(x, i) * ipow(y, j);
+            if (grad) {
+                grad[2 * k] = i == 0 ? 0.0 : i * ipow(x, i - 1) * ipow(y, j);
+                grad[2 * k + 1] = j == 0 ? 0.0 : ipow(x, i) * j * ipow(y, j - 1);
+            }
+        }
+}
+
+// Jacobi P_n^(a,b) by the three-term recurrence (src/basis/dubiner.cpp:24-47)
+static double jacobi(int n, double a, double b, double x) {
+    if (n == 0) return 1.0;
+    double p0 = 1.0, p1 = 0.5 * (a - b + (a + b + 2.0) * x);
+    for (int k = 2; k <= n; ++k) {
+        const double c = 2.0 * k + a + b;
+        const double a1 = 2.0 * k * (k + a + b) * (c - 2.0);
+        const double a2 = (c - 1.0) * (a * a - b * b);
+        const double a3 = (c - 2.0) * (c - 1.0) * c;
+        const double a4 = 2.0 * (k + a - 1.0) * (k + b - 1.0) * c;
+        const double p2 = ((a2 + a3 * x) * p1 - a4 * p0) / a1;
+        p0 = p1;
+        p1 = p2;
+    }
+    return p1;
+}
+
+// DubinerBasis (src/basis/dubiner.cpp:55-168): collapsed coordinates r = 2 xi/(1-eta) - 1,
+// s = 2 eta - 1, index order j outer / i inner, scaling 2 sqrt((2i+1)(i+j+1)).
+static void dubiner(int p, double x, double y, double* phi, double* grad) {
+    if (!(x >= 0 && y >= 0 && x + y <= 1)) {  // ReferenceTriangle::project_to_bounds
+        x = std::max(0.0, std::min(1.0, x));
+        y = std::max(0.0, std::min(1.0 - x, y));
+    }
+    const double om = 1.0 - y;
+    const bool top = std::fabs(om) < 1e-14;
+    const double r = top ? -1.0 : 2.0 * x / om - 1.0;
+    const double s = 2.0 * y - 1.0;
+    const double dr_dx = top ? 0.0 : 2.0 / om, dr_dy = top ? 0.0 : 2.0 * x / (om * om);
+    const double ds_dy = top ? 0.0 : 2.0;
+    int k = 0;
+    for (int j = 0; j <= p; ++j)
+        for (int i = 0; i <= p - j; ++i, ++k) {
+            const double Pi = jacobi(i, 0.0, 0.0, r);
+            const double Pj = jacobi(j, 2.0 * i + 1.0, 0.0, s);
+            const double nrm = 2.0 * std::sqrt((2.0 * i + 1.0) * (i + j + 1.0));
+            const double sc = std::pow(0.5 * (1.0 - s), (double)i);
+            if (phi) phi[k] = nrm * Pi * Pj * sc;
+            if (grad) {
+                const double dPi = i > 0 ? 0.5 * (i + 1.0) * jacobi(i - 1, 1.0, 1.0, r) : 0.0;
+                const double dPj = j > 0 ? 0.5 * (j + 2.0 * i + 2.0) * jacobi(j - 1, 2.0 * i + 2.0, 1.0, s) : 0.0;
+                const double dsc = i > 0 ? -0.5 * i * std::pow(0.5 * (1.0 - s), (double)(i - 1)) : 0.0;
+                const double dphi_dr = nrm * dPi * Pj * sc;
+                const double dphi_ds = nrm * Pi * (dPj * sc + Pj * dsc);
+                grad[2 * k] = dphi_dr * dr_dx;
+                grad[2 * k + 1] = dphi_dr * dr_dy + dphi_ds * ds_dy;
+            }
+        }
+}
+
+static void basis_eval(int basis, int p, double x, double y, double* phi, double* grad) {
+    if (basis == DGX_BASIS_DUBINER) dubiner(p, x, y, phi, grad);
+    else monomial(p, x, y, phi, grad);
+}
+
+// DGSpace::map_face_quad_point (src/core/space.cpp:259-271)
+static void face_point(int f, double s, double* xi) {
+    const double t = 0.5 * (s + 1.0);
+    if (f == 0) { xi[0] = t; xi[1] = 0.0; }
+    else if (f == 1) { xi[0] = 1.0 - t; xi[1] = t; }
+    else { xi[0] = 0.0; xi[1] = 1.0 - t; }
+}
+
+static const int kEdge[3][2] = {{0, 1}, {1, 2}, {2, 0}};  // ReferenceTriangle::edge_vertices
+
+static bool invert(int n, const double* A, double* X) {  // Gauss-Jordan, partial pivoting
+    std::vector<double> M(A, A + n * n);
+    for (int i = 0; i < n * n; ++i) X[i] = 0.0;
+    for (int i = 0; i < n; ++i) X[i * n + i] = 1.0;
+    for (int c = 0; c < n; ++c) {
+        int p = c;
+        for (int r = c + 1; r < n; ++r)
+            if (std::fabs(M[r * n + c]) > std::fabs(M[p * n + c])) p = r;
+        if (M[p * n + c] == 0.0) return false;
+        for (int k = 0; k < n; ++k) {
+            std::swap(M[c * n + k], M[p * n + k]);
+            std::swap(X[c * n + k], X[p * n + k]);
+        }
+        const double d = 1.0 / M[c * n + c];
+        for (int k = 0; k < n; ++k) {
+            M[c * n + k] *= d;
+            X[c * n + k] *= d;
+        }
+        for (int r = 0; r < n; ++r) {
+            if (r == c) continue;
+            const double f = M[r * n + c];
+            if (f == 0.0) continue;
+            for (int k = 0; k < n; ++k) {
+                M[r * n + k] -= f * M[c * n + k];
+                X[r * n + k] -= f * X[c * n + k];
+            }
+        }
+    }
+    return true;
+}
+
+// DGSpace ctor + precompute_basis_values (src/core/space.cpp:20-67, 230-257) and the
+// reference mass matrix of TimeDependentWeakFormulation::compute_mass_integral
+// (src/weak_forms/weak_formulation_base.cpp:198-217) divided by |J|.
+static int make_ops(int p, int basis, OpsHost& o) {
+    std::memset(&o, 0, sizeof(o));
+    const int order = 2 * p;
+    if (order > DGX_TRI_MAX_ORDER || p + 1 > DGX_GL_MAX_POINTS) return -1;
+    o.p = p;
+    o.np = n_basis(p);
+    o.nq = dgx_tri_rule_npts[order];
+    o.nfq = p + 1;
+    if (o.nq != n_quad(p)) return -1;
+    const double* qp = dgx_tri_rule_points + 2 * dgx_tri_rule_offset[order];
+    const double* qw = dgx_tri_rule_weights + dgx_tri_rule_offset[order];
+    double phi[15], g[30];
+    for (int q = 0; q < o.nq; ++q) {
+        o.qp[q][0] = qp[2 * q];
+        o.qp[q][1] = qp[2 * q + 1];
+        o.wq[q] = qw[q];
+        basis_eval(basis, p, qp[2 * q], qp[2 * q + 1], phi, g);
+        for (int i = 0; i < o.np; ++i) {
+            o.phi[q][i] = phi[i];
+            o.dr[q][i] = g[2 * i];
+            o.ds[q][i] = g[2 * i + 1];
+        }
+    }
+    for (int q = 0; q < o.nfq; ++q) {
+        o.fp[q] = dgx_gl_points[p][q];
+        o.wf[q] = dgx_gl_weights[p][q];
+    }
+    for (int f = 0; f < 3; ++f)
+        for (int q = 0; q < o.nfq; ++q) {
+            double xi[2];
+            face_point(f, o.fp[q], xi);
+            basis_eval(basis, p, xi[0], xi[1], phi, g);
+            for (int i = 0; i < o.np; ++i) {
+                o.phif[f][q][i] = phi[i];
+                o.drf[f][q][i] = g[2 * i];
+                o.dsf[f][q][i] = g[2 * i + 1];
+            }
+        }
+    std::vector<double> M(o.np * o.np, 0.0), Mi(o.np * o.np);
+    for (int q = 0; q < o.nq; ++q)
+        for (int i = 0; i < o.np; ++i)
+            for (int j = 0; j < o.np; ++j) M[i * o.np + j] += o.wq[q] * (o.phi[q][i] * o.phi[q][j]);
+    if (!invert(o.np, M.data(), Mi.data())) return -1;
+    for (int i = 0; i < o.np; ++i)
+        for (int j = 0; j < o.np; ++j) o.minv[i][j] = Mi[i * o.np + j];
+    return 0;
+}
+
+// ------------------------------------------------------------------ mesh
+struct BCDef {
+    int type;
+    double value[4];
+};
+
+struct dgx_mesh {
+    std::vector<double> verts;  // [nv][2]
+    std::vector<int> elems;     // [ne][3]
+    std::map<std::string, int> tags;
+    std::vector<int> nbr;       // [ne][3][2] face_neighbors_
+    std::vector<int> btag;      // [ne][3] boundary_face_tags_ value, -1 when absent
+    std::vector<int> ifaces;    // [n][5] L, R, fL, fR, reversed
+    std::vector<int> bfaces;    // [n][3] elem, face, tag
+    std::map<int, BCDef> bcs;   // by tag id
+    int ne() const { return (int)elems.size() / 3; }
+};
+
+// GeometricMapping::compute_mapping (src/reference/mapping.cpp:22-50) for an affine
+// triangle: J_T = dN^T V, A = inverse(J_T) by the 2x2 cofactor formula.
+static bool affine_map(const double* V, double* A, double* det) {
+    const double J00 = V[2] - V[0], J01 = V[3] - V[1];
+    const double J10 = V[4] - V[0], J11 = V[5] - V[1];
+    *det = J00 * J11 - J10 * J01;
+    if (std::fabs(*det) < 1e-12) return false;
+    const double inv = 1.0 / *det;
+    A[0] = J11 * inv;
+    A[2] = -J10 * inv;
+    A[1] = -J01 * inv;
+    A[3] = J00 * inv;
+    return true;
+}
+
+// outward normal and length of face f (DGSpace::compute_face_data, src/core/space.cpp:104-137)
+static bool face_geom(const double* V, int f, double* n, double* len) {
+    const double* v1 = V + 2 * kEdge[f][0];
+    const double* v2 = V + 2 * kEdge[f][1];
+    const double tx = v2[0] - v1[0], ty = v2[1] - v1[1];
+    *len = std::sqrt(tx * tx + ty * ty);
+    if (*len < 1e-14) return false;
+    n[0] = ty / *len;
+    n[1] = -tx / *len;
+    const double cx = (V[0] + V[2] + V[4]) / 3.0, cy = (V[1] + V[3] + V[5]) / 3.0;
+    const double mx = 0.5 * (v1[0] + v2[0]), my = 0.5 * (v1[1] + v2[1]);
+    if (n[0] * (mx - cx) + n[1] * (my - cy) < 0) {
+        n[0] = -n[0];
+        n[1] = -n[1];
+    }
+    return true;
+}
+
+static void elem_verts(const dgx_mesh* m, int e, double* V) {
+    for (int k = 0; k < 3; ++k) {
+        const int v = m->elems[3 * e + k];
+        V[2 * k] = m->verts[2 * v];
+        V[2 * k + 1] = m->verts[2 * v + 1];
+    }
+}
+
+// DGSpace::compute_face_permutation (src/core/space.cpp:173-228): reversed or not
+static bool face_reversed(const double* VL, int fL, const double* VR, int fR) {
+    const double* a1 = VL + 2 * kEdge[fL][0];
+    const double* b1 = VL + 2 * kEdge[fL][1];
+    const double* a2 = VR + 2 * kEdge[fR][0];
+    const double* b2 = VR + 2 * kEdge[fR][1];
+    auto dist = [](const double* p, const double* q) { return std::hypot(p[0] - q[0], p[1] - q[1]); };
+    const double tol = 1e-10;
+    const bool rev = dist(a1, b2) < tol && dist(b1, a2) < tol;
+    const bool same = dist(a1, a2) < tol && dist(b1, b2) < tol;
+    if (rev || same) return rev;
+    const double t1x = b1[0] - a1[0], t1y = b1[1] - a1[1];
+    const double t2x = b2[0] - a2[0], t2y = b2[1] - a2[1];
+    return (t1x * t2x + t1y * t2y) / (std::hypot(t1x, t1y) * std::hypot(t2x, t2y)) < 0.0;
+}
+
+// DGMesh::build_precomputed_faces (src/core/mesh.cpp:404-480): interior faces in
+// element-then-face order, de-duplicated by element pair; the rest are boundary faces.
+static void rebuild_faces(dgx_mesh* m) {
+    const int ne = m->ne();
+    m->ifaces.clear();
+    m->bfaces.clear();
+    std::unordered_set<unsigned long long> seen;
+    seen.reserve((size_t)ne * 2);
+    double VL[6], VR[6];
+    for (int L = 0; L < ne; ++L) {
+        elem_verts(m, L, VL);
+        for (int fL = 0; fL < 3; ++fL) {
+            const int R = m->nbr[6 * L + 2 * fL], fR = m->nbr[6 * L + 2 * fL + 1];
+            if (R >= 0) {
+                const unsigned long long key =
+                    ((unsigned long long)std::min(L, R) << 32) | (unsigned)std::max(L, R);
+                if (!seen.insert(key).second) continue;
+                elem_verts(m, R, VR);
+                const int rec[5] = {L, R, fL, fR, face_reversed(VL, fL, VR, fR) ? 1 : 0};
+                m->ifaces.insert(m->ifaces.end(), rec, rec + 5);
+            } else {
+                const int rec[3] = {L, fL, m->btag[3 * L + fL]};
+                m->bfaces.insert(m->bfaces.end(), rec, rec + 3);
+            }
+        }
+    }
+}
+
+// DGMesh ctor, build_face_connectivity and identify_boundary_faces
+// (src/core/mesh.cpp:18-51, 312-402) with a sort instead of dgfem's O(E*F) map scan.
+static int build_connectivity(dgx_mesh* m, int nbe, const int* bedges) {
+    const int ne = m->ne();
+    struct Rec { int a, b, ord; };
+    std::vector<Rec> r((size_t)ne * 3);
+    for (int e = 0; e < ne; ++e)
+        for (int f = 0; f < 3; ++f) {
+            const int v1 = m->elems[3 * e + f], v2 = m->elems[3 * e + (f + 1) % 3];
+            r[3 * e + f] = {std::min(v1, v2), std::max(v1, v2), 3 * e + f};
+        }
+    std::sort(r.begin(), r.end(), [](const Rec& x, const Rec& y) {
+        return x.a != y.a ? x.a < y.a : x.b != y.b ? x.b < y.b : x.ord < y.ord;
+    });
+    m->nbr.assign((size_t)ne * 6, -1);
+    for (size_t i = 0; i < r.size();) {
+        size_t j = i;
+        while (j < r.size() && r[j].a == r[i].a && r[j].b == r[i].b) ++j;
+        if (j - i >= 2) {  // the first two faces of a vertex pair become neighbours
+            const int e1 = r[i].ord / 3, f1 = r[i].ord % 3, e2 = r[i + 1].ord / 3, f2 = r[i + 1].ord % 3;
+            m->nbr[6 * e1 + 2 * f1] = e2;
+            m->nbr[6 * e1 + 2 * f1 + 1] = f2;
+            m->nbr[6 * e2 + 2 * f2] = e1;
+            m->nbr[6 * e2 + 2 * f2 + 1] = f1;
+        }
+        i = j;
+    }
+    m->btag.assign((size_t)ne * 3, -1);
+    if (nbe > 0) {
+        // boundary_edges is a std::map keyed by tag: later tags override earlier ones
+        std::vector<int> order(nbe);
+        for (int k = 0; k < nbe; ++k) order[k] = k;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int x, int y) { return bedges[3 * x] < bedges[3 * y]; });
+        std::map<std::pair<int, int>, int> sig;
+        for (int k : order) {
+            const int v1 = bedges[3 * k + 1], v2 = bedges[3 * k + 2];
+            sig[{std::min(v1, v2), std::max(v1, v2)}] = bedges[3 * k];
+        }
+        for (int e = 0; e < ne; ++e)
+            for (int f = 0; f < 3; ++f) {
+                if (m->nbr[6 * e + 2 * f] != -1) continue;
+                const int v1 = m->elems[3 * e + f], v2 = m->elems[3 * e + (f + 1) % 3];
+                auto it = sig.find({std::min(v1, v2), std::max(v1, v2)});
+                m->btag[3 * e + f] = it == sig.end() ? 0 : it->second;
+            }
+    }
+    rebuild_faces(m);
+    return DGX_OK;
+}
+
+extern "C" int dgx_mesh_create(int nv, const double* verts, int ne, const int* elems, int n_tags,
+                               const char* const* tag_names, const int* tag_ids, int nbe,
+                               const int* bedges, dgx_mesh** out) {
+    if (!out || nv < 0 || ne < 0 || (nv > 0 && !verts) || (ne > 0 && !elems) || (nbe > 0 && !bedges) ||
+        (n_tags > 0 && (!tag_names || !tag_ids)))
+        return fail(DGX_ERR_INVALID, "dgx_mesh_create: bad arguments");
+    for (int i = 0; i < 3 * ne; ++i)
+        if (elems[i] < 0 || elems[i] >= nv) return fail(DGX_ERR_RANGE, "element vertex index out of range");
+    for (int k = 0; k < nbe; ++k)
+        for (int c = 1; c < 3; ++c)
+            if (bedges[3 * k + c] < 0) return fail(DGX_ERR_RANGE, "boundary edge vertex index out of range");
+    auto* m = new dgx_mesh;
+    m->verts.assign(verts, verts + 2 * (size_t)nv);
+    m->elems.assign(elems, elems + 3 * (size_t)ne);
+    for (int t = 0; t < n_tags; ++t) m->tags[tag_names[t]] = tag_ids[t];
+    build_connectivity(m, nbe, bedges);
+    *out = m;
+    return DGX_OK;
+}
+
+// DGMesh::set_periodic_boundaries (src/core/mesh.cpp:482-588).  Like dgfem, the face list
+// is rebuilt, which drops the boundary conditions set before.
+extern "C" int dgx_mesh_set_periodic(dgx_mesh* m, const char* t1, const char* t2) {
+    if (!m || !t1 || !t2) return fail(DGX_ERR_INVALID, "dgx_mesh_set_periodic: null argument");
+    auto i1 = m->tags.find(t1), i2 = m->tags.find(t2);
+    if (i1 == m->tags.end()) return fail(DGX_ERR_INVALID, std::string("Unknown boundary tag: ") + t1);
+    if (i2 == m->tags.end()) return fail(DGX_ERR_INVALID, std::string("Unknown boundary tag: ") + t2);
+    const int tag1 = i1->second, tag2 = i2->second;
+    const std::string s1 = t1, s2 = t2;
+    const bool match_y = s1 == "Left" || s1 == "Right" || s2 == "Left" || s2 == "Right";
+    std::vector<int> f1, f2;
+    for (size_t i = 0; i < m->btag.size(); ++i) {
+        if (m->btag[i] < 0) continue;
+        if (m->btag[i] == tag1) f1.push_back((int)i);
+        else if (m->btag[i] == tag2) f2.push_back((int)i);
+    }
+    if (f1.empty() || f2.empty())
+        return fail(DGX_ERR_RUNTIME, "Cannot set periodic boundaries: one or both boundaries have no faces");
+    const int c = match_y ? 1 : 0;
+    auto center = [&](int slot) {
+        const int e = slot / 3, f = slot % 3;
+        const int a = m->elems[3 * e + f], b = m->elems[3 * e + (f + 1) % 3];
+        return 0.5 * (m->verts[2 * a + c] + m->verts[2 * b + c]);
+    };
+    // nearest transverse coordinate, first minimum wins: sort candidates once
+    std::vector<std::pair<double, int>> cand(f2.size());
+    for (size_t k = 0; k < f2.size(); ++k) cand[k] = {center(f2[k]), (int)k};
+    std::sort(cand.begin(), cand.end());
+    for (int s1f : f1) {
+        const double x = center(s1f);
+        auto it = std::lower_bound(cand.begin(), cand.end(), std::make_pair(x, -1));
+        double best = std::numeric_limits<double>::max();
+        int bi = -1;
+        // examine the run of equal distances on both sides; ties go to the lowest index
+        for (auto j = it; j != cand.end(); ++j) {
+            const double d = std::fabs(x - j->first);
+            if (d > best) break;
+            if (d < best || (d == best && j->second < bi)) { best = d; bi = j->second; }
+        }
+        for (auto j = it; j != cand.begin();) {
+            --j;
+            const double d = std::fabs(x - j->first);
+            if (d > best) break;
+            if (d < best || (d == best && j->second < bi)) { best = d; bi = j->second; }
+        }
+        if (bi < 0) continue;
+        const int e1 = s1f / 3, l1 = s1f % 3, e2 = f2[bi] / 3, l2 = f2[bi] % 3;
+        m->nbr[6 * e1 + 2 * l1] = e2;
+        m->nbr[6 * e1 + 2 * l1 + 1] = l2;
+        m->nbr[6 * e2 + 2 * l2] = e1;
+        m->nbr[6 * e2 + 2 * l2 + 1] = l1;
+    }
+    m->bcs.clear();
+    rebuild_faces(m);
+    return DGX_OK;
+}
+
+extern "C" int dgx_mesh_create_rectangle(int nx, int ny, double x0, double x1, double y0, double y1,
+                                         int periodic, dgx_mesh** out) {
+    if (nx < 1 || ny < 1 || !out || !(x1 > x0) || !(y1 > y0))
+        return fail(DGX_ERR_INVALID, "dgx_mesh_create_rectangle: bad arguments");
+    const int nvx = nx + 1, nvy = ny + 1;
+    std::vector<double> V((size_t)nvx * nvy * 2);
+    for (int j = 0; j < nvy; ++j)
+        for (int i = 0; i < nvx; ++i) {
+            // x = i*((x1-x0)/nx) + x0 with the last point exactly x1 (numpy.linspace)
+            const double sx = (x1 - x0) / nx, sy = (y1 - y0) / ny;
+            V[2 * ((size_t)j * nvx + i)] = i == nx ? x1 : i * sx + x0;
+            V[2 * ((size_t)j * nvx + i) + 1] = j == ny ? y1 : j * sy + y0;
+        }
+    auto vid = [&](int i, int j) { return j * nvx + i; };
+    std::vector<int> E((size_t)nx * ny * 6);
+    size_t k = 0;
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const int a = vid(i, j), b = vid(i + 1, j), c = vid(i + 1, j + 1), d = vid(i, j + 1);
+            const int t[6] = {a, b, c, a, c, d};
+            for (int q = 0; q < 6; ++q) E[k++] = t[q];
+        }
+    std::vector<int> B;
+    for (int i = 0; i < nx; ++i) B.insert(B.end(), {2, vid(i, 0), vid(i + 1, 0)});
+    for (int j = 0; j < ny; ++j) B.insert(B.end(), {3, vid(nx, j), vid(nx, j + 1)});
+    for (int i = 0; i < nx; ++i) B.insert(B.end(), {4, vid(i, ny), vid(i + 1, ny)});
+    for (int j = 0; j < ny; ++j) B.insert(B.end(), {5, vid(0, j), vid(0, j + 1)});
+    const char* names[4] = {"Bottom", "Right", "Top", "Left"};
+    const int ids[4] = {2, 3, 4, 5};
+    int rc = dgx_mesh_create(nvx * nvy, V.data(), nx * ny * 2, E.data(), 4, names, ids,
+                             (int)B.size() / 3, B.data(), out);
+    if (rc || !periodic) return rc;
+    if ((rc = dgx_mesh_set_periodic(*out, "Left", "Right")) || (rc = dgx_mesh_set_periodic(*out, "Bottom", "Top"))) {
+        dgx_mesh_destroy(*out);
+        *out = nullptr;
+    }
+    return rc;
+}
+
+extern "C" int dgx_mesh_set_bc(dgx_mesh* m, const char* tag, int type, const double* value4) {
+    if (!m || !tag) return fail(DGX_ERR_INVALID, "dgx_mesh_set_bc: null argument");
+    auto it = m->tags.find(tag);
+    if (it == m->tags.end()) return fail(DGX_ERR_INVALID, std::string("Unknown boundary tag: ") + tag);
+    if (type < DGX_BC_FAR_FIELD || type > DGX_BC_PERIODIC) return fail(DGX_ERR_INVALID, "unknown BC type");
+    BCDef d;
+    d.type = type;
+    for (int v = 0; v < 4; ++v) d.value[v] = value4 ? value4[v] : 0.0;
+    m->bcs[it->second] = d;
+    return DGX_OK;
+}
+
+extern "C" int dgx_mesh_info(const dgx_mesh* m, int* ne, int* nif, int* nbf) {
+    if (!m) return fail(DGX_ERR_INVALID, "null mesh");
+    if (ne) *ne = m->ne();
+    if (nif) *nif = (int)m->ifaces.size() / 5;
+    if (nbf) *nbf = (int)m->bfaces.size() / 3;
+    return DGX_OK;
+}
+
+extern "C" int dgx_mesh_interior_faces(const dgx_mesh* m, int* out5) {
+    if (!m || !out5) return fail(DGX_ERR_INVALID, "null argument");
+    std::copy(m->ifaces.begin(), m->ifaces.end(), out5);
+    return DGX_OK;
+}
+
+extern "C" int dgx_mesh_boundary_faces(const dgx_mesh* m, int* out3) {
+    if (!m || !out3) return fail(DGX_ERR_INVALID, "null argument");
+    std::copy(m->bfaces.begin(), m->bfaces.end(), out3);
+    return DGX_OK;
+}
+
+extern "C" int dgx_mesh_arrays(const dgx_mesh* m, int* nv, double* verts, int* elems) {
+    if (!m) return fail(DGX_ERR_INVALID, "null mesh");
+    if (nv) *nv = (int)m->verts.size() / 2;
+    if (verts) std::copy(m->verts.begin(), m->verts.end(), verts);
+    if (elems) std::copy(m->elems.begin(), m->elems.end(), elems);
+    return DGX_OK;
+}
+
+extern "C" void dgx_mesh_destroy(dgx_mesh* m) { delete m; }
+
+// ------------------------------------------------------------------ context
+struct dgx_ctx {
+    int device = 0;
+    dgx_params prm{};
+    int ne = 0, np = 0, nq = 0, nfq = 0;
+    size_t nstate = 0;  // ne*np*4
+    OpsHost ops{};
+    std::vector<double> xq;  // physical volume points
+    ElemGeom* d_geom = nullptr;
+    ElemConn* d_conn = nullptr;
+    BCSlot* d_bc = nullptr;
+    double* d_u1 = nullptr;
+    double* d_u2 = nullptr;
+    double* d_hu = nullptr;   // host-variant staging
+    double* d_hr = nullptr;
+    double* d_mon = nullptr;  // [4]
+    int* d_flag = nullptr;
+    cudaStream_t cap = nullptr;  // capture stream
+    cudaGraphExec_t graph = nullptr;
+    const double* graph_u = nullptr;
+    double graph_dt = 0.0;
+};
+
+static StepArgs base_args(const dgx_ctx* c) {
+    StepArgs a{};
+    a.ne = c->ne;
+    a.geom = c->d_geom;
+    a.conn = c->d_conn;
+    a.bc = c->d_bc;
+    a.gamma = c->prm.gamma;
+    a.mu = c->prm.mu;
+    a.prandtl = c->prm.prandtl;
+    a.sigma0 = c->prm.sigma0;
+    a.order = c->prm.order;
+    return a;
+}
+
+static int launch(const dgx_ctx* c, const StepArgs& a, cudaStream_t s) {
+    const bool visc = c->prm.physics == DGX_NAVIER_STOKES;
+    const int rc = c->prm.precision == DGX_MIXED ? launch_element_mixed(c->prm.order, visc, a, c->ops, s)
+                                                 : launch_element_fp64(c->prm.order, visc, a, c->ops, s);
+    if (rc) return fail(DGX_ERR_CUDA, std::string("element kernel launch failed: ") +
+                                          cudaGetErrorString(cudaGetLastError()));
+    return DGX_OK;
+}
+
+static void free_ctx(dgx_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    if (c->cap) cudaStreamDestroy(c->cap);
+    cudaFree(c->d_geom);
+    cudaFree(c->d_conn);
+    cudaFree(c->d_bc);
+    cudaFree(c->d_u1);
+    cudaFree(c->d_u2);
+    cudaFree(c->d_hu);
+    cudaFree(c->d_hr);
+    cudaFree(c->d_mon);
+    cudaFree(c->d_flag);
+    delete c;
+}
+
+extern "C" void dgx_destroy(dgx_ctx* c) { free_ctx(c); }
+
+extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out) {
+    if (!m || !p || !out) return fail(DGX_ERR_INVALID, "dgx_create: null argument");
+    *out = nullptr;
+    if (p->order < 1 || p->order > MAX_P)
+        return fail(DGX_ERR_INVALID, "Element order must be between 1 and 4 for the GPU kernels");
+    if (p->basis != DGX_BASIS_MONOMIAL && p->basis != DGX_BASIS_DUBINER)
+        return fail(DGX_ERR_INVALID, "unknown basis");
+    if (p->physics != DGX_EULER && p->physics != DGX_NAVIER_STOKES)
+        return fail(DGX_ERR_INVALID, "unknown physics");
+    if (p->precision != DGX_FP64 && p->precision != DGX_MIXED)
+        return fail(DGX_ERR_INVALID, "unknown precision");
+    if (p->physics == DGX_NAVIER_STOKES) {  // NavierStokesWeakFormulation ctor checks (:22-33)
+        if (p->mu <= 0.0) return fail(DGX_ERR_INVALID, "Dynamic viscosity must be positive for Navier-Stokes weak formulation");
+        if (p->prandtl <= 0.0) return fail(DGX_ERR_INVALID, "Prandtl number must be positive for Navier-Stokes weak formulation");
+        if (p->sigma0 <= 0.0) return fail(DGX_ERR_INVALID, "Penalty prefactor must be positive for Navier-Stokes weak formulation");
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(DGX_ERR_CUDA, "no CUDA device: the dgx path has no CPU fallback");
+    }
+    int dev = 0;
+    CUDA_OK(cudaGetDevice(&dev));
+    cudaDeviceProp prop;
+    CUDA_OK(cudaGetDeviceProperties(&prop, dev));
+    if (prop.major != 10 || prop.minor != 3)
+        return fail(DGX_ERR_CUDA, "dgx kernels are built for sm_103a; this device is sm_" +
+                                      std::to_string(prop.major) + std::to_string(prop.minor));
+
+    {
+        const bool visc = p->physics == DGX_NAVIER_STOKES;
+        const int rc = p->precision == DGX_MIXED ? configure_element_mixed(p->order, visc)
+                                                 : configure_element_fp64(p->order, visc);
+        if (rc) return fail(DGX_ERR_CUDA, "could not configure the element kernel");
+    }
+    auto* c = new dgx_ctx;
+    c->device = dev;
+    c->prm = *p;
+    if (make_ops(p->order, p->basis, c->ops)) {
+        delete c;
+        return fail(DGX_ERR_RUNTIME, "could not build reference operators");
+    }
+    const int ne = m->ne();
+    c->ne = ne;
+    c->np = c->ops.np;
+    c->nq = c->ops.nq;
+    c->nfq = c->ops.nfq;
+    c->nstate = (size_t)ne * c->np * NV;
+
+    // geometry: DGSpace::compute_element_data / compute_face_data (space.cpp:69-171)
+    std::vector<ElemGeom> geom(ne);
+    std::vector<ElemConn> conn(ne);
+    std::vector<double> fn((size_t)ne * 6), fl((size_t)ne * 3);
+    c->xq.resize((size_t)ne * c->nq * 2);
+    for (int e = 0; e < ne; ++e) {
+        double V[6], A[4], det;
+        elem_verts(m, e, V);
+        if (!affine_map(V, A, &det)) {
+            free_ctx(c);
+            return fail(DGX_ERR_RUNTIME, "Singular Jacobian matrix");
+        }
+        ElemGeom& g = geom[e];
+        std::memset(&g, 0, sizeof(g));
+        for (int k = 0; k < 4; ++k) g.A[k] = A[k];
+        g.detJ = std::fabs(det);
+        double h = std::numeric_limits<double>::max();
+        for (int i = 0; i < 3; ++i)
+            for (int j = i + 1; j < 3; ++j)
+                h = std::min(h, std::sqrt((V[2 * i] - V[2 * j]) * (V[2 * i] - V[2 * j]) +
+                                          (V[2 * i + 1] - V[2 * j + 1]) * (V[2 * i + 1] - V[2 * j + 1])));
+        g.pad[0] = h;
+        for (int f = 0; f < 3; ++f) {
+            if (!face_geom(V, f, &fn[6 * (size_t)e + 2 * f], &fl[3 * (size_t)e + f])) {
+                free_ctx(c);
+                return fail(DGX_ERR_RUNTIME, "Degenerate edge detected");
+            }
+            conn[e].nbr[f] = NBR_SKIP;
+        }
+        conn[e].flags = 0;
+        for (int q = 0; q < c->nq; ++q) {  // map_to_physical: V^T N
+            const double xi = c->ops.qp[q][0], eta = c->ops.qp[q][1];
+            const double N0 = 1.0 - xi - eta;
+            c->xq[((size_t)e * c->nq + q) * 2] = N0 * V[0] + xi * V[2] + eta * V[4];
+            c->xq[((size_t)e * c->nq + q) * 2 + 1] = N0 * V[1] + xi * V[3] + eta * V[5];
+        }
+    }
+    std::vector<char> taken((size_t)ne * 3, 0);
+    auto take = [&](int e, int f) {
+        if (taken[3 * (size_t)e + f]) return false;
+        taken[3 * (size_t)e + f] = 1;
+        return true;
+    };
+    const int nif = (int)m->ifaces.size() / 5;
+    for (int k = 0; k < nif; ++k) {
+        const int* F = &m->ifaces[5 * (size_t)k];
+        const int L = F[0], R = F[1], fL = F[2], fR = F[3], rev = F[4];
+        if (!take(L, fL) || !take(R, fR)) {
+            free_ctx(c);
+            return fail(DGX_ERR_RUNTIME, "unsupported mesh topology: an element face appears in two interior faces");
+        }
+        const double* nL = &fn[6 * (size_t)L + 2 * fL];
+        const double hL = fl[3 * (size_t)L + fL];
+        geom[L].n[fL][0] = nL[0];
+        geom[L].n[fL][1] = nL[1];
+        geom[L].h[fL] = hL;
+        geom[R].n[fR][0] = -nL[0];
+        geom[R].n[fR][1] = -nL[1];
+        geom[R].h[fR] = hL;
+        conn[L].nbr[fL] = R;
+        conn[L].flags |= (fR | (rev << 2) | (1 << 3)) << (4 * fL);
+        conn[R].nbr[fR] = L;
+        conn[R].flags |= (fL | (rev << 2)) << (4 * fR);
+    }
+    std::vector<BCSlot> slots;
+    std::map<int, int> slot_of_tag;
+    const int nbf = (int)m->bfaces.size() / 3;
+    for (int k = 0; k < nbf; ++k) {
+        const int e = m->bfaces[3 * (size_t)k], f = m->bfaces[3 * (size_t)k + 1], tag = m->bfaces[3 * (size_t)k + 2];
+        geom[e].n[f][0] = fn[6 * (size_t)e + 2 * f];
+        geom[e].n[f][1] = fn[6 * (size_t)e + 2 * f + 1];
+        geom[e].h[f] = fl[3 * (size_t)e + f];
+        auto it = m->bcs.find(tag);
+        if (tag < 0 || it == m->bcs.end()) continue;  // no BC: dgfem skips the face
+        if (it->second.type == DGX_BC_PERIODIC) {
+            free_ctx(c);
+            return fail(DGX_ERR_RUNTIME, "PERIODIC BC encountered in boundary_face_residual - periodic "
+                                         "boundaries should be treated as interior faces");
+        }
+        auto si = slot_of_tag.find(tag);
+        int slot;
+        if (si == slot_of_tag.end()) {
+            if ((int)slots.size() >= MAX_BC) {
+                free_ctx(c);
+                return fail(DGX_ERR_RUNTIME, "too many boundary tags with conditions");
+            }
+            BCSlot b{};
+            b.type = it->second.type;
+            for (int v = 0; v < 4; ++v) b.value[v] = it->second.value[v];
+            slot = (int)slots.size();
+            slots.push_back(b);
+            slot_of_tag[tag] = slot;
+        } else {
+            slot = si->second;
+        }
+        conn[e].nbr[f] = -1 - slot;
+        conn[e].flags |= (1 << 3) << (4 * f);
+    }
+    if (slots.empty()) slots.push_back(BCSlot{});
+
+    auto alloc = [&](void** ptr, size_t bytes) {
+        return cudaMalloc(ptr, bytes ? bytes : 16) == cudaSuccess;
+    };
+    const size_t sb = c->nstate * sizeof(double);
+    if (!alloc((void**)&c->d_geom, sizeof(ElemGeom) * ne) || !alloc((void**)&c->d_conn, sizeof(ElemConn) * ne) ||
+        !alloc((void**)&c->d_bc, sizeof(BCSlot) * slots.size()) || !alloc((void**)&c->d_u1, sb) ||
+        !alloc((void**)&c->d_u2, sb) || !alloc((void**)&c->d_mon, 4 * sizeof(double)) ||
+        !alloc((void**)&c->d_flag, sizeof(int))) {
+        cudaGetLastError();
+        free_ctx(c);
+        return fail(DGX_ERR_CUDA, "cudaMalloc failed for the solver state");
+    }
+    if (cudaMemcpy(c->d_geom, geom.data(), sizeof(ElemGeom) * ne, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(c->d_conn, conn.data(), sizeof(ElemConn) * ne, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(c->d_bc, slots.data(), sizeof(BCSlot) * slots.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->cap, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        free_ctx(c);
+        return fail(DGX_ERR_CUDA, "device upload failed");
+    }
+    *out = c;
+    return DGX_OK;
+}
+
+extern "C" int dgx_info(const dgx_ctx* c, int* ne, int* np, int* nq, int* nfq) {
+    if (!c) return fail(DGX_ERR_INVALID, "null context");
+    if (ne) *ne = c->ne;
+    if (np) *np = c->np;
+    if (nq) *nq = c->nq;
+    if (nfq) *nfq = c->nfq;
+    return DGX_OK;
+}
+
+extern "C" int dgx_residual(dgx_ctx* c, const double* u, double* r, void* stream) {
+    if (!c || (c->ne && (!u || !r))) return fail(DGX_ERR_INVALID, "dgx_residual: null argument");
+    if (u == r) return fail(DGX_ERR_INVALID, "dgx_residual: r may not alias u");
+    StepArgs a = base_args(c);
+    a.mode = MODE_RESIDUAL;
+    a.u = u;
+    a.out = r;
+    return launch(c, a, (cudaStream_t)stream);
+}
+
+extern "C" int dgx_rhs(dgx_ctx* c, const double* u, double* du, void* stream) {
+    if (!c || (c->ne && (!u || !du))) return fail(DGX_ERR_INVALID, "dgx_rhs: null argument");
+    if (u == du) return fail(DGX_ERR_INVALID, "dgx_rhs: du may not alias u");
+    StepArgs a = base_args(c);
+    a.mode = MODE_RHS;
+    a.u = u;
+    a.out = du;
+    return launch(c, a, (cudaStream_t)stream);
+}
+
+extern "C" int dgx_apply_mass_inv(dgx_ctx* c, const double* in, double* out, void* stream) {
+    if (!c || (c->ne && (!in || !out))) return fail(DGX_ERR_INVALID, "dgx_apply_mass_inv: null argument");
+    if (launch_mass_inv(c->ne, c->prm.order, c->ops, c->d_geom, in, out, (cudaStream_t)stream))
+        return fail(DGX_ERR_CUDA, "mass inverse launch failed");
+    return DGX_OK;
+}
+
+// The three SSP-RK3 stages (time_stepping.hpp:39-55):
+//   u1 = u + dt L(u);  u2 = 3/4 u + 1/4 (u1 + dt L(u1));  u <- 1/3 u + 2/3 (u2 + dt L(u2))
+// The last stage writes u in place: each element reads only its own u^n entries there.
+static int enqueue_rk3(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
+    StepArgs a = base_args(c);
+    a.mode = MODE_STAGE;
+    a.dt = dt;
+    a.u = u; a.un = nullptr; a.out = c->d_u1; a.a = 0.0; a.b = 1.0;
+    int rc = launch(c, a, s);
+    if (rc) return rc;
+    a.u = c->d_u1; a.un = u; a.out = c->d_u2; a.a = 0.75; a.b = 0.25;
+    if ((rc = launch(c, a, s))) return rc;
+    a.u = c->d_u2; a.un = u; a.out = u; a.a = 1.0 / 3.0; a.b = 2.0 / 3.0;
+    return launch(c, a, s);
+}
+
+extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void* stream) {
+    if (!c || (c->ne && !u) || n_steps < 0) return fail(DGX_ERR_INVALID, "dgx_rk3_step: bad argument");
+    if (c->ne == 0 || n_steps == 0) return DGX_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!c->graph || c->graph_u != u || c->graph_dt != dt) {
+        if (c->graph) {
+            cudaGraphExecDestroy(c->graph);
+            c->graph = nullptr;
+        }
+        cudaGraph_t g;
+        CUDA_OK(cudaStreamBeginCapture(c->cap, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_rk3(c, u, dt, c->cap);
+        const cudaError_t ec = cudaStreamEndCapture(c->cap, &g);
+        if (rc) return rc;
+        if (ec != cudaSuccess) return fail(DGX_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
+        const cudaError_t ei = cudaGraphInstantiate(&c->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+            c->graph = nullptr;
+            return fail(DGX_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+        }
+        c->graph_u = u;
+        c->graph_dt = dt;
+    }
+    for (int i = 0; i < n_steps; ++i) CUDA_OK(cudaGraphLaunch(c->graph, s));
+    return DGX_OK;
+}
+
+extern "C" int dgx_max_cfl(dgx_ctx* c, const double* u, double dt, double* cfl, void* stream) {
+    if (!c || !cfl || (c->ne && !u)) return fail(DGX_ERR_INVALID, "dgx_max_cfl: null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (launch_monitor(c->ne, c->prm.order, c->ops, c->d_geom, u, dt, c->prm.gamma, c->d_mon, s))
+        return fail(DGX_ERR_CUDA, "monitor launch failed");
+    double h[4];
+    CUDA_OK(cudaMemcpyAsync(h, c->d_mon, sizeof(h), cudaMemcpyDeviceToHost, s));
+    CUDA_OK(cudaStreamSynchronize(s));
+    *cfl = h[3] > 0.0 ? INFINITY : h[0];
+    return DGX_OK;
+}
+
+extern "C" int dgx_density_range(dgx_ctx* c, const double* u, double* rmin, double* rmax, void* stream) {
+    if (!c || !rmin || !rmax || (c->ne && !u)) return fail(DGX_ERR_INVALID, "dgx_density_range: null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (launch_monitor(c->ne, c->prm.order, c->ops, c->d_geom, u, 0.0, c->prm.gamma, c->d_mon, s))
+        return fail(DGX_ERR_CUDA, "monitor launch failed");
+    double h[4];
+    CUDA_OK(cudaMemcpyAsync(h, c->d_mon, sizeof(h), cudaMemcpyDeviceToHost, s));
+    CUDA_OK(cudaStreamSynchronize(s));
+    if (!std::isfinite(h[1]) || !std::isfinite(h[2])) {
+        *rmin = *rmax = NAN;
+    } else {
+        *rmin = h[1];
+        *rmax = h[2];
+    }
+    return DGX_OK;
+}
+
+extern "C" int dgx_has_nan(dgx_ctx* c, const double* u, int* has_nan, void* stream) {
+    if (!c || !has_nan || (c->ne && !u)) return fail(DGX_ERR_INVALID, "dgx_has_nan: null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (launch_has_nan(c->nstate, u, c->d_flag, s)) return fail(DGX_ERR_CUDA, "nan scan launch failed");
+    int f = 0;
+    CUDA_OK(cudaMemcpyAsync(&f, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_OK(cudaStreamSynchronize(s));
+    *has_nan = f ? 1 : 0;
+    return DGX_OK;
+}
+
+extern "C" int dgx_quad_points(const dgx_ctx* c, double* xq) {
+    if (!c || !xq) return fail(DGX_ERR_INVALID, "dgx_quad_points: null argument");
+    std::copy(c->xq.begin(), c->xq.end(), xq);
+    return DGX_OK;
+}
+
+extern "C" int dgx_project(dgx_ctx* c, const double* uq, double* u, void* stream) {
+    if (!c || (c->ne && (!uq || !u))) return fail(DGX_ERR_INVALID, "dgx_project: null argument");
+    if (launch_project(c->ne, c->prm.order, c->ops, c->d_geom, uq, u, (cudaStream_t)stream))
+        return fail(DGX_ERR_CUDA, "projection launch failed");
+    return DGX_OK;
+}
+
+static int ensure_host_buffers(dgx_ctx* c) {
+    if (c->d_hu) return DGX_OK;
+    const size_t sb = (c->nstate ? c->nstate : 1) * sizeof(double);
+    if (cudaMalloc((void**)&c->d_hu, sb) != cudaSuccess || cudaMalloc((void**)&c->d_hr, sb) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(DGX_ERR_CUDA, "cudaMalloc failed for host-variant buffers");
+    }
+    return DGX_OK;
+}
+
+extern "C" int dgx_residual_host(dgx_ctx* c, const double* u, double* r) {
+    if (!c || (c->ne && (!u || !r))) return fail(DGX_ERR_INVALID, "dgx_residual_host: null argument");
+    int rc = ensure_host_buffers(c);
+    if (rc) return rc;
+    const size_t sb = c->nstate * sizeof(double);
+    CUDA_OK(cudaMemcpyAsync(c->d_hu, u, sb, cudaMemcpyHostToDevice, c->cap));
+    if ((rc = dgx_residual(c, c->d_hu, c->d_hr, c->cap))) return rc;
+    CUDA_OK(cudaMemcpyAsync(r, c->d_hr, sb, cudaMemcpyDeviceToHost, c->cap));
+    CUDA_OK(cudaStreamSynchronize(c->cap));
+    return DGX_OK;
+}
+
+extern "C" int dgx_rk3_step_host(dgx_ctx* c, double* u, double dt, int n_steps) {
+    if (!c || (c->ne && !u) || n_steps < 0) return fail(DGX_ERR_INVALID, "dgx_rk3_step_host: bad argument");
+    int rc = ensure_host_buffers(c);
+    if (rc) return rc;
+    const size_t sb = c->nstate * sizeof(double);
+    CUDA_OK(cudaMemcpyAsync(c->d_hu, u, sb, cudaMemcpyHostToDevice, c->cap));
+    if ((rc = dgx_rk3_step(c, c->d_hu, dt, n_steps, c->cap))) return rc;
+    CUDA_OK(cudaMemcpyAsync(u, c->d_hu, sb, cudaMemcpyDeviceToHost, c->cap));
+    CUDA_OK(cudaStreamSynchronize(c->cap));
+    return DGX_OK;
+}

@@ -1,0 +1,130 @@
+// Internal layouts shared by the host side (dgx_host.cpp) and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace dgx {
+
+constexpr int NV = 4;      // conserved variables (rho, rho u, rho v, E), assembler.cpp:154
+constexpr int MAX_P = 4;   // orders with compiled kernels
+constexpr int TILE = 128;  // elements per CTA in the element kernels (one per thread)
+
+__host__ __device__ constexpr int n_basis(int p) { return (p + 1) * (p + 2) / 2; }
+// volume points of the degree-2p triangle rule DGSpace uses (space.cpp:40-41)
+__host__ __device__ constexpr int n_quad(int p) {
+    return p == 1 ? 3 : p == 2 ? 6 : p == 3 ? 12 : p == 4 ? 16 : 0;
+}
+
+// Per-element geometry, 128 B, one record per element in element order.
+struct alignas(128) ElemGeom {
+    double A[4];      // dxi/dx = inverse(J_T), row-major (mapping.cpp:33-47)
+    double detJ;      // |det J_T|
+    double h[3];      // face length; the L side's length for interior faces
+    double n[3][2];   // face normal as seen from this element (= +/- the L side's normal)
+    double pad[2];    // pad[0]: shortest vertex distance (compute_max_cfl's h_elem)
+};
+static_assert(sizeof(ElemGeom) == 128, "ElemGeom must stay 128 B");
+
+// Per-element face connectivity, 16 B.
+//   nbr[f] >= 0       interior face: neighbour element
+//   nbr[f] = -1 - s   boundary face with boundary-condition slot s
+//   nbr[f] = SKIP     face that takes no part in the residual (no BC set)
+// flags, 4 bits per face f at bit 4f: [1:0] neighbour's face, [2] reversed point order,
+// [3] this element is the L side of the face in dgfem's face list.
+struct alignas(16) ElemConn {
+    int nbr[3];
+    int flags;
+};
+constexpr int NBR_SKIP = -0x40000000;
+
+struct BCSlot {
+    int type;  // DGX_BC_*
+    int pad;
+    double value[4];
+};
+constexpr int MAX_BC = 64;
+
+// Reference-element operators for order P, stored in precision T.
+template <int P, typename T>
+struct Ops {
+    static constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1;
+    T phi[NQ][NP];        // basis at volume points
+    T dr[NQ][NP];         // d/dxi at volume points
+    T ds[NQ][NP];         // d/deta at volume points
+    T phif[3][NFQ][NP];   // basis at face points (face f, point q)
+    T drf[3][NFQ][NP];    // d/dxi at face points
+    T dsf[3][NFQ][NP];    // d/deta at face points
+    T wq[NQ];             // volume weights
+    T wf[NFQ];            // Gauss-Legendre weights on [-1, 1]
+    T minv[NP][NP];       // inverse of the reference mass matrix sum_q w_q phi phi^T
+};
+
+// Host copy of all operators in double precision, sized for MAX_P.
+struct OpsHost {
+    int p, np, nq, nfq;
+    double phi[16][15], dr[16][15], ds[16][15];
+    double phif[3][5][15], drf[3][5][15], dsf[3][5][15];
+    double wq[16], wf[5];
+    double minv[15][15];
+    double qp[16][2];  // volume points on the reference triangle
+    double fp[5];      // face points on [-1, 1]
+};
+
+template <int P, typename T>
+inline void fill_ops(const OpsHost& h, Ops<P, T>& o) {
+    constexpr int NP = Ops<P, T>::NP, NQ = Ops<P, T>::NQ, NFQ = Ops<P, T>::NFQ;
+    for (int q = 0; q < NQ; ++q)
+        for (int i = 0; i < NP; ++i) {
+            o.phi[q][i] = (T)h.phi[q][i];
+            o.dr[q][i] = (T)h.dr[q][i];
+            o.ds[q][i] = (T)h.ds[q][i];
+        }
+    for (int f = 0; f < 3; ++f)
+        for (int q = 0; q < NFQ; ++q)
+            for (int i = 0; i < NP; ++i) {
+                o.phif[f][q][i] = (T)h.phif[f][q][i];
+                o.drf[f][q][i] = (T)h.drf[f][q][i];
+                o.dsf[f][q][i] = (T)h.dsf[f][q][i];
+            }
+    for (int q = 0; q < NQ; ++q) o.wq[q] = (T)h.wq[q];
+    for (int q = 0; q < NFQ; ++q) o.wf[q] = (T)h.wf[q];
+    for (int i = 0; i < NP; ++i)
+        for (int j = 0; j < NP; ++j) o.minv[i][j] = (T)h.minv[i][j];
+}
+
+enum Mode { MODE_RESIDUAL = 0, MODE_RHS = 1, MODE_STAGE = 2 };
+
+// Arguments of one element-kernel launch.
+struct StepArgs {
+    int ne;
+    int mode;              // Mode
+    const double* u;       // stage state (neighbours are read from it)
+    const double* un;      // u^n for MODE_STAGE (own element only); may be null when a == 0
+    double* out;           // residual, M^-1 R, or the next stage state
+    const ElemGeom* geom;
+    const ElemConn* conn;
+    const BCSlot* bc;
+    double dt, a, b;       // MODE_STAGE: out = a*un + b*(u + dt*du); a == 0: out = u + dt*du
+    double gamma, mu, prandtl, sigma0;
+    int order;
+    int* status;           // device flag: bit 0 set when a non-finite value was produced
+};
+
+// Launchers (one translation unit per precision).
+int launch_element_fp64(int p, bool viscous, const StepArgs& a, const OpsHost& ops, cudaStream_t s);
+int launch_element_mixed(int p, bool viscous, const StepArgs& a, const OpsHost& ops, cudaStream_t s);
+int configure_element_fp64(int p, bool viscous);
+int configure_element_mixed(int p, bool viscous);
+
+// Small FP64 utility kernels (dgx_misc.cu).
+int launch_mass_inv(int ne, int p, const OpsHost& ops, const ElemGeom* geom, const double* in,
+                    double* out, cudaStream_t s);
+int launch_project(int ne, int p, const OpsHost& ops, const ElemGeom* geom, const double* uq,
+                   double* u, cudaStream_t s);
+int launch_monitor(int ne, int p, const OpsHost& ops, const ElemGeom* geom, const double* u,
+                   double dt, double gamma, double* d_out /*[4]*/, cudaStream_t s);
+int launch_has_nan(size_t n, const double* u, int* d_flag, cudaStream_t s);
+
+}  // namespace dgx

@@ -1,0 +1,19 @@
+// Mixed-precision element kernels: FP32 flux and contraction arithmetic, FP64 geometry,
+// FP64 inverse mass matrix and FP64 RK3 state accumulation.
+#include "dg_element.cuh"
+
+namespace dgx {
+
+int launch_element_mixed(int p, bool viscous, const StepArgs& a, const OpsHost& ops, cudaStream_t s) {
+#define ARGS (a, ops, s)
+    DGX_ELEMENT_DISPATCH(launch_element_t, float)
+#undef ARGS
+}
+
+int configure_element_mixed(int p, bool viscous) {
+#define ARGS ()
+    DGX_ELEMENT_DISPATCH(configure_element_t, float)
+#undef ARGS
+}
+
+}  // namespace dgx

@@ -1,0 +1,164 @@
+/*
+ * dgx.h -- C ABI of the GB300-native explicit DG residual-and-update path.
+ *
+ * This library replaces the hot path of dgfem (GaleAxiom/Discontinuous-Galerkin-FEM):
+ * the compressible Euler / Navier-Stokes residual (volume flux integral, Rusanov face
+ * flux lifted to element modes, SIPG-style viscous terms), the block inverse mass
+ * matrix and the SSP-RK3 stage update.  Each entry point names the dgfem interface it
+ * replaces (paths inside the dgfem project).
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  Functions return DGX_OK (0) or a negative status;
+ *    dgx_last_error() gives the message of the last failure on the calling thread.
+ *  - A state is double[n_elements][n_basis][4] (rho, rho*u, rho*v, E): dgfem's flat
+ *    DGSolution index elem*Np*4 + i*4 + v (src/core/solution.cpp:143-145), i.e. the
+ *    per-element Np x 4 matrices of `std::vector<Eigen::MatrixXd>` stored row-major.
+ *  - Functions with a `stream` argument take DEVICE pointers and are stream-ordered
+ *    (stream is a cudaStream_t; NULL = legacy default stream).  `_host` variants take
+ *    host pointers and synchronise before returning.
+ *  - A context is not thread-safe: use one per thread (dgfem's assembler is not
+ *    re-entrant either, src/solver/assembler.cpp:143-150).
+ *  - There is no CPU fallback: every compute entry point fails with DGX_ERR_CUDA when
+ *    no sm_103 device is present.
+ */
+#ifndef DGX_H
+#define DGX_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DGX_OK 0
+#define DGX_ERR_INVALID (-1)   /* std::invalid_argument in dgfem */
+#define DGX_ERR_RUNTIME (-2)   /* std::runtime_error in dgfem */
+#define DGX_ERR_RANGE (-3)     /* std::out_of_range in dgfem */
+#define DGX_ERR_CUDA (-4)      /* CUDA failure or no usable GPU */
+#define DGX_ERR_NONFINITE (-5) /* non-finite or non-positive state detected */
+
+enum { DGX_BASIS_MONOMIAL = 0, DGX_BASIS_DUBINER = 1 };
+enum { DGX_EULER = 0, DGX_NAVIER_STOKES = 1 };
+enum { DGX_FP64 = 0, DGX_MIXED = 1 };
+/* BCTypeEuler, include/dgfem/boundary/conditions.hpp:27-32 */
+enum { DGX_BC_FAR_FIELD = 0, DGX_BC_SLIP_WALL = 1, DGX_BC_NO_SLIP_WALL = 2, DGX_BC_PERIODIC = 3 };
+
+typedef struct dgx_mesh dgx_mesh;
+typedef struct dgx_ctx dgx_ctx;
+
+/* Weak form + space parameters.
+ * Replaces DGSpace(type, order) (include/dgfem/core/space.hpp:27),
+ * EulerWeakFormulation(gamma) (include/dgfem/weak_forms/euler_weak_formulation.hpp:18) and
+ * NavierStokesWeakFormulation(gamma, mu, Pr, sigma0)
+ * (include/dgfem/weak_forms/navier_stokes_weak_formulation.hpp:19-20). */
+typedef struct {
+    int order;      /* polynomial order p, 1..4 */
+    int basis;      /* DGX_BASIS_MONOMIAL (dgfem's triangle default) or DGX_BASIS_DUBINER */
+    int physics;    /* DGX_EULER or DGX_NAVIER_STOKES */
+    int precision;  /* DGX_FP64 or DGX_MIXED */
+    double gamma;   /* 1.4 */
+    double mu;      /* dynamic viscosity (Navier-Stokes) */
+    double prandtl; /* Prandtl number (Navier-Stokes) */
+    double sigma0;  /* SIPG penalty prefactor (Navier-Stokes) */
+} dgx_params;
+
+const char* dgx_last_error(void);
+const char* dgx_version(void);
+
+/* ---------------------------------------------------------------- mesh (host) */
+
+/* DGMesh(vertices, elements, element_tags, boundary_tags, boundary_edges),
+ * include/dgfem/core/mesh.hpp:31-33, src/core/mesh.cpp:18-51, 312-402.
+ * vertices: [n_vertices][2]; elements: [n_elements][3] vertex ids (triangles);
+ * tag_names/tag_ids: the boundary_tags map; boundary_edges: [n_edges][3] = (tag, v1, v2). */
+int dgx_mesh_create(int n_vertices, const double* vertices, int n_elements, const int* elements,
+                    int n_tags, const char* const* tag_names, const int* tag_ids,
+                    int n_boundary_edges, const int* boundary_edges, dgx_mesh** out);
+
+/* Structured N_x x N_y quad grid on [x0,x1]x[y0,y1], each quad split along its
+ * (i,j)-(i+1,j+1) diagonal into two counter-clockwise triangles, boundary tags
+ * Bottom=2 Right=3 Top=4 Left=5 (src/utils/mesh_creation.cpp:249-260).  With periodic!=0
+ * it also calls set_periodic("Left","Right") and set_periodic("Bottom","Top").
+ * Replaces MeshSetup::create_standard_mesh (include/dgfem/utils/example_helpers.hpp:75-102)
+ * for rectangles, without GMSH. */
+int dgx_mesh_create_rectangle(int nx, int ny, double x0, double x1, double y0, double y1,
+                              int periodic, dgx_mesh** out);
+
+/* DGMesh::set_periodic_boundaries, include/dgfem/core/mesh.hpp:102, src/core/mesh.cpp:482-588 */
+int dgx_mesh_set_periodic(dgx_mesh* m, const char* tag1, const char* tag2);
+
+/* DGMesh::set_boundary_condition_euler with a constant BoundaryConditionEuler,
+ * include/dgfem/core/mesh.hpp:84-85.  value: conserved state (FAR_FIELD) or primitive
+ * state (NO_SLIP_WALL); ignored for SLIP_WALL.  Must precede dgx_create. */
+int dgx_mesh_set_bc(dgx_mesh* m, const char* tag, int bc_type, const double* value4);
+
+/* counts: elements, interior faces (DGMesh::get_interior_faces), boundary faces */
+int dgx_mesh_info(const dgx_mesh* m, int* n_elements, int* n_interior_faces, int* n_boundary_faces);
+/* FaceConnectivity list (include/dgfem/core/mesh.hpp:147-157): [n][5] = (elem_L, elem_R,
+ * face_L, face_R, reversed) in DGMesh::build_precomputed_faces order. */
+int dgx_mesh_interior_faces(const dgx_mesh* m, int* out5);
+/* [n][3] = (elem, face, tag id) of boundary faces, in build_precomputed_faces order */
+int dgx_mesh_boundary_faces(const dgx_mesh* m, int* out3);
+/* vertices [n_vertices][2] / elements [n_elements][3]; either pointer may be NULL */
+int dgx_mesh_arrays(const dgx_mesh* m, int* n_vertices, double* vertices, int* elements);
+void dgx_mesh_destroy(dgx_mesh* m);
+
+/* ---------------------------------------------------------------- context */
+
+/* Builds the device-resident solver: DGMesh::initialize_dg_space (src/core/mesh.cpp:53-99),
+ * DGAssembler(mesh, weak_form) (include/dgfem/solver/assembler.hpp:30-31) and
+ * CompressibleDGSolverBase::compute_mass_matrix_inverse_blocks
+ * (src/solver/compressible_solver_base.cpp:41-52).  The context owns all device memory. */
+int dgx_create(const dgx_mesh* m, const dgx_params* params, dgx_ctx** out);
+void dgx_destroy(dgx_ctx* c);
+/* sizes: n_elements, n_basis (Np), n_quad (volume points), n_face_quad */
+int dgx_info(const dgx_ctx* c, int* n_elements, int* n_basis, int* n_quad, int* n_face_quad);
+
+/* ---------------------------------------------------------------- hot path (device) */
+
+/* DGAssembler::assemble_euler_residual(u_coeffs, residuals_out),
+ * include/dgfem/solver/assembler.hpp:58-59, src/solver/assembler.cpp:137-279.
+ * u, r: device states.  r may not alias u. */
+int dgx_residual(dgx_ctx* c, const double* u, double* r, void* stream);
+
+/* CompressibleDGSolverBase::apply_mass_inv, include/dgfem/solver/dg_solver.hpp:236,
+ * src/solver/compressible_solver_base.cpp:54-61 (also BlockMassMatrix::apply_inverse,
+ * include/dgfem/solver/time_stepping.hpp:114).  in may alias out. */
+int dgx_apply_mass_inv(dgx_ctx* c, const double* in, double* out, void* stream);
+
+/* rhs_func = apply_mass_inv(assemble_residual(u)), src/solver/compressible_solver_base.cpp:108-110 */
+int dgx_rhs(dgx_ctx* c, const double* u, double* du, void* stream);
+
+/* CompressibleDGSolverBase::time_step_ssp_rk3 + SSP_RK::step_rk3,
+ * include/dgfem/solver/dg_solver.hpp:239, include/dgfem/solver/time_stepping.hpp:39-55.
+ * Advances u (device, in place) by n_steps SSP-RK3 steps of size dt.  The three stages
+ * of a step are captured once into a CUDA graph and replayed. */
+int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void* stream);
+
+/* CompressibleDGSolverBase::compute_max_cfl / compute_density_range,
+ * src/solver/compressible_solver_base.cpp:114-199.  Results are written to host memory
+ * (the call synchronises the stream).  CFL is +inf when rho<=0 or p<=0 anywhere. */
+int dgx_max_cfl(dgx_ctx* c, const double* u, double dt, double* cfl, void* stream);
+int dgx_density_range(dgx_ctx* c, const double* u, double* rho_min, double* rho_max, void* stream);
+/* 1 if any entry of u is NaN (the per-step scan of run_time_integration,
+ * src/solver/compressible_solver_base.cpp:290-301), else 0; host result, synchronises. */
+int dgx_has_nan(dgx_ctx* c, const double* u, int* has_nan, void* stream);
+
+/* Physical coordinates of every volume quadrature point, [n_elements][n_quad][2] (host),
+ * GeometricMapping::map_to_physical at the points project_initial_condition uses. */
+int dgx_quad_points(const dgx_ctx* c, double* xq);
+/* CompressibleDGSolverBase::project_initial_condition, src/solver/compressible_solver_base.cpp:63-104:
+ * uq = the initial condition at dgx_quad_points, [n_elements][n_quad][4] (device). */
+int dgx_project(dgx_ctx* c, const double* uq, double* u, void* stream);
+
+/* ---------------------------------------------------------------- host-pointer variants */
+
+/* assemble_euler_residual on host states (copies in, computes, copies out). */
+int dgx_residual_host(dgx_ctx* c, const double* u, double* r);
+/* time_step_ssp_rk3 on a host state, in place (copies in, n_steps steps, copies out). */
+int dgx_rk3_step_host(dgx_ctx* c, double* u, double dt, int n_steps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
