@@ -1,0 +1,328 @@
+"""Benchmark of the explicit DG residual-and-update path on GB300.
+
+Workload (one "step" = one SSP-RK3 step = 3 RHS stages over the whole mesh):
+  Euler isentropic vortex, periodic [-5,5]^2, 512x512 quads split into 524,288 triangles,
+  Dubiner basis p=3 (10 modes x 4 variables = 20,971,520 DOF), gamma=1.4, free stream
+  rho=1 u=0.5 v=0 p=1, vortex strength 5 centred at a seeded point of [-2,2]^2,
+  CFL 0.1 (dgfem's convective CFL definition).
+
+metric: DOF * RK-stages / s.  `value` is the mixed-precision path with the state resident
+in HBM; the FP64 path, the mixed-vs-FP64 speed-up and the L2/Linf error of the mixed
+path against the FP64 path after 500 steps are reported beside it.  `e2e` times the
+host-pointer C-ABI call (dgx_rk3_step_host) with the state copied in and out each step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With --impl reference the CPU oracle (FP64 restatement of dgfem's path) is timed on all
+host cores on a bounded sample of the same workload.  Under torchrun each rank runs an
+independent replica (the path is replicated, not sharded, on one-GPU runs).
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "discontinuous-galerkin-fem_gb300"))
+
+N_CELLS, ORDER, BASIS = 512, 3, "dubiner"
+# CFL 0.1 under dgfem's CFL definition (dt * max(|u|+c) / shortest edge,
+# compressible_solver_base.cpp:114-170) is unstable for p=3: the oracle restatement of
+# dgfem's scheme diverges within 50 steps.  The workload runs at 0.05.
+GAMMA, CFL, ACC_STEPS = 1.4, 0.05, 500
+# per element per RK stage, p=3, FP64 state: 3*Np*V*8 + 92 bytes of geometry/connectivity
+ALGO_BYTES_PER_ELEM_STAGE = 1052
+MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+# dram__bytes_read.sum + dram__bytes_write.sum per element per launch of the mixed
+# element kernel, from the ncu capture summarised in profiles/element_kernel_mixed_p3.md
+NCU_TRAFFIC_BYTES_PER_ELEM = None
+
+
+def vortex(xy, t=0.0, beta=5.0, xc=0.0, yc=0.0, uinf=0.5, vinf=0.0, gamma=GAMMA, period=10.0):
+    """Shu's isentropic vortex on rho=1, p=1, advected with (uinf, vinf), conserved vars."""
+    x = xy[..., 0] - (xc + uinf * t)
+    y = xy[..., 1] - (yc + vinf * t)
+    x = (x + period / 2) % period - period / 2
+    y = (y + period / 2) % period - period / 2
+    g = beta / (2.0 * np.pi) * np.exp(0.5 * (1.0 - (x * x + y * y)))
+    u, v = uinf - y * g, vinf + x * g
+    T = 1.0 - (gamma - 1.0) / (2.0 * gamma) * g * g
+    rho = T ** (1.0 / (gamma - 1.0))
+    p = rho * T
+    return np.stack([rho, rho * u, rho * v, p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v)], -1)
+
+
+def vortex_centre(seed=0):
+    return np.random.default_rng(seed).uniform(-2.0, 2.0, size=2)
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    return rank, ws
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.dev = device_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def hbm_peak():
+    try:
+        return float(json.loads(MEASURED_PEAKS.read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class OracleWorkload:
+    """The CPU oracle on the full 512x512x2 p=3 mesh (setup excluded from timing)."""
+
+    def __init__(self, threads, seed):
+        sys.path[:0] = [str(ROOT / "oracle"), str(ROOT / "tests")]
+        import oracle as O
+        from meshes import PERIODIC_PAIRS, periodic_rectangle
+        self.O = O
+        v, e, b = periodic_rectangle(N_CELLS)
+        self.m = O.OracleMesh(v, e, b, order=ORDER, basis=O.DUBINER, periodic=PERIODIC_PAIRS)
+        xc, yc = vortex_centre(seed)
+        O.set_threads(threads)
+        self.threads = threads
+        self.u = self.m.project(vortex(self.m.quad_points(), xc=xc, yc=yc))
+        self.ph = O.euler(GAMMA)
+        self.dof = self.m.ne * self.m.np * 4
+
+    def run(self, steps, dt=1e-3):
+        """Advance `steps` SSP-RK3 steps; returns (DOF*stages/s, seconds)."""
+        t0 = time.perf_counter()
+        self.u = self.m.rk3_step(self.ph, self.u, dt, steps)
+        secs = time.perf_counter() - t0
+        return self.dof * 3 * steps / secs, secs
+
+
+def run_reference(args, rank, ws):
+    """Reference arm: dgfem's path restated (oracle) on all host cores; rank 0 only."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    w = OracleWorkload(threads, args.seed)
+    if args.warmup > 0:
+        w.run(args.warmup)
+    k = max(1, args.steps)
+    rate, secs = w.run(k)
+    line = {"metric": "DOF*RK-stages/s", "value": rate, "unit": "DOF*stages/s", "n_gpus": ws,
+            "steps": k, "warmup": args.warmup, "ms_per_step": 1e3 * secs / k, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "euler_vortex_512x512x2_p3_dubiner", "elements": 2 * N_CELLS ** 2,
+                       "order": ORDER, "dof": w.dof},
+            "cpu_baseline": {"value": rate, "unit": "DOF*stages/s", "cores": threads, "kind": "port",
+                             "sample": f"each step is one SSP-RK3 step of the full 512x512x2 p=3 mesh; "
+                                       f"FP64 oracle restatement of dgfem's path, OpenMP {threads} threads"},
+            "e2e": {"value": rate, "unit": "DOF*stages/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="dgx", choices=["dgx", "reference"])
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--acc-steps", type=int, default=ACC_STEPS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cells", type=int, default=N_CELLS, help="quads per side (profiling cases)")
+    args = ap.parse_args()
+    rank, ws = dist_init()
+    if args.impl == "reference":
+        return run_reference(args, rank, ws)
+
+    import torch
+    import dgfem_gb300 as dg
+
+    dev = torch.cuda.current_device()
+    mesh = dg.DGMesh.rectangle(args.cells, args.cells, -5.0, 5.0, -5.0, 5.0, periodic=True)
+    space = dg.DGSpace("triangle", ORDER, BASIS)
+    wf = dg.EulerWeakFormulation(GAMMA)
+    c64 = dg.DGContext(mesh, space, wf, "fp64")
+    cmx = dg.DGContext(mesh, space, wf, "mixed")
+    ne, nb = c64.n_elements, c64.n_basis
+    dof = ne * nb * 4
+    xc, yc = vortex_centre(args.seed)
+    xq = c64.quad_points()
+    u0 = c64.project(torch.tensor(vortex(xq, xc=xc, yc=yc), device="cuda"))
+    dt = CFL / c64.max_cfl(u0, 1.0)
+
+    # ---- accuracy at t_final: mixed vs FP64 (the FP64 path matches the oracle to 1e-12 per RHS)
+    acc = {}
+    if args.acc_steps > 0:
+        u64 = u0.clone()
+        umx = u0.clone()
+        c64.rk3_step(u64, dt, args.acc_steps)
+        cmx.rk3_step(umx, dt, args.acc_steps)
+        torch.cuda.synchronize()
+        exact = c64.project(torch.tensor(vortex(xq, t=dt * args.acc_steps, xc=xc, yc=yc), device="cuda"))
+        d = (umx - u64)
+        acc = {"steps": args.acc_steps, "t_final": dt * args.acc_steps,
+               "mixed_vs_fp64_l2_rel": float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(u64)),
+               "mixed_vs_fp64_linf_rel": float(d.abs().max() / u64.abs().max()),
+               "fp64_vs_exact_l2_rel": float(torch.linalg.vector_norm(u64 - exact) / torch.linalg.vector_norm(exact)),
+               "mixed_vs_exact_l2_rel": float(torch.linalg.vector_norm(umx - exact) / torch.linalg.vector_norm(exact))}
+        del u64, umx, exact
+
+    def timed(ctx, k, warm):
+        u = u0.clone()
+        ctx.rk3_step(u, dt, warm)
+        torch.cuda.synchronize()
+        barrier(ws)
+        torch.cuda.synchronize()
+        s = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        ctx.rk3_step(u, dt, k)
+        e1.record(s)
+        torch.cuda.synchronize()
+        barrier(ws)
+        return e0.elapsed_time(e1) / 1e3
+
+    with ClockSampler(dev) as clk:
+        t_mx = timed(cmx, args.steps, args.warmup)
+    clocks = clk.summary()
+    t_mx = allreduce_max(t_mx, ws)
+    k64 = max(1, min(args.steps, 50))
+    t_64 = allreduce_max(timed(c64, k64, min(args.warmup, 3)), ws)
+    v_mx = dof * 3 * args.steps * ws / t_mx
+    v_64 = dof * 3 * k64 * ws / t_64
+
+    # ---- end to end through the host-pointer C-ABI call, pinned host state
+    host = u0.cpu().pin_memory()
+    hnp = host.numpy()
+    cmx.rk3_step(hnp, dt, 1)  # warm the host path (allocations, graph)
+    ke = max(1, min(args.steps, 50))
+    torch.cuda.synchronize()
+    barrier(ws)
+    t0 = time.perf_counter()
+    lib = dg.load()
+    import ctypes as C
+    ptr = hnp.ctypes.data_as(C.POINTER(C.c_double))
+    for _ in range(ke):
+        dg._lib.check(lib.dgx_rk3_step_host(cmx._h, ptr, float(dt), 1))
+    t_e2e = allreduce_max(time.perf_counter() - t0, ws)
+    v_e2e = dof * 3 * ke * ws / t_e2e
+
+    peak, peak_kind = hbm_peak()
+    t_launch = t_mx / (3 * args.steps)
+    achieved = ALGO_BYTES_PER_ELEM_STAGE * ne / t_launch / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_kind": peak_kind,
+            "traffic": None if NCU_TRAFFIC_BYTES_PER_ELEM is None else NCU_TRAFFIC_BYTES_PER_ELEM * ne,
+            "kernel": "dgx::element_kernel<3,float,false> (mixed stage)",
+            "algorithmic_bytes_per_launch": ALGO_BYTES_PER_ELEM_STAGE * ne, "launch_ms": t_launch * 1e3}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline and args.cells == N_CELLS:
+        w = OracleWorkload(1, args.seed)
+        rate, secs = w.run(args.cpu_steps)
+        cpu = {"value": rate, "unit": "DOF*stages/s", "cores": 1, "kind": "port",
+               "sample": f"{args.cpu_steps} SSP-RK3 steps of the full 512x512x2 p=3 mesh "
+                         f"({secs:.1f} s), FP64 oracle restatement of dgfem's single-threaded path"}
+
+    if rank == 0:
+        line = {"metric": "DOF*RK-stages/s", "value": v_mx, "unit": "DOF*stages/s", "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_mx / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 flux/contractions + f64 geometry, mass inverse, RK3 state",
+                "data": "synthetic",
+                "config": {"workload": f"euler_vortex_{args.cells}x{args.cells}x2_p3_dubiner", "elements": ne, "order": ORDER,
+                           "dof": dof, "dt": dt, "cfl": CFL, "l2": "inputs larger than L2 (168 MB state "
+                           "+ two 168 MB stage buffers per context)", "parallelism": f"replicas x{ws}"},
+                "fp64": {"value": v_64, "ms_per_step": 1e3 * t_64 / k64, "steps": k64},
+                "mixed_vs_fp64": v_mx / v_64,
+                "accuracy": acc,
+                "adjoint_forward_ratio": None,
+                "e2e": {"value": v_e2e, "unit": "DOF*stages/s", "h2d_bytes_per_step": dof * 8,
+                        "d2h_bytes_per_step": dof * 8, "steps": ke},
+                "gpu_launches": 3 * args.steps,
+                "roofline": roof, "clocks": clocks, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -18,7 +18,7 @@ OUT = HERE / "libdgx.so"
 OBJ = HERE / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["dgx_host.cpp", "dgx_kernels_fp64.cu", "dgx_kernels_mixed.cu", "dgx_misc.cu"]
-HEADERS = ["dgx_internal.h", "dg_element.cuh", "quad_tables.inc"]
+HEADERS = ["dgx_internal.h", "dg_physics.cuh", "dg_element.cuh", "dg_stage.cuh", "quad_tables.inc"]
 
 
 def nvcc():

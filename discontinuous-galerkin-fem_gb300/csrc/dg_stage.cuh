@@ -1,0 +1,384 @@
+// Mixed-precision SSP-RK3 stage kernel.
+//
+// Same discretisation as the FP64 element kernel (dg_element.cuh): volume flux
+// integral, three faces with the Rusanov flux (plus the viscous terms for
+// Navier-Stokes), M^-1 and the stage combination, one thread per element.  Here:
+//  * arithmetic is FP32 and the stage state is uhi + d (StageArgs, dgx_internal.h);
+//  * M_ref^-1 is folded into the lift operators (precomputed in FP64, rounded once);
+//  * the volume, face and face-point loops are fully unrolled, so every operator of
+//    the element's own faces is an immediate constant-bank operand;
+//  * a neighbour's face operators depend on which of its faces is shared, a per-thread
+//    value; they sit in shared memory as [face][basis][point] rows read as 16-byte
+//    vectors.  Lower and upper triangles of a structured mesh share faces in a fixed
+//    pattern, so threads are mapped to elements as (even elements, odd elements): the
+//    neighbour face is then the same across a warp and the reads are broadcasts;
+//  * a neighbour's traces at all face points are formed in one pass over its
+//    coefficients (shared memory inside the tile, L1/L2 outside).
+#pragma once
+
+#include "dg_element.cuh"
+
+namespace dgx {
+
+template <int P>
+struct NbrOps {  // neighbour-face operators, [face][basis][point] with the point axis padded to 4
+    static constexpr int NP = n_basis(P), NFQ = P + 1, NFQP = (NFQ + 3) & ~3;
+    float phi[3][NP][NFQP];
+    float dr[3][NP][NFQP];
+    float ds[3][NP][NFQP];
+};
+
+template <int P, bool VISC>
+struct SArgs {
+    StageArgs s;
+    Ops<P, float> o;
+    LiftOps<P, float> l;
+    NbrOps<P> nb;
+};
+
+template <int P>
+inline void fill_nbr_ops(const OpsHost& h, NbrOps<P>& n) {
+    constexpr int NP = n_basis(P), NFQ = P + 1, NFQP = NbrOps<P>::NFQP;
+    for (int f = 0; f < 3; ++f)
+        for (int i = 0; i < NP; ++i)
+            for (int k = 0; k < NFQP; ++k) {
+                n.phi[f][i][k] = k < NFQ ? (float)h.phif[f][k][i] : 0.0f;
+                n.dr[f][i][k] = k < NFQ ? (float)h.drf[f][k][i] : 0.0f;
+                n.ds[f][i][k] = k < NFQ ? (float)h.dsf[f][k][i] : 0.0f;
+            }
+}
+
+// thread t of a 128-thread CTA works on local element el(t) = 2 (t mod 64) + t / 64;
+// local element el lives in shared-memory row row(el) = (el mod 2) * 64 + el / 2 = t.
+__device__ __forceinline__ int stage_row(int el) { return (el & 1) * (TILE / 2) + (el >> 1); }
+__device__ __forceinline__ int stage_elem(int t) { return 2 * (t & (TILE / 2 - 1)) + t / (TILE / 2); }
+
+template <int P, bool VISC>
+__global__ void __launch_bounds__(TILE) stage_kernel(const __grid_constant__ SArgs<P, VISC> ka) {
+    constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1, NB = NP * NV, STR = NB + 1, NB4 = NB / 4;
+    constexpr int NFQP = NbrOps<P>::NFQP;
+    const StageArgs& s = ka.s;
+    const Ops<P, float>& o = ka.o;
+    const LiftOps<P, float>& L = ka.l;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* sOp = reinterpret_cast<float*>(smem_raw);                 // NbrOps, 16-byte rows
+    constexpr int OPF = (VISC ? 3 : 1) * 3 * NP * NFQP;
+    float* sU = sOp + OPF;                                           // [TILE][STR]
+
+    const int e0 = blockIdx.x * TILE;
+    const int nloc = min(TILE, s.ne - e0);
+    const int tl = threadIdx.x;
+    const int el = stage_elem(tl);
+    const bool active = el < nloc;
+    const int e = e0 + el;
+
+    {   // operators for neighbour traces
+        const float* src = &ka.nb.phi[0][0][0];
+        for (int k = tl; k < OPF; k += TILE) sOp[k] = src[k];
+    }
+    {   // stage state of the tile: uhi + d, 16-byte loads of one contiguous run
+        const float4* uh = reinterpret_cast<const float4*>(s.uhi + (size_t)e0 * NB);
+        const float4* dd = s.din ? reinterpret_cast<const float4*>(s.din + (size_t)e0 * NB) : nullptr;
+        for (int g = tl; g < nloc * NB4; g += TILE) {
+            float4 a = __ldg(uh + g);
+            if (dd) {
+                const float4 b = __ldg(dd + g);
+                a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w;
+            }
+            const int le = g / NB4, k = 4 * (g - le * NB4);
+            float* r = sU + stage_row(le) * STR + k;
+            r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+        }
+    }
+    __syncthreads();
+
+    float R[NP][NV];
+#pragma unroll
+    for (int i = 0; i < NP; ++i)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) R[i][v] = 0.0f;
+
+    if (active) {
+        const ElemGeomF G = s.geom[e];
+        const float A00 = G.A[0], A01 = G.A[1], A10 = G.A[2], A11 = G.A[3];
+        const float gamma = s.gamma, mu = s.mu, kappa = s.kappa;
+        const float* Ue = sU + tl * STR;
+
+        // ---------------- volume (EulerWeakFormulation::volume_residual :72-115,
+        //                  NavierStokesWeakFormulation::viscous_volume_residual :100-140)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            float U[4] = {0.f, 0.f, 0.f, 0.f};
+            float gr[4] = {0.f, 0.f, 0.f, 0.f}, gs[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+#pragma unroll
+                for (int v = 0; v < NV; ++v) {
+                    const float c = Ue[i * NV + v];
+                    U[v] += o.phi[q][i] * c;
+                    if (VISC) {
+                        gr[v] += o.dr[q][i] * c;
+                        gs[v] += o.ds[q][i] * c;
+                    }
+                }
+            }
+            float F[4], Gf[4], u, vv, pp, ri;
+            euler_flux<float>(U, gamma - 1.0f, F, Gf, u, vv, pp, ri);
+            if (VISC) {
+                float gx[4], gy[4], Fv[4], Gv[4];
+#pragma unroll
+                for (int v = 0; v < NV; ++v) {
+                    gx[v] = A00 * gr[v] + A01 * gs[v];
+                    gy[v] = A10 * gr[v] + A11 * gs[v];
+                }
+                viscous_flux<float>(U, gx, gy, gamma, mu, kappa, Fv, Gv);
+#pragma unroll
+                for (int v = 0; v < NV; ++v) {
+                    F[v] -= Fv[v];
+                    Gf[v] -= Gv[v];
+                }
+            }
+            float Fr[4], Fs[4];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                Fr[v] = o.wq[q] * (A00 * F[v] + A10 * Gf[v]);
+                Fs[v] = o.wq[q] * (A01 * F[v] + A11 * Gf[v]);
+            }
+#pragma unroll
+            for (int i = 0; i < NP; ++i)
+#pragma unroll
+                for (int v = 0; v < NV; ++v) R[i][v] += L.pr[q][i] * Fr[v] + L.ps[q][i] * Fs[v];
+        }
+
+        // ---------------- faces (interior_face_residual :117-175, boundary_face_residual
+        //                  :177-250 and the viscous counterparts, NS :142-273)
+        const ElemConn C = s.conn[e];
+        const float inv_j = __frcp_rn(G.detJ);
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            const int nb = C.nbr[f];
+            if (nb == NBR_SKIP) continue;
+            const int fl = (C.flags >> (4 * f)) & 15;
+            const int nf = fl & 3;
+            const bool rev = (fl >> 2) & 1;
+            const float sideL = ((fl >> 3) & 1) ? 1.0f : -1.0f;
+            const float nx = G.n[f][0], ny = G.n[f][1], hF = G.h[f];
+            // neighbour traces at its own points k, then reordered to this face's points
+            float Un[NFQ][4], Nr[VISC ? NFQ : 1][4], Ns[VISC ? NFQ : 1][4];
+#pragma unroll
+            for (int k = 0; k < NFQ; ++k)
+#pragma unroll
+                for (int v = 0; v < NV; ++v) {
+                    Un[k][v] = 0.f;
+                    if (VISC) { Nr[k][v] = 0.f; Ns[k][v] = 0.f; }
+                }
+            BCSlot bc;
+            bc.type = -1;
+            float B00 = 0.f, B01 = 0.f, B10 = 0.f, B11 = 0.f;
+            if (nb >= 0) {
+                const float* rowp = nullptr;
+                if (nb >= e0 && nb < e0 + nloc) rowp = sU + stage_row(nb - e0) * STR;
+                const float* op = sOp + nf * NP * NFQP;
+#pragma unroll
+                for (int i = 0; i < NP; ++i) {
+                    float c[4];
+                    if (rowp) {
+#pragma unroll
+                        for (int v = 0; v < NV; ++v) c[v] = rowp[i * NV + v];
+                    } else {
+                        load_row_f32<NB>(s.uhi, s.din, nb, i, c);
+                    }
+                    float w[NFQP];
+#pragma unroll
+                    for (int k4 = 0; k4 < NFQP; k4 += 4) {
+                        const float4 t = *reinterpret_cast<const float4*>(op + i * NFQP + k4);
+                        w[k4] = t.x; w[k4 + 1] = t.y; w[k4 + 2] = t.z; w[k4 + 3] = t.w;
+                    }
+#pragma unroll
+                    for (int k = 0; k < NFQ; ++k)
+#pragma unroll
+                        for (int v = 0; v < NV; ++v) Un[k][v] += w[k] * c[v];
+                    if (VISC) {
+                        const float* opr = op + 3 * NP * NFQP;
+                        const float* ops = op + 6 * NP * NFQP;
+#pragma unroll
+                        for (int k4 = 0; k4 < NFQP; k4 += 4) {
+                            const float4 t = *reinterpret_cast<const float4*>(opr + i * NFQP + k4);
+                            w[k4] = t.x; w[k4 + 1] = t.y; w[k4 + 2] = t.z; w[k4 + 3] = t.w;
+                        }
+#pragma unroll
+                        for (int k = 0; k < NFQ; ++k)
+#pragma unroll
+                            for (int v = 0; v < NV; ++v) Nr[k][v] += w[k] * c[v];
+#pragma unroll
+                        for (int k4 = 0; k4 < NFQP; k4 += 4) {
+                            const float4 t = *reinterpret_cast<const float4*>(ops + i * NFQP + k4);
+                            w[k4] = t.x; w[k4 + 1] = t.y; w[k4 + 2] = t.z; w[k4 + 3] = t.w;
+                        }
+#pragma unroll
+                        for (int k = 0; k < NFQ; ++k)
+#pragma unroll
+                            for (int v = 0; v < NV; ++v) Ns[k][v] += w[k] * c[v];
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < NFQ / 2; ++j)
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) {
+                        const float a = Un[j][v], b = Un[NFQ - 1 - j][v];
+                        Un[j][v] = rev ? b : a;
+                        Un[NFQ - 1 - j][v] = rev ? a : b;
+                        if (VISC) {
+                            const float c = Nr[j][v], d = Nr[NFQ - 1 - j][v];
+                            Nr[j][v] = rev ? d : c;
+                            Nr[NFQ - 1 - j][v] = rev ? c : d;
+                            const float x = Ns[j][v], y = Ns[NFQ - 1 - j][v];
+                            Ns[j][v] = rev ? y : x;
+                            Ns[NFQ - 1 - j][v] = rev ? x : y;
+                        }
+                    }
+                if (VISC) {
+                    const ElemGeomF& GN = s.geom[nb];
+                    B00 = GN.A[0]; B01 = GN.A[1]; B10 = GN.A[2]; B11 = GN.A[3];
+                }
+            } else {
+                bc = s.bc[-1 - nb];
+            }
+            const float sigma = VISC ? s.sigma0 * mu * float((P + 1) * (P + 1)) / fmaxf(hF, 1e-12f) : 0.f;
+#pragma unroll
+            for (int j = 0; j < NFQ; ++j) {
+                float Uo[4] = {0.f, 0.f, 0.f, 0.f};
+                float gr[4] = {0.f, 0.f, 0.f, 0.f}, gs[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                for (int i = 0; i < NP; ++i)
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) {
+                        const float c = Ue[i * NV + v];
+                        Uo[v] += o.phif[f][j][i] * c;
+                        if (VISC) {
+                            gr[v] += o.drf[f][j][i] * c;
+                            gs[v] += o.dsf[f][j][i] * c;
+                        }
+                    }
+                float H[4];
+                if (nb >= 0) {
+                    rusanov<float>(Uo, Un[j], nx, ny, gamma, H);
+                } else if (bc.type == DGX_BC_FAR_FIELD || bc.type == DGX_BC_SLIP_WALL ||
+                           bc.type == DGX_BC_NO_SLIP_WALL) {
+                    float Ub[4];
+                    if (bc.type == DGX_BC_FAR_FIELD) {
+#pragma unroll
+                        for (int v = 0; v < 4; ++v) Ub[v] = (float)bc.value[v];
+                    } else if (bc.type == DGX_BC_SLIP_WALL) {
+                        const float rr = __frcp_rn(Uo[0]);
+                        const float u = Uo[1] * rr, vv = Uo[2] * rr;
+                        const float p = (gamma - 1.f) * (Uo[3] - 0.5f * Uo[0] * (u * u + vv * vv));
+                        const float un = u * nx + vv * ny;
+                        const float W[4] = {Uo[0], (u - un * nx) - un * nx, (vv - un * ny) - un * ny, p};
+                        p2c<float>(W, gamma, Ub);
+                    } else {
+                        const float W[4] = {(float)bc.value[0], (float)bc.value[1], (float)bc.value[2],
+                                            (float)bc.value[3]};
+                        p2c<float>(W, gamma, Ub);
+                    }
+                    rusanov<float>(Uo, Ub, nx, ny, gamma, H);
+                } else {
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) H[v] = 0.f;
+                }
+                if (VISC) {
+                    float gx[4], gy[4], Fv[4], Gv[4];
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) {
+                        gx[v] = A00 * gr[v] + A01 * gs[v];
+                        gy[v] = A10 * gr[v] + A11 * gs[v];
+                    }
+                    viscous_flux<float>(Uo, gx, gy, gamma, mu, kappa, Fv, Gv);
+                    if (nb >= 0) {
+                        float hx[4], hy[4], Fn2[4], Gn2[4];
+#pragma unroll
+                        for (int v = 0; v < NV; ++v) {
+                            hx[v] = B00 * Nr[j][v] + B01 * Ns[j][v];
+                            hy[v] = B10 * Nr[j][v] + B11 * Ns[j][v];
+                        }
+                        viscous_flux<float>(Un[j], hx, hy, gamma, mu, kappa, Fn2, Gn2);
+#pragma unroll
+                        for (int v = 0; v < NV; ++v) {
+                            const float jmp = 0.5f * ((Fv[v] * nx + Gv[v] * ny) - (Fn2[v] * nx + Gn2[v] * ny));
+                            H[v] += sideL * jmp - sigma * (Un[j][v] - Uo[v]);
+                        }
+                    } else if (bc.type >= 0) {
+                        float Ub[4] = {Uo[0], Uo[1], Uo[2], Uo[3]};
+                        if (bc.type == DGX_BC_NO_SLIP_WALL) {
+                            const float W[4] = {(float)bc.value[0], (float)bc.value[1], (float)bc.value[2],
+                                                (float)bc.value[3]};
+                            p2c<float>(W, gamma, Ub);
+                        } else {
+#pragma unroll
+                            for (int v = 0; v < 4; ++v) Ub[v] = (float)bc.value[v];
+                        }
+#pragma unroll
+                        for (int v = 0; v < NV; ++v) H[v] += (Fv[v] * nx + Gv[v] * ny) - sigma * (Ub[v] - Uo[v]);
+                    }
+                }
+                const float w = o.wf[j] * hF * 0.5f * inv_j;
+#pragma unroll
+                for (int i = 0; i < NP; ++i) {
+                    const float sc = w * L.pf[f][j][i];
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) R[i][v] -= sc * H[v];
+                }
+            }
+        }
+    }
+    __syncthreads();  // every neighbour read of sU is done
+    if (active) {
+#pragma unroll
+        for (int i = 0; i < NP; ++i)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) sU[tl * STR + i * NV + v] = R[i][v];
+    }
+    __syncthreads();
+    const size_t base = (size_t)e0 * NB;
+    for (int g = tl; g < nloc * NB; g += TILE) {
+        const int le = g / NB;
+        const float du = sU[stage_row(le) * STR + (g - le * NB)];
+        if (s.stage == 1) {
+            s.dout[base + g] = s.dt * du;
+        } else if (s.stage == 2) {
+            s.dout[base + g] = 0.25f * (__ldg(s.din + base + g) + s.dt * du);
+        } else {
+            const float delta = (2.0f / 3.0f) * (__ldg(s.din + base + g) + s.dt * du);
+            const double r = s.u64[base + g] + (double)delta;
+            s.u64[base + g] = r;
+            s.uhi_out[base + g] = (float)r;
+        }
+    }
+}
+
+template <int P, bool VISC>
+inline size_t stage_smem_bytes() {
+    constexpr int OPF = (VISC ? 3 : 1) * 3 * n_basis(P) * NbrOps<P>::NFQP;
+    return (size_t)(OPF + TILE * (n_basis(P) * NV + 1)) * sizeof(float);
+}
+
+template <int P, typename T, bool VISC>
+inline int configure_stage_t() {
+    return cudaFuncSetAttribute(stage_kernel<P, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)stage_smem_bytes<P, VISC>()) == cudaSuccess ? 0 : -1;
+}
+
+template <int P, typename T, bool VISC>
+inline int launch_stage_t(const StageArgs& a, const OpsHost& oh, cudaStream_t st) {
+    SArgs<P, VISC> ka;
+    ka.s = a;
+    fill_ops<P, float>(oh, ka.o);
+    fill_lift<P, float>(oh, ka.l);
+    fill_nbr_ops<P>(oh, ka.nb);
+    const int grid = (a.ne + TILE - 1) / TILE;
+    if (grid == 0) return 0;
+    stage_kernel<P, VISC><<<grid, TILE, stage_smem_bytes<P, VISC>(), st>>>(ka);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace dgx

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <map>
 #include <string>
@@ -524,6 +525,7 @@ struct dgx_ctx {
     OpsHost ops{};
     std::vector<double> xq;  // physical volume points
     ElemGeom* d_geom = nullptr;
+    ElemGeomF* d_geomf = nullptr;  // FP32 rounding of d_geom (mixed precision)
     ElemConn* d_conn = nullptr;
     BCSlot* d_bc = nullptr;
     double* d_u1 = nullptr;
@@ -532,8 +534,13 @@ struct dgx_ctx {
     double* d_hr = nullptr;
     double* d_mon = nullptr;  // [4]
     int* d_flag = nullptr;
+    float* d_uhi[2] = {nullptr, nullptr};  // FP32 copies of u^n (mixed RK3), ping-ponged
+    float* d_d1 = nullptr;                  // FP32 stage increments (mixed RK3)
+    float* d_d2 = nullptr;
+    int minv_diag = 0;
     cudaStream_t cap = nullptr;  // capture stream
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph = nullptr;   // one step (FP64) or two steps (mixed)
+    cudaGraphExec_t graph1 = nullptr;  // mixed: one step
     const double* graph_u = nullptr;
     double graph_dt = 0.0;
 };
@@ -549,6 +556,7 @@ static StepArgs base_args(const dgx_ctx* c) {
     a.prandtl = c->prm.prandtl;
     a.sigma0 = c->prm.sigma0;
     a.order = c->prm.order;
+    a.minv_diag = c->minv_diag;
     return a;
 }
 
@@ -565,8 +573,14 @@ static void free_ctx(dgx_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->graph) cudaGraphExecDestroy(c->graph);
+    if (c->graph1) cudaGraphExecDestroy(c->graph1);
+    cudaFree(c->d_uhi[0]);
+    cudaFree(c->d_uhi[1]);
+    cudaFree(c->d_d1);
+    cudaFree(c->d_d2);
     if (c->cap) cudaStreamDestroy(c->cap);
     cudaFree(c->d_geom);
+    cudaFree(c->d_geomf);
     cudaFree(c->d_conn);
     cudaFree(c->d_bc);
     cudaFree(c->d_u1);
@@ -621,6 +635,13 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
     if (make_ops(p->order, p->basis, c->ops)) {
         delete c;
         return fail(DGX_ERR_RUNTIME, "could not build reference operators");
+    }
+    {   // Dubiner: M_ref is diagonal up to round-off, so M_ref^-1 is applied as a scaling
+        double dmax = 0.0, omax = 0.0;
+        for (int i = 0; i < c->ops.np; ++i)
+            for (int j = 0; j < c->ops.np; ++j)
+                (i == j ? dmax : omax) = std::max(i == j ? dmax : omax, std::fabs(c->ops.minv[i][j]));
+        c->minv_diag = omax <= 1e-12 * dmax ? 1 : 0;
     }
     const int ne = m->ne();
     c->ne = ne;
@@ -736,10 +757,37 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
     if (!alloc((void**)&c->d_geom, sizeof(ElemGeom) * ne) || !alloc((void**)&c->d_conn, sizeof(ElemConn) * ne) ||
         !alloc((void**)&c->d_bc, sizeof(BCSlot) * slots.size()) || !alloc((void**)&c->d_u1, sb) ||
         !alloc((void**)&c->d_u2, sb) || !alloc((void**)&c->d_mon, 4 * sizeof(double)) ||
-        !alloc((void**)&c->d_flag, sizeof(int))) {
+        !alloc((void**)&c->d_flag, sizeof(int)) ||
+        (p->precision == DGX_MIXED &&
+         (!alloc((void**)&c->d_uhi[0], c->nstate * sizeof(float)) ||
+          !alloc((void**)&c->d_uhi[1], c->nstate * sizeof(float)) ||
+          !alloc((void**)&c->d_d1, c->nstate * sizeof(float)) ||
+          !alloc((void**)&c->d_d2, c->nstate * sizeof(float))))) {
         cudaGetLastError();
         free_ctx(c);
         return fail(DGX_ERR_CUDA, "cudaMalloc failed for the solver state");
+    }
+    if (p->precision == DGX_MIXED) {
+        std::vector<ElemGeomF> gf(ne);
+        for (int e = 0; e < ne; ++e) {
+            const ElemGeom& g = geom[e];
+            ElemGeomF& h = gf[e];
+            for (int k = 0; k < 4; ++k) h.A[k] = (float)g.A[k];
+            h.detJ = (float)g.detJ;
+            for (int f = 0; f < 3; ++f) {
+                h.h[f] = (float)g.h[f];
+                h.n[f][0] = (float)g.n[f][0];
+                h.n[f][1] = (float)g.n[f][1];
+            }
+            h.hmin = (float)g.pad[0];
+            h.pad = 0.0f;
+        }
+        if (!alloc((void**)&c->d_geomf, sizeof(ElemGeomF) * ne) ||
+            cudaMemcpy(c->d_geomf, gf.data(), sizeof(ElemGeomF) * ne, cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaGetLastError();
+            free_ctx(c);
+            return fail(DGX_ERR_CUDA, "device upload failed (FP32 geometry)");
+        }
     }
     if (cudaMemcpy(c->d_geom, geom.data(), sizeof(ElemGeom) * ne, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(c->d_conn, conn.data(), sizeof(ElemConn) * ne, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -805,31 +853,83 @@ static int enqueue_rk3(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
     return launch(c, a, s);
 }
 
+// Mixed precision: the three stages of one step, reading the FP32 copy uhi[src] of u^n
+// and writing the FP32 copy of u^{n+1} to uhi[1 - src] (see StageArgs).
+static int enqueue_rk3_mixed(dgx_ctx* c, double* u, double dt, int src, cudaStream_t s) {
+    StageArgs a{};
+    a.ne = c->ne;
+    a.geom = c->d_geomf;
+    a.conn = c->d_conn;
+    a.bc = c->d_bc;
+    a.dt = (float)dt;
+    a.gamma = (float)c->prm.gamma;
+    a.mu = (float)c->prm.mu;
+    a.kappa = c->prm.physics == DGX_NAVIER_STOKES
+                  ? (float)(c->prm.mu * c->prm.gamma / (c->prm.prandtl * (c->prm.gamma - 1.0)))
+                  : 0.0f;
+    a.sigma0 = (float)c->prm.sigma0;
+    a.uhi = c->d_uhi[src];
+    a.u64 = u;
+    a.uhi_out = c->d_uhi[1 - src];
+    const bool visc = c->prm.physics == DGX_NAVIER_STOKES;
+    const StageArgs s1 = [&] { StageArgs t = a; t.stage = 1; t.din = nullptr; t.dout = c->d_d1; return t; }();
+    const StageArgs s2 = [&] { StageArgs t = a; t.stage = 2; t.din = c->d_d1; t.dout = c->d_d2; return t; }();
+    const StageArgs s3 = [&] { StageArgs t = a; t.stage = 3; t.din = c->d_d2; t.dout = nullptr; return t; }();
+    for (const StageArgs* t : {&s1, &s2, &s3})
+        if (launch_stage_mixed(c->prm.order, visc, *t, c->ops, s))
+            return fail(DGX_ERR_CUDA, std::string("stage kernel launch failed: ") +
+                                          cudaGetErrorString(cudaGetLastError()));
+    return DGX_OK;
+}
+
+static int capture(dgx_ctx* c, cudaGraphExec_t* out, const std::function<int(cudaStream_t)>& body) {
+    cudaGraph_t g;
+    CUDA_OK(cudaStreamBeginCapture(c->cap, cudaStreamCaptureModeThreadLocal));
+    const int rc = body(c->cap);
+    const cudaError_t ec = cudaStreamEndCapture(c->cap, &g);
+    if (rc) return rc;
+    if (ec != cudaSuccess) return fail(DGX_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
+    const cudaError_t ei = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        *out = nullptr;
+        return fail(DGX_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+    }
+    return DGX_OK;
+}
+
 extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void* stream) {
     if (!c || (c->ne && !u) || n_steps < 0) return fail(DGX_ERR_INVALID, "dgx_rk3_step: bad argument");
     if (c->ne == 0 || n_steps == 0) return DGX_OK;
     cudaStream_t s = (cudaStream_t)stream;
+    const bool mixed = c->prm.precision == DGX_MIXED;
     if (!c->graph || c->graph_u != u || c->graph_dt != dt) {
-        if (c->graph) {
-            cudaGraphExecDestroy(c->graph);
-            c->graph = nullptr;
+        if (c->graph) cudaGraphExecDestroy(c->graph);
+        if (c->graph1) cudaGraphExecDestroy(c->graph1);
+        c->graph = c->graph1 = nullptr;
+        int rc;
+        if (mixed) {
+            // two steps per replay: uhi[0] -> uhi[1] -> uhi[0]
+            rc = capture(c, &c->graph, [&](cudaStream_t cs) {
+                int r = enqueue_rk3_mixed(c, u, dt, 0, cs);
+                return r ? r : enqueue_rk3_mixed(c, u, dt, 1, cs);
+            });
+            if (!rc) rc = capture(c, &c->graph1, [&](cudaStream_t cs) { return enqueue_rk3_mixed(c, u, dt, 0, cs); });
+        } else {
+            rc = capture(c, &c->graph, [&](cudaStream_t cs) { return enqueue_rk3(c, u, dt, cs); });
         }
-        cudaGraph_t g;
-        CUDA_OK(cudaStreamBeginCapture(c->cap, cudaStreamCaptureModeThreadLocal));
-        const int rc = enqueue_rk3(c, u, dt, c->cap);
-        const cudaError_t ec = cudaStreamEndCapture(c->cap, &g);
         if (rc) return rc;
-        if (ec != cudaSuccess) return fail(DGX_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
-        const cudaError_t ei = cudaGraphInstantiate(&c->graph, g, 0);
-        cudaGraphDestroy(g);
-        if (ei != cudaSuccess) {
-            c->graph = nullptr;
-            return fail(DGX_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
-        }
         c->graph_u = u;
         c->graph_dt = dt;
     }
-    for (int i = 0; i < n_steps; ++i) CUDA_OK(cudaGraphLaunch(c->graph, s));
+    if (!mixed) {
+        for (int i = 0; i < n_steps; ++i) CUDA_OK(cudaGraphLaunch(c->graph, s));
+        return DGX_OK;
+    }
+    // the FP32 copy of the caller's state, then pairs of steps and a last single step
+    if (launch_f64_to_f32(c->nstate, u, c->d_uhi[0], s)) return fail(DGX_ERR_CUDA, "conversion launch failed");
+    for (int i = 0; i + 1 < n_steps; i += 2) CUDA_OK(cudaGraphLaunch(c->graph, s));
+    if (n_steps & 1) CUDA_OK(cudaGraphLaunch(c->graph1, s));
     return DGX_OK;
 }
 

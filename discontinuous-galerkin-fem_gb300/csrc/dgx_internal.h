@@ -27,6 +27,19 @@ struct alignas(128) ElemGeom {
 };
 static_assert(sizeof(ElemGeom) == 128, "ElemGeom must stay 128 B");
 
+// The same record rounded once to FP32 (64 B) for the mixed-precision stage kernel,
+// whose arithmetic is FP32: it holds exactly the values that kernel would obtain by
+// converting ElemGeom on load.
+struct alignas(64) ElemGeomF {
+    float A[4];
+    float detJ;
+    float h[3];
+    float n[3][2];
+    float hmin;
+    float pad;
+};
+static_assert(sizeof(ElemGeomF) == 64, "ElemGeomF must stay 64 B");
+
 // Per-element face connectivity, 16 B.
 //   nbr[f] >= 0       interior face: neighbour element
 //   nbr[f] = -1 - s   boundary face with boundary-condition slot s
@@ -109,14 +122,38 @@ struct StepArgs {
     double dt, a, b;       // MODE_STAGE: out = a*un + b*(u + dt*du); a == 0: out = u + dt*du
     double gamma, mu, prandtl, sigma0;
     int order;
+    int minv_diag;         // 1 when M_ref^-1 is diagonal (Dubiner): scale instead of a dense product
     int* status;           // device flag: bit 0 set when a non-finite value was produced
 };
+
+// Arguments of the mixed-precision SSP-RK3 stage kernel.  The stage state is uhi + d,
+// uhi the FP32 rounding of u^n and d an FP32 increment:
+//   stage 1: d1 = dt L(u^n)
+//   stage 2: d2 = 1/4 (d1 + dt L(u^n + d1))
+//   stage 3: u^{n+1} = u^n + 2/3 (d2 + dt L(u^n + d2))      (this add in FP64)
+// which is SSP_RK::step_rk3 (include/dgfem/solver/time_stepping.hpp:39-55) written in
+// increments: u1 = u^n + d1, u2 = 3/4 u^n + 1/4 (u1 + dt L(u1)) = u^n + d2, and
+// u^{n+1} = 1/3 u^n + 2/3 (u2 + dt L(u2)) = u^n + 2/3 (d2 + dt L(u2)).
+struct StageArgs {
+    int ne, stage;
+    const float* uhi;   // FP32 u^n (neighbours read it)
+    const float* din;   // increment of the stage state (null in stage 1)
+    float* dout;        // next increment (stages 1, 2)
+    double* u64;        // FP64 state, updated in place in stage 3
+    float* uhi_out;     // FP32 rounding of u^{n+1} (stage 3; not the buffer uhi points to)
+    const ElemGeomF* geom;
+    const ElemConn* conn;
+    const BCSlot* bc;
+    float dt, gamma, mu, kappa, sigma0;
+};
+
 
 // Launchers (one translation unit per precision).
 int launch_element_fp64(int p, bool viscous, const StepArgs& a, const OpsHost& ops, cudaStream_t s);
 int launch_element_mixed(int p, bool viscous, const StepArgs& a, const OpsHost& ops, cudaStream_t s);
 int configure_element_fp64(int p, bool viscous);
 int configure_element_mixed(int p, bool viscous);
+int launch_stage_mixed(int p, bool viscous, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
 
 // Small FP64 utility kernels (dgx_misc.cu).
 int launch_mass_inv(int ne, int p, const OpsHost& ops, const ElemGeom* geom, const double* in,
@@ -126,5 +163,6 @@ int launch_project(int ne, int p, const OpsHost& ops, const ElemGeom* geom, cons
 int launch_monitor(int ne, int p, const OpsHost& ops, const ElemGeom* geom, const double* u,
                    double dt, double gamma, double* d_out /*[4]*/, cudaStream_t s);
 int launch_has_nan(size_t n, const double* u, int* d_flag, cudaStream_t s);
+int launch_f64_to_f32(size_t n, const double* in, float* out, cudaStream_t s);
 
 }  // namespace dgx

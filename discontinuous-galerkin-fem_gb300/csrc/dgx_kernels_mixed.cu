@@ -1,6 +1,6 @@
 // Mixed-precision element kernels: FP32 flux and contraction arithmetic, FP64 geometry,
 // FP64 inverse mass matrix and FP64 RK3 state accumulation.
-#include "dg_element.cuh"
+#include "dg_stage.cuh"
 
 namespace dgx {
 
@@ -10,7 +10,20 @@ int launch_element_mixed(int p, bool viscous, const StepArgs& a, const OpsHost& 
 #undef ARGS
 }
 
+int launch_stage_mixed(int p, bool viscous, const StageArgs& a, const OpsHost& ops, cudaStream_t s) {
+#define ARGS (a, ops, s)
+    DGX_ELEMENT_DISPATCH(launch_stage_t, float)
+#undef ARGS
+}
+
+static int configure_stage(int p, bool viscous) {
+#define ARGS ()
+    DGX_ELEMENT_DISPATCH(configure_stage_t, float)
+#undef ARGS
+}
+
 int configure_element_mixed(int p, bool viscous) {
+    if (configure_stage(p, viscous)) return -1;
 #define ARGS ()
     DGX_ELEMENT_DISPATCH(configure_element_t, float)
 #undef ARGS

@@ -152,6 +152,11 @@ __global__ void has_nan_kernel(size_t n, const double* u, int* flag) {
     if (__any_sync(0xffffffffu, nan) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
 }
 
+__global__ void f64_to_f32_kernel(size_t n, const double* in, float* out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+
 #define DGX_DISPATCH_P(p, ...)                                      \
     switch (p) {                                                    \
     case 1: { constexpr int NP = 3, NQ = 3; __VA_ARGS__; break; }   \
@@ -199,6 +204,14 @@ int launch_has_nan(size_t n, const double* u, int* d_flag, cudaStream_t s) {
     size_t blocks = (n + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     has_nan_kernel<<<(unsigned)blocks, 256, 0, s>>>(n, u, d_flag);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_f64_to_f32(size_t n, const double* in, float* out, cudaStream_t s) {
+    if (n == 0) return 0;
+    size_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    f64_to_f32_kernel<<<(unsigned)blocks, 256, 0, s>>>(n, in, out);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

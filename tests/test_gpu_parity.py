@@ -192,3 +192,25 @@ def test_solver_api_runs_and_conserves(dg):
     # mass (Dubiner mode 0 carries the mean): conserved to round-off
     m0 = [f.reshape(128, 6, 4)[:, 0, 0].sum() for f in frames]
     assert abs(m0[-1] - m0[0]) <= 1e-12 * abs(m0[0])
+
+
+@pytest.mark.parametrize("visc", [False, True])
+@pytest.mark.parametrize("order", [2, 3, 4])
+def test_rk3_mixed_precision_vs_oracle(dg, order, visc):
+    """FP32 increments + FP64 accumulation: after 5 steps (one 2-step replay pair and a
+    single step), within 1e-6 relative L2 of the FP64 oracle."""
+    v, e, b = periodic_rectangle(8)
+    om, pm = make_pair(dg, v, e, b, order, O.DUBINER, True)
+    oph, wf = physics(dg, visc, mu=0.01)
+    u0 = vortex_state(om, noise=0.0)
+    dt = 0.02 / om.max_cfl(1.4, u0, 1.0)
+    ref = om.rk3_step(oph, u0, dt, 5)
+    assert np.isfinite(ref).all()
+    ctx = dg.DGContext(pm, dg.DGSpace("triangle", order, "dubiner"), wf, "mixed")
+    ut = torch.tensor(u0, device="cuda")
+    ctx.rk3_step(ut, dt, 3)
+    ctx.rk3_step(ut, dt, 2)
+    err = rel(ut.cpu().numpy(), ref)
+    assert err <= 1e-6, err
+    # the update itself (u^5 - u^0) is accurate to FP32 level
+    assert rel(ut.cpu().numpy() - u0, ref - u0) <= 1e-4
