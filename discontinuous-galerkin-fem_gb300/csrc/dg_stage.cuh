@@ -13,12 +13,19 @@
 //    pattern, so threads are mapped to elements as (even elements, odd elements): the
 //    neighbour face is then the same across a warp and the reads are broadcasts;
 //  * a neighbour's traces at all face points are formed in one pass over its
-//    coefficients (shared memory inside the tile, L1/L2 outside).
+//    coefficients, read through L1 (the tile was just loaded) or L2.
 #pragma once
 
 #include "dg_element.cuh"
 
 namespace dgx {
+
+// Shared-memory row stride (floats) of one element: 16-byte aligned, and stride/4 odd so
+// that eight threads reading their rows with 16-byte loads hit disjoint banks.
+template <int P>
+__host__ __device__ constexpr int stage_stride() {
+    return ((n_basis(P) * NV / 4) & 1) ? n_basis(P) * NV : n_basis(P) * NV + 4;
+}
 
 template <int P>
 struct NbrOps {  // neighbour-face operators, [face][basis][point] with the point axis padded to 4
@@ -53,9 +60,20 @@ inline void fill_nbr_ops(const OpsHost& h, NbrOps<P>& n) {
 __device__ __forceinline__ int stage_row(int el) { return (el & 1) * (TILE / 2) + (el >> 1); }
 __device__ __forceinline__ int stage_elem(int t) { return 2 * (t & (TILE / 2 - 1)) + t / (TILE / 2); }
 
-template <int P, bool VISC>
-__global__ void __launch_bounds__(TILE) stage_kernel(const __grid_constant__ SArgs<P, VISC> ka) {
-    constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1, NB = NP * NV, STR = NB + 1, NB4 = NB / 4;
+// CTAs per SM the register allocation must allow.  Measured on GB300 for p=3 Euler:
+// 4 CTAs (128 registers, 152 B of spills) beats the unconstrained 163 registers / 3 CTAs
+// by 9%.  DGX_STAGE_MIN_BLOCKS overrides it for experiments.
+__host__ __device__ constexpr int stage_min_blocks(int p, bool visc) {
+#ifdef DGX_STAGE_MIN_BLOCKS
+    return DGX_STAGE_MIN_BLOCKS + 0 * p * visc;
+#else
+    return visc ? (p <= 2 ? 3 : 2) : (p <= 3 ? 4 : 3);
+#endif
+}
+
+template <int P, bool VISC, bool BND>
+__global__ void __launch_bounds__(TILE, stage_min_blocks(P, VISC)) stage_kernel(const __grid_constant__ SArgs<P, VISC> ka) {
+    constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1, NB = NP * NV, STR = stage_stride<P>(), NB4 = NB / 4;
     constexpr int NFQP = NbrOps<P>::NFQP;
     const StageArgs& s = ka.s;
     const Ops<P, float>& o = ka.o;
@@ -86,8 +104,7 @@ __global__ void __launch_bounds__(TILE) stage_kernel(const __grid_constant__ SAr
                 a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w;
             }
             const int le = g / NB4, k = 4 * (g - le * NB4);
-            float* r = sU + stage_row(le) * STR + k;
-            r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+            *reinterpret_cast<float4*>(sU + stage_row(le) * STR + k) = a;
         }
     }
     __syncthreads();
@@ -112,13 +129,14 @@ __global__ void __launch_bounds__(TILE) stage_kernel(const __grid_constant__ SAr
             float gr[4] = {0.f, 0.f, 0.f, 0.f}, gs[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
             for (int i = 0; i < NP; ++i) {
+                const float4 c4 = *reinterpret_cast<const float4*>(Ue + i * NV);
+                const float c[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
                 for (int v = 0; v < NV; ++v) {
-                    const float c = Ue[i * NV + v];
-                    U[v] += o.phi[q][i] * c;
+                    U[v] = fmaf(o.phi[q][i], c[v], U[v]);
                     if (VISC) {
-                        gr[v] += o.dr[q][i] * c;
-                        gs[v] += o.ds[q][i] * c;
+                        gr[v] = fmaf(o.dr[q][i], c[v], gr[v]);
+                        gs[v] = fmaf(o.ds[q][i], c[v], gs[v]);
                     }
                 }
             }
@@ -147,7 +165,10 @@ __global__ void __launch_bounds__(TILE) stage_kernel(const __grid_constant__ SAr
 #pragma unroll
             for (int i = 0; i < NP; ++i)
 #pragma unroll
-                for (int v = 0; v < NV; ++v) R[i][v] += L.pr[q][i] * Fr[v] + L.ps[q][i] * Fs[v];
+                for (int v = 0; v < NV; ++v) {
+                    R[i][v] = fmaf(L.pr[q][i], Fr[v], R[i][v]);
+                    R[i][v] = fmaf(L.ps[q][i], Fs[v], R[i][v]);
+                }
         }
 
         // ---------------- faces (interior_face_residual :117-175, boundary_face_residual
@@ -157,7 +178,7 @@ __global__ void __launch_bounds__(TILE) stage_kernel(const __grid_constant__ SAr
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
             const int nb = C.nbr[f];
-            if (nb == NBR_SKIP) continue;
+            if (BND && nb == NBR_SKIP) continue;
             const int fl = (C.flags >> (4 * f)) & 15;
             const int nf = fl & 3;
             const bool rev = (fl >> 2) & 1;
@@ -175,19 +196,12 @@ __global__ void __launch_bounds__(TILE) stage_kernel(const __grid_constant__ SAr
             BCSlot bc;
             bc.type = -1;
             float B00 = 0.f, B01 = 0.f, B10 = 0.f, B11 = 0.f;
-            if (nb >= 0) {
-                const float* rowp = nullptr;
-                if (nb >= e0 && nb < e0 + nloc) rowp = sU + stage_row(nb - e0) * STR;
+            if (!BND || nb >= 0) {
                 const float* op = sOp + nf * NP * NFQP;
 #pragma unroll
                 for (int i = 0; i < NP; ++i) {
                     float c[4];
-                    if (rowp) {
-#pragma unroll
-                        for (int v = 0; v < NV; ++v) c[v] = rowp[i * NV + v];
-                    } else {
-                        load_row_f32<NB>(s.uhi, s.din, nb, i, c);
-                    }
+                    load_row_f32<NB>(s.uhi, s.din, nb, i, c);
                     float w[NFQP];
 #pragma unroll
                     for (int k4 = 0; k4 < NFQP; k4 += 4) {
@@ -197,7 +211,7 @@ __global__ void __launch_bounds__(TILE) stage_kernel(const __grid_constant__ SAr
 #pragma unroll
                     for (int k = 0; k < NFQ; ++k)
 #pragma unroll
-                        for (int v = 0; v < NV; ++v) Un[k][v] += w[k] * c[v];
+                        for (int v = 0; v < NV; ++v) Un[k][v] = fmaf(w[k], c[v], Un[k][v]);
                     if (VISC) {
                         const float* opr = op + 3 * NP * NFQP;
                         const float* ops = op + 6 * NP * NFQP;
@@ -209,7 +223,7 @@ __global__ void __launch_bounds__(TILE) stage_kernel(const __grid_constant__ SAr
 #pragma unroll
                         for (int k = 0; k < NFQ; ++k)
 #pragma unroll
-                            for (int v = 0; v < NV; ++v) Nr[k][v] += w[k] * c[v];
+                            for (int v = 0; v < NV; ++v) Nr[k][v] = fmaf(w[k], c[v], Nr[k][v]);
 #pragma unroll
                         for (int k4 = 0; k4 < NFQP; k4 += 4) {
                             const float4 t = *reinterpret_cast<const float4*>(ops + i * NFQP + k4);
@@ -218,7 +232,7 @@ __global__ void __launch_bounds__(TILE) stage_kernel(const __grid_constant__ SAr
 #pragma unroll
                         for (int k = 0; k < NFQ; ++k)
 #pragma unroll
-                            for (int v = 0; v < NV; ++v) Ns[k][v] += w[k] * c[v];
+                            for (int v = 0; v < NV; ++v) Ns[k][v] = fmaf(w[k], c[v], Ns[k][v]);
                     }
                 }
 #pragma unroll
@@ -250,18 +264,20 @@ __global__ void __launch_bounds__(TILE) stage_kernel(const __grid_constant__ SAr
                 float Uo[4] = {0.f, 0.f, 0.f, 0.f};
                 float gr[4] = {0.f, 0.f, 0.f, 0.f}, gs[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-                for (int i = 0; i < NP; ++i)
+                for (int i = 0; i < NP; ++i) {
+                    const float4 c4 = *reinterpret_cast<const float4*>(Ue + i * NV);
+                    const float c[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
                     for (int v = 0; v < NV; ++v) {
-                        const float c = Ue[i * NV + v];
-                        Uo[v] += o.phif[f][j][i] * c;
+                        Uo[v] = fmaf(o.phif[f][j][i], c[v], Uo[v]);
                         if (VISC) {
-                            gr[v] += o.drf[f][j][i] * c;
-                            gs[v] += o.dsf[f][j][i] * c;
+                            gr[v] = fmaf(o.drf[f][j][i], c[v], gr[v]);
+                            gs[v] = fmaf(o.dsf[f][j][i], c[v], gs[v]);
                         }
                     }
+                }
                 float H[4];
-                if (nb >= 0) {
+                if (!BND || nb >= 0) {
                     rusanov<float>(Uo, Un[j], nx, ny, gamma, H);
                 } else if (bc.type == DGX_BC_FAR_FIELD || bc.type == DGX_BC_SLIP_WALL ||
                            bc.type == DGX_BC_NO_SLIP_WALL) {
@@ -294,7 +310,7 @@ __global__ void __launch_bounds__(TILE) stage_kernel(const __grid_constant__ SAr
                         gy[v] = A10 * gr[v] + A11 * gs[v];
                     }
                     viscous_flux<float>(Uo, gx, gy, gamma, mu, kappa, Fv, Gv);
-                    if (nb >= 0) {
+                    if (!BND || nb >= 0) {
                         float hx[4], hy[4], Fn2[4], Gn2[4];
 #pragma unroll
                         for (int v = 0; v < NV; ++v) {
@@ -326,7 +342,7 @@ __global__ void __launch_bounds__(TILE) stage_kernel(const __grid_constant__ SAr
                 for (int i = 0; i < NP; ++i) {
                     const float sc = w * L.pf[f][j][i];
 #pragma unroll
-                    for (int v = 0; v < NV; ++v) R[i][v] -= sc * H[v];
+                    for (int v = 0; v < NV; ++v) R[i][v] = fmaf(-sc, H[v], R[i][v]);
                 }
             }
         }
@@ -335,8 +351,7 @@ __global__ void __launch_bounds__(TILE) stage_kernel(const __grid_constant__ SAr
     if (active) {
 #pragma unroll
         for (int i = 0; i < NP; ++i)
-#pragma unroll
-            for (int v = 0; v < NV; ++v) sU[tl * STR + i * NV + v] = R[i][v];
+            *reinterpret_cast<float4*>(sU + tl * STR + i * NV) = make_float4(R[i][0], R[i][1], R[i][2], R[i][3]);
     }
     __syncthreads();
     const size_t base = (size_t)e0 * NB;
@@ -359,13 +374,18 @@ __global__ void __launch_bounds__(TILE) stage_kernel(const __grid_constant__ SAr
 template <int P, bool VISC>
 inline size_t stage_smem_bytes() {
     constexpr int OPF = (VISC ? 3 : 1) * 3 * n_basis(P) * NbrOps<P>::NFQP;
-    return (size_t)(OPF + TILE * (n_basis(P) * NV + 1)) * sizeof(float);
+    return (size_t)(OPF + TILE * stage_stride<P>()) * sizeof(float);
 }
 
 template <int P, typename T, bool VISC>
 inline int configure_stage_t() {
-    return cudaFuncSetAttribute(stage_kernel<P, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)stage_smem_bytes<P, VISC>()) == cudaSuccess ? 0 : -1;
+    const int b = (int)stage_smem_bytes<P, VISC>();
+    return cudaFuncSetAttribute(stage_kernel<P, VISC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
+                       cudaSuccess &&
+                   cudaFuncSetAttribute(stage_kernel<P, VISC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        b) == cudaSuccess
+               ? 0
+               : -1;
 }
 
 template <int P, typename T, bool VISC>
@@ -377,7 +397,10 @@ inline int launch_stage_t(const StageArgs& a, const OpsHost& oh, cudaStream_t st
     fill_nbr_ops<P>(oh, ka.nb);
     const int grid = (a.ne + TILE - 1) / TILE;
     if (grid == 0) return 0;
-    stage_kernel<P, VISC><<<grid, TILE, stage_smem_bytes<P, VISC>(), st>>>(ka);
+    if (a.boundary)
+        stage_kernel<P, VISC, true><<<grid, TILE, stage_smem_bytes<P, VISC>(), st>>>(ka);
+    else
+        stage_kernel<P, VISC, false><<<grid, TILE, stage_smem_bytes<P, VISC>(), st>>>(ka);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -538,6 +538,7 @@ struct dgx_ctx {
     float* d_d1 = nullptr;                  // FP32 stage increments (mixed RK3)
     float* d_d2 = nullptr;
     int minv_diag = 0;
+    int boundary = 0;  // some face is a boundary face or takes no part
     cudaStream_t cap = nullptr;  // capture stream
     cudaGraphExec_t graph = nullptr;   // one step (FP64) or two steps (mixed)
     cudaGraphExec_t graph1 = nullptr;  // mixed: one step
@@ -748,6 +749,9 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
         conn[e].nbr[f] = -1 - slot;
         conn[e].flags |= (1 << 3) << (4 * f);
     }
+    for (int e = 0; e < ne && !c->boundary; ++e)
+        for (int f = 0; f < 3; ++f)
+            if (conn[e].nbr[f] < 0) c->boundary = 1;
     if (slots.empty()) slots.push_back(BCSlot{});
 
     auto alloc = [&](void** ptr, size_t bytes) {
@@ -868,6 +872,7 @@ static int enqueue_rk3_mixed(dgx_ctx* c, double* u, double dt, int src, cudaStre
                   ? (float)(c->prm.mu * c->prm.gamma / (c->prm.prandtl * (c->prm.gamma - 1.0)))
                   : 0.0f;
     a.sigma0 = (float)c->prm.sigma0;
+    a.boundary = c->boundary;
     a.uhi = c->d_uhi[src];
     a.u64 = u;
     a.uhi_out = c->d_uhi[1 - src];

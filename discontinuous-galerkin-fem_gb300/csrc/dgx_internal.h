@@ -145,6 +145,7 @@ struct StageArgs {
     const ElemConn* conn;
     const BCSlot* bc;
     float dt, gamma, mu, kappa, sigma0;
+    int boundary;       // 1 when some face is a boundary or skipped face
 };
 
 
