@@ -16,6 +16,7 @@
 #include <unordered_set>
 #include <vector>
 
+#include "dgx_context.h"
 #include "dgx_internal.h"
 #include "quad_tables.inc"
 
@@ -37,6 +38,8 @@ static int fail(int code, const std::string& msg) {
     } while (0)
 
 extern "C" const char* dgx_last_error(void) { return g_err.c_str(); }
+
+int dgx::set_error(int code, const std::string& msg) { return fail(code, msg); }
 extern "C" const char* dgx_version(void) { return "dgx 0.1 (sm_103a)"; }
 
 // ------------------------------------------------------------------ bases
@@ -517,34 +520,6 @@ extern "C" int dgx_mesh_arrays(const dgx_mesh* m, int* nv, double* verts, int* e
 extern "C" void dgx_mesh_destroy(dgx_mesh* m) { delete m; }
 
 // ------------------------------------------------------------------ context
-struct dgx_ctx {
-    int device = 0;
-    dgx_params prm{};
-    int ne = 0, np = 0, nq = 0, nfq = 0;
-    size_t nstate = 0;  // ne*np*4
-    OpsHost ops{};
-    std::vector<double> xq;  // physical volume points
-    ElemGeom* d_geom = nullptr;
-    ElemGeomF* d_geomf = nullptr;  // FP32 rounding of d_geom (mixed precision)
-    ElemConn* d_conn = nullptr;
-    BCSlot* d_bc = nullptr;
-    double* d_u1 = nullptr;
-    double* d_u2 = nullptr;
-    double* d_hu = nullptr;   // host-variant staging
-    double* d_hr = nullptr;
-    double* d_mon = nullptr;  // [4]
-    int* d_flag = nullptr;
-    float* d_uhi[2] = {nullptr, nullptr};  // FP32 copies of u^n (mixed RK3), ping-ponged
-    float* d_d1 = nullptr;                  // FP32 stage increments (mixed RK3)
-    float* d_d2 = nullptr;
-    int minv_diag = 0;
-    int boundary = 0;  // some face is a boundary face or takes no part
-    cudaStream_t cap = nullptr;  // capture stream
-    cudaGraphExec_t graph = nullptr;   // one step (FP64) or two steps (mixed)
-    cudaGraphExec_t graph1 = nullptr;  // mixed: one step
-    const double* graph_u = nullptr;
-    double graph_dt = 0.0;
-};
 
 static StepArgs base_args(const dgx_ctx* c) {
     StepArgs a{};

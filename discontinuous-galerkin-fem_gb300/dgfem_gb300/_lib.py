@@ -51,7 +51,9 @@ SIGNATURES = {
     "dgx_project": (C.c_int, [_vp, _vp, _vp, _vp]),
     "dgx_residual_host": (C.c_int, [_vp, _dp, _dp]),
     "dgx_rk3_step_host": (C.c_int, [_vp, _dp, C.c_double, C.c_int]),
+    "dgx_rk3_step_static": (C.c_int, [_vp, _vp, C.c_double, C.c_int, _vp]),
 }
+STATIC_MAX_STATE = 1 << 20  # DGX_STATIC_MAX_STATE
 
 
 class Params(C.Structure):

@@ -158,6 +158,24 @@ int dgx_residual_host(dgx_ctx* c, const double* u, double* r);
 /* time_step_ssp_rk3 on a host state, in place (copies in, n_steps steps, copies out). */
 int dgx_rk3_step_host(dgx_ctx* c, double* u, double dt, int n_steps);
 
+/* ---------------------------------------------------------------- allocation-free stepping */
+
+/* No counterpart in dgfem.  For callers that may not allocate device memory while they
+ * run (a host framework that owns all device memory through its own pool, or a loop that
+ * must never enter the CUDA allocator): the same SSP-RK3 steps as dgx_rk3_step on the
+ * device state u (in place), with the stage buffers taken from one static device array
+ * of the library instead of memory the library allocates.  The call allocates nothing.
+ *  - Limit: n_elements * n_basis * 4 <= DGX_STATIC_MAX_STATE; larger states are rejected
+ *    with DGX_ERR_INVALID.  The array (2 * DGX_STATIC_MAX_STATE doubles, 16 MiB) is held
+ *    by every GPU that loads the library until the process exits.
+ *  - All calls share the array; calls whose GPU work overlaps (other streams or threads)
+ *    race on it.  Nothing in it needs to start at zero.
+ *  - The first call on a device looks up the array's device address (with the context's
+ *    device current); make that first call before any stream capture.
+ *  - The context's device must be current.  Kernels are launched directly on `stream`. */
+#define DGX_STATIC_MAX_STATE (1 << 20)
+int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
