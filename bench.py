@@ -39,11 +39,14 @@ N_CELLS, ORDER, BASIS = 512, 3, "dubiner"
 GAMMA, CFL, ACC_STEPS = 1.4, 0.05, 500
 # per element per RK stage, p=3, FP64 state: 3*Np*V*8 + 92 bytes of geometry/connectivity
 ALGO_BYTES_PER_ELEM_STAGE = 1052
+# what the mixed stage kernels need per element, averaged over the three stages
+# (stage 1: 400 B, stage 2: 560 B, stage 3: 1200 B; FP32 stage state, FP64 u^n)
+DESIGN_BYTES_PER_ELEM_STAGE = 720
 MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 # dram__bytes_read.sum + dram__bytes_write.sum per element per launch of the mixed
 # element kernel, from the ncu capture summarised in profiles/element_kernel_mixed_p3.md
-NCU_TRAFFIC_BYTES_PER_ELEM = None
+NCU_TRAFFIC_BYTES_PER_ELEM = 522  # stage 2 capture; its algorithmic bytes are 560
 
 
 def vortex(xy, t=0.0, beta=5.0, xc=0.0, yc=0.0, uinf=0.5, vinf=0.0, gamma=GAMMA, period=10.0):
@@ -57,6 +60,19 @@ def vortex(xy, t=0.0, beta=5.0, xc=0.0, yc=0.0, uinf=0.5, vinf=0.0, gamma=GAMMA,
     T = 1.0 - (gamma - 1.0) / (2.0 * gamma) * g * g
     rho = T ** (1.0 / (gamma - 1.0))
     p = rho * T
+    return np.stack([rho, rho * u, rho * v, p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v)], -1)
+
+
+def taylor_green(xy, seed=0, gamma=GAMMA, mach=0.1, noise=1e-3):
+    """Decaying Taylor-Green-type vortex on [0, 2 pi]^2 (conserved variables): rho=1,
+    u=sin x cos y, v=-cos x sin y, p = 1/(gamma M^2) + (cos 2x + cos 2y)/4, plus seeded
+    Gaussian noise of amplitude `noise` on the velocity."""
+    x, y = xy[..., 0], xy[..., 1]
+    rng = np.random.default_rng(seed)
+    u = np.sin(x) * np.cos(y) + noise * rng.standard_normal(x.shape)
+    v = -np.cos(x) * np.sin(y) + noise * rng.standard_normal(x.shape)
+    p = 1.0 / (gamma * mach * mach) + 0.25 * (np.cos(2 * x) + np.cos(2 * y))
+    rho = np.ones_like(x)
     return np.stack([rho, rho * u, rho * v, p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v)], -1)
 
 
@@ -206,6 +222,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--cells", type=int, default=N_CELLS, help="quads per side (profiling cases)")
+    ap.add_argument("--ns-steps", type=int, default=20, help="timed steps of the Navier-Stokes leg (0: skip)")
     args = ap.parse_args()
     rank, ws = dist_init()
     if args.impl == "reference":
@@ -290,8 +307,52 @@ def main():
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_kind": peak_kind,
             "traffic": None if NCU_TRAFFIC_BYTES_PER_ELEM is None else NCU_TRAFFIC_BYTES_PER_ELEM * ne,
-            "kernel": "dgx::element_kernel<3,float,false> (mixed stage)",
-            "algorithmic_bytes_per_launch": ALGO_BYTES_PER_ELEM_STAGE * ne, "launch_ms": t_launch * 1e3}
+            "kernel": "dgx::stage_kernel<3, Euler, no boundary> (mixed SSP-RK3 stage)",
+            "algorithmic_bytes_per_launch": ALGO_BYTES_PER_ELEM_STAGE * ne, "launch_ms": t_launch * 1e3,
+            "design_bytes_per_launch": DESIGN_BYTES_PER_ELEM_STAGE * ne,
+            "achieved_design_bytes": DESIGN_BYTES_PER_ELEM_STAGE * ne / t_launch / 1e9,
+            "traffic_note": "ncu dram read+write of one stage-2 launch (522 B/element, its design bytes are 560)"}
+
+    # ---- Navier-Stokes leg: Taylor-Green-type vortex, [0,2pi]^2, 256x256x2, p=4, Re=1600
+    ns = None
+    if args.ns_steps > 0:
+        import math
+        del c64, cmx, u0
+        torch.cuda.empty_cache()
+        nmesh = dg.DGMesh.rectangle(256, 256, 0.0, 2 * math.pi, 0.0, 2 * math.pi, periodic=True)
+        nsp = dg.DGSpace("triangle", 4, "dubiner")
+        nwf = dg.NavierStokesWeakFormulation(GAMMA, 1.0 / 1600.0, 0.71, 5.0)
+        n64 = dg.DGContext(nmesh, nsp, nwf, "fp64")
+        nmx = dg.DGContext(nmesh, nsp, nwf, "mixed")
+        nu0 = n64.project(torch.tensor(taylor_green(n64.quad_points(), args.seed), device="cuda"))
+        # combined CFL: dgfem defines only the convective one; with its SIPG penalty and
+        # half-jump viscous face flux, p=4 is stable in the oracle at convective CFL 0.025
+        # (it diverges at 0.05 within 22 steps), and the viscous bound 0.05 h^2 rho / mu
+        # (h the shortest edge) is far larger here
+        h = 2 * math.pi / 256
+        ndt = min(0.025 / n64.max_cfl(nu0, 1.0), 0.05 * h * h * 1600.0)
+        ndof = n64.n_elements * n64.n_basis * 4
+
+        def ntimed(ctx, k):
+            u = nu0.clone()
+            ctx.rk3_step(u, ndt, 2)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            ctx.rk3_step(u, ndt, k)
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / 1e3, u
+
+        tn_mx, umx = ntimed(nmx, args.ns_steps)
+        tn_64, u64 = ntimed(n64, args.ns_steps)
+        ns = {"workload": "navier_stokes_taylor_green_256x256x2_p4_dubiner_re1600", "elements": n64.n_elements,
+              "dof": ndof, "dt": ndt, "steps": args.ns_steps,
+              "mixed": {"value": ndof * 3 * args.ns_steps / tn_mx, "ms_per_step": 1e3 * tn_mx / args.ns_steps},
+              "fp64": {"value": ndof * 3 * args.ns_steps / tn_64, "ms_per_step": 1e3 * tn_64 / args.ns_steps},
+              "mixed_vs_fp64": tn_64 / tn_mx,
+              "mixed_vs_fp64_l2_rel": float(torch.linalg.vector_norm(umx - u64) / torch.linalg.vector_norm(u64))}
+        del n64, nmx
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline and args.cells == N_CELLS:
@@ -313,6 +374,7 @@ def main():
                 "fp64": {"value": v_64, "ms_per_step": 1e3 * t_64 / k64, "steps": k64},
                 "mixed_vs_fp64": v_mx / v_64,
                 "accuracy": acc,
+                "navier_stokes": ns,
                 "adjoint_forward_ratio": None,
                 "e2e": {"value": v_e2e, "unit": "DOF*stages/s", "h2d_bytes_per_step": dof * 8,
                         "d2h_bytes_per_step": dof * 8, "steps": ke},

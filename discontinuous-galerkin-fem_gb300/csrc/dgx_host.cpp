@@ -999,3 +999,34 @@ extern "C" int dgx_rk3_step_host(dgx_ctx* c, double* u, double dt, int n_steps) 
     CUDA_OK(cudaStreamSynchronize(c->cap));
     return DGX_OK;
 }
+
+extern "C" int dgx_apply_mass_inv_host(dgx_ctx* c, const double* in, double* out) {
+    if (!c || (c->ne && (!in || !out))) return fail(DGX_ERR_INVALID, "dgx_apply_mass_inv_host: null argument");
+    int rc = ensure_host_buffers(c);
+    if (rc) return rc;
+    const size_t sb = c->nstate * sizeof(double);
+    CUDA_OK(cudaMemcpyAsync(c->d_hu, in, sb, cudaMemcpyHostToDevice, c->cap));
+    if ((rc = dgx_apply_mass_inv(c, c->d_hu, c->d_hr, c->cap))) return rc;
+    CUDA_OK(cudaMemcpyAsync(out, c->d_hr, sb, cudaMemcpyDeviceToHost, c->cap));
+    CUDA_OK(cudaStreamSynchronize(c->cap));
+    return DGX_OK;
+}
+
+extern "C" int dgx_monitor_host(dgx_ctx* c, const double* u, double dt, double* cfl, double* rho_min,
+                                double* rho_max, int* has_nan) {
+    if (!c || (c->ne && !u)) return fail(DGX_ERR_INVALID, "dgx_monitor_host: null argument");
+    int rc = ensure_host_buffers(c);
+    if (rc) return rc;
+    CUDA_OK(cudaMemcpyAsync(c->d_hu, u, c->nstate * sizeof(double), cudaMemcpyHostToDevice, c->cap));
+    double a = 0.0, lo = 0.0, hi = 0.0;
+    int nan = 0;
+    if (cfl && (rc = dgx_max_cfl(c, c->d_hu, dt, &a, c->cap))) return rc;
+    if ((rho_min || rho_max) && (rc = dgx_density_range(c, c->d_hu, &lo, &hi, c->cap))) return rc;
+    if (has_nan && (rc = dgx_has_nan(c, c->d_hu, &nan, c->cap))) return rc;
+    CUDA_OK(cudaStreamSynchronize(c->cap));
+    if (cfl) *cfl = a;
+    if (rho_min) *rho_min = lo;
+    if (rho_max) *rho_max = hi;
+    if (has_nan) *has_nan = nan;
+    return DGX_OK;
+}

@@ -52,6 +52,8 @@ SIGNATURES = {
     "dgx_residual_host": (C.c_int, [_vp, _dp, _dp]),
     "dgx_rk3_step_host": (C.c_int, [_vp, _dp, C.c_double, C.c_int]),
     "dgx_rk3_step_static": (C.c_int, [_vp, _vp, C.c_double, C.c_int, _vp]),
+    "dgx_apply_mass_inv_host": (C.c_int, [_vp, _dp, _dp]),
+    "dgx_monitor_host": (C.c_int, [_vp, _dp, C.c_double, _dp, _dp, _dp, _ip]),
 }
 STATIC_MAX_STATE = 1 << 20  # DGX_STATIC_MAX_STATE
 

@@ -157,6 +157,12 @@ int dgx_project(dgx_ctx* c, const double* uq, double* u, void* stream);
 int dgx_residual_host(dgx_ctx* c, const double* u, double* r);
 /* time_step_ssp_rk3 on a host state, in place (copies in, n_steps steps, copies out). */
 int dgx_rk3_step_host(dgx_ctx* c, double* u, double dt, int n_steps);
+/* apply_mass_inv on host states (copies in, computes, copies out). */
+int dgx_apply_mass_inv_host(dgx_ctx* c, const double* in, double* out);
+/* compute_max_cfl, compute_density_range and the NaN scan of run_time_integration on a host
+ * state; any output pointer may be NULL. */
+int dgx_monitor_host(dgx_ctx* c, const double* u, double dt, double* cfl, double* rho_min,
+                     double* rho_max, int* has_nan);
 
 /* ---------------------------------------------------------------- allocation-free stepping */
 
