@@ -25,13 +25,8 @@
 // are bank-conflict free; neighbours outside the tile are read through L1/L2.
 #pragma once
 
+#include "../../include/dgx.h"
 #include "dg_physics.cuh"
-
-#ifndef DGX_BC_FAR_FIELD  // values of the DGX_BC_* enum of include/dgx.h
-#define DGX_BC_FAR_FIELD 0
-#define DGX_BC_SLIP_WALL 1
-#define DGX_BC_NO_SLIP_WALL 2
-#endif
 
 namespace dgx {
 
@@ -106,9 +101,10 @@ __device__ __forceinline__ void load_row_f32(const float* uhi, const float* d, i
 // The residual (or, with FOLD, M_K^-1 times the residual) of one element, accumulated
 // into R.  Ue: this element's coefficients (shared memory); sU/e0/nloc: the tile, for
 // in-tile neighbours; getrow(nb, i, c): coefficient row i of an out-of-tile neighbour.
-// NBREG keeps a neighbour's coefficients in registers across the face's points.
-template <int P, typename T, bool VISC, bool FOLD, bool NBREG, class GetRow>
-__device__ __forceinline__ void element_residual(const Ops<P, T>& o, const LiftOps<P, T>* L,
+// NBREG keeps a neighbour's coefficients in registers across the face's points.  OT is
+// the type the operators are stored in (T itself, or double when T carries derivatives).
+template <int P, typename T, bool VISC, bool FOLD, bool NBREG, class GetRow, typename OT>
+__device__ __forceinline__ void element_residual(const Ops<P, OT>& o, const LiftOps<P, OT>* L,
                                                  const T* Ue, const T* sU, int e0, int nloc,
                                                  const ElemGeom& G, const ElemConn& C,
                                                  const BCSlot* bcs, const ElemGeom* geoms,
@@ -369,7 +365,7 @@ __global__ void __launch_bounds__(TILE) element_kernel(const __grid_constant__ K
         const T kappa = VISC ? (T)(s.mu * s.gamma / (s.prandtl * (s.gamma - 1.0))) : T(0);
         const double* ug = s.u;
         auto getrow = [ug](int nb, int i, T c[4]) { load_row_f64<T, NB>(ug, nb, i, c); };
-        element_residual<P, T, VISC, false, false>(ka.o, nullptr, sU + tl * STR, sU, e0, nloc, s.geom[e],
+        element_residual<P, T, VISC, false, false>(ka.o, (const LiftOps<P, T>*)nullptr, sU + tl * STR, sU, e0, nloc, s.geom[e],
                                                    s.conn[e], s.bc, s.geom, (T)s.gamma, mu, kappa,
                                                    (T)s.sigma0, getrow, R);
     }

@@ -31,6 +31,8 @@ struct dgx_ctx {
     float* d_d2 = nullptr;
     int minv_diag = 0;
     int boundary = 0;  // some face is a boundary face or takes no part
+    int has_slip_wall = 0;
+    double* d_adj[3] = {nullptr, nullptr, nullptr};  // adjoint scratch (allocated on first use)
     cudaStream_t cap = nullptr;  // capture stream
     cudaGraphExec_t graph = nullptr;   // one step (FP64) or two steps (mixed)
     cudaGraphExec_t graph1 = nullptr;  // mixed: one step

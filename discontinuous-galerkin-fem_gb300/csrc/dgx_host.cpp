@@ -550,6 +550,7 @@ static void free_ctx(dgx_ctx* c) {
     cudaSetDevice(c->device);
     if (c->graph) cudaGraphExecDestroy(c->graph);
     if (c->graph1) cudaGraphExecDestroy(c->graph1);
+    for (double* a : c->d_adj) cudaFree(a);
     cudaFree(c->d_uhi[0]);
     cudaFree(c->d_uhi[1]);
     cudaFree(c->d_d1);
@@ -714,6 +715,7 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
             }
             BCSlot b{};
             b.type = it->second.type;
+            if (b.type == DGX_BC_SLIP_WALL) c->has_slip_wall = 1;
             for (int v = 0; v < 4; ++v) b.value[v] = it->second.value[v];
             slot = (int)slots.size();
             slots.push_back(b);

@@ -6,10 +6,10 @@ from ._lib import DGXError, DGXInvalidArgument, DGXOutOfRange, LIB_PATH, load
 from .api import (BCTypeEuler, BoundaryConditionEuler, CompressibleDGSolverBase, DGAssembler,
                   DGContext, DGMesh, DGSpace, EulerDGSolver, EulerWeakFormulation,
                   NavierStokesDGSolver, NavierStokesWeakFormulation, conserved_to_primitive,
-                  primitive_to_conserved)
+                  kinetic_energy, primitive_to_conserved, rk3_trajectory)
 
 __all__ = ["DGXError", "DGXInvalidArgument", "DGXOutOfRange", "LIB_PATH", "load",
            "BCTypeEuler", "BoundaryConditionEuler", "CompressibleDGSolverBase", "DGAssembler",
            "DGContext", "DGMesh", "DGSpace", "EulerDGSolver", "EulerWeakFormulation",
            "NavierStokesDGSolver", "NavierStokesWeakFormulation", "conserved_to_primitive",
-           "primitive_to_conserved"]
+           "primitive_to_conserved", "kinetic_energy", "rk3_trajectory"]

@@ -54,6 +54,12 @@ SIGNATURES = {
     "dgx_rk3_step_static": (C.c_int, [_vp, _vp, C.c_double, C.c_int, _vp]),
     "dgx_apply_mass_inv_host": (C.c_int, [_vp, _dp, _dp]),
     "dgx_monitor_host": (C.c_int, [_vp, _dp, C.c_double, _dp, _dp, _dp, _ip]),
+    "dgx_residual_jvp": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "dgx_residual_vjp": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "dgx_rk3_step_tlm": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int, _vp]),
+    "dgx_rk3_step_adjoint": (C.c_int, [_vp, _vp, _vp, C.c_double, _vp]),
+    "dgx_kinetic_energy": (C.c_int, [_vp, _vp, _dp, _vp, _vp]),
+    "dgx_kinetic_energy_gradient": (C.c_int, [_vp, _vp, C.c_double, C.c_int, C.c_int, _dp, _vp, _vp]),
 }
 STATIC_MAX_STATE = 1 << 20  # DGX_STATIC_MAX_STATE
 

@@ -323,6 +323,51 @@ class DGContext:
         check(L.load().dgx_has_nan(self._h, self._dev(u), C.byref(f), _stream_of(u)))
         return bool(f.value)
 
+    # ---- differentiation (FP64 contexts)
+    def residual_jvp(self, u, du):
+        """(dR/du) du, the tangent of assemble_euler_residual."""
+        import torch
+        out = torch.empty_like(u)
+        check(L.load().dgx_residual_jvp(self._h, self._dev(u), self._dev(du), self._dev(out), _stream_of(u)))
+        return out
+
+    def residual_vjp(self, u, rbar):
+        """(dR/du)^T rbar (Euler)."""
+        import torch
+        out = torch.empty_like(u)
+        check(L.load().dgx_residual_vjp(self._h, self._dev(u), self._dev(rbar), self._dev(out), _stream_of(u)))
+        return out
+
+    def rk3_step_tlm(self, u, du, dt: float, n_steps: int = 1):
+        """Advance (u, du) in place through n_steps tangent-linear SSP-RK3 steps."""
+        check(L.load().dgx_rk3_step_tlm(self._h, self._dev(u), self._dev(du), float(dt), int(n_steps),
+                                        _stream_of(u)))
+        return u, du
+
+    def rk3_step_adjoint(self, u_n, ubar, dt: float):
+        """Replace ubar (cotangent of u^{n+1}) by the cotangent of u_n, in place."""
+        check(L.load().dgx_rk3_step_adjoint(self._h, self._dev(u_n), self._dev(ubar), float(dt), _stream_of(u_n)))
+        return ubar
+
+    def kinetic_energy(self, u, grad: bool = False):
+        """J = integral of rho |u|^2 / 2 at the volume points (and dJ/du when grad)."""
+        import torch
+        J = C.c_double()
+        g = torch.empty_like(u) if grad else None
+        check(L.load().dgx_kinetic_energy(self._h, self._dev(u), C.byref(J),
+                                          self._dev(g) if grad else None, _stream_of(u)))
+        return (J.value, g) if grad else J.value
+
+    def kinetic_energy_gradient(self, u0, dt: float, n_steps: int, checkpoint_every: int = 50):
+        """(J(u(T)), dJ/du0) by the checkpointed adjoint."""
+        import torch
+        J = C.c_double()
+        g = torch.empty_like(u0)
+        check(L.load().dgx_kinetic_energy_gradient(self._h, self._dev(u0), float(dt), int(n_steps),
+                                                   int(checkpoint_every), C.byref(J), self._dev(g),
+                                                   _stream_of(u0)))
+        return J.value, g
+
 
 class DGAssembler:
     """DGAssembler(mesh, weak_form) with assemble_euler_residual (assembler.hpp:58-59)."""
@@ -404,3 +449,64 @@ class NavierStokesDGSolver(CompressibleDGSolverBase):
                  prandtl=0.72, penalty_prefactor=5.0, precision: str = "fp64"):
         super().__init__(mesh, NavierStokesWeakFormulation(gamma, dynamic_viscosity, prandtl,
                                                             penalty_prefactor), space, precision)
+
+
+def _autograd():
+    import torch
+
+    class RK3Trajectory(torch.autograd.Function):
+        """u(T) = n_steps SSP-RK3 steps from u0; the backward pass is the hand-written adjoint
+        with a checkpoint every `checkpoint_every` steps and recomputation in between."""
+
+        @staticmethod
+        def forward(fctx, u0, dgctx, dt, n_steps, checkpoint_every):
+            u = u0.detach().clone()
+            cks = [u.clone()]
+            for n in range(n_steps):
+                dgctx.rk3_step(u, dt, 1)
+                if (n + 1) % checkpoint_every == 0 and n + 1 < n_steps:
+                    cks.append(u.clone())
+            fctx.dgctx, fctx.dt, fctx.n, fctx.ce, fctx.cks = dgctx, dt, n_steps, checkpoint_every, cks
+            return u
+
+        @staticmethod
+        def backward(fctx, gT):
+            dg, dt, n, ce = fctx.dgctx, fctx.dt, fctx.n, fctx.ce
+            ubar = gT.detach().clone().contiguous()
+            nseg = len(fctx.cks)
+            for g in range(nseg - 1, -1, -1):
+                n0, n1 = g * ce, min(n, (g + 1) * ce)
+                states = [fctx.cks[g].clone()]
+                for _ in range(n0, n1 - 1):
+                    u = states[-1].clone()
+                    dg.rk3_step(u, dt, 1)
+                    states.append(u)
+                for k in range(n1 - n0 - 1, -1, -1):
+                    dg.rk3_step_adjoint(states[k], ubar, dt)
+            return ubar, None, None, None, None
+
+    class KineticEnergy(torch.autograd.Function):
+        """J = integral of rho |u|^2 / 2 over the domain at the volume quadrature points."""
+
+        @staticmethod
+        def forward(fctx, u, dgctx):
+            J, g = dgctx.kinetic_energy(u.detach().contiguous(), grad=True)
+            fctx.save_for_backward(g)
+            return torch.tensor(J, dtype=torch.float64, device=u.device)
+
+        @staticmethod
+        def backward(fctx, gJ):
+            (g,) = fctx.saved_tensors
+            return gJ * g, None
+
+    return RK3Trajectory, KineticEnergy
+
+
+def rk3_trajectory(u0, dgctx: DGContext, dt: float, n_steps: int, checkpoint_every: int = 50):
+    """Differentiable SSP-RK3 trajectory (torch.autograd), FP64 Euler contexts."""
+    return _autograd()[0].apply(u0, dgctx, dt, n_steps, checkpoint_every)
+
+
+def kinetic_energy(u, dgctx: DGContext):
+    """Differentiable kinetic-energy objective (torch.autograd)."""
+    return _autograd()[1].apply(u, dgctx)

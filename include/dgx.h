@@ -164,6 +164,31 @@ int dgx_apply_mass_inv_host(dgx_ctx* c, const double* in, double* out);
 int dgx_monitor_host(dgx_ctx* c, const double* u, double dt, double* cfl, double* rho_min,
                      double* rho_max, int* has_nan);
 
+/* ---------------------------------------------------------------- differentiation (FP64 contexts) */
+
+/* Tangent of assemble_euler_residual: dr = (dR/du) du.  Dual-number evaluation of the same
+ * residual code, Euler and Navier-Stokes.  No counterpart in dgfem (it has no derivatives). */
+int dgx_residual_jvp(dgx_ctx* c, const double* u, const double* du, double* dr, void* stream);
+/* Adjoint of assemble_euler_residual: ubar = (dR/du)^T rbar.  Euler only; contexts with
+ * slip-wall faces are rejected.  No counterpart in dgfem. */
+int dgx_residual_vjp(dgx_ctx* c, const double* u, const double* rbar, double* ubar, void* stream);
+/* Tangent-linear SSP-RK3 (time_stepping.hpp:39-55): advances the state u and its tangent
+ * du together by n_steps steps, in place. */
+int dgx_rk3_step_tlm(dgx_ctx* c, double* u, double* du, double dt, int n_steps, void* stream);
+/* Adjoint of one SSP-RK3 step at u_n: ubar (the cotangent of u^{n+1}) is replaced by the
+ * cotangent of u_n.  Recomputes the two intermediate stages.  Euler only. */
+int dgx_rk3_step_adjoint(dgx_ctx* c, const double* u_n, double* ubar, double dt, void* stream);
+/* J = sum_e sum_q w_q |J_e| ((rho u)^2 + (rho v)^2) / (2 rho) over the volume points, written to
+ * host memory (synchronises) when J != NULL; its gradient dJ/du into the device state grad
+ * when grad != NULL. */
+int dgx_kinetic_energy(dgx_ctx* c, const double* u, double* J, double* grad, void* stream);
+/* dJ/du0 for J(u(T)), u(T) = n_steps SSP-RK3 steps of size dt from u0: forward sweep with a
+ * checkpoint every checkpoint_every steps, then, per segment from the last, a recomputation
+ * storing each step's stages and the adjoint steps backward.  J (host, may be NULL) and
+ * grad (device state) are outputs.  Allocates its checkpoint storage for the call.  Euler only. */
+int dgx_kinetic_energy_gradient(dgx_ctx* c, const double* u0, double dt, int n_steps, int checkpoint_every,
+                                double* J, double* grad, void* stream);
+
 /* ---------------------------------------------------------------- allocation-free stepping */
 
 /* No counterpart in dgfem.  For callers that may not allocate device memory while they
