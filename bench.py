@@ -76,6 +76,19 @@ def taylor_green(xy, seed=0, gamma=GAMMA, mach=0.1, noise=1e-3):
     return np.stack([rho, rho * u, rho * v, p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v)], -1)
 
 
+def shear_layer(xy, seed=0, gamma=GAMMA, mach=0.3, noise=1e-4):
+    """Double shear layer on the periodic unit square (conserved variables): rho=1,
+    p = 1/(gamma M^2), u = tanh((|y - 1/2| - 1/4)/0.02), v = 0.05 sin(2 pi x), plus seeded
+    Gaussian noise of amplitude `noise` on both velocity components."""
+    x, y = xy[..., 0], xy[..., 1]
+    rng = np.random.default_rng(seed + 1)
+    u = np.tanh((np.abs(y - 0.5) - 0.25) / 0.02) + noise * rng.standard_normal(x.shape)
+    v = 0.05 * np.sin(2 * np.pi * x) + noise * rng.standard_normal(x.shape)
+    rho = np.ones_like(x)
+    p = np.full_like(x, 1.0 / (gamma * mach * mach))
+    return np.stack([rho, rho * u, rho * v, p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v)], -1)
+
+
 def vortex_centre(seed=0):
     return np.random.default_rng(seed).uniform(-2.0, 2.0, size=2)
 
@@ -211,6 +224,89 @@ def run_reference(args, rank, ws):
     print(json.dumps(line), flush=True)
 
 
+def batch_leg(dg, torch, n_inst, steps, seed):
+    """Independent periodic vortex solves on [-5,5]^2: N x N x 2 with N uniform in
+    {16, 24, ..., 128}, p uniform in {2, 3}, beta ~ U(1,5), free stream u ~ U(0.2,0.8),
+    centre ~ U([-2,2]^2); each instance's dt = CFL / its max CFL number.  Times `steps`
+    mixed-precision steps of all instances through one DGBatch (one persistent launch per
+    stage) against the same steps through one mixed DGContext per instance in a loop, and
+    reports each instance's error against its own FP64 run."""
+    rng = np.random.default_rng(seed + 4242)
+    Ns = rng.choice(np.arange(16, 129, 8), size=n_inst)
+    ps = rng.choice([2, 3], size=n_inst)
+    betas = rng.uniform(1.0, 5.0, n_inst)
+    uinfs = rng.uniform(0.2, 0.8, n_inst)
+    centres = rng.uniform(-2.0, 2.0, (n_inst, 2))
+    wf = dg.EulerWeakFormulation(GAMMA)
+    meshes = [dg.DGMesh.rectangle(int(N), int(N), -5.0, 5.0, -5.0, 5.0, periodic=True) for N in Ns]
+    spaces = [dg.DGSpace("triangle", int(p), BASIS) for p in ps]
+    u0s, dts, refs, dofs = [], [], [], []
+    t0 = time.perf_counter()
+    for i in range(n_inst):  # initial states and each instance's FP64 run
+        c = dg.DGContext(meshes[i], spaces[i], wf, "fp64")
+        xq = c.quad_points()
+        u0 = c.project(torch.tensor(vortex(xq, beta=betas[i], xc=centres[i, 0], yc=centres[i, 1], uinf=uinfs[i]),
+                                    device="cuda"))
+        dt = CFL / c.max_cfl(u0, 1.0)
+        u = u0.clone()
+        c.rk3_step(u, dt, steps)
+        u0s.append(u0)
+        dts.append(dt)
+        refs.append(u)
+        dofs.append(c.n_elements * c.n_basis * 4)
+        del c
+    torch.cuda.synchronize()
+    t_ref = time.perf_counter() - t0
+    total = int(sum(dofs)) * 3 * steps  # DOF * stages of the whole ensemble
+
+    batch = dg.DGBatch(meshes, spaces, wf)
+    for i in range(n_inst):
+        batch.state(i).copy_(u0s[i])
+    batch.rk3_step(dts, 2)  # warm-up: launch-shape tuning and graph capture
+    for i in range(n_inst):
+        batch.state(i).copy_(u0s[i])
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    batch.rk3_step(dts, steps)
+    e1.record()
+    torch.cuda.synchronize()
+    t_batch = e0.elapsed_time(e1) / 1e3
+    outs = [batch.state(i) for i in range(n_inst)]
+    l2 = [float(torch.linalg.vector_norm(outs[i] - refs[i]) / torch.linalg.vector_norm(refs[i])) for i in range(n_inst)]
+    linf = [float((outs[i] - refs[i]).abs().max() / refs[i].abs().max()) for i in range(n_inst)]
+    grid, tiles = batch.launch_shape()
+
+    ctxs = [dg.DGContext(meshes[i], spaces[i], wf, "mixed") for i in range(n_inst)]
+    us = [u0s[i].clone() for i in range(n_inst)]
+    for i in range(n_inst):  # warm-up per context, then back to the initial state
+        ctxs[i].rk3_step(us[i], dts[i], 2)
+        us[i].copy_(u0s[i])
+    torch.cuda.synchronize()
+    e0.record()
+    for i in range(n_inst):
+        ctxs[i].rk3_step(us[i], dts[i], steps)
+    e1.record()
+    torch.cuda.synchronize()
+    t_loop = e0.elapsed_time(e1) / 1e3
+    same = max(float(torch.linalg.vector_norm(us[i] - outs[i]) / torch.linalg.vector_norm(us[i]))
+               for i in range(n_inst))
+    del ctxs, us, batch
+    torch.cuda.empty_cache()
+    return {"workload": f"euler_vortex_ensemble_{n_inst}_instances_N16-128_p2-3_dubiner_mixed",
+            "instances": n_inst, "steps": steps, "elements": int(sum(2 * int(N) * int(N) for N in Ns)),
+            "orders": {"p2": int((ps == 2).sum()), "p3": int((ps == 3).sum())}, "dof": int(sum(dofs)),
+            "value": total / t_batch, "unit": "DOF*stages/s", "s": t_batch,
+            "single_solve_loop": {"value": total / t_loop, "s": t_loop},
+            "batched_vs_loop": t_loop / t_batch,
+            "launch_shape": {"grid": grid, "tiles": tiles},
+            "gpu_launches": 3 * steps + len(set(ps.tolist())),
+            "batched_vs_loop_max_rel_diff": same,
+            "per_instance_vs_fp64": {"l2_rel_max": max(l2), "l2_rel_median": float(np.median(l2)),
+                                     "linf_rel_max": max(linf)},
+            "fp64_reference_runs_s": t_ref}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -223,6 +319,10 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--cells", type=int, default=N_CELLS, help="quads per side (profiling cases)")
     ap.add_argument("--ns-steps", type=int, default=20, help="timed steps of the Navier-Stokes leg (0: skip)")
+    ap.add_argument("--adj-steps", type=int, default=1000, help="steps of the adjoint leg (0: skip)")
+    ap.add_argument("--adj-dirs", type=int, default=16, help="finite-difference directions of the adjoint check")
+    ap.add_argument("--batch-instances", type=int, default=256, help="instances of the batched leg (0: skip)")
+    ap.add_argument("--batch-steps", type=int, default=300, help="SSP-RK3 steps of each batched instance")
     args = ap.parse_args()
     rank, ws = dist_init()
     if args.impl == "reference":
@@ -354,6 +454,74 @@ def main():
               "mixed_vs_fp64_l2_rel": float(torch.linalg.vector_norm(umx - u64) / torch.linalg.vector_norm(u64))}
         del n64, nmx
 
+    # ---- adjoint leg: shear layer 128x128x2, p=3, J = kinetic energy after adj_steps steps,
+    #      checkpoints every 50 steps; adjoint/forward time ratio and FD / tangent-linear checks
+    adj = None
+    if args.adj_steps > 0:
+        amesh = dg.DGMesh.rectangle(128, 128, 0.0, 1.0, 0.0, 1.0, periodic=True)
+        actx = dg.DGContext(amesh, dg.DGSpace("triangle", 3, "dubiner"), dg.EulerWeakFormulation(GAMMA), "fp64")
+        au0 = actx.project(torch.tensor(shear_layer(actx.quad_points(), args.seed), device="cuda"))
+        adt = CFL / actx.max_cfl(au0, 1.0)
+        na, ce = args.adj_steps, 50
+        w = au0.clone()
+        actx.rk3_step(w, adt, 3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        w = au0.clone()
+        actx.rk3_step(w, adt, na)
+        torch.cuda.synchronize()
+        t_fwd = time.perf_counter() - t0
+        actx.kinetic_energy_gradient(au0, adt, 2, 1)  # warm the adjoint kernels
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Jv, grad = actx.kinetic_energy_gradient(au0, adt, na, ce)
+        torch.cuda.synchronize()
+        t_grad = time.perf_counter() - t0
+        rng = np.random.default_rng(1234)
+        h = 1e-6
+        fd_err, tlm_err, fd_abs = [], [], []
+        axq = actx.quad_points()
+        for k in range(args.adj_dirs):
+            # seeded random smooth direction: a few random Fourier modes per variable,
+            # projected into the DG space (unit-size perturbations of every variable).
+            # Wavenumbers start at 0: the layer varies along y only, so modes with kx >= 1
+            # alone are nearly orthogonal to dJ/du and their derivatives drown in rounding
+            field = np.zeros(axq.shape[:-1] + (4,))
+            for var in range(4):
+                for _ in range(3):
+                    kx, ky = rng.integers(0, 4, size=2)
+                    ph_x, ph_y = rng.uniform(0, 2 * np.pi, size=2)
+                    field[..., var] += rng.standard_normal() * np.sin(2 * np.pi * kx * axq[..., 0] + ph_x) * \
+                        np.cos(2 * np.pi * ky * axq[..., 1] + ph_y)
+            d = actx.project(torch.tensor(field, device="cuda"))
+            up, um = au0 + h * d, au0 - h * d
+            actx.rk3_step(up, adt, na)
+            actx.rk3_step(um, adt, na)
+            fd = (actx.kinetic_energy(up) - actx.kinetic_energy(um)) / (2 * h)
+            ad = float(torch.sum(grad * d))
+            fd_err.append(abs(ad - fd) / max(abs(fd), 1e-300))
+            fd_abs.append(abs(fd))
+            if k < 2:
+                ut, dut = au0.clone(), d.clone()
+                actx.rk3_step_tlm(ut, dut, adt, na)
+                _, gT = actx.kinetic_energy(ut, grad=True)
+                tl = float(torch.sum(gT * dut))
+                tlm_err.append(abs(ad - tl) / max(abs(tl), 1e-300))
+        adj = {"workload": "euler_shear_layer_128x128x2_p3_dubiner_fp64", "elements": actx.n_elements,
+               "steps": na, "checkpoint_every": ce, "dt": adt, "J": Jv,
+               "forward_ms_per_step": 1e3 * t_fwd / na, "gradient_s": t_grad,
+               "gradient_vs_forward_solve": t_grad / t_fwd,
+               "adjoint_step_vs_forward_step": (t_grad - t_fwd) / t_fwd,
+               "fd_directions": args.adj_dirs, "fd_h": h, "fd_max_rel_err": max(fd_err) if fd_err else None,
+               "fd_median_rel_err": float(np.median(fd_err)) if fd_err else None,
+               "fd_min_abs_derivative": min(fd_abs) if fd_abs else None,
+               "tlm_directions": len(tlm_err), "tlm_max_rel_err": max(tlm_err) if tlm_err else None}
+        del actx
+
+    bat = None
+    if args.batch_instances > 0:
+        bat = batch_leg(dg, torch, args.batch_instances, args.batch_steps, args.seed)
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline and args.cells == N_CELLS:
         w = OracleWorkload(1, args.seed)
@@ -375,7 +543,9 @@ def main():
                 "mixed_vs_fp64": v_mx / v_64,
                 "accuracy": acc,
                 "navier_stokes": ns,
-                "adjoint_forward_ratio": None,
+                "adjoint_forward_ratio": None if adj is None else adj["adjoint_step_vs_forward_step"],
+                "adjoint": adj,
+                "batched": bat,
                 "e2e": {"value": v_e2e, "unit": "DOF*stages/s", "h2d_bytes_per_step": dof * 8,
                         "d2h_bytes_per_step": dof * 8, "steps": ke},
                 "gpu_launches": 3 * args.steps,

@@ -410,10 +410,31 @@ __global__ void kinetic_kernel(const __grid_constant__ VArgs<P> ka, double* J, d
             for (int i = 0; i < NP; ++i)
                 for (int v = 0; v < NV; ++v) grad[(size_t)e * NB + i * NV + v] = g[i][v];
     }
-    if (J) {
+    if (J) {  // per-block partial sums, combined in a fixed order by kinetic_sum_kernel
         for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-        if ((threadIdx.x & 31) == 0) atomicAdd(J, acc);
+        __shared__ double warp_sums[32];
+        if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double b = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += warp_sums[w];
+            J[blockIdx.x] = b;
+        }
     }
+}
+
+// Compensated (Kahan) sum of the per-block partial sums, in block order: the objective is
+// a deterministic function of the state.
+__global__ void kinetic_sum_kernel(const double* partial, int n, double* J) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s = 0.0, c = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double y = partial[i] - c;
+        const double t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    *J = s;
 }
 
 template <int P, bool VISC>

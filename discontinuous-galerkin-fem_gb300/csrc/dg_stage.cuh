@@ -71,29 +71,29 @@ __host__ __device__ constexpr int stage_min_blocks(int p, bool visc) {
 #endif
 }
 
+// Floats of shared memory the neighbour-face operators take (16-byte rows).
+template <int P, bool VISC>
+__host__ __device__ constexpr int stage_op_floats() {
+    return (VISC ? 3 : 1) * 3 * n_basis(P) * NbrOps<P>::NFQP;
+}
+
+// One tile of TILE elements: stage it, compute the element residuals, write the stage.
+// sOp: the neighbour-face operators; sU: [TILE][stride] floats; sDt: [TILE] floats.
 template <int P, bool VISC, bool BND>
-__global__ void __launch_bounds__(TILE, stage_min_blocks(P, VISC)) stage_kernel(const __grid_constant__ SArgs<P, VISC> ka) {
+__device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float* sOp, float* sU, float* sDt,
+                                           int tile) {
     constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1, NB = NP * NV, STR = stage_stride<P>(), NB4 = NB / 4;
     constexpr int NFQP = NbrOps<P>::NFQP;
     const StageArgs& s = ka.s;
     const Ops<P, float>& o = ka.o;
     const LiftOps<P, float>& L = ka.l;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float* sOp = reinterpret_cast<float*>(smem_raw);                 // NbrOps, 16-byte rows
-    constexpr int OPF = (VISC ? 3 : 1) * 3 * NP * NFQP;
-    float* sU = sOp + OPF;                                           // [TILE][STR]
 
-    const int e0 = blockIdx.x * TILE;
+    const int e0 = tile * TILE;
     const int nloc = min(TILE, s.ne - e0);
     const int tl = threadIdx.x;
     const int el = stage_elem(tl);
     const bool active = el < nloc;
     const int e = e0 + el;
-
-    {   // operators for neighbour traces
-        const float* src = &ka.nb.phi[0][0][0];
-        for (int k = tl; k < OPF; k += TILE) sOp[k] = src[k];
-    }
     {   // stage state of the tile: uhi + d, 16-byte loads of one contiguous run
         const float4* uh = reinterpret_cast<const float4*>(s.uhi + (size_t)e0 * NB);
         const float4* dd = s.din ? reinterpret_cast<const float4*>(s.din + (size_t)e0 * NB) : nullptr;
@@ -120,6 +120,7 @@ __global__ void __launch_bounds__(TILE, stage_min_blocks(P, VISC)) stage_kernel(
         const float A00 = G.A[0], A01 = G.A[1], A10 = G.A[2], A11 = G.A[3];
         const float gamma = s.gamma, mu = s.mu, kappa = s.kappa;
         const float* Ue = sU + tl * STR;
+        if (s.dt_inst) sDt[tl] = s.dt_inst[__float_as_int(G.pad)];  // batched: per-instance dt
 
         // ---------------- volume (EulerWeakFormulation::volume_residual :72-115,
         //                  NavierStokesWeakFormulation::viscous_volume_residual :100-140)
@@ -358,23 +359,42 @@ __global__ void __launch_bounds__(TILE, stage_min_blocks(P, VISC)) stage_kernel(
     for (int g = tl; g < nloc * NB; g += TILE) {
         const int le = g / NB;
         const float du = sU[stage_row(le) * STR + (g - le * NB)];
+        const float dt = s.dt_inst ? sDt[stage_row(le)] : s.dt;
         if (s.stage == 1) {
-            s.dout[base + g] = s.dt * du;
+            s.dout[base + g] = dt * du;
         } else if (s.stage == 2) {
-            s.dout[base + g] = 0.25f * (__ldg(s.din + base + g) + s.dt * du);
+            s.dout[base + g] = 0.25f * (__ldg(s.din + base + g) + dt * du);
         } else {
-            const float delta = (2.0f / 3.0f) * (__ldg(s.din + base + g) + s.dt * du);
+            const float delta = (2.0f / 3.0f) * (__ldg(s.din + base + g) + dt * du);
             const double r = s.u64[base + g] + (double)delta;
             s.u64[base + g] = r;
             s.uhi_out[base + g] = (float)r;
         }
     }
+    __syncthreads();  // the next tile reuses sU / sDt
+}
+
+// Persistent stage kernel: each CTA loads the neighbour-face operators once, then walks
+// the tiles with a grid stride.  The grid size is picked by the autotuner.
+template <int P, bool VISC, bool BND>
+__global__ void __launch_bounds__(TILE, stage_min_blocks(P, VISC)) stage_kernel(const __grid_constant__ SArgs<P, VISC> ka) {
+    constexpr int OPF = stage_op_floats<P, VISC>();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* sOp = reinterpret_cast<float*>(smem_raw);
+    float* sDt = sOp + OPF;
+    float* sU = sDt + TILE;
+    {
+        const float* src = &ka.nb.phi[0][0][0];
+        for (int k = threadIdx.x; k < OPF; k += TILE) sOp[k] = src[k];
+    }
+    __syncthreads();
+    const int ntiles = (ka.s.ne + TILE - 1) / TILE;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) stage_tile<P, VISC, BND>(ka, sOp, sU, sDt, t);
 }
 
 template <int P, bool VISC>
 inline size_t stage_smem_bytes() {
-    constexpr int OPF = (VISC ? 3 : 1) * 3 * n_basis(P) * NbrOps<P>::NFQP;
-    return (size_t)(OPF + TILE * stage_stride<P>()) * sizeof(float);
+    return (size_t)(stage_op_floats<P, VISC>() + TILE + TILE * stage_stride<P>()) * sizeof(float);
 }
 
 template <int P, typename T, bool VISC>
@@ -395,8 +415,9 @@ inline int launch_stage_t(const StageArgs& a, const OpsHost& oh, cudaStream_t st
     fill_ops<P, float>(oh, ka.o);
     fill_lift<P, float>(oh, ka.l);
     fill_nbr_ops<P>(oh, ka.nb);
-    const int grid = (a.ne + TILE - 1) / TILE;
-    if (grid == 0) return 0;
+    const int ntiles = (a.ne + TILE - 1) / TILE;
+    if (ntiles == 0) return 0;
+    const int grid = a.grid > 0 && a.grid < ntiles ? a.grid : ntiles;
     if (a.boundary)
         stage_kernel<P, VISC, true><<<grid, TILE, stage_smem_bytes<P, VISC>(), st>>>(ka);
     else

@@ -51,6 +51,7 @@ int configure_vjp_t() {
                                 (int)vjp_smem_bytes<P>()) == cudaSuccess ? 0 : -1;
 }
 
+// J: device buffer of (n_blocks + 1) doubles (partial sums, then the total in the last slot)
 template <int P>
 int launch_kinetic_t(const AdjArgs& a, const OpsHost& oh, double* J, double* grad, cudaStream_t st) {
     VArgs<P> ka;
@@ -58,6 +59,7 @@ int launch_kinetic_t(const AdjArgs& a, const OpsHost& oh, double* J, double* gra
     fill_ops<P, double>(oh, ka.o);
     const int grid = (a.ne + 127) / 128;
     kinetic_kernel<P><<<grid, 128, 0, st>>>(ka, J, grad);
+    if (J) kinetic_sum_kernel<<<1, 32, 0, st>>>(J, grid, J + grid);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -260,16 +262,23 @@ extern "C" int dgx_rk3_step_adjoint(dgx_ctx* c, const double* u_n, double* ubar,
 extern "C" int dgx_kinetic_energy(dgx_ctx* c, const double* u, double* J, double* grad, void* stream) {
     if (!c || (c->ne && !u)) return dgx::set_error(DGX_ERR_INVALID, "dgx_kinetic_energy: null argument");
     cudaStream_t s = (cudaStream_t)stream;
+    if (c->ne == 0) {
+        if (J) *J = 0.0;
+        return DGX_OK;
+    }
+    const int nblk = (c->ne + 127) / 128;
+    if (J && !c->d_kin) {
+        if (cudaMalloc((void**)&c->d_kin, sizeof(double) * (nblk + 1)) != cudaSuccess) {
+            cudaGetLastError();
+            return dgx::set_error(DGX_ERR_CUDA, "cudaMalloc failed for the objective reduction");
+        }
+    }
     AdjArgs a = base(c);
     a.u = u;
-    if (J) {
-        if (cudaMemsetAsync(c->d_mon, 0, sizeof(double), s) != cudaSuccess)
-            return dgx::set_error(DGX_ERR_CUDA, "memset failed");
-    }
-    if (c->ne && launch_kinetic(c->prm.order, a, c->ops, J ? c->d_mon : nullptr, grad, s))
+    if (launch_kinetic(c->prm.order, a, c->ops, J ? c->d_kin : nullptr, grad, s))
         return dgx::set_error(DGX_ERR_CUDA, "kinetic energy launch failed");
     if (J) {
-        if (cudaMemcpyAsync(J, c->d_mon, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        if (cudaMemcpyAsync(J, c->d_kin + nblk, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess)
             return dgx::set_error(DGX_ERR_CUDA, "kinetic energy read-back failed");
     }

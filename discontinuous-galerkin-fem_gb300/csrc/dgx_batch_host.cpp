@@ -1,0 +1,292 @@
+// Batched independent solves behind include/dgx.h's dgx_batch_* entry points.
+//
+// dgfem advances one mesh per solver object (CompressibleDGSolverBase::solve,
+// src/solver/compressible_solver_base.cpp:236-312); an ensemble is a loop over solver
+// objects.  Here an ensemble of mixed-precision Euler solves shares one device layout:
+// the instances of each order are concatenated into one element range (geometry in FP32
+// with the instance number in the spare slot, connectivity and boundary slots offset into
+// the range), every RK3 stage of every instance is one launch of the batched stage kernel
+// (dgx_batch.cu), and a step is a CUDA graph of three such launches.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dgx_context.h"
+
+using namespace dgx;
+
+namespace {
+struct Group {  // the instances of one order, concatenated
+    int ne = 0;
+    size_t nstate = 0;  // ne * np * 4
+    ElemGeomF* geomf = nullptr;
+    ElemConn* conn = nullptr;
+    BCSlot* bc = nullptr;
+    double* u = nullptr;                  // FP64 state of every instance of this order
+    float* uhi[2] = {nullptr, nullptr};   // FP32 copies of u^n, ping-ponged
+    float* d1 = nullptr;                  // FP32 stage increments
+    float* d2 = nullptr;
+};
+}  // namespace
+
+struct dgx_batch {
+    int device = 0;
+    int n_inst = 0;
+    dgx_params prm{};
+    Group grp[MAX_P];
+    OpsHost ops[MAX_P] = {};                         // reference operators of each order present
+    std::vector<int> inst_order, inst_e0, inst_ne;  // per instance: order, first element in its group, elements
+    float* d_dt = nullptr;                           // per-instance time step (FP32, as the stage arithmetic)
+    std::vector<float> dt_uploaded;
+    int boundary = 0;
+    int grid = 0;  // stage-kernel grid picked by the autotuner (0: not yet)
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t graph = nullptr;   // two steps
+    cudaGraphExec_t graph1 = nullptr;  // one step
+};
+
+static void free_batch(dgx_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->graph1) cudaGraphExecDestroy(b->graph1);
+    for (Group& g : b->grp) {
+        cudaFree(g.geomf);
+        cudaFree(g.conn);
+        cudaFree(g.bc);
+        cudaFree(g.u);
+        cudaFree(g.uhi[0]);
+        cudaFree(g.uhi[1]);
+        cudaFree(g.d1);
+        cudaFree(g.d2);
+    }
+    cudaFree(b->d_dt);
+    if (b->cap) cudaStreamDestroy(b->cap);
+    delete b;
+}
+
+extern "C" void dgx_batch_destroy(dgx_batch* b) { free_batch(b); }
+
+extern "C" int dgx_batch_create(int n_inst, const dgx_mesh* const* meshes, const dgx_params* params, dgx_batch** out) {
+    if (!out) return set_error(DGX_ERR_INVALID, "dgx_batch_create: null argument");
+    *out = nullptr;
+    if (n_inst < 1 || !meshes || !params) return set_error(DGX_ERR_INVALID, "dgx_batch_create: no instances");
+    const dgx_params& p0 = params[0];
+    for (int i = 0; i < n_inst; ++i) {
+        const dgx_params& p = params[i];
+        const std::string at = " (instance " + std::to_string(i) + ")";
+        if (!meshes[i]) return set_error(DGX_ERR_INVALID, "dgx_batch_create: null mesh" + at);
+        if (p.order < 1 || p.order > MAX_P)
+            return set_error(DGX_ERR_INVALID, "Element order must be between 1 and 4 for the GPU kernels" + at);
+        if (p.physics != DGX_EULER)
+            return set_error(DGX_ERR_INVALID, "batched solves cover the Euler equations" + at);
+        if (p.precision != DGX_MIXED)
+            return set_error(DGX_ERR_INVALID, "batched solves run in mixed precision" + at);
+        if (p.basis != p0.basis || p.gamma != p0.gamma)
+            return set_error(DGX_ERR_INVALID, "batched instances must share the basis and gamma" + at);
+        if (p.basis != DGX_BASIS_MONOMIAL && p.basis != DGX_BASIS_DUBINER)
+            return set_error(DGX_ERR_INVALID, "unknown basis" + at);
+    }
+    int dev = 0;
+    if (int rc = check_device(&dev)) return rc;
+    if (configure_batch_stage()) return set_error(DGX_ERR_CUDA, "could not configure the batched stage kernel");
+
+    auto* b = new dgx_batch;
+    b->device = dev;
+    b->n_inst = n_inst;
+    b->prm = p0;
+    b->inst_order.resize(n_inst);
+    b->inst_e0.resize(n_inst);
+    b->inst_ne.resize(n_inst);
+    bool have[MAX_P] = {};
+    for (int i = 0; i < n_inst; ++i) have[params[i].order - 1] = true;
+    for (int p = 1; p <= MAX_P; ++p)
+        if (have[p - 1] && make_ops(p, p0.basis, b->ops[p - 1])) {
+            free_batch(b);
+            return set_error(DGX_ERR_RUNTIME, "could not build reference operators");
+        }
+
+    // per order: concatenated FP32 geometry, connectivity and boundary slots
+    std::vector<ElemGeomF> gf[MAX_P];
+    std::vector<ElemConn> cn[MAX_P];
+    std::vector<BCSlot> bs[MAX_P];
+    for (int i = 0; i < n_inst; ++i) {
+        const int pi = params[i].order - 1;
+        HostGeometry hg;
+        if (int rc = build_geometry(meshes[i], b->ops[pi], hg)) {
+            free_batch(b);
+            return set_error(rc, std::string(dgx_last_error()) + " (instance " + std::to_string(i) + ")");
+        }
+        const int e0 = (int)gf[pi].size(), s0 = (int)bs[pi].size();
+        const int ne = (int)hg.geom.size();
+        b->inst_order[i] = pi + 1;
+        b->inst_e0[i] = e0;
+        b->inst_ne[i] = ne;
+        if (hg.boundary) b->boundary = 1;
+        for (int e = 0; e < ne; ++e) {
+            gf[pi].push_back(geom_to_f32(hg.geom[e], i));
+            ElemConn c = hg.conn[e];
+            for (int f = 0; f < 3; ++f) {
+                if (c.nbr[f] == NBR_SKIP) continue;
+                c.nbr[f] = c.nbr[f] >= 0 ? c.nbr[f] + e0 : c.nbr[f] - s0;  // -1 - slot -> -1 - (slot + s0)
+            }
+            cn[pi].push_back(c);
+        }
+        if (!hg.boundary) continue;
+        bs[pi].insert(bs[pi].end(), hg.slots.begin(), hg.slots.end());
+    }
+    auto up = [](void** dst, const void* src, size_t bytes) {
+        if (cudaMalloc(dst, bytes ? bytes : 16) != cudaSuccess) return false;
+        return !bytes || cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+    };
+    for (int p = 0; p < MAX_P; ++p) {
+        Group& g = b->grp[p];
+        g.ne = (int)gf[p].size();
+        if (g.ne == 0) continue;
+        if (bs[p].empty()) bs[p].push_back(BCSlot{});
+        g.nstate = (size_t)g.ne * n_basis(p + 1) * NV;
+        if (!up((void**)&g.geomf, gf[p].data(), gf[p].size() * sizeof(ElemGeomF)) ||
+            !up((void**)&g.conn, cn[p].data(), cn[p].size() * sizeof(ElemConn)) ||
+            !up((void**)&g.bc, bs[p].data(), bs[p].size() * sizeof(BCSlot)) ||
+            cudaMalloc((void**)&g.u, g.nstate * sizeof(double)) != cudaSuccess ||
+            cudaMemset(g.u, 0, g.nstate * sizeof(double)) != cudaSuccess ||
+            cudaMalloc((void**)&g.uhi[0], g.nstate * sizeof(float)) != cudaSuccess ||
+            cudaMalloc((void**)&g.uhi[1], g.nstate * sizeof(float)) != cudaSuccess ||
+            cudaMalloc((void**)&g.d1, g.nstate * sizeof(float)) != cudaSuccess ||
+            cudaMalloc((void**)&g.d2, g.nstate * sizeof(float)) != cudaSuccess) {
+            cudaGetLastError();
+            free_batch(b);
+            return set_error(DGX_ERR_CUDA, "cudaMalloc / upload failed for the batched state");
+        }
+    }
+    if (cudaMalloc((void**)&b->d_dt, n_inst * sizeof(float)) != cudaSuccess ||
+        cudaMemset(b->d_dt, 0, n_inst * sizeof(float)) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        free_batch(b);
+        return set_error(DGX_ERR_CUDA, "cudaMalloc failed for the batched time steps");
+    }
+    b->dt_uploaded.assign(n_inst, 0.0f);
+    *out = b;
+    return DGX_OK;
+}
+
+extern "C" int dgx_batch_info(const dgx_batch* b, int inst, int* ne, int* np, double** u) {
+    if (!b) return set_error(DGX_ERR_INVALID, "null batch");
+    if (inst < 0 || inst >= b->n_inst) return set_error(DGX_ERR_RANGE, "instance index out of range");
+    const int p = b->inst_order[inst];
+    if (ne) *ne = b->inst_ne[inst];
+    if (np) *np = n_basis(p);
+    if (u) *u = b->grp[p - 1].u + (size_t)b->inst_e0[inst] * n_basis(p) * NV;
+    return DGX_OK;
+}
+
+extern "C" int dgx_batch_launch_shape(const dgx_batch* b, int* grid, int* tiles) {
+    if (!b) return set_error(DGX_ERR_INVALID, "null batch");
+    int t = 0;
+    for (const Group& g : b->grp) t += (g.ne + TILE - 1) / TILE;
+    if (grid) *grid = b->grid;
+    if (tiles) *tiles = t;
+    return DGX_OK;
+}
+
+// Stage arguments of every order for one step reading uhi[src].
+static void batch_stage_args(const dgx_batch* b, int src, int stage, StageArgs* a) {
+    for (int p = 0; p < MAX_P; ++p) {
+        const Group& g = b->grp[p];
+        StageArgs& s = a[p];
+        s = StageArgs{};
+        s.ne = g.ne;
+        if (!g.ne) continue;
+        s.stage = stage;
+        s.uhi = g.uhi[src];
+        s.din = stage == 1 ? nullptr : stage == 2 ? g.d1 : g.d2;
+        s.dout = stage == 1 ? g.d1 : stage == 2 ? g.d2 : nullptr;
+        s.u64 = g.u;
+        s.uhi_out = g.uhi[1 - src];
+        s.geom = g.geomf;
+        s.conn = g.conn;
+        s.bc = g.bc;
+        s.dt = 0.0f;
+        s.gamma = (float)b->prm.gamma;
+        s.boundary = b->boundary;
+        s.dt_inst = b->d_dt;
+        s.grid = b->grid;
+    }
+}
+
+static int enqueue_batch_step(dgx_batch* b, int src, cudaStream_t s) {
+    for (int stage = 1; stage <= 3; ++stage) {
+        StageArgs a[MAX_P];
+        batch_stage_args(b, src, stage, a);
+        if (launch_batch_stage(a, b->ops, b->boundary, b->grid, s))
+            return set_error(DGX_ERR_CUDA, std::string("batched stage launch failed: ") +
+                                               cudaGetErrorString(cudaGetLastError()));
+    }
+    return DGX_OK;
+}
+
+static int capture_batch(dgx_batch* b, cudaGraphExec_t* out, int steps) {
+    cudaGraph_t g;
+    if (cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return set_error(DGX_ERR_CUDA, "graph capture could not start");
+    int rc = DGX_OK;
+    for (int k = 0; k < steps && !rc; ++k) rc = enqueue_batch_step(b, k & 1, b->cap);
+    const cudaError_t ec = cudaStreamEndCapture(b->cap, &g);
+    if (rc) return rc;
+    if (ec != cudaSuccess) return set_error(DGX_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
+    const cudaError_t ei = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        *out = nullptr;
+        return set_error(DGX_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+    }
+    return DGX_OK;
+}
+
+extern "C" int dgx_batch_rk3_step(dgx_batch* b, const double* dt, int n_steps, void* stream) {
+    if (!b || !dt || n_steps < 0) return set_error(DGX_ERR_INVALID, "dgx_batch_rk3_step: bad argument");
+    for (int i = 0; i < b->n_inst; ++i)
+        if (!(dt[i] > 0.0) || !std::isfinite(dt[i]))
+            return set_error(DGX_ERR_INVALID, "dgx_batch_rk3_step: time step of instance " + std::to_string(i) +
+                                                  " must be positive and finite");
+    if (n_steps == 0) return DGX_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<float> dtf(b->n_inst);
+    for (int i = 0; i < b->n_inst; ++i) dtf[i] = (float)dt[i];
+    if (dtf != b->dt_uploaded) {  // pageable source: the copy has read it when the call returns
+        if (cudaMemcpyAsync(b->d_dt, dtf.data(), dtf.size() * sizeof(float), cudaMemcpyHostToDevice, s) != cudaSuccess)
+            return set_error(DGX_ERR_CUDA, "time-step upload failed");
+        b->dt_uploaded = dtf;
+    }
+    for (const Group& g : b->grp)
+        if (g.ne && launch_f64_to_f32(g.nstate, g.u, g.uhi[0], s))
+            return set_error(DGX_ERR_CUDA, "conversion launch failed");
+    if (b->grid == 0) {
+        // launch shape: timed on stage 1, which writes only the increment scratch
+        std::string key = "batch";
+        for (int p = 0; p < MAX_P; ++p) key += " p" + std::to_string(p + 1) + ":" + std::to_string(b->grp[p].ne);
+        if (b->boundary) key += " bnd";
+        StageArgs a[MAX_P];
+        batch_stage_args(b, 0, 1, a);
+        const OpsHost* ops = b->ops;
+        int grid = 0;
+        const int rc = tune_grid(key, grid_candidates(batch_tiles(a)), [&](int g, cudaStream_t ts) {
+            return launch_batch_stage(a, ops, b->boundary, g, ts);
+        }, s, &grid);
+        if (rc) return rc;
+        b->grid = grid;
+    }
+    if (!b->graph) {
+        int rc = capture_batch(b, &b->graph, 2);
+        if (!rc) rc = capture_batch(b, &b->graph1, 1);
+        if (rc) return rc;
+    }
+    for (int i = 0; i + 1 < n_steps; i += 2)
+        if (cudaGraphLaunch(b->graph, s) != cudaSuccess)
+            return set_error(DGX_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(cudaGetLastError()));
+    if ((n_steps & 1) && cudaGraphLaunch(b->graph1, s) != cudaSuccess)
+        return set_error(DGX_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(cudaGetLastError()));
+    return DGX_OK;
+}

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -33,9 +34,11 @@ struct dgx_ctx {
     int boundary = 0;  // some face is a boundary face or takes no part
     int has_slip_wall = 0;
     double* d_adj[3] = {nullptr, nullptr, nullptr};  // adjoint scratch (allocated on first use)
+    double* d_kin = nullptr;  // objective partial sums (allocated on first use)
     cudaStream_t cap = nullptr;  // capture stream
     cudaGraphExec_t graph = nullptr;   // one step (FP64) or two steps (mixed)
     cudaGraphExec_t graph1 = nullptr;  // mixed: one step
+    int stage_grid = 0;  // mixed: stage-kernel grid picked by the autotuner (0: not yet)
     const double* graph_u = nullptr;
     double graph_dt = 0.0;
 };
@@ -43,4 +46,33 @@ struct dgx_ctx {
 namespace dgx {
 // Records the message returned by dgx_last_error() on this thread and returns `code`.
 int set_error(int code, const std::string& msg);
+
+// Reference operators of order p in the given basis (returns nonzero on failure).
+int make_ops(int p, int basis, OpsHost& o);
+
+// Host copy of a mesh's device geometry: per-element affine map, face normals and lengths,
+// face connectivity, boundary-condition slots and the physical volume quadrature points.
+struct HostGeometry {
+    std::vector<ElemGeom> geom;
+    std::vector<ElemConn> conn;
+    std::vector<BCSlot> slots;
+    std::vector<double> xq;
+    int boundary = 0;       // some face is a boundary face or takes no part
+    int has_slip_wall = 0;
+};
+// Returns a DGX status code; on failure the message is set for dgx_last_error().
+int build_geometry(const dgx_mesh* m, const OpsHost& ops, HostGeometry& g);
+// FP32 rounding of an element's geometry; `instance` is stored in the spare slot.
+ElemGeomF geom_to_f32(const ElemGeom& g, int instance);
+// Checks that a CUDA device of compute capability 10.3 is current; returns its ordinal.
+int check_device(int* dev);
+
+// Autotuner (dgx_tune.cpp): launch(grid, stream) enqueues one kernel launch with that grid.
+using GridLaunch = std::function<int(int grid, cudaStream_t s)>;
+// Candidate persistent grid sizes for a kernel over `ntiles` tiles: ntiles first (one CTA
+// per tile), then the multiples of the SM count below it.
+std::vector<int> grid_candidates(int ntiles);
+// Picks the fastest candidate grid by timing on stream s (cached per key).
+int tune_grid(const std::string& key, const std::vector<int>& candidates, const GridLaunch& launch, cudaStream_t s,
+              int* best);
 }  // namespace dgx

@@ -159,7 +159,7 @@ static bool invert(int n, const double* A, double* X) {  // Gauss-Jordan, partia
 // DGSpace ctor + precompute_basis_values (src/core/space.cpp:20-67, 230-257) and the
 // reference mass matrix of TimeDependentWeakFormulation::compute_mass_integral
 // (src/weak_forms/weak_formulation_base.cpp:198-217) divided by |J|.
-static int make_ops(int p, int basis, OpsHost& o) {
+int dgx::make_ops(int p, int basis, OpsHost& o) {
     std::memset(&o, 0, sizeof(o));
     const int order = 2 * p;
     if (order > DGX_TRI_MAX_ORDER || p + 1 > DGX_GL_MAX_POINTS) return -1;
@@ -551,6 +551,7 @@ static void free_ctx(dgx_ctx* c) {
     if (c->graph) cudaGraphExecDestroy(c->graph);
     if (c->graph1) cudaGraphExecDestroy(c->graph1);
     for (double* a : c->d_adj) cudaFree(a);
+    cudaFree(c->d_kin);
     cudaFree(c->d_uhi[0]);
     cudaFree(c->d_uhi[1]);
     cudaFree(c->d_d1);
@@ -571,6 +572,143 @@ static void free_ctx(dgx_ctx* c) {
 
 extern "C" void dgx_destroy(dgx_ctx* c) { free_ctx(c); }
 
+// Element geometry, face slots and boundary-condition slots of a mesh:
+// DGSpace::compute_element_data / compute_face_data (src/core/space.cpp:69-171).
+int dgx::build_geometry(const dgx_mesh* m, const OpsHost& ops, HostGeometry& g) {
+    const int ne = m->ne();
+    g.geom.assign(ne, ElemGeom{});
+    g.conn.assign(ne, ElemConn{});
+    g.slots.clear();
+    g.boundary = g.has_slip_wall = 0;
+    std::vector<ElemGeom>& geom = g.geom;
+    std::vector<ElemConn>& conn = g.conn;
+    std::vector<BCSlot>& slots = g.slots;
+    std::vector<double> fn((size_t)ne * 6), fl((size_t)ne * 3);
+    g.xq.resize((size_t)ne * ops.nq * 2);
+    for (int e = 0; e < ne; ++e) {
+        double V[6], A[4], det;
+        elem_verts(m, e, V);
+        if (!affine_map(V, A, &det)) {
+            return fail(DGX_ERR_RUNTIME, "Singular Jacobian matrix");
+        }
+        ElemGeom& ge = geom[e];
+        std::memset(&ge, 0, sizeof(ge));
+        for (int k = 0; k < 4; ++k) ge.A[k] = A[k];
+        ge.detJ = std::fabs(det);
+        double h = std::numeric_limits<double>::max();
+        for (int i = 0; i < 3; ++i)
+            for (int j = i + 1; j < 3; ++j)
+                h = std::min(h, std::sqrt((V[2 * i] - V[2 * j]) * (V[2 * i] - V[2 * j]) +
+                                          (V[2 * i + 1] - V[2 * j + 1]) * (V[2 * i + 1] - V[2 * j + 1])));
+        ge.pad[0] = h;
+        for (int f = 0; f < 3; ++f) {
+            if (!face_geom(V, f, &fn[6 * (size_t)e + 2 * f], &fl[3 * (size_t)e + f])) {
+                    return fail(DGX_ERR_RUNTIME, "Degenerate edge detected");
+            }
+            conn[e].nbr[f] = NBR_SKIP;
+        }
+        conn[e].flags = 0;
+        for (int q = 0; q < ops.nq; ++q) {  // map_to_physical: V^T N
+            const double xi = ops.qp[q][0], eta = ops.qp[q][1];
+            const double N0 = 1.0 - xi - eta;
+            g.xq[((size_t)e * ops.nq + q) * 2] = N0 * V[0] + xi * V[2] + eta * V[4];
+            g.xq[((size_t)e * ops.nq + q) * 2 + 1] = N0 * V[1] + xi * V[3] + eta * V[5];
+        }
+    }
+    std::vector<char> taken((size_t)ne * 3, 0);
+    auto take = [&](int e, int f) {
+        if (taken[3 * (size_t)e + f]) return false;
+        taken[3 * (size_t)e + f] = 1;
+        return true;
+    };
+    const int nif = (int)m->ifaces.size() / 5;
+    for (int k = 0; k < nif; ++k) {
+        const int* F = &m->ifaces[5 * (size_t)k];
+        const int L = F[0], R = F[1], fL = F[2], fR = F[3], rev = F[4];
+        if (!take(L, fL) || !take(R, fR)) {
+            return fail(DGX_ERR_RUNTIME, "unsupported mesh topology: an element face appears in two interior faces");
+        }
+        const double* nL = &fn[6 * (size_t)L + 2 * fL];
+        const double hL = fl[3 * (size_t)L + fL];
+        geom[L].n[fL][0] = nL[0];
+        geom[L].n[fL][1] = nL[1];
+        geom[L].h[fL] = hL;
+        geom[R].n[fR][0] = -nL[0];
+        geom[R].n[fR][1] = -nL[1];
+        geom[R].h[fR] = hL;
+        conn[L].nbr[fL] = R;
+        conn[L].flags |= (fR | (rev << 2) | (1 << 3)) << (4 * fL);
+        conn[R].nbr[fR] = L;
+        conn[R].flags |= (fL | (rev << 2)) << (4 * fR);
+    }
+    std::map<int, int> slot_of_tag;
+    const int nbf = (int)m->bfaces.size() / 3;
+    for (int k = 0; k < nbf; ++k) {
+        const int e = m->bfaces[3 * (size_t)k], f = m->bfaces[3 * (size_t)k + 1], tag = m->bfaces[3 * (size_t)k + 2];
+        geom[e].n[f][0] = fn[6 * (size_t)e + 2 * f];
+        geom[e].n[f][1] = fn[6 * (size_t)e + 2 * f + 1];
+        geom[e].h[f] = fl[3 * (size_t)e + f];
+        auto it = m->bcs.find(tag);
+        if (tag < 0 || it == m->bcs.end()) continue;  // no BC: dgfem skips the face
+        if (it->second.type == DGX_BC_PERIODIC) {
+            return fail(DGX_ERR_RUNTIME, "PERIODIC BC encountered in boundary_face_residual - periodic "
+                                         "boundaries should be treated as interior faces");
+        }
+        auto si = slot_of_tag.find(tag);
+        int slot;
+        if (si == slot_of_tag.end()) {
+            if ((int)slots.size() >= MAX_BC) {
+                    return fail(DGX_ERR_RUNTIME, "too many boundary tags with conditions");
+            }
+            BCSlot b{};
+            b.type = it->second.type;
+            if (b.type == DGX_BC_SLIP_WALL) g.has_slip_wall = 1;
+            for (int v = 0; v < 4; ++v) b.value[v] = it->second.value[v];
+            slot = (int)slots.size();
+            slots.push_back(b);
+            slot_of_tag[tag] = slot;
+        } else {
+            slot = si->second;
+        }
+        conn[e].nbr[f] = -1 - slot;
+        conn[e].flags |= (1 << 3) << (4 * f);
+    }
+    for (int e = 0; e < ne && !g.boundary; ++e)
+        for (int f = 0; f < 3; ++f)
+            if (conn[e].nbr[f] < 0) g.boundary = 1;
+    if (slots.empty()) slots.push_back(BCSlot{});
+    return DGX_OK;
+}
+
+ElemGeomF dgx::geom_to_f32(const ElemGeom& g, int instance) {
+    ElemGeomF h;
+    for (int k = 0; k < 4; ++k) h.A[k] = (float)g.A[k];
+    h.detJ = (float)g.detJ;
+    for (int f = 0; f < 3; ++f) {
+        h.h[f] = (float)g.h[f];
+        h.n[f][0] = (float)g.n[f][0];
+        h.n[f][1] = (float)g.n[f][1];
+    }
+    h.hmin = (float)g.pad[0];
+    std::memcpy(&h.pad, &instance, sizeof(float));  // batched solves: the element's instance
+    return h;
+}
+
+int dgx::check_device(int* dev) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(DGX_ERR_CUDA, "no CUDA device: the dgx path has no CPU fallback");
+    }
+    CUDA_OK(cudaGetDevice(dev));
+    cudaDeviceProp prop;
+    CUDA_OK(cudaGetDeviceProperties(&prop, *dev));
+    if (prop.major != 10 || prop.minor != 3)
+        return fail(DGX_ERR_CUDA, "dgx kernels are built for sm_103a; this device is sm_" +
+                                      std::to_string(prop.major) + std::to_string(prop.minor));
+    return DGX_OK;
+}
+
 extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out) {
     if (!m || !p || !out) return fail(DGX_ERR_INVALID, "dgx_create: null argument");
     *out = nullptr;
@@ -587,18 +725,8 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
         if (p->prandtl <= 0.0) return fail(DGX_ERR_INVALID, "Prandtl number must be positive for Navier-Stokes weak formulation");
         if (p->sigma0 <= 0.0) return fail(DGX_ERR_INVALID, "Penalty prefactor must be positive for Navier-Stokes weak formulation");
     }
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
-        cudaGetLastError();
-        return fail(DGX_ERR_CUDA, "no CUDA device: the dgx path has no CPU fallback");
-    }
     int dev = 0;
-    CUDA_OK(cudaGetDevice(&dev));
-    cudaDeviceProp prop;
-    CUDA_OK(cudaGetDeviceProperties(&prop, dev));
-    if (prop.major != 10 || prop.minor != 3)
-        return fail(DGX_ERR_CUDA, "dgx kernels are built for sm_103a; this device is sm_" +
-                                      std::to_string(prop.major) + std::to_string(prop.minor));
+    if (int rc = check_device(&dev)) return rc;
 
     {
         const bool visc = p->physics == DGX_NAVIER_STOKES;
@@ -627,109 +755,17 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
     c->nfq = c->ops.nfq;
     c->nstate = (size_t)ne * c->np * NV;
 
-    // geometry: DGSpace::compute_element_data / compute_face_data (space.cpp:69-171)
-    std::vector<ElemGeom> geom(ne);
-    std::vector<ElemConn> conn(ne);
-    std::vector<double> fn((size_t)ne * 6), fl((size_t)ne * 3);
-    c->xq.resize((size_t)ne * c->nq * 2);
-    for (int e = 0; e < ne; ++e) {
-        double V[6], A[4], det;
-        elem_verts(m, e, V);
-        if (!affine_map(V, A, &det)) {
-            free_ctx(c);
-            return fail(DGX_ERR_RUNTIME, "Singular Jacobian matrix");
-        }
-        ElemGeom& g = geom[e];
-        std::memset(&g, 0, sizeof(g));
-        for (int k = 0; k < 4; ++k) g.A[k] = A[k];
-        g.detJ = std::fabs(det);
-        double h = std::numeric_limits<double>::max();
-        for (int i = 0; i < 3; ++i)
-            for (int j = i + 1; j < 3; ++j)
-                h = std::min(h, std::sqrt((V[2 * i] - V[2 * j]) * (V[2 * i] - V[2 * j]) +
-                                          (V[2 * i + 1] - V[2 * j + 1]) * (V[2 * i + 1] - V[2 * j + 1])));
-        g.pad[0] = h;
-        for (int f = 0; f < 3; ++f) {
-            if (!face_geom(V, f, &fn[6 * (size_t)e + 2 * f], &fl[3 * (size_t)e + f])) {
-                free_ctx(c);
-                return fail(DGX_ERR_RUNTIME, "Degenerate edge detected");
-            }
-            conn[e].nbr[f] = NBR_SKIP;
-        }
-        conn[e].flags = 0;
-        for (int q = 0; q < c->nq; ++q) {  // map_to_physical: V^T N
-            const double xi = c->ops.qp[q][0], eta = c->ops.qp[q][1];
-            const double N0 = 1.0 - xi - eta;
-            c->xq[((size_t)e * c->nq + q) * 2] = N0 * V[0] + xi * V[2] + eta * V[4];
-            c->xq[((size_t)e * c->nq + q) * 2 + 1] = N0 * V[1] + xi * V[3] + eta * V[5];
-        }
+    HostGeometry hg;
+    if (int rc = build_geometry(m, c->ops, hg)) {
+        free_ctx(c);
+        return rc;
     }
-    std::vector<char> taken((size_t)ne * 3, 0);
-    auto take = [&](int e, int f) {
-        if (taken[3 * (size_t)e + f]) return false;
-        taken[3 * (size_t)e + f] = 1;
-        return true;
-    };
-    const int nif = (int)m->ifaces.size() / 5;
-    for (int k = 0; k < nif; ++k) {
-        const int* F = &m->ifaces[5 * (size_t)k];
-        const int L = F[0], R = F[1], fL = F[2], fR = F[3], rev = F[4];
-        if (!take(L, fL) || !take(R, fR)) {
-            free_ctx(c);
-            return fail(DGX_ERR_RUNTIME, "unsupported mesh topology: an element face appears in two interior faces");
-        }
-        const double* nL = &fn[6 * (size_t)L + 2 * fL];
-        const double hL = fl[3 * (size_t)L + fL];
-        geom[L].n[fL][0] = nL[0];
-        geom[L].n[fL][1] = nL[1];
-        geom[L].h[fL] = hL;
-        geom[R].n[fR][0] = -nL[0];
-        geom[R].n[fR][1] = -nL[1];
-        geom[R].h[fR] = hL;
-        conn[L].nbr[fL] = R;
-        conn[L].flags |= (fR | (rev << 2) | (1 << 3)) << (4 * fL);
-        conn[R].nbr[fR] = L;
-        conn[R].flags |= (fL | (rev << 2)) << (4 * fR);
-    }
-    std::vector<BCSlot> slots;
-    std::map<int, int> slot_of_tag;
-    const int nbf = (int)m->bfaces.size() / 3;
-    for (int k = 0; k < nbf; ++k) {
-        const int e = m->bfaces[3 * (size_t)k], f = m->bfaces[3 * (size_t)k + 1], tag = m->bfaces[3 * (size_t)k + 2];
-        geom[e].n[f][0] = fn[6 * (size_t)e + 2 * f];
-        geom[e].n[f][1] = fn[6 * (size_t)e + 2 * f + 1];
-        geom[e].h[f] = fl[3 * (size_t)e + f];
-        auto it = m->bcs.find(tag);
-        if (tag < 0 || it == m->bcs.end()) continue;  // no BC: dgfem skips the face
-        if (it->second.type == DGX_BC_PERIODIC) {
-            free_ctx(c);
-            return fail(DGX_ERR_RUNTIME, "PERIODIC BC encountered in boundary_face_residual - periodic "
-                                         "boundaries should be treated as interior faces");
-        }
-        auto si = slot_of_tag.find(tag);
-        int slot;
-        if (si == slot_of_tag.end()) {
-            if ((int)slots.size() >= MAX_BC) {
-                free_ctx(c);
-                return fail(DGX_ERR_RUNTIME, "too many boundary tags with conditions");
-            }
-            BCSlot b{};
-            b.type = it->second.type;
-            if (b.type == DGX_BC_SLIP_WALL) c->has_slip_wall = 1;
-            for (int v = 0; v < 4; ++v) b.value[v] = it->second.value[v];
-            slot = (int)slots.size();
-            slots.push_back(b);
-            slot_of_tag[tag] = slot;
-        } else {
-            slot = si->second;
-        }
-        conn[e].nbr[f] = -1 - slot;
-        conn[e].flags |= (1 << 3) << (4 * f);
-    }
-    for (int e = 0; e < ne && !c->boundary; ++e)
-        for (int f = 0; f < 3; ++f)
-            if (conn[e].nbr[f] < 0) c->boundary = 1;
-    if (slots.empty()) slots.push_back(BCSlot{});
+    std::vector<ElemGeom>& geom = hg.geom;
+    std::vector<ElemConn>& conn = hg.conn;
+    std::vector<BCSlot>& slots = hg.slots;
+    c->xq = std::move(hg.xq);
+    c->boundary = hg.boundary;
+    c->has_slip_wall = hg.has_slip_wall;
 
     auto alloc = [&](void** ptr, size_t bytes) {
         return cudaMalloc(ptr, bytes ? bytes : 16) == cudaSuccess;
@@ -750,19 +786,7 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
     }
     if (p->precision == DGX_MIXED) {
         std::vector<ElemGeomF> gf(ne);
-        for (int e = 0; e < ne; ++e) {
-            const ElemGeom& g = geom[e];
-            ElemGeomF& h = gf[e];
-            for (int k = 0; k < 4; ++k) h.A[k] = (float)g.A[k];
-            h.detJ = (float)g.detJ;
-            for (int f = 0; f < 3; ++f) {
-                h.h[f] = (float)g.h[f];
-                h.n[f][0] = (float)g.n[f][0];
-                h.n[f][1] = (float)g.n[f][1];
-            }
-            h.hmin = (float)g.pad[0];
-            h.pad = 0.0f;
-        }
+        for (int e = 0; e < ne; ++e) gf[e] = geom_to_f32(geom[e], 0);
         if (!alloc((void**)&c->d_geomf, sizeof(ElemGeomF) * ne) ||
             cudaMemcpy(c->d_geomf, gf.data(), sizeof(ElemGeomF) * ne, cudaMemcpyHostToDevice) != cudaSuccess) {
             cudaGetLastError();
@@ -779,6 +803,13 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
         return fail(DGX_ERR_CUDA, "device upload failed");
     }
     *out = c;
+    return DGX_OK;
+}
+
+extern "C" int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles) {
+    if (!c) return fail(DGX_ERR_INVALID, "null context");
+    if (grid) *grid = c->stage_grid;
+    if (tiles) *tiles = (c->ne + TILE - 1) / TILE;
     return DGX_OK;
 }
 
@@ -836,7 +867,7 @@ static int enqueue_rk3(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
 
 // Mixed precision: the three stages of one step, reading the FP32 copy uhi[src] of u^n
 // and writing the FP32 copy of u^{n+1} to uhi[1 - src] (see StageArgs).
-static int enqueue_rk3_mixed(dgx_ctx* c, double* u, double dt, int src, cudaStream_t s) {
+static StageArgs mixed_stage_args(const dgx_ctx* c, double* u, double dt, int src) {
     StageArgs a{};
     a.ne = c->ne;
     a.geom = c->d_geomf;
@@ -853,6 +884,12 @@ static int enqueue_rk3_mixed(dgx_ctx* c, double* u, double dt, int src, cudaStre
     a.uhi = c->d_uhi[src];
     a.u64 = u;
     a.uhi_out = c->d_uhi[1 - src];
+    a.grid = c->stage_grid;
+    return a;
+}
+
+static int enqueue_rk3_mixed(dgx_ctx* c, double* u, double dt, int src, cudaStream_t s) {
+    const StageArgs a = mixed_stage_args(c, u, dt, src);
     const bool visc = c->prm.physics == DGX_NAVIER_STOKES;
     const StageArgs s1 = [&] { StageArgs t = a; t.stage = 1; t.din = nullptr; t.dout = c->d_d1; return t; }();
     const StageArgs s2 = [&] { StageArgs t = a; t.stage = 2; t.din = c->d_d1; t.dout = c->d_d2; return t; }();
@@ -885,6 +922,27 @@ extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void*
     if (c->ne == 0 || n_steps == 0) return DGX_OK;
     cudaStream_t s = (cudaStream_t)stream;
     const bool mixed = c->prm.precision == DGX_MIXED;
+    // mixed: the FP32 copy of the caller's state, read by the first stage
+    if (mixed && launch_f64_to_f32(c->nstate, u, c->d_uhi[0], s)) return fail(DGX_ERR_CUDA, "conversion launch failed");
+    if (mixed && c->stage_grid == 0) {
+        // launch shape of the stage kernel: timed on stage 1, which writes only scratch
+        const StageArgs a = mixed_stage_args(c, u, dt, 0);
+        const bool visc = c->prm.physics == DGX_NAVIER_STOKES;
+        const std::string key = "stage p" + std::to_string(c->prm.order) + (visc ? " ns" : " euler") +
+                                (c->boundary ? " bnd" : "") + " ne" + std::to_string(c->ne);
+        int rc = tune_grid(key, grid_candidates((c->ne + TILE - 1) / TILE), [&](int grid, cudaStream_t ts) {
+            StageArgs t = a;
+            t.stage = 1;
+            t.din = nullptr;
+            t.dout = c->d_d1;
+            t.grid = grid;
+            return launch_stage_mixed(c->prm.order, visc, t, c->ops, ts);
+        }, s, &c->stage_grid);
+        if (rc) return rc;
+        if (c->graph) cudaGraphExecDestroy(c->graph);
+        if (c->graph1) cudaGraphExecDestroy(c->graph1);
+        c->graph = c->graph1 = nullptr;
+    }
     if (!c->graph || c->graph_u != u || c->graph_dt != dt) {
         if (c->graph) cudaGraphExecDestroy(c->graph);
         if (c->graph1) cudaGraphExecDestroy(c->graph1);
@@ -908,8 +966,7 @@ extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void*
         for (int i = 0; i < n_steps; ++i) CUDA_OK(cudaGraphLaunch(c->graph, s));
         return DGX_OK;
     }
-    // the FP32 copy of the caller's state, then pairs of steps and a last single step
-    if (launch_f64_to_f32(c->nstate, u, c->d_uhi[0], s)) return fail(DGX_ERR_CUDA, "conversion launch failed");
+    // pairs of steps and a last single step
     for (int i = 0; i + 1 < n_steps; i += 2) CUDA_OK(cudaGraphLaunch(c->graph, s));
     if (n_steps & 1) CUDA_OK(cudaGraphLaunch(c->graph1, s));
     return DGX_OK;

@@ -146,6 +146,8 @@ struct StageArgs {
     const BCSlot* bc;
     float dt, gamma, mu, kappa, sigma0;
     int boundary;       // 1 when some face is a boundary or skipped face
+    const float* dt_inst;  // batched solves: dt per instance, instance id in ElemGeomF::pad (else null)
+    int grid;           // persistent grid size (0: one CTA per tile)
 };
 
 
@@ -155,6 +157,11 @@ int launch_element_mixed(int p, bool viscous, const StepArgs& a, const OpsHost& 
 int configure_element_fp64(int p, bool viscous);
 int configure_element_mixed(int p, bool viscous);
 int launch_stage_mixed(int p, bool viscous, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
+// Batched solves (dgx_batch.cu): one launch of the stage over the element ranges of
+// orders 1..MAX_P (per_order[p-1], ne = 0 for an absent order), grid <= 0: one CTA per tile.
+int launch_batch_stage(const StageArgs* per_order, const OpsHost* ops, int boundary, int grid, cudaStream_t s);
+int batch_tiles(const StageArgs* per_order);
+int configure_batch_stage();
 
 // Small FP64 utility kernels (dgx_misc.cu).
 int launch_mass_inv(int ne, int p, const OpsHost& ops, const ElemGeom* geom, const double* in,

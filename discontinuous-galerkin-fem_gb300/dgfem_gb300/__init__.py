@@ -3,13 +3,13 @@ Navier-Stokes (drop-in for dgfem's DGAssembler / SSP-RK3 path).  The compute liv
 libdgx.so (include/dgx.h); this package is its Python front end."""
 
 from ._lib import DGXError, DGXInvalidArgument, DGXOutOfRange, LIB_PATH, load
-from .api import (BCTypeEuler, BoundaryConditionEuler, CompressibleDGSolverBase, DGAssembler,
+from .api import (BCTypeEuler, BoundaryConditionEuler, CompressibleDGSolverBase, DGAssembler, DGBatch,
                   DGContext, DGMesh, DGSpace, EulerDGSolver, EulerWeakFormulation,
                   NavierStokesDGSolver, NavierStokesWeakFormulation, conserved_to_primitive,
                   kinetic_energy, primitive_to_conserved, rk3_trajectory)
 
 __all__ = ["DGXError", "DGXInvalidArgument", "DGXOutOfRange", "LIB_PATH", "load",
-           "BCTypeEuler", "BoundaryConditionEuler", "CompressibleDGSolverBase", "DGAssembler",
+           "BCTypeEuler", "BoundaryConditionEuler", "CompressibleDGSolverBase", "DGAssembler", "DGBatch",
            "DGContext", "DGMesh", "DGSpace", "EulerDGSolver", "EulerWeakFormulation",
            "NavierStokesDGSolver", "NavierStokesWeakFormulation", "conserved_to_primitive",
            "primitive_to_conserved", "kinetic_energy", "rk3_trajectory"]

@@ -296,6 +296,12 @@ class DGContext:
         check(lib.dgx_rk3_step_host(self._h, _dptr(u), float(dt), int(n_steps)))
         return u
 
+    def launch_shape(self) -> Tuple[int, int]:
+        """(grid, tiles) of the mixed stage kernel; grid is 0 until the first rk3_step."""
+        g, t = C.c_int(), C.c_int()
+        check(L.load().dgx_launch_shape(self._h, C.byref(g), C.byref(t)))
+        return g.value, t.value
+
     def quad_points(self) -> np.ndarray:
         xq = np.zeros((self.n_elements, self.n_quad, 2))
         check(L.load().dgx_quad_points(self._h, _dptr(xq)))
@@ -367,6 +373,76 @@ class DGContext:
                                                    int(checkpoint_every), C.byref(J), self._dev(g),
                                                    _stream_of(u0)))
         return J.value, g
+
+
+class _DeviceArray:
+    """CUDA array interface over float64 device memory owned by a DGBatch (torch.as_tensor
+    wraps it without a copy; the tensor keeps this object, and so the batch, alive)."""
+
+    def __init__(self, owner, ptr: int, shape):
+        self._owner = owner
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": "<f8", "data": (int(ptr), False),
+                                         "version": 2, "strides": None}
+
+
+class DGBatch:
+    """Independent mixed-precision Euler solves advanced together (include/dgx.h dgx_batch_*).
+
+    ``meshes[i]`` and ``spaces[i]`` (order 1..4, one basis for all) define instance i; every
+    RK3 stage of every instance is one persistent kernel launch.  ``state(i)`` is a CUDA
+    float64 tensor view of instance i's state, shape (n_elements, n_basis, 4), owned by the
+    batch.  No counterpart in dgfem, where an ensemble is a loop over solver objects."""
+
+    def __init__(self, meshes: Sequence[DGMesh], spaces: Sequence[DGSpace],
+                 weak_form: Optional[EulerWeakFormulation] = None):
+        if len(meshes) != len(spaces) or not meshes:
+            raise ValueError("DGBatch needs one space per mesh and at least one instance")
+        wf = weak_form or EulerWeakFormulation()
+        if wf.has_viscous_terms():
+            raise ValueError("batched solves cover the Euler equations")
+        lib = L.load()
+        n = len(meshes)
+        prm = (L.Params * n)(*[L.Params(s.order, s.basis, L.EULER, L.MIXED, wf.gamma, 0.0, 0.0, 0.0)
+                                for s in spaces])
+        hs = (C.c_void_p * n)(*[m._h.value for m in meshes])
+        self._h = C.c_void_p()
+        check(lib.dgx_batch_create(n, hs, C.cast(prm, C.c_void_p), C.byref(self._h)))
+        self.n_instances = n
+        self.meshes, self.spaces, self.weak_form = list(meshes), list(spaces), wf
+        self.shapes = []
+        self._ptrs = []
+        for i in range(n):
+            ne, nb, ptr = C.c_int(), C.c_int(), C.c_void_p()
+            check(lib.dgx_batch_info(self._h, i, C.byref(ne), C.byref(nb), C.byref(ptr)))
+            self.shapes.append((ne.value, nb.value, 4))
+            self._ptrs.append(ptr.value)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            L.load().dgx_batch_destroy(h)
+            self._h = None
+
+    def state(self, i: int):
+        """Instance i's FP64 state as a CUDA tensor view (write initial states into it)."""
+        import torch
+        if not 0 <= i < self.n_instances:
+            raise IndexError("instance index out of range")
+        return torch.as_tensor(_DeviceArray(self, self._ptrs[i], self.shapes[i]), device="cuda")
+
+    def rk3_step(self, dt, n_steps: int = 1):
+        """n_steps SSP-RK3 steps of every instance on torch's current stream; dt is one step
+        for all instances or a sequence with one per instance."""
+        import torch
+        d = np.broadcast_to(np.asarray(dt, dtype=np.float64), (self.n_instances,)).copy()
+        stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        check(L.load().dgx_batch_rk3_step(self._h, _dptr(d), int(n_steps), stream))
+
+    def launch_shape(self) -> Tuple[int, int]:
+        """(grid, tiles) of the batched stage kernel; grid is 0 until the first step."""
+        g, t = C.c_int(), C.c_int()
+        check(L.load().dgx_batch_launch_shape(self._h, C.byref(g), C.byref(t)))
+        return g.value, t.value
 
 
 class DGAssembler:

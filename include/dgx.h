@@ -207,6 +207,37 @@ int dgx_kinetic_energy_gradient(dgx_ctx* c, const double* u0, double dt, int n_s
 #define DGX_STATIC_MAX_STATE (1 << 20)
 int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps, void* stream);
 
+/* ---------------------------------------------------------------- launch shape */
+
+/* The stage-kernel grid the autotuner picked for a mixed-precision context (CTAs; each
+ * walks the 128-element tiles with a grid stride) and the number of tiles.  grid is 0
+ * until the first dgx_rk3_step, which times the candidates (one CTA per tile, 1..8 CTAs
+ * per SM) on its stream.  Setting DGX_AUTOTUNE=0 in the environment skips the timing and
+ * takes one CTA per tile.  No counterpart in dgfem. */
+int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles);
+
+/* ---------------------------------------------------------------- batched solves */
+
+/* No counterpart in dgfem, where an ensemble is a loop over solver objects.  n_inst
+ * independent mixed-precision Euler solves, each on its own mesh and order (1..4, params[i]
+ * .order), advanced together: every SSP-RK3 stage of every instance is one persistent
+ * kernel launch, and dgx_batch_rk3_step replays CUDA graphs of those launches.  All
+ * instances share the basis and gamma (params[0]); other precisions and physics are
+ * rejected with DGX_ERR_INVALID.  Meshes are read at creation only. */
+typedef struct dgx_batch dgx_batch;
+int dgx_batch_create(int n_inst, const dgx_mesh* const* meshes, const dgx_params* params, dgx_batch** out);
+void dgx_batch_destroy(dgx_batch* b);
+/* Instance inst: element count, basis size and the device address of its FP64 state
+ * (n_elements * n_basis * 4 doubles, dgx_residual's layout).  The batch owns the state
+ * (zero after creation); callers write initial states there and read results back. */
+int dgx_batch_info(const dgx_batch* b, int inst, int* n_elements, int* n_basis, double** u);
+/* n_steps SSP-RK3 steps of every instance; dt: n_inst host doubles, > 0, instance i's
+ * step.  The first call times the launch shapes (see dgx_launch_shape) and captures the
+ * graphs; stream-ordered on `stream` after that. */
+int dgx_batch_rk3_step(dgx_batch* b, const double* dt, int n_steps, void* stream);
+/* The batched kernel's grid (0 until the first step) and its total number of tiles. */
+int dgx_batch_launch_shape(const dgx_batch* b, int* grid, int* tiles);
+
 #ifdef __cplusplus
 }
 #endif
