@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <functional>
@@ -730,8 +731,9 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
 
     {
         const bool visc = p->physics == DGX_NAVIER_STOKES;
-        const int rc = p->precision == DGX_MIXED ? configure_element_mixed(p->order, visc)
-                                                 : configure_element_fp64(p->order, visc);
+        int rc = p->precision == DGX_MIXED ? configure_element_mixed(p->order, visc)
+                                           : configure_element_fp64(p->order, visc);
+        if (!rc && p->precision == DGX_MIXED && !visc) rc = configure_stage_tc(p->order);
         if (rc) return fail(DGX_ERR_CUDA, "could not configure the element kernel");
     }
     auto* c = new dgx_ctx;
@@ -806,9 +808,10 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
     return DGX_OK;
 }
 
-extern "C" int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles) {
+extern "C" int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles, int* tensor_cores) {
     if (!c) return fail(DGX_ERR_INVALID, "null context");
-    if (grid) *grid = c->stage_grid;
+    if (grid) *grid = c->stage_grid & ~STAGE_TC;
+    if (tensor_cores) *tensor_cores = (c->stage_grid & STAGE_TC) ? 1 : 0;
     if (tiles) *tiles = (c->ne + TILE - 1) / TILE;
     return DGX_OK;
 }
@@ -928,9 +931,22 @@ extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void*
         // launch shape of the stage kernel: timed on stage 1, which writes only scratch
         const StageArgs a = mixed_stage_args(c, u, dt, 0);
         const bool visc = c->prm.physics == DGX_NAVIER_STOKES;
+        // candidates: the CUDA-core kernel at each grid, and the tensor-core kernel (Euler);
+        // DGX_STAGE_KERNEL=tc or =cuda restricts the choice to one of them
+        const int ntiles = (c->ne + TILE - 1) / TILE;
+        const char* mode = std::getenv("DGX_STAGE_KERNEL");
+        const bool only_tc = mode && std::strcmp(mode, "tc") == 0, only_cuda = mode && std::strcmp(mode, "cuda") == 0;
+        std::vector<int> cands;
+        if (!only_tc || visc) cands = grid_candidates(ntiles);
+        if (!visc && !only_cuda) {
+            int sms = 152;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+            cands.push_back(STAGE_TC | std::min(ntiles, sms * stage_tc_ctas_per_sm(c->prm.order)));
+        }
         const std::string key = "stage p" + std::to_string(c->prm.order) + (visc ? " ns" : " euler") +
-                                (c->boundary ? " bnd" : "") + " ne" + std::to_string(c->ne);
-        int rc = tune_grid(key, grid_candidates((c->ne + TILE - 1) / TILE), [&](int grid, cudaStream_t ts) {
+                                (c->boundary ? " bnd" : "") + " ne" + std::to_string(c->ne) +
+                                (only_tc ? " tc" : only_cuda ? " cuda" : "");
+        int rc = tune_grid(key, cands, [&](int grid, cudaStream_t ts) {
             StageArgs t = a;
             t.stage = 1;
             t.din = nullptr;

@@ -157,6 +157,12 @@ int launch_element_mixed(int p, bool viscous, const StepArgs& a, const OpsHost& 
 int configure_element_fp64(int p, bool viscous);
 int configure_element_mixed(int p, bool viscous);
 int launch_stage_mixed(int p, bool viscous, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
+// Tensor-core form of the mixed Euler stage (dgx_kernels_tc.cu).  A StageArgs::grid with
+// STAGE_TC set selects it; the low bits are its grid (<= 0: one CTA per tile).
+constexpr int STAGE_TC = 1 << 30;
+int launch_stage_tc(int p, const StageArgs& a, const OpsHost& ops, int grid, cudaStream_t s);
+int configure_stage_tc(int p);
+int stage_tc_ctas_per_sm(int p);
 // Batched solves (dgx_batch.cu): one launch of the stage over the element ranges of
 // orders 1..MAX_P (per_order[p-1], ne = 0 for an absent order), grid <= 0: one CTA per tile.
 int launch_batch_stage(const StageArgs* per_order, const OpsHost* ops, int boundary, int grid, cudaStream_t s);

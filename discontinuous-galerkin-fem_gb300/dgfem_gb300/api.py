@@ -296,11 +296,12 @@ class DGContext:
         check(lib.dgx_rk3_step_host(self._h, _dptr(u), float(dt), int(n_steps)))
         return u
 
-    def launch_shape(self) -> Tuple[int, int]:
-        """(grid, tiles) of the mixed stage kernel; grid is 0 until the first rk3_step."""
-        g, t = C.c_int(), C.c_int()
-        check(L.load().dgx_launch_shape(self._h, C.byref(g), C.byref(t)))
-        return g.value, t.value
+    def launch_shape(self) -> Tuple[int, int, bool]:
+        """(grid, tiles, tensor_cores) of the mixed stage kernel; grid is 0 until the first
+        rk3_step; tensor_cores is True for the 3xTF32 tcgen05 form."""
+        g, t, k = C.c_int(), C.c_int(), C.c_int()
+        check(L.load().dgx_launch_shape(self._h, C.byref(g), C.byref(t), C.byref(k)))
+        return g.value, t.value, bool(k.value)
 
     def quad_points(self) -> np.ndarray:
         xq = np.zeros((self.n_elements, self.n_quad, 2))

@@ -209,12 +209,14 @@ int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps, void* str
 
 /* ---------------------------------------------------------------- launch shape */
 
-/* The stage-kernel grid the autotuner picked for a mixed-precision context (CTAs; each
- * walks the 128-element tiles with a grid stride) and the number of tiles.  grid is 0
- * until the first dgx_rk3_step, which times the candidates (one CTA per tile, 1..8 CTAs
- * per SM) on its stream.  Setting DGX_AUTOTUNE=0 in the environment skips the timing and
- * takes one CTA per tile.  No counterpart in dgfem. */
-int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles);
+/* The stage kernel the autotuner picked for a mixed-precision context: its grid (CTAs;
+ * each walks the 128-element tiles with a grid stride), the number of tiles, and
+ * tensor_cores = 1 for the 3xTF32 tcgen05 form (Euler), 0 for the CUDA-core form.  grid is
+ * 0 until the first dgx_rk3_step, which times the candidates (CUDA cores at one CTA per
+ * tile and 1..8 CTAs per SM; tensor cores) on its stream.  Environment: DGX_AUTOTUNE=0
+ * skips the timing (CUDA cores, one CTA per tile); DGX_STAGE_KERNEL=tc or =cuda restricts
+ * the choice to one form.  No counterpart in dgfem. */
+int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles, int* tensor_cores);
 
 /* ---------------------------------------------------------------- batched solves */
 

@@ -136,7 +136,7 @@ def test_context_autotuner_and_switch(dg, monkeypatch):
     assert ctx.launch_shape()[0] == 0
     u = torch.tensor(u0, device="cuda")
     ctx.rk3_step(u, dt, 2)
-    grid, tiles = ctx.launch_shape()
+    grid, tiles, _ = ctx.launch_shape()
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     assert grid == tiles or (grid % sms == 0 and grid < tiles)
     ref = om.rk3_step(O.euler(1.4), u0, dt, 2)
@@ -147,5 +147,5 @@ def test_context_autotuner_and_switch(dg, monkeypatch):
     ctx2 = dg.DGContext(pm2, dg.DGSpace("triangle", 2, "dubiner"), dg.EulerWeakFormulation(1.4), "mixed")
     u2 = torch.tensor(om2.project(isentropic_vortex(om2.quad_points(), beta=3.0)), device="cuda")
     ctx2.rk3_step(u2, dt, 1)
-    g2, t2 = ctx2.launch_shape()
-    assert g2 == t2
+    g2, t2, tc2 = ctx2.launch_shape()
+    assert g2 == t2 and not tc2
