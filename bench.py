@@ -224,6 +224,31 @@ def run_reference(args, rank, ws):
     print(json.dumps(line), flush=True)
 
 
+def config1_leg(dg, torch):
+    """The plain-form workload: periodic [-5,5]^2, 16x16x2 = 512 triangles, Dubiner p=2,
+    beta = 5 vortex at the origin on the free stream (1, 0.5, 0, 1), CFL 0.1 (dgfem's
+    definition), 200 FP64 SSP-RK3 steps.  Reports the 512x6x4 state's norm and its relative
+    L2 error (coefficients; the Dubiner basis is orthonormal, so this is the L2 norm of the
+    field on this uniform mesh) against the exactly advected vortex."""
+    mesh = dg.DGMesh.rectangle(16, 16, -5.0, 5.0, -5.0, 5.0, periodic=True)
+    ctx = dg.DGContext(mesh, dg.DGSpace("triangle", 2, BASIS), dg.EulerWeakFormulation(GAMMA), "fp64")
+    xq = ctx.quad_points()
+    u = ctx.project(torch.tensor(vortex(xq), device="cuda"))
+    dt = 0.1 / ctx.max_cfl(u, 1.0)
+    ctx.rk3_step(u.clone(), dt, 3)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    ctx.rk3_step(u, dt, 200)
+    e1.record()
+    torch.cuda.synchronize()
+    exact = ctx.project(torch.tensor(vortex(xq, t=200 * dt), device="cuda"))
+    return {"workload": "euler_vortex_16x16x2_p2_dubiner_fp64_cfl0.1", "elements": ctx.n_elements,
+            "state_shape": list(u.shape), "dt": dt, "steps": 200, "ms_per_step": e0.elapsed_time(e1) / 200,
+            "state_l2_norm": float(torch.linalg.vector_norm(u)),
+            "l2_rel_err_vs_exact": float(torch.linalg.vector_norm(u - exact) / torch.linalg.vector_norm(exact))}
+
+
 def batch_leg(dg, torch, n_inst, steps, seed):
     """Independent periodic vortex solves on [-5,5]^2: N x N x 2 with N uniform in
     {16, 24, ..., 128}, p uniform in {2, 3}, beta ~ U(1,5), free stream u ~ U(0.2,0.8),
@@ -318,7 +343,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--cells", type=int, default=N_CELLS, help="quads per side (profiling cases)")
-    ap.add_argument("--ns-steps", type=int, default=20, help="timed steps of the Navier-Stokes leg (0: skip)")
+    ap.add_argument("--ns-steps", type=int, default=1000, help="steps of the Navier-Stokes leg (0: skip)")
     ap.add_argument("--adj-steps", type=int, default=1000, help="steps of the adjoint leg (0: skip)")
     ap.add_argument("--adj-dirs", type=int, default=16, help="finite-difference directions of the adjoint check")
     ap.add_argument("--batch-instances", type=int, default=256, help="instances of the batched leg (0: skip)")
@@ -380,6 +405,25 @@ def main():
         t_mx = timed(cmx, args.steps, args.warmup)
     clocks = clk.summary()
     t_mx = allreduce_max(t_mx, ws)
+    grid, tiles, on_tc = cmx.launch_shape()
+    # the tensor-core (3xTF32 tcgen05) form of the same stage, forced, timed the same way
+    os.environ["DGX_STAGE_KERNEL"] = "tc"
+    ctc = dg.DGContext(mesh, space, wf, "mixed")
+    t_tc = allreduce_max(timed(ctc, args.steps, args.warmup), ws)
+    del os.environ["DGX_STAGE_KERNEL"]
+    tc_acc = None
+    if args.acc_steps > 0:
+        u64 = u0.clone()
+        utc = u0.clone()
+        c64.rk3_step(u64, dt, args.acc_steps)
+        ctc.rk3_step(utc, dt, args.acc_steps)
+        torch.cuda.synchronize()
+        tc_acc = float(torch.linalg.vector_norm(utc - u64) / torch.linalg.vector_norm(u64))
+        del u64, utc
+    tensor_core = {"kernel": "dgx::stage_tc_kernel<3, no boundary> (3xTF32 tcgen05, TMEM accumulators)",
+                   "ms_per_step": 1e3 * t_tc / args.steps, "value": dof * 3 * args.steps * ws / t_tc,
+                   "vs_cuda_core_stage": t_tc / t_mx, "mixed_vs_fp64_l2_rel": tc_acc}
+    del ctc
     k64 = max(1, min(args.steps, 50))
     t_64 = allreduce_max(timed(c64, k64, min(args.warmup, 3)), ws)
     v_mx = dof * 3 * args.steps * ws / t_mx
@@ -518,6 +562,8 @@ def main():
                "tlm_directions": len(tlm_err), "tlm_max_rel_err": max(tlm_err) if tlm_err else None}
         del actx
 
+    cfg1 = config1_leg(dg, torch)
+
     bat = None
     if args.batch_instances > 0:
         bat = batch_leg(dg, torch, args.batch_instances, args.batch_steps, args.seed)
@@ -539,6 +585,9 @@ def main():
                 "config": {"workload": f"euler_vortex_{args.cells}x{args.cells}x2_p3_dubiner", "elements": ne, "order": ORDER,
                            "dof": dof, "dt": dt, "cfl": CFL, "l2": "inputs larger than L2 (168 MB state "
                            "+ two 168 MB stage buffers per context)", "parallelism": f"replicas x{ws}"},
+                "stage_kernel": {"form": "tensor cores" if on_tc else "cuda cores", "grid": grid, "tiles": tiles,
+                                 "picked_by": "autotuner (timed on the first step)"},
+                "tensor_core_form": tensor_core,
                 "fp64": {"value": v_64, "ms_per_step": 1e3 * t_64 / k64, "steps": k64},
                 "mixed_vs_fp64": v_mx / v_64,
                 "accuracy": acc,
@@ -546,6 +595,7 @@ def main():
                 "adjoint_forward_ratio": None if adj is None else adj["adjoint_step_vs_forward_step"],
                 "adjoint": adj,
                 "batched": bat,
+                "config1": cfg1,
                 "e2e": {"value": v_e2e, "unit": "DOF*stages/s", "h2d_bytes_per_step": dof * 8,
                         "d2h_bytes_per_step": dof * 8, "steps": ke},
                 "gpu_launches": 3 * args.steps,

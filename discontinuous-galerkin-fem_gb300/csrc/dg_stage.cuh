@@ -71,6 +71,64 @@ __host__ __device__ constexpr int stage_min_blocks(int p, bool visc) {
 #endif
 }
 
+// Stage combination of one tile in the increment form, 16-byte accesses:
+//   stage 1: dout = dt R;  stage 2: dout = (din + dt R) / 4;
+//   stage 3: u64 += 2/3 (din + dt R) (FP64), uhi_out = (float)u64.
+// R (M^-1-scaled residual) of local element le is row rowof(le) of sR; the loads of CH
+// consecutive float4 slots of a thread are issued before any of them is used.
+template <int NB, int STR, int THREADS, int CH, typename RowOf>
+__device__ __forceinline__ void stage_combine(const StageArgs& s, const float* sR, const float* sDt, int e0,
+                                              int nloc, RowOf rowof) {
+    constexpr int NB4 = NB / 4;
+    const int n4 = nloc * NB4;
+    const size_t b4 = (size_t)e0 * NB4;
+    const int t = threadIdx.x;
+    for (int g0 = t; g0 < n4; g0 += CH * THREADS) {
+        float4 dv[CH];
+        double2 ua[CH], ub[CH];
+#pragma unroll
+        for (int k = 0; k < CH; ++k) {
+            const int g = g0 + k * THREADS;
+            if (g < n4) {
+                if (s.stage >= 2) dv[k] = __ldg(reinterpret_cast<const float4*>(s.din) + b4 + g);
+                if (s.stage == 3) {
+                    ua[k] = reinterpret_cast<const double2*>(s.u64)[2 * (b4 + g)];
+                    ub[k] = reinterpret_cast<const double2*>(s.u64)[2 * (b4 + g) + 1];
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < CH; ++k) {
+            const int g = g0 + k * THREADS;
+            if (g >= n4) break;
+            const int le = g / NB4, c = 4 * (g - le * NB4);
+            const int row = rowof(le);
+            const float4 du = *reinterpret_cast<const float4*>(sR + row * STR + c);
+            const float dt = s.dt_inst ? sDt[row] : s.dt;
+            if (s.stage == 1) {
+                reinterpret_cast<float4*>(s.dout)[b4 + g] = make_float4(dt * du.x, dt * du.y, dt * du.z, dt * du.w);
+            } else if (s.stage == 2) {
+                reinterpret_cast<float4*>(s.dout)[b4 + g] =
+                    make_float4(0.25f * (dv[k].x + dt * du.x), 0.25f * (dv[k].y + dt * du.y),
+                                0.25f * (dv[k].z + dt * du.z), 0.25f * (dv[k].w + dt * du.w));
+            } else {
+                const float d0 = (2.0f / 3.0f) * (dv[k].x + dt * du.x), d1 = (2.0f / 3.0f) * (dv[k].y + dt * du.y);
+                const float d2 = (2.0f / 3.0f) * (dv[k].z + dt * du.z), d3 = (2.0f / 3.0f) * (dv[k].w + dt * du.w);
+                const double2 ra = make_double2(ua[k].x + (double)d0, ua[k].y + (double)d1);
+                const double2 rb = make_double2(ub[k].x + (double)d2, ub[k].y + (double)d3);
+                reinterpret_cast<double2*>(s.u64)[2 * (b4 + g)] = ra;
+                reinterpret_cast<double2*>(s.u64)[2 * (b4 + g) + 1] = rb;
+                reinterpret_cast<float4*>(s.uhi_out)[b4 + g] = make_float4((float)ra.x, (float)ra.y, (float)rb.x, (float)rb.y);
+            }
+        }
+    }
+}
+
+// hint: bring [p, p + bytes) into L2 (bulk async prefetch; 16-byte aligned, bytes % 16 == 0)
+__device__ __forceinline__ void prefetch_l2_bulk(const void* p, unsigned bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(bytes) : "memory");
+}
+
 // Floats of shared memory the neighbour-face operators take (16-byte rows).
 template <int P, bool VISC>
 __host__ __device__ constexpr int stage_op_floats() {
@@ -94,6 +152,8 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
     const int el = stage_elem(tl);
     const bool active = el < nloc;
     const int e = e0 + el;
+    if (tl == 0 && s.stage == 3)  // the FP64 state is read back in the stage combination
+        prefetch_l2_bulk(s.u64 + (size_t)e0 * NB, (unsigned)(nloc * NB * sizeof(double)));
     {   // stage state of the tile: uhi + d, 16-byte loads of one contiguous run
         const float4* uh = reinterpret_cast<const float4*>(s.uhi + (size_t)e0 * NB);
         const float4* dd = s.din ? reinterpret_cast<const float4*>(s.din + (size_t)e0 * NB) : nullptr;

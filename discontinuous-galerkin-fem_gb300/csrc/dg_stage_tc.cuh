@@ -70,12 +70,56 @@ __host__ __device__ constexpr int tc_smem_floats() {
 
 static __device__ int g_tc_timeout;  // set when a bounded mbarrier wait gave up (never expected)
 
-// H' = -(w_j h_F / (2|J|)) * numerical flux at the points of face f, written to A2 (hi, lo)
+// Traces of face f's neighbour at this face's points, from the neighbour's coefficients
+// (independent of GEMM1, so they are formed while it runs).
 template <int P, bool BND>
-__device__ __forceinline__ void tc_face(const TArgs<P>& ka, const float* sOp, uint32_t tl, const ElemGeomF& G,
-                                        const ElemConn& C, int f) {
+__device__ __forceinline__ void tc_face_nbr(const TArgs<P>& ka, const float* sOp, const ElemConn& C, int f,
+                                            float (&Un)[P + 1][4]) {
     using S = TcShape<P>;
     constexpr int NP = S::NP, NFQ = S::NFQ, NB = S::NB, NFQP = NbrOps<P>::NFQP;
+    const StageArgs& s = ka.s;
+#pragma unroll
+    for (int k = 0; k < NFQ; ++k)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) Un[k][v] = 0.f;
+    const int nb = C.nbr[f];
+    if (BND && nb < 0) return;
+    const int fl = (C.flags >> (4 * f)) & 15;
+    const int nf = fl & 3;
+    const bool rev = (fl >> 2) & 1;
+    const float* op = sOp + nf * NP * NFQP;
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+        float c[4];
+        load_row_f32<NB>(s.uhi, s.din, nb, i, c);
+        float w[NFQP];
+#pragma unroll
+        for (int k4 = 0; k4 < NFQP; k4 += 4) {
+            const float4 t = *reinterpret_cast<const float4*>(op + i * NFQP + k4);
+            w[k4] = t.x; w[k4 + 1] = t.y; w[k4 + 2] = t.z; w[k4 + 3] = t.w;
+        }
+#pragma unroll
+        for (int k = 0; k < NFQ; ++k)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) Un[k][v] = fmaf(w[k], c[v], Un[k][v]);
+    }
+#pragma unroll
+    for (int j = 0; j < NFQ / 2; ++j)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            const float a = Un[j][v], b = Un[NFQ - 1 - j][v];
+            Un[j][v] = rev ? b : a;
+            Un[NFQ - 1 - j][v] = rev ? a : b;
+        }
+}
+
+// H' = -(w_j h_F / (2|J|)) * numerical flux at the points of face f, written to A2 (hi, lo).
+// Own traces come from D1; Un are the neighbour traces (unused on boundary faces).
+template <int P, bool BND>
+__device__ __forceinline__ void tc_face_flux(const TArgs<P>& ka, uint32_t tl, const ElemGeomF& G, const ElemConn& C,
+                                             int f, const float (&Un)[P + 1][4]) {
+    using S = TcShape<P>;
+    constexpr int NFQ = S::NFQ;
     const StageArgs& s = ka.s;
     float Uo[NFQ][4];
 #pragma unroll
@@ -83,44 +127,9 @@ __device__ __forceinline__ void tc_face(const TArgs<P>& ka, const float* sOp, ui
 #pragma unroll
         for (int v = 0; v < NV; ++v) tc::ld1(tl + v * S::N1 + S::NQ4 + f * NFQ + j, Uo[j][v]);
     const int nb = C.nbr[f];
-    const int fl = (C.flags >> (4 * f)) & 15;
-    const int nf = fl & 3;
-    const bool rev = (fl >> 2) & 1;
     const float nx = G.n[f][0], ny = G.n[f][1], hF = G.h[f];
     const float gamma = s.gamma;
-    float Un[NFQ][4];
-#pragma unroll
-    for (int k = 0; k < NFQ; ++k)
-#pragma unroll
-        for (int v = 0; v < NV; ++v) Un[k][v] = 0.f;
     const bool interior = !BND || nb >= 0;
-    if (interior) {  // neighbour traces at its own points, from its coefficients
-        const float* op = sOp + nf * NP * NFQP;
-#pragma unroll
-        for (int i = 0; i < NP; ++i) {
-            float c[4];
-            load_row_f32<NB>(s.uhi, s.din, nb, i, c);
-            float w[NFQP];
-#pragma unroll
-            for (int k4 = 0; k4 < NFQP; k4 += 4) {
-                const float4 t = *reinterpret_cast<const float4*>(op + i * NFQP + k4);
-                w[k4] = t.x; w[k4 + 1] = t.y; w[k4 + 2] = t.z; w[k4 + 3] = t.w;
-            }
-#pragma unroll
-            for (int k = 0; k < NFQ; ++k)
-#pragma unroll
-                for (int v = 0; v < NV; ++v) Un[k][v] = fmaf(w[k], c[v], Un[k][v]);
-        }
-#pragma unroll
-        for (int j = 0; j < NFQ / 2; ++j)
-#pragma unroll
-            for (int v = 0; v < NV; ++v) {
-                const float a = Un[j][v], b = Un[NFQ - 1 - j][v];
-                Un[j][v] = rev ? b : a;
-                Un[NFQ - 1 - j][v] = rev ? a : b;
-            }
-    }
-    __syncwarp();
     tc::wait_ld();
     const float inv_j = __frcp_rn(G.detJ);
     float Hh[NFQ][4], Hl[NFQ][4];
@@ -213,6 +222,15 @@ __global__ void __launch_bounds__(2 * TILE, 1) stage_tc_kernel(const __grid_cons
         const int nloc = min(TILE, s.ne - e0);
         const bool active = e < nloc;
         const int ee = active ? e0 + e : e0;  // inactive lanes work on a valid element; results unused
+        if (t == 0) {  // L2 prefetch: this tile's FP64 state (read in the epilogue), the next tile's inputs
+            if (s.stage == 3) tc::prefetch_l2(s.u64 + (size_t)e0 * NB, (uint32_t)(nloc * NB * sizeof(double)));
+            const int nt = tile + gridDim.x;
+            if (nt < ntiles) {
+                const int n0 = nt * TILE, nn = min(TILE, s.ne - n0);
+                tc::prefetch_l2(s.uhi + (size_t)n0 * NB, (uint32_t)(nn * NB * sizeof(float)));
+                if (s.din) tc::prefetch_l2(s.din + (size_t)n0 * NB, (uint32_t)(nn * NB * sizeof(float)));
+            }
+        }
         {   // stage state of the tile, rows = elements
             const float4* uh = reinterpret_cast<const float4*>(s.uhi + (size_t)e0 * NB);
             const float4* dd = s.din ? reinterpret_cast<const float4*>(s.din + (size_t)e0 * NB) : nullptr;
@@ -266,6 +284,16 @@ __global__ void __launch_bounds__(2 * TILE, 1) stage_tc_kernel(const __grid_cons
             }
             tc::commit(&mbar[0]);
         }
+        // neighbour traces while GEMM1 runs: half 0 face 0, half 1 faces 1 and 2
+        const ElemGeomF G = s.geom[ee];
+        const ElemConn C = s.conn[ee];
+        float UnA[P + 1][4], UnB[P + 1][4];
+        if (half == 0) {
+            tc_face_nbr<P, BND>(ka, sOp, C, 0, UnA);
+        } else {
+            tc_face_nbr<P, BND>(ka, sOp, C, 1, UnA);
+            tc_face_nbr<P, BND>(ka, sOp, C, 2, UnB);
+        }
         const bool ok1 = tc::mbar_wait(&mbar[0], phase, WAIT_LIMIT);
         if (__syncthreads_or(!ok1)) {
             failed = true;
@@ -274,8 +302,6 @@ __global__ void __launch_bounds__(2 * TILE, 1) stage_tc_kernel(const __grid_cons
         tc::fence_after();
 
         // ---- fluxes between the GEMMs
-        const ElemGeomF G = s.geom[ee];
-        const ElemConn C = s.conn[ee];
         if (half == 0) {
             if (active && s.dt_inst) sDt[e] = s.dt_inst[__float_as_int(G.pad)];
             __syncwarp();
@@ -312,10 +338,10 @@ __global__ void __launch_bounds__(2 * TILE, 1) stage_tc_kernel(const __grid_cons
                     tc::st4(tl + S::A2 + (4 + v) * S::K2 + S::NQ4 + q0, sl[v]);
                 }
             }
-            tc_face<P, BND>(ka, sOp, tl, G, C, 0);
+            tc_face_flux<P, BND>(ka, tl, G, C, 0, UnA);
         } else {
-            tc_face<P, BND>(ka, sOp, tl, G, C, 1);
-            tc_face<P, BND>(ka, sOp, tl, G, C, 2);
+            tc_face_flux<P, BND>(ka, tl, G, C, 1, UnA);
+            tc_face_flux<P, BND>(ka, tl, G, C, 2, UnB);
         }
         __syncwarp();
         tc::wait_st();
@@ -359,22 +385,8 @@ __global__ void __launch_bounds__(2 * TILE, 1) stage_tc_kernel(const __grid_cons
         }
         tc::fence_before();
         __syncthreads();
-        const size_t base = (size_t)e0 * NB;
-        for (int g = t; g < nloc * NB; g += S::THREADS) {
-            const int le = g / NB;
-            const float du = sU[le * STR + (g - le * NB)];
-            const float dt = s.dt_inst ? sDt[le] : s.dt;
-            if (s.stage == 1) {
-                s.dout[base + g] = dt * du;
-            } else if (s.stage == 2) {
-                s.dout[base + g] = 0.25f * (__ldg(s.din + base + g) + dt * du);
-            } else {
-                const float delta = (2.0f / 3.0f) * (__ldg(s.din + base + g) + dt * du);
-                const double r = s.u64[base + g] + (double)delta;
-                s.u64[base + g] = r;
-                s.uhi_out[base + g] = (float)r;
-            }
-        }
+        stage_combine<NB, STR, S::THREADS, (TILE * NB4 + S::THREADS - 1) / S::THREADS>(s, sU, sDt, e0, nloc,
+                                                                                       [](int le) { return le; });
         __syncthreads();
     }
     if (failed) {  // an MMA group did not signal in time: flag it, let outstanding MMAs drain

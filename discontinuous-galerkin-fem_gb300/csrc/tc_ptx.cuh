@@ -100,6 +100,11 @@ __device__ __forceinline__ void st4(uint32_t a, const float* x) {
 }
 __device__ __forceinline__ void wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
+// hint: bring [p, p + bytes) into L2 (bulk async prefetch; 16-byte aligned, bytes % 16 == 0)
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(bytes) : "memory");
+}
+
 // 3xTF32 split: x = hi + lo with hi, lo both TF32 (low 13 mantissa bits zero)
 __device__ __forceinline__ float tf32_hi(float x) {
     uint32_t r;

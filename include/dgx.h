@@ -212,10 +212,11 @@ int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps, void* str
 /* The stage kernel the autotuner picked for a mixed-precision context: its grid (CTAs;
  * each walks the 128-element tiles with a grid stride), the number of tiles, and
  * tensor_cores = 1 for the 3xTF32 tcgen05 form (Euler), 0 for the CUDA-core form.  grid is
- * 0 until the first dgx_rk3_step, which times the candidates (CUDA cores at one CTA per
- * tile and 1..8 CTAs per SM; tensor cores) on its stream.  Environment: DGX_AUTOTUNE=0
- * skips the timing (CUDA cores, one CTA per tile); DGX_STAGE_KERNEL=tc or =cuda restricts
- * the choice to one form.  No counterpart in dgfem. */
+ * 0 until the first dgx_rk3_step, which times the candidates on its stream: the CUDA-core
+ * form at one CTA per tile and at 1..8 CTAs per SM.  Environment: DGX_STAGE_KERNEL=tc takes
+ * the tensor-core form, =auto adds it to the timed candidates (it is opt-in: slower at the
+ * sizes measured, and its long-run error is larger); DGX_AUTOTUNE=0 skips the timing (one
+ * CTA per tile).  No counterpart in dgfem. */
 int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles, int* tensor_cores);
 
 /* ---------------------------------------------------------------- batched solves */

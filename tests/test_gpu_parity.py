@@ -214,3 +214,27 @@ def test_rk3_mixed_precision_vs_oracle(dg, order, visc):
     assert err <= 1e-6, err
     # the update itself (u^5 - u^0) is accurate to FP32 level
     assert rel(ut.cpu().numpy() - u0, ref - u0) <= 1e-4
+
+
+def test_config1_vortex_200_steps_fp64(dg):
+    """The plain-form workload: periodic [-5,5]^2, 16x16x2 = 512 triangles, Dubiner p=2,
+    beta = 5 vortex at the origin on the free stream (1, 0.5, 0, 1), CFL 0.1 under dgfem's
+    definition, 200 SSP-RK3 steps.  The 512x6x4 FP64 state equals the oracle's to 1e-10
+    after 200 steps (rounding accumulates over 600 RHS evaluations), and both carry the
+    same error against the exactly advected vortex."""
+    v, e, b = periodic_rectangle(16)
+    om, pm = make_pair(dg, v, e, b, 2, O.DUBINER, True)
+    u0 = om.project(isentropic_vortex(om.quad_points(), beta=5.0))
+    ctx = dg.DGContext(pm, dg.DGSpace("triangle", 2, "dubiner"), dg.EulerWeakFormulation(1.4), "fp64")
+    ut = torch.tensor(u0, device="cuda")
+    dt_gpu = 0.1 / ctx.max_cfl(ut, 1.0)
+    dt = 0.1 / om.max_cfl(1.4, u0, 1.0)
+    assert abs(dt_gpu - dt) <= 1e-14 * dt
+    ref = om.rk3_step(O.euler(1.4), u0, dt, 200)
+    ctx.rk3_step(ut, dt, 200)
+    out = ut.cpu().numpy()
+    assert out.shape == (512, 6, 4)
+    assert rel(out, ref) <= 1e-10
+    exact = om.project(isentropic_vortex(om.quad_points(), t=200 * dt, beta=5.0))
+    assert abs(rel(out, exact) - rel(ref, exact)) <= 1e-8
+    assert rel(out, exact) < 2e-3

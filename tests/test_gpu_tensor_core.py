@@ -1,5 +1,5 @@
 """The tensor-core (3xTF32 tcgen05) form of the mixed-precision Euler stage, through the
-C ABI: DGX_STAGE_KERNEL=tc makes the autotuner take it, =cuda the CUDA-core form.
+C ABI: DGX_STAGE_KERNEL=tc makes the autotuner take it; unset, the CUDA-core form runs.
 
 * p = 1..4, periodic and with far-field / no-slip / slip faces: 5 RK3 steps within 1e-6
   relative L2 of the FP64 oracle (the mixed-precision bar), and within 1e-6 of the
@@ -60,7 +60,10 @@ def case(dg, n, order, walls):
 
 
 def run(dg, monkeypatch, pm, order, u0, dt, kernel, steps=(3, 2), wf=None):
-    monkeypatch.setenv("DGX_STAGE_KERNEL", kernel)
+    if kernel:
+        monkeypatch.setenv("DGX_STAGE_KERNEL", kernel)
+    else:
+        monkeypatch.delenv("DGX_STAGE_KERNEL", raising=False)
     ctx = dg.DGContext(pm, dg.DGSpace("triangle", order, "dubiner"), wf or dg.EulerWeakFormulation(1.4), "mixed")
     u = torch.tensor(u0, device="cuda")
     for n in steps:
@@ -77,7 +80,7 @@ def test_tensor_core_stage_vs_oracle(dg, monkeypatch, order, walls):
     assert np.isfinite(ref).all()
     u_tc, (grid, tiles, tc) = run(dg, monkeypatch, pm, order, u0, dt, "tc")
     assert tc and grid == tiles
-    u_cc, (_, _, tc2) = run(dg, monkeypatch, pm, order, u0, dt, "cuda")
+    u_cc, (_, _, tc2) = run(dg, monkeypatch, pm, order, u0, dt, "")
     assert not tc2
     assert rel(u_tc, ref) <= 1e-6, rel(u_tc, ref)
     assert rel(u_tc - u0, ref - u0) <= 1e-4
@@ -97,3 +100,10 @@ def test_navier_stokes_keeps_cuda_cores(dg, monkeypatch):
     _, (grid, tiles, tc) = run(dg, monkeypatch, pm, 2, u0, dt, "tc", steps=(1,),
                                wf=dg.NavierStokesWeakFormulation(1.4, 0.01, 0.72, 5.0))
     assert not tc and grid > 0
+
+
+def test_auto_mode_times_both_forms(dg, monkeypatch):
+    om, pm, u0, dt = case(dg, 9, 3, False)
+    u, (grid, tiles, tc) = run(dg, monkeypatch, pm, 3, u0, dt, "auto", steps=(2,))
+    ref = om.rk3_step(O.euler(1.4), u0, dt, 2)
+    assert grid > 0 and rel(u, ref) <= 1e-6
