@@ -259,19 +259,10 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
             float B00 = 0.f, B01 = 0.f, B10 = 0.f, B11 = 0.f;
             if (!BND || nb >= 0) {
                 const float* op = sOp + nf * NP * NFQP;
-                // a neighbour inside the tile is read from its shared-memory row (uhi + d
-                // already summed there), one outside through L1/L2
-                const int lnb = nb - e0;
-                const float* srow = (unsigned)lnb < (unsigned)nloc ? sU + stage_row(lnb) * STR : nullptr;
 #pragma unroll
                 for (int i = 0; i < NP; ++i) {
                     float c[4];
-                    if (srow) {
-                        const float4 t = *reinterpret_cast<const float4*>(srow + i * NV);
-                        c[0] = t.x; c[1] = t.y; c[2] = t.z; c[3] = t.w;
-                    } else {
-                        load_row_f32<NB>(s.uhi, s.din, nb, i, c);
-                    }
+                    load_row_f32<NB>(s.uhi, s.din, nb, i, c);
                     float w[NFQP];
 #pragma unroll
                     for (int k4 = 0; k4 < NFQP; k4 += 4) {

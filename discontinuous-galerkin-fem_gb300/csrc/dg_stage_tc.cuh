@@ -73,8 +73,8 @@ static __device__ int g_tc_timeout;  // set when a bounded mbarrier wait gave up
 // Traces of face f's neighbour at this face's points, from the neighbour's coefficients
 // (independent of GEMM1, so they are formed while it runs).
 template <int P, bool BND>
-__device__ __forceinline__ void tc_face_nbr(const TArgs<P>& ka, const float* sOp, const float* sU, int e0, int nloc,
-                                            const ElemConn& C, int f, float (&Un)[P + 1][4]) {
+__device__ __forceinline__ void tc_face_nbr(const TArgs<P>& ka, const float* sOp, const ElemConn& C, int f,
+                                            float (&Un)[P + 1][4]) {
     using S = TcShape<P>;
     constexpr int NP = S::NP, NFQ = S::NFQ, NB = S::NB, NFQP = NbrOps<P>::NFQP;
     const StageArgs& s = ka.s;
@@ -88,17 +88,10 @@ __device__ __forceinline__ void tc_face_nbr(const TArgs<P>& ka, const float* sOp
     const int nf = fl & 3;
     const bool rev = (fl >> 2) & 1;
     const float* op = sOp + nf * NP * NFQP;
-    const int lnb = nb - e0;  // inside the tile: its shared-memory row (uhi + d summed there)
-    const float* srow = (unsigned)lnb < (unsigned)nloc ? sU + lnb * stage_stride<P>() : nullptr;
 #pragma unroll
     for (int i = 0; i < NP; ++i) {
         float c[4];
-        if (srow) {
-            const float4 t = *reinterpret_cast<const float4*>(srow + i * NV);
-            c[0] = t.x; c[1] = t.y; c[2] = t.z; c[3] = t.w;
-        } else {
-            load_row_f32<NB>(s.uhi, s.din, nb, i, c);
-        }
+        load_row_f32<NB>(s.uhi, s.din, nb, i, c);
         float w[NFQP];
 #pragma unroll
         for (int k4 = 0; k4 < NFQP; k4 += 4) {
@@ -296,10 +289,10 @@ __global__ void __launch_bounds__(2 * TILE, 1) stage_tc_kernel(const __grid_cons
         const ElemConn C = s.conn[ee];
         float UnA[P + 1][4], UnB[P + 1][4];
         if (half == 0) {
-            tc_face_nbr<P, BND>(ka, sOp, sU, e0, nloc, C, 0, UnA);
+            tc_face_nbr<P, BND>(ka, sOp, C, 0, UnA);
         } else {
-            tc_face_nbr<P, BND>(ka, sOp, sU, e0, nloc, C, 1, UnA);
-            tc_face_nbr<P, BND>(ka, sOp, sU, e0, nloc, C, 2, UnB);
+            tc_face_nbr<P, BND>(ka, sOp, C, 1, UnA);
+            tc_face_nbr<P, BND>(ka, sOp, C, 2, UnB);
         }
         const bool ok1 = tc::mbar_wait(&mbar[0], phase, WAIT_LIMIT);
         if (__syncthreads_or(!ok1)) {
