@@ -94,13 +94,18 @@ def vortex_centre(seed=0):
 
 
 def dist_init():
+    """One process per GPU under torchrun (NCCL); gloo on a host without GPUs (CPU tests).
+    Replicas only: the ranks share nothing but the barrier and the max of their times."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if ws > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
     return rank, ws
 
 
@@ -115,7 +120,8 @@ def allreduce_max(x, ws):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -351,7 +357,11 @@ def main():
     args = ap.parse_args()
     rank, ws = dist_init()
     if args.impl == "reference":
-        return run_reference(args, rank, ws)
+        run_reference(args, rank, ws)
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
 
     import torch
     import dgfem_gb300 as dg
