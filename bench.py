@@ -436,6 +436,23 @@ def main():
     del ctc
     k64 = max(1, min(args.steps, 50))
     t_64 = allreduce_max(timed(c64, k64, min(args.warmup, 3)), ws)
+    # the double-float form of the FP64 path (same algorithm and FP64 state, residual in
+    # pairs of FP32 numbers on the FP32 pipe), and its distance from FP64 after acc_steps
+    cdf = dg.DGContext(mesh, space, wf, "df64")
+    t_df = allreduce_max(timed(cdf, k64, min(args.warmup, 3)), ws)
+    df_acc = None
+    if args.acc_steps > 0:
+        u64 = u0.clone()
+        udf = u0.clone()
+        c64.rk3_step(u64, dt, args.acc_steps)
+        cdf.rk3_step(udf, dt, args.acc_steps)
+        torch.cuda.synchronize()
+        df_acc = float(torch.linalg.vector_norm(udf - u64) / torch.linalg.vector_norm(u64))
+        del u64, udf
+    df64 = {"kernel": "dgx::element_kernel<3, f2> (double-float arithmetic, FP64 state)",
+            "value": dof * 3 * k64 * ws / t_df, "ms_per_step": 1e3 * t_df / k64, "steps": k64,
+            "vs_fp64": t_64 / t_df, "vs_fp64_l2_rel_after_acc_steps": df_acc}
+    del cdf
     v_mx = dof * 3 * args.steps * ws / t_mx
     v_64 = dof * 3 * k64 * ws / t_64
 
@@ -614,6 +631,7 @@ def main():
                                  "picked_by": "autotuner (timed on the first step)"},
                 "tensor_core_form": tensor_core,
                 "fp64": {"value": v_64, "ms_per_step": 1e3 * t_64 / k64, "steps": k64},
+                "df64": df64,
                 "mixed_vs_fp64": v_mx / v_64,
                 "accuracy": acc,
                 "navier_stokes": ns,

@@ -539,8 +539,9 @@ static StepArgs base_args(const dgx_ctx* c) {
 
 static int launch(const dgx_ctx* c, const StepArgs& a, cudaStream_t s) {
     const bool visc = c->prm.physics == DGX_NAVIER_STOKES;
-    const int rc = c->prm.precision == DGX_MIXED ? launch_element_mixed(c->prm.order, visc, a, c->ops, s)
-                                                 : launch_element_fp64(c->prm.order, visc, a, c->ops, s);
+    const int rc = c->prm.precision == DGX_MIXED  ? launch_element_mixed(c->prm.order, visc, a, c->ops, s)
+                   : c->prm.precision == DGX_DF64 ? launch_element_df64(c->prm.order, visc, a, c->ops, s)
+                                                  : launch_element_fp64(c->prm.order, visc, a, c->ops, s);
     if (rc) return fail(DGX_ERR_CUDA, std::string("element kernel launch failed: ") +
                                           cudaGetErrorString(cudaGetLastError()));
     return DGX_OK;
@@ -719,7 +720,7 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
         return fail(DGX_ERR_INVALID, "unknown basis");
     if (p->physics != DGX_EULER && p->physics != DGX_NAVIER_STOKES)
         return fail(DGX_ERR_INVALID, "unknown physics");
-    if (p->precision != DGX_FP64 && p->precision != DGX_MIXED)
+    if (p->precision != DGX_FP64 && p->precision != DGX_MIXED && p->precision != DGX_DF64)
         return fail(DGX_ERR_INVALID, "unknown precision");
     if (p->physics == DGX_NAVIER_STOKES) {  // NavierStokesWeakFormulation ctor checks (:22-33)
         if (p->mu <= 0.0) return fail(DGX_ERR_INVALID, "Dynamic viscosity must be positive for Navier-Stokes weak formulation");
@@ -731,8 +732,9 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
 
     {
         const bool visc = p->physics == DGX_NAVIER_STOKES;
-        int rc = p->precision == DGX_MIXED ? configure_element_mixed(p->order, visc)
-                                           : configure_element_fp64(p->order, visc);
+        int rc = p->precision == DGX_MIXED  ? configure_element_mixed(p->order, visc)
+                 : p->precision == DGX_DF64 ? configure_element_df64(p->order, visc)
+                                            : configure_element_fp64(p->order, visc);
         if (!rc && p->precision == DGX_MIXED && !visc) rc = configure_stage_tc(p->order);
         if (rc) return fail(DGX_ERR_CUDA, "could not configure the element kernel");
     }

@@ -156,6 +156,9 @@ int launch_element_fp64(int p, bool viscous, const StepArgs& a, const OpsHost& o
 int launch_element_mixed(int p, bool viscous, const StepArgs& a, const OpsHost& ops, cudaStream_t s);
 int configure_element_fp64(int p, bool viscous);
 int configure_element_mixed(int p, bool viscous);
+// double-float form of the FP64 element kernel (dgx_kernels_df64.cu)
+int launch_element_df64(int p, bool viscous, const StepArgs& a, const OpsHost& ops, cudaStream_t s);
+int configure_element_df64(int p, bool viscous);
 int launch_stage_mixed(int p, bool viscous, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
 // Tensor-core form of the mixed Euler stage (dgx_kernels_tc.cu).  A StageArgs::grid with
 // STAGE_TC set selects it; the low bits are its grid (<= 0: one CTA per tile).

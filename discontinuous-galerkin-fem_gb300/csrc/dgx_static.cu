@@ -84,13 +84,17 @@ extern "C" int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps
         a.minv_diag = c->minv_diag;
         a.mode = MODE_STAGE;
         a.dt = dt;
+        auto launch = [&](const StepArgs& x) {
+            return c->prm.precision == DGX_DF64 ? launch_element_df64(c->prm.order, visc, x, c->ops, s)
+                                                : launch_element_fp64(c->prm.order, visc, x, c->ops, s);
+        };
         for (int n = 0; n < n_steps && !rc; ++n) {
             a.u = u; a.un = nullptr; a.out = u1; a.a = 0.0; a.b = 1.0;
-            rc = launch_element_fp64(c->prm.order, visc, a, c->ops, s);
+            rc = launch(a);
             a.u = u1; a.un = u; a.out = u2; a.a = 0.75; a.b = 0.25;
-            if (!rc) rc = launch_element_fp64(c->prm.order, visc, a, c->ops, s);
+            if (!rc) rc = launch(a);
             a.u = u2; a.un = u; a.out = u; a.a = 1.0 / 3.0; a.b = 2.0 / 3.0;
-            if (!rc) rc = launch_element_fp64(c->prm.order, visc, a, c->ops, s);
+            if (!rc) rc = launch(a);
         }
     } else {
         // FP32 copies of u^n (ping-ponged) and the two FP32 stage increments: 4 * nstate

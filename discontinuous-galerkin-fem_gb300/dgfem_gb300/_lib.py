@@ -18,7 +18,7 @@ OK = 0
 ERR_INVALID, ERR_RUNTIME, ERR_RANGE, ERR_CUDA, ERR_NONFINITE = -1, -2, -3, -4, -5
 BASIS_MONOMIAL, BASIS_DUBINER = 0, 1
 EULER, NAVIER_STOKES = 0, 1
-FP64, MIXED = 0, 1
+FP64, MIXED, DF64 = 0, 1, 2
 BC_FAR_FIELD, BC_SLIP_WALL, BC_NO_SLIP_WALL, BC_PERIODIC = 0, 1, 2, 3
 
 # every function include/dgx.h declares, with (restype, argtypes)

@@ -228,7 +228,7 @@ class DGContext:
         lib = L.load()
         visc = weak_form.has_viscous_terms()
         p = L.Params(space.order, space.basis, L.NAVIER_STOKES if visc else L.EULER,
-                     {"fp64": L.FP64, "mixed": L.MIXED}[precision], weak_form.gamma,
+                     {"fp64": L.FP64, "mixed": L.MIXED, "df64": L.DF64}[precision], weak_form.gamma,
                      getattr(weak_form, "mu", 0.0), getattr(weak_form, "prandtl", 0.0),
                      getattr(weak_form, "sigma0", 0.0))
         self._h = C.c_void_p()

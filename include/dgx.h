@@ -39,7 +39,11 @@ extern "C" {
 
 enum { DGX_BASIS_MONOMIAL = 0, DGX_BASIS_DUBINER = 1 };
 enum { DGX_EULER = 0, DGX_NAVIER_STOKES = 1 };
-enum { DGX_FP64 = 0, DGX_MIXED = 1 };
+/* DGX_FP64: FP64 arithmetic and state (the plain form).  DGX_MIXED: FP32 flux and
+ * contraction arithmetic, FP64 geometry, M^-1 and RK3 state.  DGX_DF64: the FP64 path's
+ * algorithm and FP64 state with the residual computed in double-float arithmetic (pairs of
+ * FP32 numbers, about 48 significant bits) on the FP32 pipe; no dgfem counterpart. */
+enum { DGX_FP64 = 0, DGX_MIXED = 1, DGX_DF64 = 2 };
 /* BCTypeEuler, include/dgfem/boundary/conditions.hpp:27-32 */
 enum { DGX_BC_FAR_FIELD = 0, DGX_BC_SLIP_WALL = 1, DGX_BC_NO_SLIP_WALL = 2, DGX_BC_PERIODIC = 3 };
 
@@ -55,7 +59,7 @@ typedef struct {
     int order;      /* polynomial order p, 1..4 */
     int basis;      /* DGX_BASIS_MONOMIAL (dgfem's triangle default) or DGX_BASIS_DUBINER */
     int physics;    /* DGX_EULER or DGX_NAVIER_STOKES */
-    int precision;  /* DGX_FP64 or DGX_MIXED */
+    int precision;  /* DGX_FP64, DGX_MIXED or DGX_DF64 */
     double gamma;   /* 1.4 */
     double mu;      /* dynamic viscosity (Navier-Stokes) */
     double prandtl; /* Prandtl number (Navier-Stokes) */

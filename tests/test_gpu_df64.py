@@ -1,0 +1,115 @@
+"""The double-float (df64) form of the FP64 path: the FP64 path's algorithm, FP64 state,
+geometry, M^-1 and RK3 combination, with the residual computed in pairs of FP32 numbers
+(about 48 bits) on the FP32 pipe.  Held to the FP64 path's own bars against the oracle:
+residual <= 1e-12 relative, RK3 steps <= 1e-11 (Dubiner) / 1e-10 (monomial)."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from meshes import TAGS, periodic_rectangle, primitive_to_conserved, two_triangle_mesh
+from test_gpu_parity import BASES, make_pair, physics, rel, vortex_state
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def dg():
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    import dgfem_gb300 as d
+    return d
+
+
+@pytest.mark.parametrize("visc", [False, True])
+@pytest.mark.parametrize("basis", ["monomial", "dubiner"])
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_residual_df64_periodic(dg, order, basis, visc):
+    v, e, b = periodic_rectangle(6)
+    om, pm = make_pair(dg, v, e, b, order, BASES[basis], True)
+    oph, wf = physics(dg, visc)
+    u = vortex_state(om)
+    ctx = dg.DGContext(pm, dg.DGSpace("triangle", order, basis), wf, "df64")
+    R_gpu = ctx.residual(torch.tensor(u, device="cuda")).cpu().numpy()
+    assert rel(R_gpu, om.residual(oph, u)) <= 1e-12
+
+
+@pytest.mark.parametrize("visc", [False, True])
+def test_residual_df64_unstructured_with_boundaries(dg, visc):
+    rng = np.random.default_rng(11)
+    v, e, b = periodic_rectangle(7, 0.0, 1.0, 0.0, 1.0)
+    inner = (v[:, 0] > 0) & (v[:, 0] < 1) & (v[:, 1] > 0) & (v[:, 1] < 1)
+    v = v.copy()
+    v[inner] += rng.uniform(-0.03, 0.03, size=(inner.sum(), 2))
+    e = e[rng.permutation(len(e))]
+    U_inf = primitive_to_conserved([1.0, 0.4, 0.1, 1.0])
+    bcs = [("Bottom", 2, O.SLIP_WALL, [0, 0, 0, 0]), ("Right", 3, O.FAR_FIELD, U_inf),
+           ("Top", 4, O.NO_SLIP_WALL, [1.0, 0.0, 0.0, 1.0]), ("Left", 5, O.FAR_FIELD, U_inf)]
+    om, pm = make_pair(dg, v, e, b, 3, O.DUBINER, False, bcs=bcs)
+    oph, wf = physics(dg, visc)
+    u = om.project(np.broadcast_to(U_inf, om.quad_points().shape[:-1] + (4,)).copy())
+    u = u + 1e-2 * np.random.default_rng(1).standard_normal(u.shape) * np.abs(u).max()
+    ctx = dg.DGContext(pm, dg.DGSpace("triangle", 3, "dubiner"), wf, "df64")
+    R_gpu = ctx.residual(torch.tensor(u, device="cuda")).cpu().numpy()
+    assert rel(R_gpu, om.residual(oph, u)) <= 1e-12
+
+
+def test_residual_df64_two_triangle_navier_stokes(dg):
+    v, e, b = two_triangle_mesh()
+    tags = {"bottom": 1, "right": 2, "top": 3, "left": 4}
+    bcs = [(n, t, O.NO_SLIP_WALL, [1.0, 0.0, 0.0, 1.0]) for n, t in tags.items()]
+    om, pm = make_pair(dg, v, e, b, 1, O.MONOMIAL, False, tags=tags, bcs=bcs)
+    oph, wf = physics(dg, True, mu=1e-3)
+    u = np.zeros((2, 3, 4))
+    u[:, 0, :] = primitive_to_conserved([1.0, 0.5, 0.0, 1.0])
+    ctx = dg.DGContext(pm, dg.DGSpace("triangle", 1, "monomial"), wf, "df64")
+    assert rel(ctx.residual(u), om.residual(oph, u)) <= 1e-12
+
+
+@pytest.mark.parametrize("visc", [False, True])
+@pytest.mark.parametrize("order,basis", [(2, "dubiner"), (3, "dubiner"), (3, "monomial")])
+def test_rk3_steps_df64(dg, order, basis, visc):
+    v, e, b = periodic_rectangle(6)
+    om, pm = make_pair(dg, v, e, b, order, BASES[basis], True)
+    oph, wf = physics(dg, visc, mu=0.01)
+    u0 = vortex_state(om, noise=0.0)
+    dt = 0.02
+    ref = om.rk3_step(oph, u0, dt, 4)
+    ctx = dg.DGContext(pm, dg.DGSpace("triangle", order, basis), wf, "df64")
+    ut = torch.tensor(u0, device="cuda")
+    ctx.rk3_step(ut, dt, 2)
+    ctx.rk3_step(ut, dt, 2)
+    tol = 1e-11 if basis == "dubiner" else 1e-10
+    assert rel(ut.cpu().numpy(), ref) <= tol
+    # the allocation-free entry point takes the same kernels
+    import ctypes as C
+    from dgfem_gb300 import _lib as L
+    us = torch.tensor(u0, device="cuda")
+    L.check(L.load().dgx_rk3_step_static(ctx._h, C.c_void_p(us.data_ptr()), dt, 4,
+                                         C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    torch.cuda.synchronize()
+    assert rel(us.cpu().numpy(), ref) <= tol
+
+
+def test_df64_long_run_tracks_fp64(dg):
+    """200 steps of the p=3 vortex: df64 stays within 1e-11 of the FP64 GPU path."""
+    v, e, b = periodic_rectangle(12)
+    om, pm = make_pair(dg, v, e, b, 3, O.DUBINER, True)
+    u0 = vortex_state(om, noise=0.0)
+    dt = 0.05 / om.max_cfl(1.4, u0, 1.0)
+    out = {}
+    for prec in ("fp64", "df64"):
+        ctx = dg.DGContext(pm, dg.DGSpace("triangle", 3, "dubiner"), dg.EulerWeakFormulation(1.4), prec)
+        ut = torch.tensor(u0, device="cuda")
+        ctx.rk3_step(ut, dt, 200)
+        out[prec] = ut.cpu().numpy()
+    assert rel(out["df64"], out["fp64"]) <= 1e-11
+
+
+def test_adjoint_and_batch_reject_df64(dg):
+    m = dg.DGMesh.rectangle(4, 4, -5, 5, -5, 5, periodic=True)
+    ctx = dg.DGContext(m, dg.DGSpace("triangle", 2, "dubiner"), dg.EulerWeakFormulation(), "df64")
+    u = torch.ones(ctx.shape, dtype=torch.float64, device="cuda")
+    with pytest.raises(ValueError):
+        ctx.residual_vjp(u, u)
