@@ -122,7 +122,9 @@ __device__ __forceinline__ void element_residual(const Ops<P, OT>& o, const Lift
 #pragma unroll
         for (int i = 0; i < NP; ++i)
 #pragma unroll
-            for (int v = 0; v < NV; ++v) U[v] += o.phi[q][i] * Ue[i * NV + v];
+            for (int v = 0; v < NV; ++v) U[v] = mac(U[v], o.phi[q][i], Ue[i * NV + v]);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) U[v] = settle(U[v]);
         T F[4], Gf[4], u, vv, pp, ri;
         euler_flux<T>(U, gamma - T(1), F, Gf, u, vv, pp, ri);
         if (VISC) {
@@ -131,9 +133,14 @@ __device__ __forceinline__ void element_residual(const Ops<P, OT>& o, const Lift
             for (int i = 0; i < NP; ++i)
 #pragma unroll
                 for (int v = 0; v < NV; ++v) {
-                    gr[v] += o.dr[q][i] * Ue[i * NV + v];
-                    gs[v] += o.ds[q][i] * Ue[i * NV + v];
+                    gr[v] = mac(gr[v], o.dr[q][i], Ue[i * NV + v]);
+                    gs[v] = mac(gs[v], o.ds[q][i], Ue[i * NV + v]);
                 }
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                gr[v] = settle(gr[v]);
+                gs[v] = settle(gs[v]);
+            }
             T gx[4], gy[4], Fv[4], Gv[4];
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
@@ -159,7 +166,7 @@ __device__ __forceinline__ void element_residual(const Ops<P, OT>& o, const Lift
             const T a = FOLD ? L->pr[q][i] : o.dr[q][i];
             const T b = FOLD ? L->ps[q][i] : o.ds[q][i];
 #pragma unroll
-            for (int v = 0; v < NV; ++v) R[i][v] += a * Fr[v] + b * Fs[v];
+            for (int v = 0; v < NV; ++v) R[i][v] = mac(mac(R[i][v], a, Fr[v]), b, Fs[v]);
         }
     }
 
@@ -209,7 +216,9 @@ __device__ __forceinline__ void element_residual(const Ops<P, OT>& o, const Lift
 #pragma unroll
             for (int i = 0; i < NP; ++i)
 #pragma unroll
-                for (int v = 0; v < NV; ++v) Uo[v] += o.phif[f][j][i] * Ue[i * NV + v];
+                for (int v = 0; v < NV; ++v) Uo[v] = mac(Uo[v], o.phif[f][j][i], Ue[i * NV + v]);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) Uo[v] = settle(Uo[v]);
             T Un[4] = {T(0), T(0), T(0), T(0)};
             const int k = rev ? NFQ - 1 - j : j;
             if (nb >= 0) {
@@ -227,8 +236,10 @@ __device__ __forceinline__ void element_residual(const Ops<P, OT>& o, const Lift
                     }
                     const T ph = o.phif[nf][k][i];
 #pragma unroll
-                    for (int v = 0; v < NV; ++v) Un[v] += ph * c[v];
+                    for (int v = 0; v < NV; ++v) Un[v] = mac(Un[v], ph, c[v]);
                 }
+#pragma unroll
+                for (int v = 0; v < NV; ++v) Un[v] = settle(Un[v]);
             }
             T H[4];
             if (nb >= 0) {
@@ -261,9 +272,14 @@ __device__ __forceinline__ void element_residual(const Ops<P, OT>& o, const Lift
                 for (int i = 0; i < NP; ++i)
 #pragma unroll
                     for (int v = 0; v < NV; ++v) {
-                        gr[v] += o.drf[f][j][i] * Ue[i * NV + v];
-                        gs[v] += o.dsf[f][j][i] * Ue[i * NV + v];
+                        gr[v] = mac(gr[v], o.drf[f][j][i], Ue[i * NV + v]);
+                        gs[v] = mac(gs[v], o.dsf[f][j][i], Ue[i * NV + v]);
                     }
+#pragma unroll
+                for (int v = 0; v < NV; ++v) {
+                    gr[v] = settle(gr[v]);
+                    gs[v] = settle(gs[v]);
+                }
                 T gx[4], gy[4], Fv[4], Gv[4];
 #pragma unroll
                 for (int v = 0; v < NV; ++v) {
@@ -287,9 +303,14 @@ __device__ __forceinline__ void element_residual(const Ops<P, OT>& o, const Lift
                         }
 #pragma unroll
                         for (int v = 0; v < NV; ++v) {
-                            nr[v] += o.drf[nf][k][i] * c[v];
-                            ns[v] += o.dsf[nf][k][i] * c[v];
+                            nr[v] = mac(nr[v], o.drf[nf][k][i], c[v]);
+                            ns[v] = mac(ns[v], o.dsf[nf][k][i], c[v]);
                         }
+                    }
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) {
+                        nr[v] = settle(nr[v]);
+                        ns[v] = settle(ns[v]);
                     }
                     T hx[4], hy[4], Fn2[4], Gn2[4];
 #pragma unroll
@@ -323,7 +344,7 @@ __device__ __forceinline__ void element_residual(const Ops<P, OT>& o, const Lift
             for (int i = 0; i < NP; ++i) {
                 const T sc = w * (FOLD ? L->pf[f][j][i] : o.phif[f][j][i]);
 #pragma unroll
-                for (int v = 0; v < NV; ++v) R[i][v] -= sc * H[v];
+                for (int v = 0; v < NV; ++v) R[i][v] = mac(R[i][v], -sc, H[v]);
             }
         }
     }

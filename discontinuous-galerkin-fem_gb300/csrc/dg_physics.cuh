@@ -20,6 +20,13 @@ __device__ __forceinline__ double sqrt_<double>(double x) { return sqrt(x); }
 template <>
 __device__ __forceinline__ float sqrt_<float>(float x) { return __fsqrt_rn(x); }
 
+// acc + a*b (one FMA for float / double); settle(x): x with its representation normalised.
+// Types with their own fused form (double-float) provide overloads.
+template <typename C, typename A, typename B>
+__device__ __forceinline__ C mac(C acc, A a, B b) { return acc + a * b; }
+template <typename C>
+__device__ __forceinline__ C settle(C x) { return x; }
+
 // get_fluxes_and_primitive, src/weak_forms/euler_weak_formulation.cpp:27-43
 template <typename T>
 __device__ __forceinline__ void euler_flux(const T U[4], T gm1, T F[4], T G[4], T& u, T& v, T& p,
