@@ -641,7 +641,7 @@ def main():
                 "config1": cfg1,
                 "e2e": {"value": v_e2e, "unit": "DOF*stages/s", "h2d_bytes_per_step": dof * 8,
                         "d2h_bytes_per_step": dof * 8, "steps": ke},
-                "gpu_launches": 3 * args.steps,
+                "gpu_launches": 3 * args.steps + 1,
                 "roofline": roof, "clocks": clocks, "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
     if ws > 1:
