@@ -71,6 +71,18 @@ __host__ __device__ constexpr int stage_min_blocks(int p, bool visc) {
 #endif
 }
 
+// acc[0..3] += s * c[0..3] as two packed FP32-pair FMAs (variables (0,1) and (2,3)); the
+// same rounding as four fmaf, half the instructions on sm_100-family FP32 pipes.
+__device__ __forceinline__ void fma4(float s, const float (&c)[4], float (&acc)[4]) {
+    const float2 ss = make_float2(s, s);
+    const float2 a = __ffma2_rn(ss, make_float2(c[0], c[1]), make_float2(acc[0], acc[1]));
+    const float2 b = __ffma2_rn(ss, make_float2(c[2], c[3]), make_float2(acc[2], acc[3]));
+    acc[0] = a.x;
+    acc[1] = a.y;
+    acc[2] = b.x;
+    acc[3] = b.y;
+}
+
 // Stage combination of one tile in the increment form, 16-byte accesses:
 //   stage 1: dout = dt R;  stage 2: dout = (din + dt R) / 4;
 //   stage 3: u64 += 2/3 (din + dt R) (FP64), uhi_out = (float)u64.
@@ -192,13 +204,10 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
             for (int i = 0; i < NP; ++i) {
                 const float4 c4 = *reinterpret_cast<const float4*>(Ue + i * NV);
                 const float c[4] = {c4.x, c4.y, c4.z, c4.w};
-#pragma unroll
-                for (int v = 0; v < NV; ++v) {
-                    U[v] = fmaf(o.phi[q][i], c[v], U[v]);
-                    if (VISC) {
-                        gr[v] = fmaf(o.dr[q][i], c[v], gr[v]);
-                        gs[v] = fmaf(o.ds[q][i], c[v], gs[v]);
-                    }
+                fma4(o.phi[q][i], c, U);
+                if (VISC) {
+                    fma4(o.dr[q][i], c, gr);
+                    fma4(o.ds[q][i], c, gs);
                 }
             }
             float F[4], Gf[4], u, vv, pp, ri;
@@ -224,12 +233,10 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
                 Fs[v] = o.wq[q] * (A01 * F[v] + A11 * Gf[v]);
             }
 #pragma unroll
-            for (int i = 0; i < NP; ++i)
-#pragma unroll
-                for (int v = 0; v < NV; ++v) {
-                    R[i][v] = fmaf(L.pr[q][i], Fr[v], R[i][v]);
-                    R[i][v] = fmaf(L.ps[q][i], Fs[v], R[i][v]);
-                }
+            for (int i = 0; i < NP; ++i) {
+                fma4(L.pr[q][i], Fr, R[i]);
+                fma4(L.ps[q][i], Fs, R[i]);
+            }
         }
 
         // ---------------- faces (interior_face_residual :117-175, boundary_face_residual
@@ -270,9 +277,7 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
                         w[k4] = t.x; w[k4 + 1] = t.y; w[k4 + 2] = t.z; w[k4 + 3] = t.w;
                     }
 #pragma unroll
-                    for (int k = 0; k < NFQ; ++k)
-#pragma unroll
-                        for (int v = 0; v < NV; ++v) Un[k][v] = fmaf(w[k], c[v], Un[k][v]);
+                    for (int k = 0; k < NFQ; ++k) fma4(w[k], c, Un[k]);
                     if (VISC) {
                         const float* opr = op + 3 * NP * NFQP;
                         const float* ops = op + 6 * NP * NFQP;
@@ -282,18 +287,14 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
                             w[k4] = t.x; w[k4 + 1] = t.y; w[k4 + 2] = t.z; w[k4 + 3] = t.w;
                         }
 #pragma unroll
-                        for (int k = 0; k < NFQ; ++k)
-#pragma unroll
-                            for (int v = 0; v < NV; ++v) Nr[k][v] = fmaf(w[k], c[v], Nr[k][v]);
+                        for (int k = 0; k < NFQ; ++k) fma4(w[k], c, Nr[k]);
 #pragma unroll
                         for (int k4 = 0; k4 < NFQP; k4 += 4) {
                             const float4 t = *reinterpret_cast<const float4*>(ops + i * NFQP + k4);
                             w[k4] = t.x; w[k4 + 1] = t.y; w[k4 + 2] = t.z; w[k4 + 3] = t.w;
                         }
 #pragma unroll
-                        for (int k = 0; k < NFQ; ++k)
-#pragma unroll
-                            for (int v = 0; v < NV; ++v) Ns[k][v] = fmaf(w[k], c[v], Ns[k][v]);
+                        for (int k = 0; k < NFQ; ++k) fma4(w[k], c, Ns[k]);
                     }
                 }
 #pragma unroll
@@ -328,13 +329,10 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
                 for (int i = 0; i < NP; ++i) {
                     const float4 c4 = *reinterpret_cast<const float4*>(Ue + i * NV);
                     const float c[4] = {c4.x, c4.y, c4.z, c4.w};
-#pragma unroll
-                    for (int v = 0; v < NV; ++v) {
-                        Uo[v] = fmaf(o.phif[f][j][i], c[v], Uo[v]);
-                        if (VISC) {
-                            gr[v] = fmaf(o.drf[f][j][i], c[v], gr[v]);
-                            gs[v] = fmaf(o.dsf[f][j][i], c[v], gs[v]);
-                        }
+                    fma4(o.phif[f][j][i], c, Uo);
+                    if (VISC) {
+                        fma4(o.drf[f][j][i], c, gr);
+                        fma4(o.dsf[f][j][i], c, gs);
                     }
                 }
                 float H[4];
@@ -400,11 +398,7 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
                 }
                 const float w = o.wf[j] * hF * 0.5f * inv_j;
 #pragma unroll
-                for (int i = 0; i < NP; ++i) {
-                    const float sc = w * L.pf[f][j][i];
-#pragma unroll
-                    for (int v = 0; v < NV; ++v) R[i][v] = fmaf(-sc, H[v], R[i][v]);
-                }
+                for (int i = 0; i < NP; ++i) fma4(-(w * L.pf[f][j][i]), H, R[i]);
             }
         }
     }

@@ -99,9 +99,7 @@ __device__ __forceinline__ void tc_face_nbr(const TArgs<P>& ka, const float* sOp
             w[k4] = t.x; w[k4 + 1] = t.y; w[k4 + 2] = t.z; w[k4 + 3] = t.w;
         }
 #pragma unroll
-        for (int k = 0; k < NFQ; ++k)
-#pragma unroll
-            for (int v = 0; v < NV; ++v) Un[k][v] = fmaf(w[k], c[v], Un[k][v]);
+        for (int k = 0; k < NFQ; ++k) fma4(w[k], c, Un[k]);
     }
 #pragma unroll
     for (int j = 0; j < NFQ / 2; ++j)
