@@ -1,7 +1,9 @@
 """The double-float (df64) form of the FP64 path: the FP64 path's algorithm, FP64 state,
 geometry, M^-1 and RK3 combination, with the residual computed in pairs of FP32 numbers
-(about 48 bits) on the FP32 pipe.  Held to the FP64 path's own bars against the oracle:
-residual <= 1e-12 relative, RK3 steps <= 1e-11 (Dubiner) / 1e-10 (monomial)."""
+(about 48 bits) on the FP32 pipe.  On the perturbed states of the FP64 parity tests it
+meets the FP64 path's bars against the oracle (residual <= 1e-12 relative, RK3 steps
+<= 1e-11 Dubiner / 1e-10 monomial).  Where the residual is a small difference of large
+flux terms (a smooth, nearly steady vortex) the 5 missing bits show: its bar there is 1e-11."""
 
 import numpy as np
 import pytest
@@ -90,6 +92,19 @@ def test_rk3_steps_df64(dg, order, basis, visc):
                                          C.c_void_p(torch.cuda.current_stream().cuda_stream)))
     torch.cuda.synchronize()
     assert rel(us.cpu().numpy(), ref) <= tol
+
+
+def test_residual_df64_smooth_vortex(dg):
+    v, e, b = periodic_rectangle(8)
+    om, pm = make_pair(dg, v, e, b, 3, O.DUBINER, True)
+    u = vortex_state(om, noise=0.0)
+    ref = om.residual(O.euler(1.4), u)
+    out = {}
+    for prec in ("fp64", "df64"):
+        ctx = dg.DGContext(pm, dg.DGSpace("triangle", 3, "dubiner"), dg.EulerWeakFormulation(1.4), prec)
+        out[prec] = rel(ctx.residual(torch.tensor(u, device="cuda")).cpu().numpy(), ref)
+    assert out["fp64"] <= 1e-12
+    assert out["df64"] <= 1e-11
 
 
 def test_df64_long_run_tracks_fp64(dg):
