@@ -1046,6 +1046,20 @@ extern "C" int dgx_project(dgx_ctx* c, const double* uq, double* u, void* stream
     return DGX_OK;
 }
 
+extern "C" int dgx_eval_points(dgx_ctx* c, int n_points, const double* ref_xy, const double* u, double* out,
+                               void* stream) {
+    if (!c || n_points < 0 || (n_points && !ref_xy) || (c->ne && n_points && (!u || !out)))
+        return fail(DGX_ERR_INVALID, "dgx_eval_points: bad argument");
+    if (n_points > EVAL_MAX_POINTS)
+        return fail(DGX_ERR_INVALID, "dgx_eval_points: at most " + std::to_string(EVAL_MAX_POINTS) + " points");
+    std::vector<double> phi((size_t)n_points * c->np), grad(2 * 15);
+    for (int k = 0; k < n_points; ++k) basis_eval(c->prm.basis, c->prm.order, ref_xy[2 * k], ref_xy[2 * k + 1],
+                                                   &phi[(size_t)k * c->np], grad.data());
+    if (launch_eval_points(c->ne, c->np, n_points, phi.data(), u, out, (cudaStream_t)stream))
+        return fail(DGX_ERR_CUDA, "point evaluation launch failed");
+    return DGX_OK;
+}
+
 static int ensure_host_buffers(dgx_ctx* c) {
     if (c->d_hu) return DGX_OK;
     const size_t sb = (c->nstate ? c->nstate : 1) * sizeof(double);

@@ -180,6 +180,9 @@ int launch_project(int ne, int p, const OpsHost& ops, const ElemGeom* geom, cons
 int launch_monitor(int ne, int p, const OpsHost& ops, const ElemGeom* geom, const double* u,
                    double dt, double gamma, double* d_out /*[4]*/, cudaStream_t s);
 int launch_has_nan(size_t n, const double* u, int* d_flag, cudaStream_t s);
+// Basis evaluation at reference points (dgx_misc.cu), at most EVAL_MAX_POINTS points.
+constexpr int EVAL_MAX_POINTS = 128;
+int launch_eval_points(int ne, int np, int npts, const double* phi, const double* u, double* out, cudaStream_t s);
 int launch_f64_to_f32(size_t n, const double* in, float* out, cudaStream_t s);
 
 }  // namespace dgx

@@ -215,4 +215,40 @@ int launch_f64_to_f32(size_t n, const double* in, float* out, cudaStream_t s) {
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+
+// Point evaluation: out[(e * npts + k) * 4 + v] = sum_i phi[k][i] * u[(e * np + i) * 4 + v],
+// one thread per (element, point).  phi holds the basis at reference points (host-built).
+struct EvalArgs {
+    int npts, np;
+    double phi[EVAL_MAX_POINTS][15];
+};
+
+__global__ void eval_points_kernel(const __grid_constant__ EvalArgs a, int ne, const double* u, double* out) {
+    const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (size_t)ne * a.npts) return;
+    const int e = (int)(g / a.npts), k = (int)(g - (size_t)e * a.npts);
+    const double* ue = u + (size_t)e * a.np * NV;
+    double r[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int i = 0; i < a.np; ++i) {
+        const double ph = a.phi[k][i];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) r[v] = fma(ph, ue[i * NV + v], r[v]);
+    }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) out[g * NV + v] = r[v];
+}
+
+int launch_eval_points(int ne, int np, int npts, const double* phi, const double* u, double* out, cudaStream_t s) {
+    if (ne == 0 || npts == 0) return 0;
+    if (npts > EVAL_MAX_POINTS || np > 15) return -1;
+    EvalArgs a;
+    a.npts = npts;
+    a.np = np;
+    for (int k = 0; k < npts; ++k)
+        for (int i = 0; i < np; ++i) a.phi[k][i] = phi[k * np + i];
+    const size_t n = (size_t)ne * npts;
+    eval_points_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, ne, u, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 }  // namespace dgx

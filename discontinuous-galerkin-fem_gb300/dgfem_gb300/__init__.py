@@ -7,9 +7,10 @@ from .api import (BCTypeEuler, BoundaryConditionEuler, CompressibleDGSolverBase,
                   DGContext, DGMesh, DGSpace, EulerDGSolver, EulerWeakFormulation,
                   NavierStokesDGSolver, NavierStokesWeakFormulation, conserved_to_primitive,
                   kinetic_energy, primitive_to_conserved, rk3_trajectory)
+from .vtk import VTKWriter
 
 __all__ = ["DGXError", "DGXInvalidArgument", "DGXOutOfRange", "LIB_PATH", "load",
            "BCTypeEuler", "BoundaryConditionEuler", "CompressibleDGSolverBase", "DGAssembler", "DGBatch",
            "DGContext", "DGMesh", "DGSpace", "EulerDGSolver", "EulerWeakFormulation",
            "NavierStokesDGSolver", "NavierStokesWeakFormulation", "conserved_to_primitive",
-           "primitive_to_conserved", "kinetic_energy", "rk3_trajectory"]
+           "primitive_to_conserved", "kinetic_energy", "rk3_trajectory", "VTKWriter"]

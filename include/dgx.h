@@ -211,6 +211,15 @@ int dgx_kinetic_energy_gradient(dgx_ctx* c, const double* u0, double dt, int n_s
 #define DGX_STATIC_MAX_STATE (1 << 20)
 int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps, void* stream);
 
+/* ---------------------------------------------------------------- output */
+
+/* The solution at reference points of every element, for visualisation: out (device,
+ * n_elements * n_points * 4 doubles) = sum_i phi_i(ref_xy[k]) u[e][i][:], ref_xy (host,
+ * n_points (xi, eta) pairs on the reference triangle (0,0),(1,0),(0,1)), at most 128 points.
+ * Replaces the per-point basis evaluation of VTKWriter::evaluate_at_points
+ * (src/utils/vtk_writer.cpp:285-323). */
+int dgx_eval_points(dgx_ctx* c, int n_points, const double* ref_xy, const double* u, double* out, void* stream);
+
 /* ---------------------------------------------------------------- launch shape */
 
 /* The stage kernel the autotuner picked for a mixed-precision context: its grid (CTAs;
