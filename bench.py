@@ -46,7 +46,7 @@ MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 # dram__bytes_read.sum + dram__bytes_write.sum per element per launch of the mixed
 # element kernel, from the ncu capture summarised in profiles/element_kernel_mixed_p3.md
-NCU_TRAFFIC_BYTES_PER_ELEM = 522  # stage 2 capture; its algorithmic bytes are 560
+NCU_TRAFFIC_BYTES_PER_ELEM = 518  # stage 2 capture (271.5 MB / 524,288 elements); its design bytes are 560
 
 
 def vortex(xy, t=0.0, beta=5.0, xc=0.0, yc=0.0, uinf=0.5, vinf=0.0, gamma=GAMMA, period=10.0):
@@ -482,7 +482,7 @@ def main():
             "algorithmic_bytes_per_launch": ALGO_BYTES_PER_ELEM_STAGE * ne, "launch_ms": t_launch * 1e3,
             "design_bytes_per_launch": DESIGN_BYTES_PER_ELEM_STAGE * ne,
             "achieved_design_bytes": DESIGN_BYTES_PER_ELEM_STAGE * ne / t_launch / 1e9,
-            "traffic_note": "ncu dram read+write of one stage-2 launch (522 B/element, its design bytes are 560)"}
+            "traffic_note": "ncu dram read+write of one stage-2 launch (518 B/element, its design bytes are 560)"}
 
     # ---- Navier-Stokes leg: Taylor-Green-type vortex, [0,2pi]^2, 256x256x2, p=4, Re=1600
     ns = None
