@@ -565,7 +565,7 @@ def main():
         t_grad = time.perf_counter() - t0
         rng = np.random.default_rng(1234)
         h = 1e-6
-        fd_err, tlm_err, fd_abs = [], [], []
+        fd_err, tlm_err, fd_abs, fd_cs = [], [], [], []
         axq = actx.quad_points()
         for k in range(args.adj_dirs):
             # seeded random smooth direction: a few random Fourier modes per variable,
@@ -587,6 +587,7 @@ def main():
             ad = float(torch.sum(grad * d))
             fd_err.append(abs(ad - fd) / max(abs(fd), 1e-300))
             fd_abs.append(abs(fd))
+            fd_cs.append(abs(ad - fd) / float(torch.linalg.vector_norm(grad) * torch.linalg.vector_norm(d)))
             if k < 2:
                 ut, dut = au0.clone(), d.clone()
                 actx.rk3_step_tlm(ut, dut, adt, na)
@@ -601,6 +602,7 @@ def main():
                "fd_directions": args.adj_dirs, "fd_h": h, "fd_max_rel_err": max(fd_err) if fd_err else None,
                "fd_median_rel_err": float(np.median(fd_err)) if fd_err else None,
                "fd_min_abs_derivative": min(fd_abs) if fd_abs else None,
+               "fd_max_err_vs_grad_norm": max(fd_cs) if fd_cs else None,
                "tlm_directions": len(tlm_err), "tlm_max_rel_err": max(tlm_err) if tlm_err else None}
         del actx
 
