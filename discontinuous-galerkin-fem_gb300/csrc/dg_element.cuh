@@ -353,8 +353,13 @@ __device__ __forceinline__ void element_residual(const Ops<P, OT>& o, const Lift
 // ---------------------------------------------------------------------------------
 // Element kernel with FP64 input/output states: the FP64 path (T = double) and the
 // mixed path's residual / rhs entry points (T = float).
+// CTAs per SM the register allocation must allow (1: unconstrained).  DGX_ELEMENT_MIN_BLOCKS
+// overrides it for experiments.
+#ifndef DGX_ELEMENT_MIN_BLOCKS
+#define DGX_ELEMENT_MIN_BLOCKS 1
+#endif
 template <int P, typename T, bool VISC>
-__global__ void __launch_bounds__(TILE) element_kernel(const __grid_constant__ KArgs<P, T, VISC> ka) {
+__global__ void __launch_bounds__(TILE, DGX_ELEMENT_MIN_BLOCKS) element_kernel(const __grid_constant__ KArgs<P, T, VISC> ka) {
     constexpr int NP = n_basis(P), NB = NP * NV, STR = NB + 1;
     const StepArgs& s = ka.s;
     extern __shared__ __align__(16) unsigned char smem_raw[];
