@@ -59,12 +59,13 @@ struct TArgs {
     float wf[S::NFQ];
 };
 
-// shared memory: A1 [2][4][TILE * KP] | B1 [2][N1 * KP] | B2 [2][N2 * K2] | U tile [TILE][STR]
-//                | neighbour-face operators | dt [TILE] | 2 mbarriers | TMEM address
+// shared memory: A1 [2][4][TILE * KP] | B1 [2][N1 * KP] | B2 [2][N2 * K2] | staged inputs
+//                [2][TILE * NB] (uhi, d; bulk-copied) | U tile [TILE][STR] | neighbour-face
+//                operators | dt [TILE] | 3 mbarriers | TMEM address
 template <int P>
 __host__ __device__ constexpr int tc_smem_floats() {
     using S = TcShape<P>;
-    return 8 * TILE * S::KP + 2 * S::N1 * S::KP + 2 * S::N2 * S::K2 + TILE * stage_stride<P>() +
+    return 8 * TILE * S::KP + 2 * S::N1 * S::KP + 2 * S::N2 * S::K2 + 2 * TILE * S::NB + TILE * stage_stride<P>() +
            stage_op_floats<P, false>() + TILE + 8;
 }
 
@@ -185,11 +186,12 @@ __global__ void __launch_bounds__(2 * TILE, 1) stage_tc_kernel(const __grid_cons
     float* sA1 = reinterpret_cast<float*>(tc_smem_raw);
     float* sB1 = sA1 + 8 * TILE * KP;
     float* sB2 = sB1 + 2 * S::N1 * KP;
-    float* sU = sB2 + 2 * S::N2 * S::K2;
+    float* sIn = sB2 + 2 * S::N2 * S::K2;  // [2][TILE * NB]: the next tile's uhi and d, bulk-copied
+    float* sU = sIn + 2 * TILE * NB;
     float* sOp = sU + TILE * STR;
     float* sDt = sOp + OPF;
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(sDt + TILE);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sDt + TILE);  // GEMM1, GEMM2, input copy
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 3);
 
     const int t = threadIdx.x, warp = t >> 5;
     const int e = t & (TILE - 1), half = t >> 7;  // element (= TMEM lane), half
@@ -199,6 +201,7 @@ __global__ void __launch_bounds__(2 * TILE, 1) stage_tc_kernel(const __grid_cons
     if (t == 0) {
         tc::mbar_init(&mbar[0], 1);
         tc::mbar_init(&mbar[1], 1);
+        tc::mbar_init(&mbar[2], 1);
     }
     if (warp == 0) tc::tmem_alloc(tslot, S::COLS);
     tc::fence_before();
@@ -215,27 +218,38 @@ __global__ void __launch_bounds__(2 * TILE, 1) stage_tc_kernel(const __grid_cons
     uint32_t phase = 0;
     bool failed = false;
     const int ntiles = (s.ne + TILE - 1) / TILE;
+    // bulk copy of a tile's inputs into sIn, completing on mbar[2]
+    auto stage_in = [&](int tile) {
+        const int n0 = tile * TILE, nn = min(TILE, s.ne - n0);
+        const uint32_t bytes = (uint32_t)(nn * NB * sizeof(float));
+        tc::mbar_expect_tx(&mbar[2], s.din ? 2 * bytes : bytes);
+        tc::bulk_g2s(sIn, s.uhi + (size_t)n0 * NB, bytes, &mbar[2]);
+        if (s.din) tc::bulk_g2s(sIn + TILE * NB, s.din + (size_t)n0 * NB, bytes, &mbar[2]);
+    };
+    if (t == 0 && (int)blockIdx.x < ntiles) stage_in(blockIdx.x);
+    bool copy_pending = (int)blockIdx.x < ntiles;
+    uint32_t copy_parity = 0;  // the phase of mbar[2] the pending copy completes
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, phase ^= 1) {
         const int e0 = tile * TILE;
         const int nloc = min(TILE, s.ne - e0);
         const bool active = e < nloc;
         const int ee = active ? e0 + e : e0;  // inactive lanes work on a valid element; results unused
-        if (t == 0) {  // L2 prefetch: this tile's FP64 state (read in the epilogue), the next tile's inputs
-            if (s.stage == 3) tc::prefetch_l2(s.u64 + (size_t)e0 * NB, (uint32_t)(nloc * NB * sizeof(double)));
-            const int nt = tile + gridDim.x;
-            if (nt < ntiles) {
-                const int n0 = nt * TILE, nn = min(TILE, s.ne - n0);
-                tc::prefetch_l2(s.uhi + (size_t)n0 * NB, (uint32_t)(nn * NB * sizeof(float)));
-                if (s.din) tc::prefetch_l2(s.din + (size_t)n0 * NB, (uint32_t)(nn * NB * sizeof(float)));
-            }
+        if (t == 0 && s.stage == 3)  // this tile's FP64 state, read in the stage combination
+            tc::prefetch_l2(s.u64 + (size_t)e0 * NB, (uint32_t)(nloc * NB * sizeof(double)));
+        // the tile's inputs, bulk-copied into sIn while the previous tile was computed
+        const bool okin = tc::mbar_wait(&mbar[2], phase, WAIT_LIMIT);
+        if (__syncthreads_or(!okin)) {
+            failed = true;
+            break;
         }
+        copy_pending = false;
         {   // stage state of the tile, rows = elements
-            const float4* uh = reinterpret_cast<const float4*>(s.uhi + (size_t)e0 * NB);
-            const float4* dd = s.din ? reinterpret_cast<const float4*>(s.din + (size_t)e0 * NB) : nullptr;
+            const float4* uh = reinterpret_cast<const float4*>(sIn);
+            const float4* dd = s.din ? reinterpret_cast<const float4*>(sIn + TILE * NB) : nullptr;
             for (int g = t; g < nloc * NB4; g += S::THREADS) {
-                float4 a = __ldg(uh + g);
+                float4 a = uh[g];
                 if (dd) {
-                    const float4 b = __ldg(dd + g);
+                    const float4 b = dd[g];
                     a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w;
                 }
                 const int le = g / NB4, k = 4 * (g - le * NB4);
@@ -243,6 +257,14 @@ __global__ void __launch_bounds__(2 * TILE, 1) stage_tc_kernel(const __grid_cons
             }
         }
         __syncthreads();
+        if (tile + (int)gridDim.x < ntiles) {  // sIn is free: start the next tile's copy
+            if (t == 0) {
+                tc::fence_async_smem();
+                stage_in(tile + gridDim.x);
+            }
+            copy_pending = true;
+            copy_parity = phase ^ 1;
+        }
         // A1: the split state in the K-major operand layout, variables 2*half and 2*half + 1
 #pragma unroll
         for (int vv = 0; vv < 2; ++vv) {
@@ -387,11 +409,12 @@ __global__ void __launch_bounds__(2 * TILE, 1) stage_tc_kernel(const __grid_cons
                                                                                        [](int le) { return le; });
         __syncthreads();
     }
-    if (failed) {  // an MMA group did not signal in time: flag it, let outstanding MMAs drain
+    if (failed) {  // a wait gave up: flag it, let outstanding MMAs and copies drain
         if (t == 0) atomicExch(&g_tc_timeout, 1);
         tc::mbar_wait(&mbar[0], phase, WAIT_LIMIT);
         tc::mbar_wait(&mbar[1], phase, WAIT_LIMIT);
     }
+    if (copy_pending) tc::mbar_wait(&mbar[2], copy_parity, WAIT_LIMIT);
     tc::fence_before();
     __syncthreads();
     if (warp == 0) {
