@@ -95,6 +95,7 @@ __device__ __forceinline__ void stage_combine(const StageArgs& s, const float* s
     const int n4 = nloc * NB4;
     const size_t b4 = (size_t)e0 * NB4;
     const int t = threadIdx.x;
+    bool bad = false;
     for (int g0 = t; g0 < n4; g0 += CH * THREADS) {
         float4 dv[CH];
         double2 ua[CH], ub[CH];
@@ -131,9 +132,11 @@ __device__ __forceinline__ void stage_combine(const StageArgs& s, const float* s
                 reinterpret_cast<double2*>(s.u64)[2 * (b4 + g)] = ra;
                 reinterpret_cast<double2*>(s.u64)[2 * (b4 + g) + 1] = rb;
                 reinterpret_cast<float4*>(s.uhi_out)[b4 + g] = make_float4((float)ra.x, (float)ra.y, (float)rb.x, (float)rb.y);
+                bad |= !(isfinite(ra.x) && isfinite(ra.y) && isfinite(rb.x) && isfinite(rb.y));
             }
         }
     }
+    if (bad && s.status) atomicOr(s.status, 1);
 }
 
 // hint: bring [p, p + bytes) into L2 (bulk async prefetch; 16-byte aligned, bytes % 16 == 0)
@@ -410,6 +413,7 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
     }
     __syncthreads();
     const size_t base = (size_t)e0 * NB;
+    bool bad = false;
     for (int g = tl; g < nloc * NB; g += TILE) {
         const int le = g / NB;
         const float du = sU[stage_row(le) * STR + (g - le * NB)];
@@ -423,8 +427,10 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
             const double r = s.u64[base + g] + (double)delta;
             s.u64[base + g] = r;
             s.uhi_out[base + g] = (float)r;
+            bad |= !isfinite(r);
         }
     }
+    if (bad && s.status) atomicOr(s.status, 1);
     __syncthreads();  // the next tile reuses sU / sDt
 }
 

@@ -569,6 +569,7 @@ static void free_ctx(dgx_ctx* c) {
     cudaFree(c->d_hr);
     cudaFree(c->d_mon);
     cudaFree(c->d_flag);
+    cudaFree(c->d_status);
     delete c;
 }
 
@@ -778,7 +779,7 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
     if (!alloc((void**)&c->d_geom, sizeof(ElemGeom) * ne) || !alloc((void**)&c->d_conn, sizeof(ElemConn) * ne) ||
         !alloc((void**)&c->d_bc, sizeof(BCSlot) * slots.size()) || !alloc((void**)&c->d_u1, sb) ||
         !alloc((void**)&c->d_u2, sb) || !alloc((void**)&c->d_mon, 4 * sizeof(double)) ||
-        !alloc((void**)&c->d_flag, sizeof(int)) ||
+        !alloc((void**)&c->d_flag, sizeof(int)) || !alloc((void**)&c->d_status, sizeof(int)) ||
         (p->precision == DGX_MIXED &&
          (!alloc((void**)&c->d_uhi[0], c->nstate * sizeof(float)) ||
           !alloc((void**)&c->d_uhi[1], c->nstate * sizeof(float)) ||
@@ -798,7 +799,8 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
             return fail(DGX_ERR_CUDA, "device upload failed (FP32 geometry)");
         }
     }
-    if (cudaMemcpy(c->d_geom, geom.data(), sizeof(ElemGeom) * ne, cudaMemcpyHostToDevice) != cudaSuccess ||
+    if (cudaMemset(c->d_status, 0, sizeof(int)) != cudaSuccess ||
+        cudaMemcpy(c->d_geom, geom.data(), sizeof(ElemGeom) * ne, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(c->d_conn, conn.data(), sizeof(ElemConn) * ne, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(c->d_bc, slots.data(), sizeof(BCSlot) * slots.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->cap, cudaStreamNonBlocking) != cudaSuccess) {
@@ -860,6 +862,7 @@ extern "C" int dgx_apply_mass_inv(dgx_ctx* c, const double* in, double* out, voi
 static int enqueue_rk3(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
     StepArgs a = base_args(c);
     a.mode = MODE_STAGE;
+    a.status = c->d_status;
     a.dt = dt;
     a.u = u; a.un = nullptr; a.out = c->d_u1; a.a = 0.0; a.b = 1.0;
     int rc = launch(c, a, s);
@@ -890,6 +893,7 @@ static StageArgs mixed_stage_args(const dgx_ctx* c, double* u, double dt, int sr
     a.u64 = u;
     a.uhi_out = c->d_uhi[1 - src];
     a.grid = c->stage_grid;
+    a.status = c->d_status;
     return a;
 }
 
@@ -1031,6 +1035,17 @@ extern "C" int dgx_has_nan(dgx_ctx* c, const double* u, int* has_nan, void* stre
     CUDA_OK(cudaStreamSynchronize(s));
     *has_nan = f ? 1 : 0;
     return DGX_OK;
+}
+
+extern "C" int dgx_step_status(dgx_ctx* c, int* nonfinite, void* stream) {
+    if (!c) return fail(DGX_ERR_INVALID, "null context");
+    cudaStream_t s = (cudaStream_t)stream;
+    int f = 0;
+    CUDA_OK(cudaMemcpyAsync(&f, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_OK(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+    CUDA_OK(cudaStreamSynchronize(s));
+    if (nonfinite) *nonfinite = f & 1;
+    return (f & 1) ? fail(DGX_ERR_NONFINITE, "an SSP-RK3 step produced a non-finite value") : DGX_OK;
 }
 
 extern "C" int dgx_quad_points(const dgx_ctx* c, double* xq) {

@@ -148,6 +148,7 @@ struct StageArgs {
     int boundary;       // 1 when some face is a boundary or skipped face
     const float* dt_inst;  // batched solves: dt per instance, instance id in ElemGeomF::pad (else null)
     int grid;           // persistent grid size (0: one CTA per tile)
+    int* status;        // device flag: bit 0 set when stage 3 produced a non-finite value
 };
 
 

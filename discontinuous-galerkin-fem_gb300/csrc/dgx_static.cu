@@ -84,6 +84,7 @@ extern "C" int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps
         a.minv_diag = c->minv_diag;
         a.mode = MODE_STAGE;
         a.dt = dt;
+        a.status = c->d_status;
         auto launch = [&](const StepArgs& x) {
             return c->prm.precision == DGX_DF64 ? launch_element_df64(c->prm.order, visc, x, c->ops, s)
                                                 : launch_element_fp64(c->prm.order, visc, x, c->ops, s);
@@ -106,6 +107,7 @@ extern "C" int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps
         if (launch_f64_to_f32(c->nstate, u, uhi[0], s))
             return dgx::set_error(DGX_ERR_CUDA, "dgx_rk3_step_static: conversion launch failed");
         StageArgs a{};
+        a.status = c->d_status;
         a.ne = c->ne;
         a.geom = c->d_geomf;
         a.conn = c->d_conn;

@@ -325,6 +325,16 @@ class DGContext:
         check(L.load().dgx_density_range(self._h, self._dev(u), C.byref(lo), C.byref(hi), _stream_of(u)))
         return lo.value, hi.value
 
+    def step_nonfinite(self) -> bool:
+        """True when an RK3 step since the last call produced a NaN or Inf (device flag, read
+        and cleared on torch's current stream)."""
+        import torch
+        f = C.c_int()
+        rc = L.load().dgx_step_status(self._h, C.byref(f), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        if rc not in (L.OK, L.ERR_NONFINITE):
+            check(rc)
+        return bool(f.value)
+
     def has_nan(self, u) -> bool:
         f = C.c_int()
         check(L.load().dgx_has_nan(self._h, self._dev(u), C.byref(f), _stream_of(u)))
@@ -507,7 +517,7 @@ class CompressibleDGSolverBase:
             step += 1
             self.telemetry["steps_completed"] += 1
             self.telemetry["rhs_evaluations"] += 3
-            if self.ctx.has_nan(u):
+            if self.ctx.step_nonfinite():  # dgfem's per-step NaN check: stop the run
                 break
         if step % save_every != 0:
             frames.append(u.clone())

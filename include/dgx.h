@@ -148,6 +148,13 @@ int dgx_density_range(dgx_ctx* c, const double* u, double* rho_min, double* rho_
  * src/solver/compressible_solver_base.cpp:290-301), else 0; host result, synchronises. */
 int dgx_has_nan(dgx_ctx* c, const double* u, int* has_nan, void* stream);
 
+/* Failure detection: whether an SSP-RK3 step on this context (dgx_rk3_step, the host and
+ * allocation-free variants) produced a NaN or Inf since the last call.  The stage kernels set
+ * a device flag as they write u^{n+1}; this call reads and clears it (synchronising with
+ * `stream`).  Returns DGX_ERR_NONFINITE with *nonfinite = 1, or DGX_OK with 0.  dgfem scans
+ * the state after each step and stops the run (compressible_solver_base.cpp:290-301). */
+int dgx_step_status(dgx_ctx* c, int* nonfinite, void* stream);
+
 /* Physical coordinates of every volume quadrature point, [n_elements][n_quad][2] (host),
  * GeometricMapping::map_to_physical at the points project_initial_condition uses. */
 int dgx_quad_points(const dgx_ctx* c, double* xq);
