@@ -36,10 +36,11 @@ def test_linear_field_at_lattice_points(dg, tmp_path, order, basis):
     xy = np.array([[float(a) for a in l.split()[:2]] for l in text[5:5 + npts]])
     i = text.index("SCALARS rho double 1")
     rho = np.array([float(l) for l in text[i + 2:i + 2 + npts]])
-    assert np.allclose(rho, linear(xy)[:, 0], rtol=0, atol=1e-12)
+    # the file carries 11 significant digits (dgfem's scientific, precision 10)
+    assert np.allclose(rho, linear(xy)[:, 0], rtol=1e-10, atol=0)
     i = text.index("SCALARS E double 1")
     E = np.array([float(l) for l in text[i + 2:i + 2 + npts]])
-    assert np.allclose(E, linear(xy)[:, 3], rtol=0, atol=1e-12)
+    assert np.allclose(E, linear(xy)[:, 3], rtol=1e-10, atol=0)
 
 
 @pytest.mark.parametrize("basis", ["monomial", "dubiner"])
@@ -60,4 +61,5 @@ def test_eval_points_then_projection_is_identity(dg, order, basis):
     u = torch.tensor(np.random.default_rng(4).standard_normal(ctx.shape), device="cuda")
     uq = dg.VTKWriter.evaluate_at_points(ctx, u, ref)
     back = ctx.project(uq.contiguous())
-    assert float(torch.linalg.vector_norm(back - u) / torch.linalg.vector_norm(u)) <= 1e-12
+    tol = 1e-12 if basis == "dubiner" else 1e-9  # cond(M) of the monomial basis amplifies rounding
+    assert float(torch.linalg.vector_norm(back - u) / torch.linalg.vector_norm(u)) <= tol
