@@ -165,12 +165,55 @@ static void dubiner_grad(int p, double x, double y, double* g) {
     }
 }
 
+/* LegendreBasis (quads), legendre.cpp:27-110: phi_{i,j} = P_i(x) P_j(y), j outer, i inner;
+ * P_n by the three-term recurrence, P'_n by n (x P_n - P_{n-1}) / (x^2 - 1) with the
+ * endpoint values n (n+1)/2 (+-1)^(n+1) at |x| = 1 (within 1e-12). */
+static void legendre_seq(int p, double x, double* P) {
+    P[0] = 1.0;
+    if (p >= 1) P[1] = x;
+    for (int i = 2; i <= p; ++i) P[i] = ((2 * i - 1) * x * P[i - 1] - (i - 1) * P[i - 2]) / i;
+}
+static double legendre_d(int n, double x, const double* P) {
+    if (n == 0) return 0.0;
+    if (fabs(fabs(x) - 1.0) < 1e-12) {
+        double sign = x > 0 ? 1.0 : -1.0, parity = (n % 2 == 0) ? 1.0 : -1.0;
+        return 0.5 * n * (n + 1) * parity * sign;
+    }
+    return n * (x * P[n] - P[n - 1]) / (x * x - 1.0);
+}
+static void legendre_eval(int p, double x, double y, double* phi) {
+    double Px[16], Py[16];
+    legendre_seq(p, x, Px);
+    legendre_seq(p, y, Py);
+    int idx = 0;
+    for (int j = 0; j <= p; ++j)
+        for (int i = 0; i <= p; ++i) phi[idx++] = Px[i] * Py[j];
+}
+static void legendre_grad(int p, double x, double y, double* g) {
+    double Px[16], Py[16], dx[16], dy[16];
+    legendre_seq(p, x, Px);
+    legendre_seq(p, y, Py);
+    for (int i = 0; i <= p; ++i) {
+        dx[i] = legendre_d(i, x, Px);
+        dy[i] = legendre_d(i, y, Py);
+    }
+    int idx = 0;
+    for (int j = 0; j <= p; ++j)
+        for (int i = 0; i <= p; ++i) {
+            g[2 * idx] = dx[i] * Py[j];
+            g[2 * idx + 1] = Px[i] * dy[j];
+            ++idx;
+        }
+}
+
 void orc_basis_eval(int basis, int p, double x, double y, double* phi) {
-    if (basis == ORC_BASIS_DUBINER) dubiner_eval(p, x, y, phi);
+    if (basis == ORC_BASIS_LEGENDRE) legendre_eval(p, x, y, phi);
+    else if (basis == ORC_BASIS_DUBINER) dubiner_eval(p, x, y, phi);
     else monomial_eval(p, x, y, phi);
 }
 void orc_basis_grad(int basis, int p, double x, double y, double* g) {
-    if (basis == ORC_BASIS_DUBINER) dubiner_grad(p, x, y, g);
+    if (basis == ORC_BASIS_LEGENDRE) legendre_grad(p, x, y, g);
+    else if (basis == ORC_BASIS_DUBINER) dubiner_grad(p, x, y, g);
     else monomial_grad(p, x, y, g);
 }
 
@@ -178,18 +221,36 @@ void orc_basis_grad(int basis, int p, double x, double y, double* g) {
 /* GeometricMapping::compute_mapping, mapping.cpp:22-50, with the P1 triangle shape
  * functions of ReferenceTriangle::compute_shape_functions, elements.cpp:40-56.
  * J_T = dN^T * vertices; dxi_dx = inverse(J_T) by the 2x2 cofactor formula. */
-int orc_compute_mapping(const double* V, double xi, double eta, double* xp, double* J_det,
-                        double* A) {
-    double N[3] = {1.0 - xi - eta, xi, eta};
-    static const double dN[3][2] = {{-1.0, -1.0}, {1.0, 0.0}, {0.0, 1.0}};
+int orc_compute_mapping_nv(int nv, const double* V, double xi, double eta, double* xp, double* J_det,
+                           double* A) {
+    double N[4], dN[4][2];
+    if (nv == 4) { /* ReferenceQuad::compute_shape_functions, elements.cpp:92-111 */
+        N[0] = 0.25 * (1.0 - xi) * (1.0 - eta);
+        N[1] = 0.25 * (1.0 + xi) * (1.0 - eta);
+        N[2] = 0.25 * (1.0 + xi) * (1.0 + eta);
+        N[3] = 0.25 * (1.0 - xi) * (1.0 + eta);
+        dN[0][0] = -0.25 * (1.0 - eta); dN[0][1] = -0.25 * (1.0 - xi);
+        dN[1][0] = 0.25 * (1.0 - eta);  dN[1][1] = -0.25 * (1.0 + xi);
+        dN[2][0] = 0.25 * (1.0 + eta);  dN[2][1] = 0.25 * (1.0 + xi);
+        dN[3][0] = -0.25 * (1.0 + eta); dN[3][1] = 0.25 * (1.0 - xi);
+    } else {
+        N[0] = 1.0 - xi - eta; N[1] = xi; N[2] = eta;
+        dN[0][0] = -1.0; dN[0][1] = -1.0; dN[1][0] = 1.0; dN[1][1] = 0.0; dN[2][0] = 0.0; dN[2][1] = 1.0;
+    }
     if (xp) {
-        xp[0] = N[0] * V[0] + N[1] * V[2] + N[2] * V[4];
-        xp[1] = N[0] * V[1] + N[1] * V[3] + N[2] * V[5];
+        xp[0] = xp[1] = 0.0;
+        for (int k = 0; k < nv; ++k) {
+            xp[0] += N[k] * V[2 * k];
+            xp[1] += N[k] * V[2 * k + 1];
+        }
     }
     double J[2][2];
     for (int r = 0; r < 2; ++r)
-        for (int c = 0; c < 2; ++c)
-            J[r][c] = dN[0][r] * V[c] + dN[1][r] * V[2 + c] + dN[2][r] * V[4 + c];
+        for (int c = 0; c < 2; ++c) {
+            double a = 0.0;
+            for (int k = 0; k < nv; ++k) a += dN[k][r] * V[2 * k + c];
+            J[r][c] = a;
+        }
     double det = J[0][0] * J[1][1] - J[1][0] * J[0][1];
     if (J_det) *J_det = det;
     if (fabs(det) < 1e-12) return -1; /* "Singular Jacobian matrix", mapping.cpp:42-44 */
@@ -203,16 +264,31 @@ int orc_compute_mapping(const double* V, double xi, double eta, double* xp, doub
     return 0;
 }
 
-/* DGSpace::map_face_quad_point (triangle), space.cpp:259-271 */
-void orc_map_face_point(int face, double s, double* xi) {
+int orc_compute_mapping(const double* V, double xi, double eta, double* xp, double* J_det, double* A) {
+    return orc_compute_mapping_nv(3, V, xi, eta, xp, J_det, A);
+}
+
+/* DGSpace::map_face_quad_point, space.cpp:259-288: triangle faces (t, 0), (1-t, t),
+ * (0, 1-t) with t = (s+1)/2; quad faces (s, -1), (1, s), (-s, 1), (-1, -s) */
+void orc_map_face_point_nv(int nv, int face, double s, double* xi) {
+    if (nv == 4) {
+        if (face == 0) { xi[0] = s; xi[1] = -1.0; }
+        else if (face == 1) { xi[0] = 1.0; xi[1] = s; }
+        else if (face == 2) { xi[0] = -s; xi[1] = 1.0; }
+        else { xi[0] = -1.0; xi[1] = -s; }
+        return;
+    }
     double t = 0.5 * (s + 1.0);
     if (face == 0) { xi[0] = t; xi[1] = 0.0; }
     else if (face == 1) { xi[0] = 1.0 - t; xi[1] = t; }
     else { xi[0] = 0.0; xi[1] = 1.0 - t; }
 }
+void orc_map_face_point(int face, double s, double* xi) { orc_map_face_point_nv(3, face, s, xi); }
 
-/* ReferenceTriangle::edge_vertices, elements.cpp:27-38 */
-static const int k_edge[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+/* ReferenceTriangle / ReferenceQuad::edge_vertices, elements.cpp:27-38, 73-90: edge f
+ * runs from vertex f to vertex (f + 1) mod nv */
+#define EDGE_A(f, nv) (f)
+#define EDGE_B(f, nv) (((f) + 1) % (nv))
 
 /* ------------------------------------------------------------------ mesh */
 typedef struct {
@@ -224,6 +300,8 @@ typedef struct {
 
 struct orc_mesh {
     int nv, ne;
+    int nvpe;  /* vertices (= faces) per element: 3 triangles, 4 quads */
+    double* own_q;  /* quads: the tensor Gauss-Legendre rule, [nq][2] points then [nq] weights */
     double* verts;
     int* elems;
     int* nbr;   /* [ne][3][2]  face_neighbors_ */
@@ -265,31 +343,34 @@ static int face_rec_cmp(const void* x, const void* y) {
  * become neighbours (once a key has two entries dgfem connects them and never undoes
  * it).  Boundary tags: a later tag overrides an earlier one for the same edge; faces
  * without a tagged edge get tag 0; with no boundary edges at all no face is tagged. */
-orc_mesh* orc_mesh_create(int nv, const double* verts, int ne, const int* elems, int nbe,
-                          const int* bedges) {
+orc_mesh* orc_mesh_create_nv(int nvpe, int nv, const double* verts, int ne, const int* elems, int nbe,
+                             const int* bedges) {
+    if (nvpe != 3 && nvpe != 4) return NULL;
+    const int K = nvpe;
     orc_mesh* m = (orc_mesh*)calloc(1, sizeof(orc_mesh));
     m->nv = nv;
     m->ne = ne;
-    m->verts = (double*)malloc(sizeof(double) * 2 * (size_t)nv);
+    m->nvpe = nvpe;
+    m->verts = (double*)malloc(sizeof(double) * 2 * (size_t)(nv ? nv : 1));
     memcpy(m->verts, verts, sizeof(double) * 2 * (size_t)nv);
-    m->elems = (int*)malloc(sizeof(int) * 3 * (size_t)ne);
-    memcpy(m->elems, elems, sizeof(int) * 3 * (size_t)ne);
-    m->nbr = (int*)malloc(sizeof(int) * 6 * (size_t)ne);
-    for (size_t i = 0; i < 6 * (size_t)ne; ++i) m->nbr[i] = -1;
-    m->btag = (int*)malloc(sizeof(int) * 3 * (size_t)ne);
-    for (size_t i = 0; i < 3 * (size_t)ne; ++i) m->btag[i] = -1;
+    m->elems = (int*)malloc(sizeof(int) * K * (size_t)(ne ? ne : 1));
+    memcpy(m->elems, elems, sizeof(int) * K * (size_t)ne);
+    m->nbr = (int*)malloc(sizeof(int) * 2 * K * (size_t)(ne ? ne : 1));
+    for (size_t i = 0; i < 2 * K * (size_t)ne; ++i) m->nbr[i] = -1;
+    m->btag = (int*)malloc(sizeof(int) * K * (size_t)(ne ? ne : 1));
+    for (size_t i = 0; i < K * (size_t)ne; ++i) m->btag[i] = -1;
 
-    size_t nf = 3 * (size_t)ne;
-    face_rec* r = (face_rec*)malloc(sizeof(face_rec) * nf);
+    size_t nf = K * (size_t)ne;
+    face_rec* r = (face_rec*)malloc(sizeof(face_rec) * (nf ? nf : 1));
     for (int e = 0; e < ne; ++e)
-        for (int f = 0; f < 3; ++f) {
-            int v1 = elems[3 * e + f], v2 = elems[3 * e + (f + 1) % 3];
-            face_rec* x = &r[3 * e + f];
+        for (int f = 0; f < K; ++f) {
+            int v1 = elems[K * e + f], v2 = elems[K * e + (f + 1) % K];
+            face_rec* x = &r[K * e + f];
             x->a = v1 < v2 ? v1 : v2;
             x->b = v1 < v2 ? v2 : v1;
             x->e = e;
             x->f = f;
-            x->ord = 3 * e + f;
+            x->ord = K * e + f;
         }
     qsort(r, nf, sizeof(face_rec), face_rec_cmp);
     for (size_t i = 0; i < nf;) {
@@ -297,10 +378,10 @@ orc_mesh* orc_mesh_create(int nv, const double* verts, int ne, const int* elems,
         while (j < nf && r[j].a == r[i].a && r[j].b == r[i].b) ++j;
         if (j - i >= 2) {
             int e1 = r[i].e, f1 = r[i].f, e2 = r[i + 1].e, f2 = r[i + 1].f;
-            m->nbr[6 * e1 + 2 * f1] = e2;
-            m->nbr[6 * e1 + 2 * f1 + 1] = f2;
-            m->nbr[6 * e2 + 2 * f2] = e1;
-            m->nbr[6 * e2 + 2 * f2 + 1] = f1;
+            m->nbr[2 * K * e1 + 2 * f1] = e2;
+            m->nbr[2 * K * e1 + 2 * f1 + 1] = f2;
+            m->nbr[2 * K * e2 + 2 * f2] = e1;
+            m->nbr[2 * K * e2 + 2 * f2 + 1] = f1;
         }
         i = j;
     }
@@ -316,9 +397,9 @@ orc_mesh* orc_mesh_create(int nv, const double* verts, int ne, const int* elems,
         }
         qsort(be, (size_t)nbe, sizeof(face_rec), face_rec_cmp);
         for (int e = 0; e < ne; ++e)
-            for (int f = 0; f < 3; ++f) {
-                if (m->nbr[6 * e + 2 * f] != -1) continue;
-                int v1 = elems[3 * e + f], v2 = elems[3 * e + (f + 1) % 3];
+            for (int f = 0; f < K; ++f) {
+                if (m->nbr[2 * K * e + 2 * f] != -1) continue;
+                int v1 = elems[K * e + f], v2 = elems[K * e + (f + 1) % K];
                 face_rec key = {v1 < v2 ? v1 : v2, v1 < v2 ? v2 : v1, 0, 0, 0};
                 int lo = 0, hi = nbe, tag = 0;
                 while (lo < hi) { /* first entry with sig >= key */
@@ -327,7 +408,7 @@ orc_mesh* orc_mesh_create(int nv, const double* verts, int ne, const int* elems,
                     else hi = mid;
                 }
                 while (lo < nbe && be[lo].a == key.a && be[lo].b == key.b) tag = be[lo++].e;
-                m->btag[3 * e + f] = tag;
+                m->btag[K * e + f] = tag;
             }
         free(be);
     }
@@ -335,9 +416,14 @@ orc_mesh* orc_mesh_create(int nv, const double* verts, int ne, const int* elems,
     return m;
 }
 
+orc_mesh* orc_mesh_create(int nv, const double* verts, int ne, const int* elems, int nbe, const int* bedges) {
+    return orc_mesh_create_nv(3, nv, verts, ne, elems, nbe, bedges);
+}
+
 static void mesh_free_space(orc_mesh* m) {
     free(m->phi_vol); free(m->dphi_vol); free(m->phi_face); free(m->jdet); free(m->dphi_dx);
-    free(m->fnormal); free(m->flen); free(m->fqp); free(m->dphi_dx_face); free(m->minv);
+    free(m->fnormal); free(m->flen); free(m->fqp); free(m->dphi_dx_face); free(m->minv); free(m->own_q);
+    m->own_q = NULL;
     m->phi_vol = m->dphi_vol = m->phi_face = m->jdet = m->dphi_dx = NULL;
     m->fnormal = m->flen = m->fqp = m->dphi_dx_face = m->minv = NULL;
 }
@@ -358,19 +444,19 @@ void orc_mesh_destroy(orc_mesh* m) {
 }
 
 static void elem_verts(const orc_mesh* m, int e, double* V) {
-    for (int k = 0; k < 3; ++k) {
-        int v = m->elems[3 * e + k];
+    for (int k = 0; k < m->nvpe; ++k) {
+        int v = m->elems[m->nvpe * e + k];
         V[2 * k] = m->verts[2 * v];
         V[2 * k + 1] = m->verts[2 * v + 1];
     }
 }
 
 /* DGSpace::compute_face_permutation, space.cpp:173-228: true when reversed */
-static int face_perm_reversed(const double* VL, int fL, const double* VR, int fR) {
-    const double* a1 = VL + 2 * k_edge[fL][0];
-    const double* b1 = VL + 2 * k_edge[fL][1];
-    const double* a2 = VR + 2 * k_edge[fR][0];
-    const double* b2 = VR + 2 * k_edge[fR][1];
+static int face_perm_reversed(int nv, const double* VL, int fL, const double* VR, int fR) {
+    const double* a1 = VL + 2 * EDGE_A(fL, nv);
+    const double* b1 = VL + 2 * EDGE_B(fL, nv);
+    const double* a2 = VR + 2 * EDGE_A(fR, nv);
+    const double* b2 = VR + 2 * EDGE_B(fR, nv);
     const double tol = 1e-10;
 #define NRM(p, q) sqrt(((p)[0] - (q)[0]) * ((p)[0] - (q)[0]) + ((p)[1] - (q)[1]) * ((p)[1] - (q)[1]))
     int rev = NRM(a1, b2) < tol && NRM(b1, a2) < tol;
@@ -403,30 +489,31 @@ static int pair_set_insert(pair_set* s, uint64_t k) {
 int orc_mesh_rebuild_faces(orc_mesh* m) {
     mesh_free_faces(m);
     int ne = m->ne;
-    m->ifaces = (int*)malloc(sizeof(int) * 5 * (size_t)ne * 3);
-    m->bfaces = (int*)malloc(sizeof(int) * 3 * (size_t)ne * 3);
+    const int K = m->nvpe;
+    m->ifaces = (int*)malloc(sizeof(int) * 5 * (size_t)(ne ? ne : 1) * K);
+    m->bfaces = (int*)malloc(sizeof(int) * 3 * (size_t)(ne ? ne : 1) * K);
     pair_set ps;
     ps.cap = 1;
     while (ps.cap < (size_t)ne * 4 + 16) ps.cap <<= 1;
     ps.keys = (uint64_t*)malloc(sizeof(uint64_t) * ps.cap);
     memset(ps.keys, 0xff, sizeof(uint64_t) * ps.cap);
     int nif = 0, nbf = 0;
-    double VL[6], VR[6];
+    double VL[8], VR[8];
     for (int L = 0; L < ne; ++L) {
         elem_verts(m, L, VL);
-        for (int fL = 0; fL < 3; ++fL) {
-            int R = m->nbr[6 * L + 2 * fL], fR = m->nbr[6 * L + 2 * fL + 1];
+        for (int fL = 0; fL < K; ++fL) {
+            int R = m->nbr[2 * K * L + 2 * fL], fR = m->nbr[2 * K * L + 2 * fL + 1];
             if (R >= 0) {
                 uint64_t lo = (uint64_t)(L < R ? L : R), hi = (uint64_t)(L < R ? R : L);
                 if (pair_set_insert(&ps, (lo << 32) | hi)) {
                     elem_verts(m, R, VR);
                     int* F = &m->ifaces[5 * nif++];
                     F[0] = L; F[1] = R; F[2] = fL; F[3] = fR;
-                    F[4] = face_perm_reversed(VL, fL, VR, fR);
+                    F[4] = face_perm_reversed(K, VL, fL, VR, fR);
                 }
             } else {
                 int* B = &m->bfaces[3 * nbf++];
-                B[0] = L; B[1] = fL; B[2] = m->btag[3 * L + fL];
+                B[0] = L; B[1] = fL; B[2] = m->btag[K * L + fL];
             }
         }
     }
@@ -454,9 +541,10 @@ int orc_mesh_rebuild_faces(orc_mesh* m) {
 /* DGMesh::set_periodic_boundaries, mesh.cpp:482-588 */
 int orc_mesh_set_periodic(orc_mesh* m, int tag1, int tag2, int match_on_y) {
     int ne = m->ne;
-    int *f1 = (int*)malloc(sizeof(int) * 3 * (size_t)ne), *f2 = (int*)malloc(sizeof(int) * 3 * (size_t)ne);
+    const int K = m->nvpe;
+    int *f1 = (int*)malloc(sizeof(int) * K * (size_t)(ne ? ne : 1)), *f2 = (int*)malloc(sizeof(int) * K * (size_t)(ne ? ne : 1));
     int n1 = 0, n2 = 0;
-    for (int i = 0; i < 3 * ne; ++i) { /* boundary_face_tags_ iterates in (elem, face) order */
+    for (int i = 0; i < K * ne; ++i) { /* boundary_face_tags_ iterates in (elem, face) order */
         if (m->btag[i] < 0) continue;
         if (m->btag[i] == tag1) f1[n1++] = i;
         else if (m->btag[i] == tag2) f2[n2++] = i;
@@ -464,14 +552,14 @@ int orc_mesh_set_periodic(orc_mesh* m, int tag1, int tag2, int match_on_y) {
     if (n1 == 0 || n2 == 0) { free(f1); free(f2); return -1; }
     double* c2 = (double*)malloc(sizeof(double) * (size_t)n2);
     for (int k = 0; k < n2; ++k) {
-        int e = f2[k] / 3, f = f2[k] % 3;
-        int va = m->elems[3 * e + f], vb = m->elems[3 * e + (f + 1) % 3];
+        int e = f2[k] / K, f = f2[k] % K;
+        int va = m->elems[K * e + f], vb = m->elems[K * e + (f + 1) % K];
         int c = match_on_y ? 1 : 0;
         c2[k] = 0.5 * (m->verts[2 * va + c] + m->verts[2 * vb + c]);
     }
     for (int k = 0; k < n1; ++k) {
-        int e1 = f1[k] / 3, l1 = f1[k] % 3;
-        int va = m->elems[3 * e1 + l1], vb = m->elems[3 * e1 + (l1 + 1) % 3];
+        int e1 = f1[k] / K, l1 = f1[k] % K;
+        int va = m->elems[K * e1 + l1], vb = m->elems[K * e1 + (l1 + 1) % K];
         int c = match_on_y ? 1 : 0;
         double c1 = 0.5 * (m->verts[2 * va + c] + m->verts[2 * vb + c]);
         double best = 1.79769313486231570815e308;
@@ -481,11 +569,11 @@ int orc_mesh_set_periodic(orc_mesh* m, int tag1, int tag2, int match_on_y) {
             if (d < best) { best = d; bi = j; }
         }
         if (bi >= 0) {
-            int e2 = f2[bi] / 3, l2 = f2[bi] % 3;
-            m->nbr[6 * e1 + 2 * l1] = e2;
-            m->nbr[6 * e1 + 2 * l1 + 1] = l2;
-            m->nbr[6 * e2 + 2 * l2] = e1;
-            m->nbr[6 * e2 + 2 * l2 + 1] = l1;
+            int e2 = f2[bi] / K, l2 = f2[bi] % K;
+            m->nbr[2 * K * e1 + 2 * l1] = e2;
+            m->nbr[2 * K * e1 + 2 * l1 + 1] = l2;
+            m->nbr[2 * K * e2 + 2 * l2] = e1;
+            m->nbr[2 * K * e2 + 2 * l2 + 1] = l1;
         }
     }
     free(c2); free(f1); free(f2);
@@ -497,49 +585,70 @@ int orc_mesh_set_periodic(orc_mesh* m, int tag1, int tag2, int match_on_y) {
  * space.cpp:20-67, 69-171, 230-257; mesh.cpp:53-99 */
 int orc_mesh_init_space(orc_mesh* m, int order, int basis) {
     if (order < 1 || order > 10) return -1;
+    const int K = m->nvpe;
+    if (K == 4 && basis != ORC_BASIS_LEGENDRE) return -1; /* DGSpace::create_basis, space.cpp:307-319 */
+    if (K == 3 && basis == ORC_BASIS_LEGENDRE) return -1;
     int nq;
-    if (orc_tri_rule(2 * order, &nq, &m->qp, &m->qw)) return -1;
-    if (orc_gl_rule(order + 1, &m->fp, &m->fw)) return -1;
     mesh_free_space(m);
+    if (K == 3) {
+        if (orc_tri_rule(2 * order, &nq, &m->qp, &m->qw)) return -1;
+    } else { /* QuadratureFactory::gauss_legendre_quad, factory.cpp:33-59: j outer, i inner */
+        const double *gp, *gw;
+        if (orc_gl_rule(order + 1, &gp, &gw)) return -1;
+        int n1 = order + 1;
+        nq = n1 * n1;
+        m->own_q = (double*)malloc(sizeof(double) * 3 * nq);
+        for (int j = 0; j < n1; ++j)
+            for (int i = 0; i < n1; ++i) {
+                int q = j * n1 + i;
+                m->own_q[2 * q] = gp[i];
+                m->own_q[2 * q + 1] = gp[j];
+                m->own_q[2 * nq + q] = gw[i] * gw[j];
+            }
+        m->qp = m->own_q;
+        m->qw = m->own_q + 2 * nq;
+    }
+    if (orc_gl_rule(order + 1, &m->fp, &m->fw)) return -1;
     m->order = order;
     m->basis = basis;
-    int np = m->np = orc_n_basis(order);
+    int np = m->np = K == 3 ? orc_n_basis(order) : (order + 1) * (order + 1);
     m->nq = nq;
     int nfq = m->nfq = order + 1;
     int ne = m->ne;
     m->phi_vol = (double*)malloc(sizeof(double) * nq * np);
     m->dphi_vol = (double*)malloc(sizeof(double) * nq * np * 2);
-    m->phi_face = (double*)malloc(sizeof(double) * 3 * nfq * np);
+    m->phi_face = (double*)malloc(sizeof(double) * K * nfq * np);
     for (int q = 0; q < nq; ++q) {
         orc_basis_eval(basis, order, m->qp[2 * q], m->qp[2 * q + 1], m->phi_vol + q * np);
         orc_basis_grad(basis, order, m->qp[2 * q], m->qp[2 * q + 1], m->dphi_vol + q * np * 2);
     }
-    for (int f = 0; f < 3; ++f)
+    for (int f = 0; f < K; ++f)
         for (int q = 0; q < nfq; ++q) {
             double xi[2];
-            orc_map_face_point(f, m->fp[q], xi);
+            orc_map_face_point_nv(K, f, m->fp[q], xi);
             orc_basis_eval(basis, order, xi[0], xi[1], m->phi_face + (f * nfq + q) * np);
         }
-    m->jdet = (double*)malloc(sizeof(double) * (size_t)ne * nq);
-    m->dphi_dx = (double*)malloc(sizeof(double) * (size_t)ne * nq * np * 2);
-    m->fnormal = (double*)malloc(sizeof(double) * (size_t)ne * 6);
-    m->flen = (double*)malloc(sizeof(double) * (size_t)ne * 3);
-    m->fqp = (double*)malloc(sizeof(double) * (size_t)ne * 3 * 2 * nfq);
-    m->dphi_dx_face = (double*)malloc(sizeof(double) * (size_t)ne * 3 * nfq * np * 2);
-    double* gface = (double*)malloc(sizeof(double) * 3 * nfq * np * 2);
-    for (int f = 0; f < 3; ++f)
+    size_t nes = ne ? (size_t)ne : 1;
+    m->jdet = (double*)malloc(sizeof(double) * nes * nq);
+    m->dphi_dx = (double*)malloc(sizeof(double) * nes * nq * np * 2);
+    m->fnormal = (double*)malloc(sizeof(double) * nes * 2 * K);
+    m->flen = (double*)malloc(sizeof(double) * nes * K);
+    m->fqp = (double*)malloc(sizeof(double) * nes * K * 2 * nfq);
+    m->dphi_dx_face = (double*)malloc(sizeof(double) * nes * K * nfq * np * 2);
+    double* gface = (double*)malloc(sizeof(double) * K * nfq * np * 2);
+    for (int f = 0; f < K; ++f)
         for (int q = 0; q < nfq; ++q) {
             double xi[2];
-            orc_map_face_point(f, m->fp[q], xi);
+            orc_map_face_point_nv(K, f, m->fp[q], xi);
             orc_basis_grad(basis, order, xi[0], xi[1], gface + (f * nfq + q) * np * 2);
         }
     int err = 0;
     for (int e = 0; e < ne; ++e) {
-        double V[6], A[4], det;
+        double V[8], A[4], det;
         elem_verts(m, e, V);
         /* compute_element_data, space.cpp:69-102 */
         for (int q = 0; q < nq; ++q) {
-            if (orc_compute_mapping(V, m->qp[2 * q], m->qp[2 * q + 1], NULL, &det, A)) err = -2;
+            if (orc_compute_mapping_nv(K, V, m->qp[2 * q], m->qp[2 * q + 1], NULL, &det, A)) err = -2;
             m->jdet[(size_t)e * nq + q] = det;
             for (int i = 0; i < np; ++i) {
                 const double* g = m->dphi_vol + (q * np + i) * 2;
@@ -549,30 +658,36 @@ int orc_mesh_init_space(orc_mesh* m, int order, int basis) {
             }
         }
         /* compute_face_data, space.cpp:104-171 */
-        double cx = (V[0] + V[2] + V[4]) / 3.0, cy = (V[1] + V[3] + V[5]) / 3.0;
-        for (int f = 0; f < 3; ++f) {
-            const double* v1 = V + 2 * k_edge[f][0];
-            const double* v2 = V + 2 * k_edge[f][1];
+        double cx = 0.0, cy = 0.0;
+        for (int k = 0; k < K; ++k) {
+            cx += V[2 * k];
+            cy += V[2 * k + 1];
+        }
+        cx /= K;
+        cy /= K;
+        for (int f = 0; f < K; ++f) {
+            const double* v1 = V + 2 * EDGE_A(f, K);
+            const double* v2 = V + 2 * EDGE_B(f, K);
             double tx = v2[0] - v1[0], ty = v2[1] - v1[1];
             double len = sqrt(tx * tx + ty * ty);
             if (len < 1e-14) err = -3; /* "Degenerate edge detected" */
             double nx = ty / len, ny = -tx / len;
             double mx = 0.5 * (v1[0] + v2[0]), my = 0.5 * (v1[1] + v2[1]);
             if (nx * (mx - cx) + ny * (my - cy) < 0) { nx = -nx; ny = -ny; }
-            m->fnormal[(size_t)e * 6 + 2 * f] = nx;
-            m->fnormal[(size_t)e * 6 + 2 * f + 1] = ny;
-            m->flen[(size_t)e * 3 + f] = len;
-            double* qpo = m->fqp + ((size_t)e * 3 + f) * 2 * nfq;
+            m->fnormal[(size_t)e * 2 * K + 2 * f] = nx;
+            m->fnormal[(size_t)e * 2 * K + 2 * f + 1] = ny;
+            m->flen[(size_t)e * K + f] = len;
+            double* qpo = m->fqp + ((size_t)e * K + f) * 2 * nfq;
             for (int q = 0; q < nfq; ++q) {
                 double t = 0.5 * (m->fp[q] + 1.0);
                 qpo[q] = (1.0 - t) * v1[0] + t * v2[0];
                 qpo[q + nfq] = (1.0 - t) * v1[1] + t * v2[1];
                 double xi[2];
-                orc_map_face_point(f, m->fp[q], xi);
-                if (orc_compute_mapping(V, xi[0], xi[1], NULL, &det, A)) err = -2;
+                orc_map_face_point_nv(K, f, m->fp[q], xi);
+                if (orc_compute_mapping_nv(K, V, xi[0], xi[1], NULL, &det, A)) err = -2;
                 for (int i = 0; i < np; ++i) {
                     const double* g = gface + ((f * nfq + q) * np + i) * 2;
-                    double* o = m->dphi_dx_face + (((size_t)e * 3 + f) * nfq * np + q * np + i) * 2;
+                    double* o = m->dphi_dx_face + (((size_t)e * K + f) * nfq * np + q * np + i) * 2;
                     o[0] = A[0] * g[0] + A[1] * g[1];
                     o[1] = A[2] * g[0] + A[3] * g[1];
                 }
@@ -594,8 +709,9 @@ void orc_mesh_boundary_faces(const orc_mesh* m, int* out) {
     memcpy(out, m->bfaces, sizeof(int) * 3 * (size_t)m->nbf);
 }
 void orc_mesh_neighbors(const orc_mesh* m, int* out) {
-    memcpy(out, m->nbr, sizeof(int) * 6 * (size_t)m->ne);
+    memcpy(out, m->nbr, sizeof(int) * 2 * m->nvpe * (size_t)m->ne);
 }
+int orc_mesh_nvpe(const orc_mesh* m) { return m->nvpe; }
 void orc_mesh_space_dims(const orc_mesh* m, int* np, int* nq, int* nfq) {
     *np = m->np; *nq = m->nq; *nfq = m->nfq;
 }
@@ -605,17 +721,18 @@ void orc_mesh_element_data(const orc_mesh* m, int e, double* J_det, double* dphi
 }
 void orc_mesh_face_data(const orc_mesh* m, int e, int f, double* normal, double* length,
                         double* quad_points, double* dphi_dx_face) {
-    normal[0] = m->fnormal[(size_t)e * 6 + 2 * f];
-    normal[1] = m->fnormal[(size_t)e * 6 + 2 * f + 1];
-    *length = m->flen[(size_t)e * 3 + f];
-    memcpy(quad_points, m->fqp + ((size_t)e * 3 + f) * 2 * m->nfq, sizeof(double) * 2 * m->nfq);
-    memcpy(dphi_dx_face, m->dphi_dx_face + ((size_t)e * 3 + f) * m->nfq * m->np * 2,
+    const int K = m->nvpe;
+    normal[0] = m->fnormal[(size_t)e * 2 * K + 2 * f];
+    normal[1] = m->fnormal[(size_t)e * 2 * K + 2 * f + 1];
+    *length = m->flen[(size_t)e * K + f];
+    memcpy(quad_points, m->fqp + ((size_t)e * K + f) * 2 * m->nfq, sizeof(double) * 2 * m->nfq);
+    memcpy(dphi_dx_face, m->dphi_dx_face + ((size_t)e * K + f) * m->nfq * m->np * 2,
            sizeof(double) * m->nfq * m->np * 2);
 }
 void orc_space_tables(const orc_mesh* m, double* phi_vol, double* phi_face, double* vol_w,
                       double* face_w) {
     memcpy(phi_vol, m->phi_vol, sizeof(double) * m->nq * m->np);
-    memcpy(phi_face, m->phi_face, sizeof(double) * 3 * m->nfq * m->np);
+    memcpy(phi_face, m->phi_face, sizeof(double) * m->nvpe * m->nfq * m->np);
     memcpy(vol_w, m->qw, sizeof(double) * m->nq);
     memcpy(face_w, m->fw, sizeof(double) * m->nfq);
 }
@@ -623,11 +740,11 @@ void orc_space_tables(const orc_mesh* m, double* phi_vol, double* phi_face, doub
 /* GeometricMapping::map_to_physical (mapping.cpp:52-58) at every volume point */
 void orc_mesh_quad_points(const orc_mesh* m, double* xq) {
     for (int e = 0; e < m->ne; ++e) {
-        double V[6];
+        double V[8];
         elem_verts(m, e, V);
         for (int q = 0; q < m->nq; ++q)
-            orc_compute_mapping(V, m->qp[2 * q], m->qp[2 * q + 1], xq + ((size_t)e * m->nq + q) * 2,
-                                NULL, NULL);
+            orc_compute_mapping_nv(m->nvpe, V, m->qp[2 * q], m->qp[2 * q + 1], xq + ((size_t)e * m->nq + q) * 2,
+                                   NULL, NULL);
     }
 }
 
@@ -803,10 +920,11 @@ int orc_interior_face_residual(const orc_mesh* m, const orc_physics* ph, int k, 
     const double* uR = UE(u, Rr, np);
     const double* phiL = m->phi_face + fL * nfq * np;
     const double* phiR = m->phi_face + fR * nfq * np;
-    const double* n = m->fnormal + (size_t)L * 6 + 2 * fL;
-    double hF = m->flen[(size_t)L * 3 + fL];
-    const double* gL = m->dphi_dx_face + ((size_t)L * 3 + fL) * nfq * np * 2;
-    const double* gR = m->dphi_dx_face + ((size_t)Rr * 3 + fR) * nfq * np * 2;
+    const int K = m->nvpe;
+    const double* n = m->fnormal + (size_t)L * 2 * K + 2 * fL;
+    double hF = m->flen[(size_t)L * K + fL];
+    const double* gL = m->dphi_dx_face + ((size_t)L * K + fL) * nfq * np * 2;
+    const double* gR = m->dphi_dx_face + ((size_t)Rr * K + fR) * nfq * np * 2;
     double sigma = viscous ? orc_penalty(ph, m->order, hF) : 0.0;
     memset(RL, 0, sizeof(double) * np * NV);
     memset(RR, 0, sizeof(double) * np * NV);
@@ -866,10 +984,11 @@ int orc_boundary_face_residual(const orc_mesh* m, const orc_physics* ph, int k, 
     const orc_bc* bc = (tag >= 0 && tag < MAX_TAGS && m->bc[tag].set) ? &m->bc[tag] : NULL;
     const double* ue = UE(u, e, np);
     const double* phi = m->phi_face + f * nfq * np;
-    const double* n = m->fnormal + (size_t)e * 6 + 2 * f;
-    double hF = m->flen[(size_t)e * 3 + f];
-    const double* qp = m->fqp + ((size_t)e * 3 + f) * 2 * nfq;
-    const double* g = m->dphi_dx_face + ((size_t)e * 3 + f) * nfq * np * 2;
+    const int K = m->nvpe;
+    const double* n = m->fnormal + (size_t)e * 2 * K + 2 * f;
+    double hF = m->flen[(size_t)e * K + f];
+    const double* qp = m->fqp + ((size_t)e * K + f) * 2 * nfq;
+    const double* g = m->dphi_dx_face + ((size_t)e * K + f) * nfq * np * 2;
     double sigma = viscous ? orc_penalty(ph, m->order, hF) : 0.0;
     memset(R, 0, sizeof(double) * np * NV);
     if (!viscous && !bc) return -1;
@@ -1126,11 +1245,11 @@ double orc_max_cfl(const orc_mesh* m, double gamma, const double* u, double dt) 
     int np = m->np, nq = m->nq;
     double max_cfl = 0.0;
     for (int e = 0; e < m->ne; ++e) {
-        double V[6];
+        double V[8];
         elem_verts(m, e, V);
         double h = 1.79769313486231570815e308;
-        for (int i = 0; i < 3; ++i)
-            for (int j = i + 1; j < 3; ++j) {
+        for (int i = 0; i < m->nvpe; ++i)
+            for (int j = i + 1; j < m->nvpe; ++j) {
                 double dx = V[2 * i] - V[2 * j], dy = V[2 * i + 1] - V[2 * j + 1];
                 double d = sqrt(dx * dx + dy * dy);
                 h = fmin(h, d);

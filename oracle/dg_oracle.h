@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-enum { ORC_BASIS_MONOMIAL = 0, ORC_BASIS_DUBINER = 1 };
+enum { ORC_BASIS_MONOMIAL = 0, ORC_BASIS_DUBINER = 1, ORC_BASIS_LEGENDRE = 2 /* quads */ };
 enum { ORC_BC_FAR_FIELD = 0, ORC_BC_SLIP_WALL = 1, ORC_BC_NO_SLIP_WALL = 2, ORC_BC_PERIODIC = 3 };
 
 typedef void (*orc_bc_fn)(double x, double y, double* out4, void* user);
@@ -51,11 +51,19 @@ int orc_gl_rule(int n, const double** pts, const double** wts);
 int orc_n_basis(int p);
 void orc_basis_eval(int basis, int p, double x, double y, double* phi);
 void orc_basis_grad(int basis, int p, double x, double y, double* grad /* [np][2] */);
+/* nv = 3 (P1 triangle on (0,0),(1,0),(0,1)) or 4 (bilinear quad on [-1,1]^2) */
+int orc_compute_mapping_nv(int nv, const double* verts, double xi, double eta, double* xp, double* J_det,
+                           double* dxi_dx);
+void orc_map_face_point_nv(int nv, int face, double s, double* xi);
 int orc_compute_mapping(const double* verts /* [3][2] */, double xi, double eta,
                         double* x_phys /* [2] */, double* J_det, double* dxi_dx /* [2][2] */);
 void orc_map_face_point(int face, double s, double* xi /* [2] */);
 
 /* mesh: DGMesh(vertices, elements, tags, boundary_tags, boundary_edges) */
+/* nvpe = 3 (triangles) or 4 (quads: elements [n][4], counter-clockwise) */
+orc_mesh* orc_mesh_create_nv(int nvpe, int nv, const double* verts, int ne, const int* elems, int n_bedge,
+                             const int* bedges);
+int orc_mesh_nvpe(const orc_mesh* m);
 orc_mesh* orc_mesh_create(int n_vert, const double* vertices, int n_elem, const int* elements,
                           int n_bedge, const int* bedges /* [n][3]: tag, v1, v2 (tag-sorted) */);
 void orc_mesh_destroy(orc_mesh* m);

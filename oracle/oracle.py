@@ -18,7 +18,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "liboracle.so"
 
-MONOMIAL, DUBINER = 0, 1
+MONOMIAL, DUBINER, LEGENDRE = 0, 1, 2  # LEGENDRE: the quad basis
 FAR_FIELD, SLIP_WALL, NO_SLIP_WALL, PERIODIC = 0, 1, 2, 3
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -62,6 +62,10 @@ def lib():
         L.orc_basis_grad.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, _dp]
         L.orc_compute_mapping.argtypes = [_dp, C.c_double, C.c_double, _dp, _dp, _dp]
         L.orc_map_face_point.argtypes = [C.c_int, C.c_double, _dp]
+        L.orc_compute_mapping_nv.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _dp, _dp, _dp]
+        L.orc_map_face_point_nv.argtypes = [C.c_int, C.c_int, C.c_double, _dp]
+        L.orc_mesh_create_nv.restype = C.c_void_p
+        L.orc_mesh_create_nv.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _ip, C.c_int, _ip]
         L.orc_mesh_create.restype = C.c_void_p
         L.orc_mesh_create.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _ip]
         L.orc_mesh_destroy.argtypes = [C.c_void_p]
@@ -128,36 +132,37 @@ def gl_rule(n):
     return np.ctypeslib.as_array(p, (n,)).copy(), np.ctypeslib.as_array(w, (n,)).copy()
 
 
-def n_basis(p):
-    return (p + 1) * (p + 2) // 2
+def n_basis(p, basis=MONOMIAL):
+    return (p + 1) * (p + 1) if basis == LEGENDRE else (p + 1) * (p + 2) // 2
 
 
 def basis_eval(basis, p, x, y):
-    out = np.zeros(n_basis(p))
+    out = np.zeros(n_basis(p, basis))
     lib().orc_basis_eval(basis, p, x, y, out)
     return out
 
 
 def basis_grad(basis, p, x, y):
-    out = np.zeros((n_basis(p), 2))
+    out = np.zeros((n_basis(p, basis), 2))
     lib().orc_basis_grad(basis, p, x, y, out)
     return out
 
 
 def compute_mapping(verts, xi, eta):
-    """Returns (x_phys, J_det, dxi_dx) or raises RuntimeError on a singular Jacobian."""
-    V = np.ascontiguousarray(verts, dtype=np.float64).reshape(3, 2)
+    """Returns (x_phys, J_det, dxi_dx) or raises RuntimeError on a singular Jacobian.
+    verts: 3 (triangle) or 4 (quad) vertices."""
+    V = np.ascontiguousarray(verts, dtype=np.float64).reshape(-1, 2)
     x = np.zeros(2)
     d = np.zeros(1)
     A = np.zeros((2, 2))
-    if lib().orc_compute_mapping(V, xi, eta, x, d, A):
+    if lib().orc_compute_mapping_nv(len(V), np.ascontiguousarray(V), xi, eta, x, d, A):
         raise RuntimeError("Singular Jacobian matrix")
     return x, d[0], A
 
 
-def map_face_point(face, s):
+def map_face_point(face, s, nv=3):
     out = np.zeros(2)
-    lib().orc_map_face_point(face, s, out)
+    lib().orc_map_face_point_nv(nv, face, s, out)
     return out
 
 
@@ -187,13 +192,15 @@ class OracleMesh:
                  periodic=()):
         L = lib()
         self.vertices = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 2)
-        self.elements = np.ascontiguousarray(elements, dtype=np.int32).reshape(-1, 3)
+        nvpe = np.asarray(elements).shape[-1]
+        self.nvpe = nvpe
+        self.elements = np.ascontiguousarray(elements, dtype=np.int32).reshape(-1, nvpe)
         be = np.zeros((0, 3), np.int32) if boundary_edges is None else \
             np.ascontiguousarray(boundary_edges, dtype=np.int32).reshape(-1, 3)
         # dgfem's boundary_edges is a std::map keyed by tag: iterate tags in ascending order
         be = be[np.argsort(be[:, 0], kind="stable")] if len(be) else be
-        self.h = L.orc_mesh_create(len(self.vertices), self.vertices, len(self.elements),
-                                   self.elements, len(be), np.ascontiguousarray(be))
+        self.h = L.orc_mesh_create_nv(nvpe, len(self.vertices), self.vertices, len(self.elements),
+                                      self.elements, len(be), np.ascontiguousarray(be))
         self.order = order
         self.basis = basis
         rc = L.orc_mesh_init_space(self.h, order, basis)
@@ -230,7 +237,7 @@ class OracleMesh:
         return out
 
     def neighbors(self):
-        out = np.zeros((self.ne, 3, 2), np.int32)
+        out = np.zeros((self.ne, self.nvpe, 2), np.int32)
         lib().orc_mesh_neighbors(self.h, out)
         return out
 
@@ -250,7 +257,7 @@ class OracleMesh:
 
     def tables(self):
         pv = np.zeros((self.nq, self.np))
-        pf = np.zeros((3, self.nfq, self.np))
+        pf = np.zeros((self.nvpe, self.nfq, self.np))
         vw = np.zeros(self.nq)
         fw = np.zeros(self.nfq)
         lib().orc_space_tables(self.h, pv, pf, vw, fw)

@@ -6,6 +6,8 @@
 * ``periodic_rectangle`` is an N x N quad grid split along each quad's (i,j)-(i+1,j+1)
   diagonal into two counter-clockwise triangles, with dgfem's GMSH physical tags
   Bottom=2, Right=3, Top=4, Left=5 (src/utils/mesh_creation.cpp:249-260).
+* ``quad_rectangle`` is the same grid as counter-clockwise quadrilaterals, optionally
+  with its interior vertices displaced (bilinear, non-affine elements).
 """
 
 import numpy as np
@@ -75,3 +77,34 @@ def isentropic_vortex(xy, t=0.0, beta=5.0, xc=0.0, yc=0.0, uinf=0.5, vinf=0.0, g
     rho = T ** (1.0 / (gamma - 1.0))
     p = rho * T
     return primitive_to_conserved(np.stack([rho, u, v, p], axis=-1), gamma)
+
+
+def quad_rectangle(n, x0=-5.0, x1=5.0, y0=-5.0, y1=5.0, nx=None, distort=0.0, seed=0):
+    nx = n if nx is None else nx
+    ny = n
+    xs = np.linspace(x0, x1, nx + 1)
+    ys = np.linspace(y0, y1, ny + 1)
+    X, Y = np.meshgrid(xs, ys)
+    verts = np.stack([X.ravel(), Y.ravel()], axis=1)
+    if distort:
+        rng = np.random.default_rng(seed)
+        hx, hy = (x1 - x0) / nx, (y1 - y0) / ny
+        inner = (np.abs(verts[:, 0] - x0) > 1e-12) & (np.abs(verts[:, 0] - x1) > 1e-12) & \
+                (np.abs(verts[:, 1] - y0) > 1e-12) & (np.abs(verts[:, 1] - y1) > 1e-12)
+        verts = verts.copy()
+        verts[inner] += distort * np.array([hx, hy]) * rng.uniform(-1, 1, (inner.sum(), 2))
+
+    def vid(i, j):
+        return j * (nx + 1) + i
+
+    elems = [(vid(i, j), vid(i + 1, j), vid(i + 1, j + 1), vid(i, j + 1)) for j in range(ny) for i in range(nx)]
+    be = []
+    for i in range(nx):
+        be.append((BOTTOM, vid(i, 0), vid(i + 1, 0)))
+    for j in range(ny):
+        be.append((RIGHT, vid(nx, j), vid(nx, j + 1)))
+    for i in range(nx):
+        be.append((TOP, vid(i, ny), vid(i + 1, ny)))
+    for j in range(ny):
+        be.append((LEFT, vid(0, j), vid(0, j + 1)))
+    return verts, np.array(elems, dtype=np.int32), np.array(be, dtype=np.int32)
