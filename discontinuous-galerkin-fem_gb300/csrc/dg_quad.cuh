@@ -1,0 +1,440 @@
+// Element kernel for bilinear quadrilaterals (DGSpace("quad", p) with dgfem's LegendreBasis):
+// volume flux integral, the four faces' numerical fluxes, the element's inverse mass
+// matrix and the SSP-RK3 stage combination, one thread per element, 128 elements per CTA.
+//
+// The residual is dgfem's (src/solver/assembler.cpp:137-279 with
+// src/weak_forms/euler_weak_formulation.cpp:72-250 and
+// src/weak_forms/navier_stokes_weak_formulation.cpp:100-273), organised per element as in
+// the triangle kernel: each element evaluates its own faces with its own outward normal,
+// the R side of an interior face carrying -n_L and the L side's face length.
+//
+// Quadrilateral specifics:
+//  * the bilinear map is not affine: J_T, |J| and A = inverse(J_T) are evaluated at every
+//    volume and face point from six per-element coefficients (QuadGeom); no per-point
+//    geometry is stored.  In the volume term |J| A needs no division:
+//      |J| A = sign(det) [[J11, -J01], [-J10, J00]].
+//  * M_K = Phi^T diag(w_q |J_q|) Phi with Phi the (p+1)^2 x (p+1)^2 matrix of basis values at
+//    the tensor Gauss-Legendre points.  Phi is square and, because that rule integrates
+//    the Legendre products exactly, Phi^T W Phi = D, the diagonal reference mass matrix.
+//    Hence Phi^-1 = D^-1 Phi^T W and
+//      M_K^-1 = D^-1 Phi^T diag(w_q / |J_q|) Phi D^-1,
+//    two contractions with the interpolation table and a pointwise scaling, instead of
+//    the dense per-element inverse dgfem stores
+//    (CompressibleDGSolverBase::compute_mass_matrix_inverse_blocks,
+//    src/solver/compressible_solver_base.cpp:41-61).
+#pragma once
+
+#include "../../include/dgx.h"
+#include "dg_physics.cuh"
+
+namespace dgx {
+
+template <int P, typename T>
+struct QuadOps {
+    static constexpr int N1 = P + 1, NP = N1 * N1, NQ = NP, NFQ = N1;
+    T phi[NQ][NP];        // basis at volume points (q = j (p+1) + i at (x_i, x_j))
+    T dr[NQ][NP];         // d/dxi at volume points
+    T ds[NQ][NP];         // d/deta at volume points
+    T phif[4][NFQ][NP];   // basis at face points
+    T drf[4][NFQ][NP];
+    T dsf[4][NFQ][NP];
+    T wq[NQ];             // tensor Gauss-Legendre weights
+    T xq[NQ][2];          // volume points (xi, eta)
+    T wf[NFQ];            // Gauss-Legendre weights on [-1, 1]
+    T xf[4][NFQ][2];      // face points on the reference square
+    double dinv[NP];      // 1 / D_kk, D = sum_q w_q phi phi^T (diagonal)
+};
+
+template <int P, typename T>
+inline void fill_quad_ops(const OpsHost& h, QuadOps<P, T>& o) {
+    using Q = QuadOps<P, T>;
+    for (int q = 0; q < Q::NQ; ++q) {
+        for (int i = 0; i < Q::NP; ++i) {
+            o.phi[q][i] = (T)h.phi[q][i];
+            o.dr[q][i] = (T)h.dr[q][i];
+            o.ds[q][i] = (T)h.ds[q][i];
+        }
+        o.wq[q] = (T)h.wq[q];
+        o.xq[q][0] = (T)h.qp[q][0];
+        o.xq[q][1] = (T)h.qp[q][1];
+    }
+    for (int f = 0; f < 4; ++f)
+        for (int j = 0; j < Q::NFQ; ++j) {
+            for (int i = 0; i < Q::NP; ++i) {
+                o.phif[f][j][i] = (T)h.phif[f][j][i];
+                o.drf[f][j][i] = (T)h.drf[f][j][i];
+                o.dsf[f][j][i] = (T)h.dsf[f][j][i];
+            }
+            o.xf[f][j][0] = (T)h.fxi[f][j][0];
+            o.xf[f][j][1] = (T)h.fxi[f][j][1];
+        }
+    for (int j = 0; j < Q::NFQ; ++j) o.wf[j] = (T)h.wf[j];
+    for (int i = 0; i < Q::NP; ++i) o.dinv[i] = h.minv[i][i];
+}
+
+template <int P, typename T, bool VISC>
+struct QKArgs {
+    StepArgs s;  // s.geom and s.conn are not used
+    const QuadGeom* geom;
+    const QuadConn* conn;
+    QuadOps<P, T> o;
+};
+
+// J_T at (xi, eta): rows (dx/dxi, dy/dxi) and (dx/deta, dy/deta) (mapping.cpp:22-50)
+template <typename T>
+__device__ __forceinline__ void quad_jacobian(const QuadGeom& G, T xi, T eta, T& J00, T& J01, T& J10, T& J11) {
+    J00 = (T)G.jx[0] + (T)G.jx[2] * eta;
+    J01 = (T)G.jy[0] + (T)G.jy[2] * eta;
+    J10 = (T)G.jx[1] + (T)G.jx[2] * xi;
+    J11 = (T)G.jy[1] + (T)G.jy[2] * xi;
+}
+
+// A = inverse(J_T) (mapping.cpp:33-47): dphi/dx = A0 dphi/dxi + A1 dphi/deta,
+// dphi/dy = A2 dphi/dxi + A3 dphi/deta
+template <typename T>
+__device__ __forceinline__ void quad_inverse_map(const QuadGeom& G, T xi, T eta, T A[4]) {
+    T J00, J01, J10, J11;
+    quad_jacobian<T>(G, xi, eta, J00, J01, J10, J11);
+    const T r = rcp_<T>(J00 * J11 - J10 * J01);
+    A[0] = J11 * r;
+    A[1] = -J01 * r;
+    A[2] = -J10 * r;
+    A[3] = J00 * r;
+}
+
+// Exterior state of a boundary face (boundary_face_residual, :177-250); false when the
+// face has no condition that contributes an inviscid flux.
+template <typename T>
+__device__ __forceinline__ bool quad_boundary_state(const BCSlot& bc, const T Uo[4], T nx, T ny, T gamma, T Ub[4]) {
+    if (bc.type == DGX_BC_FAR_FIELD) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) Ub[v] = (T)bc.value[v];
+        return true;
+    }
+    if (bc.type == DGX_BC_SLIP_WALL) {  // reflect the normal velocity
+        const T rr = rcp_<T>(Uo[0]);
+        const T u = Uo[1] * rr, vv = Uo[2] * rr;
+        const T p = (gamma - T(1)) * (Uo[3] - T(0.5) * Uo[0] * (u * u + vv * vv));
+        const T un = u * nx + vv * ny;
+        const T W[4] = {Uo[0], (u - un * nx) - un * nx, (vv - un * ny) - un * ny, p};
+        p2c<T>(W, gamma, Ub);
+        return true;
+    }
+    if (bc.type == DGX_BC_NO_SLIP_WALL) {  // primitive wall state
+        const T W[4] = {(T)bc.value[0], (T)bc.value[1], (T)bc.value[2], (T)bc.value[3]};
+        p2c<T>(W, gamma, Ub);
+        return true;
+    }
+    return false;
+}
+
+// Residual of one quadrilateral into R.  Ue: its coefficients (shared memory); sU, e0,
+// nloc: the tile, for in-tile neighbours; others are read from u (FP64) in global memory.
+template <int P, typename T, bool VISC>
+__device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* Ue, const T* sU, int e0, int nloc,
+                                              const double* u, const QuadGeom& G, const QuadConn& C,
+                                              const BCSlot* bcs, const QuadGeom* geoms, T gamma, T mu,
+                                              T kappa, T sigma0, T R[n_basis_quad(P)][NV]) {
+    constexpr int NP = n_basis_quad(P), NQ = NP, NFQ = P + 1, NB = NP * NV, STR = NB + 1;
+
+    // ---------------- volume: EulerWeakFormulation::volume_residual (:72-115)
+    //                  + NavierStokesWeakFormulation::viscous_volume_residual (:100-140)
+#pragma unroll 1
+    for (int q = 0; q < NQ; ++q) {
+        T U[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+        for (int i = 0; i < NP; ++i)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) U[v] = mac(U[v], o.phi[q][i], Ue[i * NV + v]);
+        T F[4], Gf[4], uu, vv, pp, ri;
+        euler_flux<T>(U, gamma - T(1), F, Gf, uu, vv, pp, ri);
+        T J00, J01, J10, J11;
+        quad_jacobian<T>(G, o.xq[q][0], o.xq[q][1], J00, J01, J10, J11);
+        const T det = J00 * J11 - J10 * J01;
+        if (VISC) {
+            T gr[4] = {T(0), T(0), T(0), T(0)}, gs[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+            for (int i = 0; i < NP; ++i)
+#pragma unroll
+                for (int v = 0; v < NV; ++v) {
+                    gr[v] = mac(gr[v], o.dr[q][i], Ue[i * NV + v]);
+                    gs[v] = mac(gs[v], o.ds[q][i], Ue[i * NV + v]);
+                }
+            const T r = rcp_<T>(det);
+            const T A0 = J11 * r, A1 = -J01 * r, A2 = -J10 * r, A3 = J00 * r;
+            T gx[4], gy[4], Fv[4], Gv[4];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                gx[v] = A0 * gr[v] + A1 * gs[v];
+                gy[v] = A2 * gr[v] + A3 * gs[v];
+            }
+            viscous_flux<T>(U, gx, gy, gamma, mu, kappa, Fv, Gv);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                F[v] -= Fv[v];
+                Gf[v] -= Gv[v];
+            }
+        }
+        // w |J| (A0 F + A2 G) and w |J| (A1 F + A3 G), |J| A = sign(det) adj(J_T)
+        const T w = det > T(0) ? o.wq[q] : -o.wq[q];
+        T Fr[4], Fs[4];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            Fr[v] = w * (J11 * F[v] - J10 * Gf[v]);
+            Fs[v] = w * (J00 * Gf[v] - J01 * F[v]);
+        }
+#pragma unroll
+        for (int i = 0; i < NP; ++i)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) R[i][v] = mac(mac(R[i][v], o.dr[q][i], Fr[v]), o.ds[q][i], Fs[v]);
+    }
+
+    // ---------------- faces: interior_face_residual (:117-175), boundary_face_residual
+    //                  (:177-250) and their viscous counterparts (NS :142-273)
+#pragma unroll 1
+    for (int f = 0; f < 4; ++f) {
+        const int nb = C.nbr[f];
+        if (nb == NBR_SKIP) continue;
+        const int fl = (C.flags >> (4 * f)) & 15;
+        const int nf = fl & 3;
+        const bool rev = (fl >> 2) & 1;
+        const T sideL = ((fl >> 3) & 1) ? T(1) : T(-1);
+        const T nx = (T)G.n[f][0], ny = (T)G.n[f][1];
+        const T hF = (T)G.h[f];
+        const T* Un_s = nullptr;
+        BCSlot bc;
+        bc.type = -1;
+        if (nb >= 0) {
+            if (nb >= e0 && nb < e0 + nloc) Un_s = sU + (nb - e0) * STR;
+        } else {
+            bc = bcs[-1 - nb];
+        }
+        auto nrow = [&](int i, T c[4]) {
+            if (Un_s) {
+#pragma unroll
+                for (int v = 0; v < NV; ++v) c[v] = Un_s[i * NV + v];
+            } else {
+                const double* p = u + (size_t)nb * NB + i * NV;
+                const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+                const double2 b = __ldg(reinterpret_cast<const double2*>(p + 2));
+                c[0] = (T)a.x;
+                c[1] = (T)a.y;
+                c[2] = (T)b.x;
+                c[3] = (T)b.y;
+            }
+        };
+        // NavierStokesWeakFormulation::compute_penalty_parameter (:275-278)
+        const T sigma = VISC ? sigma0 * mu * T((P + 1) * (P + 1)) / (hF > T(1e-12) ? hF : T(1e-12)) : T(0);
+#pragma unroll 1
+        for (int j = 0; j < NFQ; ++j) {
+            T Uo[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+            for (int i = 0; i < NP; ++i)
+#pragma unroll
+                for (int v = 0; v < NV; ++v) Uo[v] = mac(Uo[v], o.phif[f][j][i], Ue[i * NV + v]);
+            T Un[4] = {T(0), T(0), T(0), T(0)};
+            const int k = rev ? NFQ - 1 - j : j;
+            if (nb >= 0) {
+#pragma unroll
+                for (int i = 0; i < NP; ++i) {
+                    T c[4];
+                    nrow(i, c);
+                    const T ph = o.phif[nf][k][i];
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) Un[v] = mac(Un[v], ph, c[v]);
+                }
+            }
+            T H[4] = {T(0), T(0), T(0), T(0)};
+            if (nb >= 0) {
+                rusanov<T>(Uo, Un, nx, ny, gamma, H);
+            } else {
+                T Ub[4];
+                if (quad_boundary_state<T>(bc, Uo, nx, ny, gamma, Ub)) rusanov<T>(Uo, Ub, nx, ny, gamma, H);
+            }
+            if (VISC) {
+                T gr[4] = {T(0), T(0), T(0), T(0)}, gs[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+                for (int i = 0; i < NP; ++i)
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) {
+                        gr[v] = mac(gr[v], o.drf[f][j][i], Ue[i * NV + v]);
+                        gs[v] = mac(gs[v], o.dsf[f][j][i], Ue[i * NV + v]);
+                    }
+                T A[4];
+                quad_inverse_map<T>(G, o.xf[f][j][0], o.xf[f][j][1], A);
+                T gx[4], gy[4], Fv[4], Gv[4];
+#pragma unroll
+                for (int v = 0; v < NV; ++v) {
+                    gx[v] = A[0] * gr[v] + A[1] * gs[v];
+                    gy[v] = A[2] * gr[v] + A[3] * gs[v];
+                }
+                viscous_flux<T>(Uo, gx, gy, gamma, mu, kappa, Fv, Gv);
+                if (nb >= 0) {
+                    T nr[4] = {T(0), T(0), T(0), T(0)}, ns[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+                    for (int i = 0; i < NP; ++i) {
+                        T c[4];
+                        nrow(i, c);
+#pragma unroll
+                        for (int v = 0; v < NV; ++v) {
+                            nr[v] = mac(nr[v], o.drf[nf][k][i], c[v]);
+                            ns[v] = mac(ns[v], o.dsf[nf][k][i], c[v]);
+                        }
+                    }
+                    T B[4];
+                    quad_inverse_map<T>(geoms[nb], o.xf[nf][k][0], o.xf[nf][k][1], B);
+                    T hx[4], hy[4], Fn2[4], Gn2[4];
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) {
+                        hx[v] = B[0] * nr[v] + B[1] * ns[v];
+                        hy[v] = B[2] * nr[v] + B[3] * ns[v];
+                    }
+                    viscous_flux<T>(Un, hx, hy, gamma, mu, kappa, Fn2, Gn2);
+                    // own side L:  Fn = 1/2 (Fv_o - Fv_n).n - sigma (U_n - U_o)
+                    // own side R:  dgfem adds +w phi Fn_L, i.e. -= w phi (-J - P)
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) {
+                        const T jmp = T(0.5) * ((Fv[v] * nx + Gv[v] * ny) - (Fn2[v] * nx + Gn2[v] * ny));
+                        H[v] += sideL * jmp - sigma * (Un[v] - Uo[v]);
+                    }
+                } else if (bc.type >= 0) {
+                    T Ub[4] = {Uo[0], Uo[1], Uo[2], Uo[3]};
+                    if (bc.type == DGX_BC_NO_SLIP_WALL) {
+                        const T W[4] = {(T)bc.value[0], (T)bc.value[1], (T)bc.value[2], (T)bc.value[3]};
+                        p2c<T>(W, gamma, Ub);
+                    } else {
+#pragma unroll
+                        for (int v = 0; v < 4; ++v) Ub[v] = (T)bc.value[v];
+                    }
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) H[v] += (Fv[v] * nx + Gv[v] * ny) - sigma * (Ub[v] - Uo[v]);
+                }
+            }
+            const T w = o.wf[j] * hF * T(0.5);
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                const T sc = w * o.phif[f][j][i];
+#pragma unroll
+                for (int v = 0; v < NV; ++v) R[i][v] = mac(R[i][v], -sc, H[v]);
+            }
+        }
+    }
+}
+
+// M_K^-1 applied to the row r (this thread's NP x 4 values in shared memory, overwritten):
+// r <- D^-1 Phi^T diag(w_q / |J_q|) Phi D^-1 r, accumulated in acc (registers).
+template <int P, typename T>
+__device__ __forceinline__ void quad_mass_inv_row(const QuadOps<P, T>& o, const QuadGeom& G, double* r,
+                                                  double acc[n_basis_quad(P)][NV]) {
+    constexpr int NP = n_basis_quad(P), NQ = NP;
+#pragma unroll
+    for (int i = 0; i < NP; ++i)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            r[i * NV + v] *= o.dinv[i];
+            acc[i][v] = 0.0;
+        }
+#pragma unroll 1
+    for (int q = 0; q < NQ; ++q) {
+        double y[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int k = 0; k < NP; ++k)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) y[v] += (double)o.phi[q][k] * r[k * NV + v];
+        double J00, J01, J10, J11;
+        quad_jacobian<double>(G, (double)o.xq[q][0], (double)o.xq[q][1], J00, J01, J10, J11);
+        const double s = (double)o.wq[q] / fabs(J00 * J11 - J10 * J01);
+#pragma unroll
+        for (int i = 0; i < NP; ++i) {
+            const double ph = (double)o.phi[q][i] * s;
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[i][v] += ph * y[v];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < NP; ++i)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) r[i * NV + v] = o.dinv[i] * acc[i][v];
+}
+
+#ifndef DGX_QUAD_MIN_BLOCKS
+#define DGX_QUAD_MIN_BLOCKS 1
+#endif
+template <int P, typename T, bool VISC>
+__global__ void __launch_bounds__(TILE, DGX_QUAD_MIN_BLOCKS) quad_element_kernel(const __grid_constant__ QKArgs<P, T, VISC> ka) {
+    constexpr int NP = n_basis_quad(P), NB = NP * NV, STR = NB + 1;
+    const StepArgs& s = ka.s;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sU = reinterpret_cast<T*>(smem_raw);  // [TILE][STR], odd stride: conflict-free rows
+
+    const int e0 = blockIdx.x * TILE;
+    const int nloc = min(TILE, s.ne - e0);
+    const int tl = threadIdx.x;
+    const bool active = tl < nloc;
+    const int e = e0 + tl;
+
+    {   // stage the tile's coefficients: one contiguous run of nloc*NB doubles
+        const double* ug = s.u + (size_t)e0 * NB;
+        for (int g = tl; g < nloc * NB; g += TILE) {
+            const int el = g / NB;
+            sU[el * STR + (g - el * NB)] = (T)__ldg(ug + g);
+        }
+    }
+    __syncthreads();
+
+    T R[NP][NV];
+#pragma unroll
+    for (int i = 0; i < NP; ++i)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) R[i][v] = T(0);
+
+    if (active) {
+        const T mu = (T)s.mu;
+        const T kappa = VISC ? (T)(s.mu * s.gamma / (s.prandtl * (s.gamma - 1.0))) : T(0);
+        quad_residual<P, T, VISC>(ka.o, sU + tl * STR, sU, e0, nloc, s.u, ka.geom[e], ka.conn[e], s.bc, ka.geom,
+                                  (T)s.gamma, mu, kappa, (T)s.sigma0, R);
+    }
+    __syncthreads();  // all neighbour reads of sU are done
+
+    // ---------------- epilogue: residual, or M_K^-1 R (apply_mass_inv,
+    // compressible_solver_base.cpp:54-61) and the SSP-RK3 combination (time_stepping.hpp:39-55)
+    double* sD = reinterpret_cast<double*>(smem_raw);  // [TILE][STR] doubles, reuses sU
+    if (active) {
+#pragma unroll
+        for (int i = 0; i < NP; ++i)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) sD[tl * STR + i * NV + v] = (double)R[i][v];
+        if (s.mode != MODE_RESIDUAL) {
+            double acc[NP][NV];
+            quad_mass_inv_row<P, T>(ka.o, ka.geom[e], sD + tl * STR, acc);
+        }
+    }
+    __syncthreads();
+    double* og = s.out + (size_t)e0 * NB;
+    const double* ug = s.u + (size_t)e0 * NB;
+    const double* ung = s.un ? s.un + (size_t)e0 * NB : nullptr;
+    bool bad = false;
+    for (int g = tl; g < nloc * NB; g += TILE) {
+        const int el = g / NB;
+        const double d = sD[el * STR + (g - el * NB)];
+        double r;
+        if (s.mode != MODE_STAGE) {
+            r = d;
+        } else if (s.a == 0.0) {
+            r = ug[g] + s.dt * d;
+        } else {
+            const double t = ug[g] + s.dt * d;
+            r = s.a * __ldg(ung + g) + s.b * t;
+        }
+        bad |= !isfinite(r);
+        og[g] = r;
+    }
+    if (bad && s.status) atomicOr(s.status, 1);
+}
+
+template <int P, typename T>
+inline size_t quad_smem_bytes() {
+    return (size_t)TILE * (n_basis_quad(P) * NV + 1) * sizeof(double);
+}
+
+}  // namespace dgx

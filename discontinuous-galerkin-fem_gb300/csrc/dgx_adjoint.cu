@@ -194,6 +194,7 @@ int adjoint_step(dgx_ctx* c, const double* un, const double* u1, const double* u
 }  // namespace
 
 extern "C" int dgx_residual_jvp(dgx_ctx* c, const double* u, const double* du, double* dr, void* stream) {
+    if (c && c->nvpe == 4) return dgx::set_error(DGX_ERR_INVALID, "dgx_residual_jvp: triangle meshes only");
     if (!c || (c->ne && (!u || !du || !dr))) return dgx::set_error(DGX_ERR_INVALID, "dgx_residual_jvp: null argument");
     if (int rc = need_fp64(c, "dgx_residual_jvp")) return rc;
     if (c->ne == 0) return DGX_OK;
@@ -209,6 +210,7 @@ extern "C" int dgx_residual_jvp(dgx_ctx* c, const double* u, const double* du, d
 }
 
 extern "C" int dgx_residual_vjp(dgx_ctx* c, const double* u, const double* rbar, double* ubar, void* stream) {
+    if (c && c->nvpe == 4) return dgx::set_error(DGX_ERR_INVALID, "dgx_residual_vjp: triangle meshes only");
     if (!c || (c->ne && (!u || !rbar || !ubar))) return dgx::set_error(DGX_ERR_INVALID, "dgx_residual_vjp: null argument");
     if (int rc = need_adjoint(c, "dgx_residual_vjp")) return rc;
     if (c->ne == 0) return DGX_OK;
@@ -223,6 +225,7 @@ extern "C" int dgx_residual_vjp(dgx_ctx* c, const double* u, const double* rbar,
 }
 
 extern "C" int dgx_rk3_step_tlm(dgx_ctx* c, double* u, double* du, double dt, int n_steps, void* stream) {
+    if (c && c->nvpe == 4) return dgx::set_error(DGX_ERR_INVALID, "dgx_rk3_step_tlm: triangle meshes only");
     if (!c || (c->ne && (!u || !du)) || n_steps < 0) return dgx::set_error(DGX_ERR_INVALID, "dgx_rk3_step_tlm: bad argument");
     if (int rc = need_fp64(c, "dgx_rk3_step_tlm")) return rc;
     if (c->ne == 0 || n_steps == 0) return DGX_OK;
@@ -248,6 +251,7 @@ extern "C" int dgx_rk3_step_tlm(dgx_ctx* c, double* u, double* du, double dt, in
 }
 
 extern "C" int dgx_rk3_step_adjoint(dgx_ctx* c, const double* u_n, double* ubar, double dt, void* stream) {
+    if (c && c->nvpe == 4) return dgx::set_error(DGX_ERR_INVALID, "dgx_rk3_step_adjoint: triangle meshes only");
     if (!c || (c->ne && (!u_n || !ubar))) return dgx::set_error(DGX_ERR_INVALID, "dgx_rk3_step_adjoint: null argument");
     if (int rc = need_adjoint(c, "dgx_rk3_step_adjoint")) return rc;
     if (c->ne == 0) return DGX_OK;
@@ -260,6 +264,7 @@ extern "C" int dgx_rk3_step_adjoint(dgx_ctx* c, const double* u_n, double* ubar,
 }
 
 extern "C" int dgx_kinetic_energy(dgx_ctx* c, const double* u, double* J, double* grad, void* stream) {
+    if (c && c->nvpe == 4) return dgx::set_error(DGX_ERR_INVALID, "dgx_kinetic_energy: triangle meshes only");
     if (!c || (c->ne && !u)) return dgx::set_error(DGX_ERR_INVALID, "dgx_kinetic_energy: null argument");
     cudaStream_t s = (cudaStream_t)stream;
     if (c->ne == 0) {
@@ -287,6 +292,7 @@ extern "C" int dgx_kinetic_energy(dgx_ctx* c, const double* u, double* J, double
 
 extern "C" int dgx_kinetic_energy_gradient(dgx_ctx* c, const double* u0, double dt, int n_steps,
                                            int checkpoint_every, double* J, double* grad, void* stream) {
+    if (c && c->nvpe == 4) return dgx::set_error(DGX_ERR_INVALID, "dgx_kinetic_energy_gradient: triangle meshes only");
     if (!c || (c->ne && (!u0 || !grad)) || n_steps < 0 || checkpoint_every < 1)
         return dgx::set_error(DGX_ERR_INVALID, "dgx_kinetic_energy_gradient: bad argument");
     if (int rc = need_adjoint(c, "dgx_kinetic_energy_gradient")) return rc;

@@ -20,6 +20,9 @@ struct dgx_ctx {
     dgx::ElemGeom* d_geom = nullptr;
     dgx::ElemGeomF* d_geomf = nullptr;  // FP32 rounding of d_geom (mixed precision)
     dgx::ElemConn* d_conn = nullptr;
+    int nvpe = 3;                        // 4: quadrilateral mesh (d_qgeom/d_qconn replace d_geom/d_conn)
+    dgx::QuadGeom* d_qgeom = nullptr;
+    dgx::QuadConn* d_qconn = nullptr;
     dgx::BCSlot* d_bc = nullptr;
     double* d_u1 = nullptr;
     double* d_u2 = nullptr;
@@ -54,8 +57,10 @@ int make_ops(int p, int basis, OpsHost& o);
 // Host copy of a mesh's device geometry: per-element affine map, face normals and lengths,
 // face connectivity, boundary-condition slots and the physical volume quadrature points.
 struct HostGeometry {
-    std::vector<ElemGeom> geom;
+    std::vector<ElemGeom> geom;   // triangles
     std::vector<ElemConn> conn;
+    std::vector<QuadGeom> qgeom;  // quadrilaterals
+    std::vector<QuadConn> qconn;
     std::vector<BCSlot> slots;
     std::vector<double> xq;
     int boundary = 0;       // some face is a boundary face or takes no part

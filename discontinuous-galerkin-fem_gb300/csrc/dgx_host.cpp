@@ -111,20 +111,62 @@ static void dubiner(int p, double x, double y, double* phi, double* grad) {
         }
 }
 
+// LegendreBasis (src/basis/legendre.cpp:27-110), quadrilaterals on [-1, 1]^2:
+// phi_k = P_i(x) P_j(y), k = j (p+1) + i.  P_n by Bonnet's recurrence; P'_n from
+// (x^2 - 1) P'_n = n (x P_n - P_{n-1}), with P'_n(+-1) = (+-1)^(n+1) n (n+1) / 2 at the ends.
+static void legendre_1d(int p, double x, double* P, double* dP) {
+    P[0] = 1.0;
+    if (p >= 1) P[1] = x;
+    for (int n = 2; n <= p; ++n) P[n] = ((2 * n - 1) * x * P[n - 1] - (n - 1) * P[n - 2]) / n;
+    const bool end = std::fabs(std::fabs(x) - 1.0) < 1e-12;
+    for (int n = 0; n <= p; ++n) {
+        if (n == 0) dP[n] = 0.0;
+        else if (end) dP[n] = 0.5 * n * (n + 1) * ((n % 2 == 0) ? 1.0 : -1.0) * (x > 0 ? 1.0 : -1.0);
+        else dP[n] = n * (x * P[n] - P[n - 1]) / (x * x - 1.0);
+    }
+}
+
+static void legendre(int p, double x, double y, double* phi, double* grad) {
+    double Px[8], Py[8], dPx[8], dPy[8];
+    legendre_1d(p, x, Px, dPx);
+    legendre_1d(p, y, Py, dPy);
+    int k = 0;
+    for (int j = 0; j <= p; ++j)
+        for (int i = 0; i <= p; ++i, ++k) {
+            if (phi) phi[k] = Px[i] * Py[j];
+            if (grad) {
+                grad[2 * k] = dPx[i] * Py[j];
+                grad[2 * k + 1] = Px[i] * dPy[j];
+            }
+        }
+}
+
 static void basis_eval(int basis, int p, double x, double y, double* phi, double* grad) {
-    if (basis == DGX_BASIS_DUBINER) dubiner(p, x, y, phi, grad);
+    if (basis == DGX_BASIS_LEGENDRE) legendre(p, x, y, phi, grad);
+    else if (basis == DGX_BASIS_DUBINER) dubiner(p, x, y, phi, grad);
     else monomial(p, x, y, phi, grad);
 }
 
-// DGSpace::map_face_quad_point (src/core/space.cpp:259-271)
-static void face_point(int f, double s, double* xi) {
+// DGSpace::map_face_quad_point (src/core/space.cpp:259-288): face f of a triangle (nf = 3)
+// or a quadrilateral (nf = 4) at s in [-1, 1], running from vertex f to vertex f + 1.
+static void face_point(int nf, int f, double s, double* xi) {
+    if (nf == 4) {
+        if (f == 0) { xi[0] = s; xi[1] = -1.0; }
+        else if (f == 1) { xi[0] = 1.0; xi[1] = s; }
+        else if (f == 2) { xi[0] = -s; xi[1] = 1.0; }
+        else { xi[0] = -1.0; xi[1] = -s; }
+        return;
+    }
     const double t = 0.5 * (s + 1.0);
     if (f == 0) { xi[0] = t; xi[1] = 0.0; }
     else if (f == 1) { xi[0] = 1.0 - t; xi[1] = t; }
     else { xi[0] = 0.0; xi[1] = 1.0 - t; }
 }
 
-static const int kEdge[3][2] = {{0, 1}, {1, 2}, {2, 0}};  // ReferenceTriangle::edge_vertices
+// ReferenceTriangle / ReferenceQuad::edge_vertices (src/reference/elements.cpp:27-38, 73-90):
+// edge f runs from vertex f to vertex (f + 1) mod nv
+static inline int edge_a(int f, int) { return f; }
+static inline int edge_b(int f, int nv) { return (f + 1) % nv; }
 
 static bool invert(int n, const double* A, double* X) {  // Gauss-Jordan, partial pivoting
     std::vector<double> M(A, A + n * n);
@@ -160,18 +202,38 @@ static bool invert(int n, const double* A, double* X) {  // Gauss-Jordan, partia
 // DGSpace ctor + precompute_basis_values (src/core/space.cpp:20-67, 230-257) and the
 // reference mass matrix of TimeDependentWeakFormulation::compute_mass_integral
 // (src/weak_forms/weak_formulation_base.cpp:198-217) divided by |J|.
+//
+// Quadrilaterals (basis DGX_BASIS_LEGENDRE): the tensor Gauss-Legendre rule with p+1 points
+// per direction, point q = j (p+1) + i at (x_i, x_j) with weight w_i w_j
+// (QuadratureFactory::gauss_legendre_quad, src/quadrature/factory.cpp:33-59).
 int dgx::make_ops(int p, int basis, OpsHost& o) {
     std::memset(&o, 0, sizeof(o));
+    const bool quad = basis == DGX_BASIS_LEGENDRE;
     const int order = 2 * p;
-    if (order > DGX_TRI_MAX_ORDER || p + 1 > DGX_GL_MAX_POINTS) return -1;
+    if (p + 1 > DGX_GL_MAX_POINTS) return -1;
+    if (quad ? p > MAX_P_QUAD : order > DGX_TRI_MAX_ORDER) return -1;
     o.p = p;
-    o.np = n_basis(p);
-    o.nq = dgx_tri_rule_npts[order];
+    o.nf = quad ? 4 : 3;
+    o.np = quad ? n_basis_quad(p) : n_basis(p);
+    o.nq = quad ? n_basis_quad(p) : dgx_tri_rule_npts[order];
     o.nfq = p + 1;
-    if (o.nq != n_quad(p)) return -1;
-    const double* qp = dgx_tri_rule_points + 2 * dgx_tri_rule_offset[order];
-    const double* qw = dgx_tri_rule_weights + dgx_tri_rule_offset[order];
-    double phi[15], g[30];
+    if (!quad && o.nq != n_quad(p)) return -1;
+    std::vector<double> qp(2 * o.nq), qw(o.nq);
+    if (quad) {
+        for (int j = 0; j <= p; ++j)
+            for (int i = 0; i <= p; ++i) {
+                const int q = j * (p + 1) + i;
+                qp[2 * q] = dgx_gl_points[p][i];
+                qp[2 * q + 1] = dgx_gl_points[p][j];
+                qw[q] = dgx_gl_weights[p][i] * dgx_gl_weights[p][j];
+            }
+    } else {
+        std::copy(dgx_tri_rule_points + 2 * dgx_tri_rule_offset[order],
+                  dgx_tri_rule_points + 2 * (dgx_tri_rule_offset[order] + o.nq), qp.begin());
+        std::copy(dgx_tri_rule_weights + dgx_tri_rule_offset[order],
+                  dgx_tri_rule_weights + dgx_tri_rule_offset[order] + o.nq, qw.begin());
+    }
+    double phi[16], g[32];
     for (int q = 0; q < o.nq; ++q) {
         o.qp[q][0] = qp[2 * q];
         o.qp[q][1] = qp[2 * q + 1];
@@ -187,10 +249,12 @@ int dgx::make_ops(int p, int basis, OpsHost& o) {
         o.fp[q] = dgx_gl_points[p][q];
         o.wf[q] = dgx_gl_weights[p][q];
     }
-    for (int f = 0; f < 3; ++f)
+    for (int f = 0; f < o.nf; ++f)
         for (int q = 0; q < o.nfq; ++q) {
             double xi[2];
-            face_point(f, o.fp[q], xi);
+            face_point(o.nf, f, o.fp[q], xi);
+            o.fxi[f][q][0] = xi[0];
+            o.fxi[f][q][1] = xi[1];
             basis_eval(basis, p, xi[0], xi[1], phi, g);
             for (int i = 0; i < o.np; ++i) {
                 o.phif[f][q][i] = phi[i];
@@ -215,15 +279,16 @@ struct BCDef {
 };
 
 struct dgx_mesh {
+    int nvpe = 3;               // vertices (= faces) per element: 3 triangles, 4 quadrilaterals
     std::vector<double> verts;  // [nv][2]
-    std::vector<int> elems;     // [ne][3]
+    std::vector<int> elems;     // [ne][nvpe]
     std::map<std::string, int> tags;
-    std::vector<int> nbr;       // [ne][3][2] face_neighbors_
-    std::vector<int> btag;      // [ne][3] boundary_face_tags_ value, -1 when absent
+    std::vector<int> nbr;       // [ne][nvpe][2] face_neighbors_
+    std::vector<int> btag;      // [ne][nvpe] boundary_face_tags_ value, -1 when absent
     std::vector<int> ifaces;    // [n][5] L, R, fL, fR, reversed
     std::vector<int> bfaces;    // [n][3] elem, face, tag
     std::map<int, BCDef> bcs;   // by tag id
-    int ne() const { return (int)elems.size() / 3; }
+    int ne() const { return (int)elems.size() / nvpe; }
 };
 
 // GeometricMapping::compute_mapping (src/reference/mapping.cpp:22-50) for an affine
@@ -241,16 +306,23 @@ static bool affine_map(const double* V, double* A, double* det) {
     return true;
 }
 
-// outward normal and length of face f (DGSpace::compute_face_data, src/core/space.cpp:104-137)
-static bool face_geom(const double* V, int f, double* n, double* len) {
-    const double* v1 = V + 2 * kEdge[f][0];
-    const double* v2 = V + 2 * kEdge[f][1];
+// outward normal and length of face f of an element with nv vertices
+// (DGSpace::compute_face_data, src/core/space.cpp:104-137)
+static bool face_geom(const double* V, int nv, int f, double* n, double* len) {
+    const double* v1 = V + 2 * edge_a(f, nv);
+    const double* v2 = V + 2 * edge_b(f, nv);
     const double tx = v2[0] - v1[0], ty = v2[1] - v1[1];
     *len = std::sqrt(tx * tx + ty * ty);
     if (*len < 1e-14) return false;
     n[0] = ty / *len;
     n[1] = -tx / *len;
-    const double cx = (V[0] + V[2] + V[4]) / 3.0, cy = (V[1] + V[3] + V[5]) / 3.0;
+    double cx = 0.0, cy = 0.0;
+    for (int k = 0; k < nv; ++k) {
+        cx += V[2 * k];
+        cy += V[2 * k + 1];
+    }
+    cx /= nv;
+    cy /= nv;
     const double mx = 0.5 * (v1[0] + v2[0]), my = 0.5 * (v1[1] + v2[1]);
     if (n[0] * (mx - cx) + n[1] * (my - cy) < 0) {
         n[0] = -n[0];
@@ -260,19 +332,19 @@ static bool face_geom(const double* V, int f, double* n, double* len) {
 }
 
 static void elem_verts(const dgx_mesh* m, int e, double* V) {
-    for (int k = 0; k < 3; ++k) {
-        const int v = m->elems[3 * e + k];
+    for (int k = 0; k < m->nvpe; ++k) {
+        const int v = m->elems[(size_t)m->nvpe * e + k];
         V[2 * k] = m->verts[2 * v];
         V[2 * k + 1] = m->verts[2 * v + 1];
     }
 }
 
 // DGSpace::compute_face_permutation (src/core/space.cpp:173-228): reversed or not
-static bool face_reversed(const double* VL, int fL, const double* VR, int fR) {
-    const double* a1 = VL + 2 * kEdge[fL][0];
-    const double* b1 = VL + 2 * kEdge[fL][1];
-    const double* a2 = VR + 2 * kEdge[fR][0];
-    const double* b2 = VR + 2 * kEdge[fR][1];
+static bool face_reversed(int nv, const double* VL, int fL, const double* VR, int fR) {
+    const double* a1 = VL + 2 * edge_a(fL, nv);
+    const double* b1 = VL + 2 * edge_b(fL, nv);
+    const double* a2 = VR + 2 * edge_a(fR, nv);
+    const double* b2 = VR + 2 * edge_b(fR, nv);
     auto dist = [](const double* p, const double* q) { return std::hypot(p[0] - q[0], p[1] - q[1]); };
     const double tol = 1e-10;
     const bool rev = dist(a1, b2) < tol && dist(b1, a2) < tol;
@@ -286,25 +358,25 @@ static bool face_reversed(const double* VL, int fL, const double* VR, int fR) {
 // DGMesh::build_precomputed_faces (src/core/mesh.cpp:404-480): interior faces in
 // element-then-face order, de-duplicated by element pair; the rest are boundary faces.
 static void rebuild_faces(dgx_mesh* m) {
-    const int ne = m->ne();
+    const int ne = m->ne(), K = m->nvpe;
     m->ifaces.clear();
     m->bfaces.clear();
     std::unordered_set<unsigned long long> seen;
     seen.reserve((size_t)ne * 2);
-    double VL[6], VR[6];
+    double VL[8], VR[8];
     for (int L = 0; L < ne; ++L) {
         elem_verts(m, L, VL);
-        for (int fL = 0; fL < 3; ++fL) {
-            const int R = m->nbr[6 * L + 2 * fL], fR = m->nbr[6 * L + 2 * fL + 1];
+        for (int fL = 0; fL < K; ++fL) {
+            const int R = m->nbr[2 * ((size_t)K * L + fL)], fR = m->nbr[2 * ((size_t)K * L + fL) + 1];
             if (R >= 0) {
                 const unsigned long long key =
                     ((unsigned long long)std::min(L, R) << 32) | (unsigned)std::max(L, R);
                 if (!seen.insert(key).second) continue;
                 elem_verts(m, R, VR);
-                const int rec[5] = {L, R, fL, fR, face_reversed(VL, fL, VR, fR) ? 1 : 0};
+                const int rec[5] = {L, R, fL, fR, face_reversed(K, VL, fL, VR, fR) ? 1 : 0};
                 m->ifaces.insert(m->ifaces.end(), rec, rec + 5);
             } else {
-                const int rec[3] = {L, fL, m->btag[3 * L + fL]};
+                const int rec[3] = {L, fL, m->btag[(size_t)K * L + fL]};
                 m->bfaces.insert(m->bfaces.end(), rec, rec + 3);
             }
         }
@@ -314,31 +386,31 @@ static void rebuild_faces(dgx_mesh* m) {
 // DGMesh ctor, build_face_connectivity and identify_boundary_faces
 // (src/core/mesh.cpp:18-51, 312-402) with a sort instead of dgfem's O(E*F) map scan.
 static int build_connectivity(dgx_mesh* m, int nbe, const int* bedges) {
-    const int ne = m->ne();
+    const int ne = m->ne(), K = m->nvpe;
     struct Rec { int a, b, ord; };
-    std::vector<Rec> r((size_t)ne * 3);
+    std::vector<Rec> r((size_t)ne * K);
     for (int e = 0; e < ne; ++e)
-        for (int f = 0; f < 3; ++f) {
-            const int v1 = m->elems[3 * e + f], v2 = m->elems[3 * e + (f + 1) % 3];
-            r[3 * e + f] = {std::min(v1, v2), std::max(v1, v2), 3 * e + f};
+        for (int f = 0; f < K; ++f) {
+            const int v1 = m->elems[(size_t)K * e + f], v2 = m->elems[(size_t)K * e + (f + 1) % K];
+            r[(size_t)K * e + f] = {std::min(v1, v2), std::max(v1, v2), K * e + f};
         }
     std::sort(r.begin(), r.end(), [](const Rec& x, const Rec& y) {
         return x.a != y.a ? x.a < y.a : x.b != y.b ? x.b < y.b : x.ord < y.ord;
     });
-    m->nbr.assign((size_t)ne * 6, -1);
+    m->nbr.assign((size_t)ne * 2 * K, -1);
     for (size_t i = 0; i < r.size();) {
         size_t j = i;
         while (j < r.size() && r[j].a == r[i].a && r[j].b == r[i].b) ++j;
         if (j - i >= 2) {  // the first two faces of a vertex pair become neighbours
-            const int e1 = r[i].ord / 3, f1 = r[i].ord % 3, e2 = r[i + 1].ord / 3, f2 = r[i + 1].ord % 3;
-            m->nbr[6 * e1 + 2 * f1] = e2;
-            m->nbr[6 * e1 + 2 * f1 + 1] = f2;
-            m->nbr[6 * e2 + 2 * f2] = e1;
-            m->nbr[6 * e2 + 2 * f2 + 1] = f1;
+            const int e1 = r[i].ord / K, f1 = r[i].ord % K, e2 = r[i + 1].ord / K, f2 = r[i + 1].ord % K;
+            m->nbr[2 * ((size_t)K * e1 + f1)] = e2;
+            m->nbr[2 * ((size_t)K * e1 + f1) + 1] = f2;
+            m->nbr[2 * ((size_t)K * e2 + f2)] = e1;
+            m->nbr[2 * ((size_t)K * e2 + f2) + 1] = f1;
         }
         i = j;
     }
-    m->btag.assign((size_t)ne * 3, -1);
+    m->btag.assign((size_t)ne * K, -1);
     if (nbe > 0) {
         // boundary_edges is a std::map keyed by tag: later tags override earlier ones
         std::vector<int> order(nbe);
@@ -351,34 +423,49 @@ static int build_connectivity(dgx_mesh* m, int nbe, const int* bedges) {
             sig[{std::min(v1, v2), std::max(v1, v2)}] = bedges[3 * k];
         }
         for (int e = 0; e < ne; ++e)
-            for (int f = 0; f < 3; ++f) {
-                if (m->nbr[6 * e + 2 * f] != -1) continue;
-                const int v1 = m->elems[3 * e + f], v2 = m->elems[3 * e + (f + 1) % 3];
+            for (int f = 0; f < K; ++f) {
+                if (m->nbr[2 * ((size_t)K * e + f)] != -1) continue;
+                const int v1 = m->elems[(size_t)K * e + f], v2 = m->elems[(size_t)K * e + (f + 1) % K];
                 auto it = sig.find({std::min(v1, v2), std::max(v1, v2)});
-                m->btag[3 * e + f] = it == sig.end() ? 0 : it->second;
+                m->btag[(size_t)K * e + f] = it == sig.end() ? 0 : it->second;
             }
     }
     rebuild_faces(m);
     return DGX_OK;
 }
 
-extern "C" int dgx_mesh_create(int nv, const double* verts, int ne, const int* elems, int n_tags,
-                               const char* const* tag_names, const int* tag_ids, int nbe,
-                               const int* bedges, dgx_mesh** out) {
+extern "C" int dgx_mesh_create_nv(int nvpe, int nv, const double* verts, int ne, const int* elems, int n_tags,
+                                  const char* const* tag_names, const int* tag_ids, int nbe, const int* bedges,
+                                  dgx_mesh** out) {
     if (!out || nv < 0 || ne < 0 || (nv > 0 && !verts) || (ne > 0 && !elems) || (nbe > 0 && !bedges) ||
         (n_tags > 0 && (!tag_names || !tag_ids)))
         return fail(DGX_ERR_INVALID, "dgx_mesh_create: bad arguments");
-    for (int i = 0; i < 3 * ne; ++i)
+    if (nvpe != 3 && nvpe != 4)  // DGMesh ctor (src/core/mesh.cpp:23-35)
+        return fail(DGX_ERR_INVALID, "Unknown element type with " + std::to_string(nvpe) + " vertices");
+    for (size_t i = 0; i < (size_t)nvpe * ne; ++i)
         if (elems[i] < 0 || elems[i] >= nv) return fail(DGX_ERR_RANGE, "element vertex index out of range");
     for (int k = 0; k < nbe; ++k)
         for (int c = 1; c < 3; ++c)
             if (bedges[3 * k + c] < 0) return fail(DGX_ERR_RANGE, "boundary edge vertex index out of range");
     auto* m = new dgx_mesh;
+    m->nvpe = nvpe;
     m->verts.assign(verts, verts + 2 * (size_t)nv);
-    m->elems.assign(elems, elems + 3 * (size_t)ne);
+    m->elems.assign(elems, elems + (size_t)nvpe * ne);
     for (int t = 0; t < n_tags; ++t) m->tags[tag_names[t]] = tag_ids[t];
     build_connectivity(m, nbe, bedges);
     *out = m;
+    return DGX_OK;
+}
+
+extern "C" int dgx_mesh_create(int nv, const double* verts, int ne, const int* elems, int n_tags,
+                               const char* const* tag_names, const int* tag_ids, int nbe,
+                               const int* bedges, dgx_mesh** out) {
+    return dgx_mesh_create_nv(3, nv, verts, ne, elems, n_tags, tag_names, tag_ids, nbe, bedges, out);
+}
+
+extern "C" int dgx_mesh_vertices_per_element(const dgx_mesh* m, int* nvpe) {
+    if (!m || !nvpe) return fail(DGX_ERR_INVALID, "null argument");
+    *nvpe = m->nvpe;
     return DGX_OK;
 }
 
@@ -400,10 +487,10 @@ extern "C" int dgx_mesh_set_periodic(dgx_mesh* m, const char* t1, const char* t2
     }
     if (f1.empty() || f2.empty())
         return fail(DGX_ERR_RUNTIME, "Cannot set periodic boundaries: one or both boundaries have no faces");
-    const int c = match_y ? 1 : 0;
+    const int c = match_y ? 1 : 0, K = m->nvpe;
     auto center = [&](int slot) {
-        const int e = slot / 3, f = slot % 3;
-        const int a = m->elems[3 * e + f], b = m->elems[3 * e + (f + 1) % 3];
+        const int e = slot / K, f = slot % K;
+        const int a = m->elems[(size_t)K * e + f], b = m->elems[(size_t)K * e + (f + 1) % K];
         return 0.5 * (m->verts[2 * a + c] + m->verts[2 * b + c]);
     };
     // nearest transverse coordinate, first minimum wins: sort candidates once
@@ -428,11 +515,11 @@ extern "C" int dgx_mesh_set_periodic(dgx_mesh* m, const char* t1, const char* t2
             if (d < best || (d == best && j->second < bi)) { best = d; bi = j->second; }
         }
         if (bi < 0) continue;
-        const int e1 = s1f / 3, l1 = s1f % 3, e2 = f2[bi] / 3, l2 = f2[bi] % 3;
-        m->nbr[6 * e1 + 2 * l1] = e2;
-        m->nbr[6 * e1 + 2 * l1 + 1] = l2;
-        m->nbr[6 * e2 + 2 * l2] = e1;
-        m->nbr[6 * e2 + 2 * l2 + 1] = l1;
+        const int e1 = s1f / K, l1 = s1f % K, e2 = f2[bi] / K, l2 = f2[bi] % K;
+        m->nbr[2 * ((size_t)K * e1 + l1)] = e2;
+        m->nbr[2 * ((size_t)K * e1 + l1) + 1] = l2;
+        m->nbr[2 * ((size_t)K * e2 + l2)] = e1;
+        m->nbr[2 * ((size_t)K * e2 + l2) + 1] = l1;
     }
     m->bcs.clear();
     rebuild_faces(m);
@@ -539,7 +626,8 @@ static StepArgs base_args(const dgx_ctx* c) {
 
 static int launch(const dgx_ctx* c, const StepArgs& a, cudaStream_t s) {
     const bool visc = c->prm.physics == DGX_NAVIER_STOKES;
-    const int rc = c->prm.precision == DGX_MIXED  ? launch_element_mixed(c->prm.order, visc, a, c->ops, s)
+    const int rc = c->nvpe == 4 ? launch_quad_element(c->prm.order, visc, a, c->d_qgeom, c->d_qconn, c->ops, s)
+                   : c->prm.precision == DGX_MIXED  ? launch_element_mixed(c->prm.order, visc, a, c->ops, s)
                    : c->prm.precision == DGX_DF64 ? launch_element_df64(c->prm.order, visc, a, c->ops, s)
                                                   : launch_element_fp64(c->prm.order, visc, a, c->ops, s);
     if (rc) return fail(DGX_ERR_CUDA, std::string("element kernel launch failed: ") +
@@ -562,6 +650,8 @@ static void free_ctx(dgx_ctx* c) {
     cudaFree(c->d_geom);
     cudaFree(c->d_geomf);
     cudaFree(c->d_conn);
+    cudaFree(c->d_qgeom);
+    cudaFree(c->d_qconn);
     cudaFree(c->d_bc);
     cudaFree(c->d_u1);
     cudaFree(c->d_u2);
@@ -575,53 +665,21 @@ static void free_ctx(dgx_ctx* c) {
 
 extern "C" void dgx_destroy(dgx_ctx* c) { free_ctx(c); }
 
-// Element geometry, face slots and boundary-condition slots of a mesh:
-// DGSpace::compute_element_data / compute_face_data (src/core/space.cpp:69-171).
-int dgx::build_geometry(const dgx_mesh* m, const OpsHost& ops, HostGeometry& g) {
+// Face slots and boundary-condition slots shared by both element shapes: fn/fl hold every
+// element's own outward normals and face lengths ([ne][NF][2], [ne][NF]).
+template <int NF, class Geom, class Conn>
+static int face_slots(const dgx_mesh* m, const std::vector<double>& fn, const std::vector<double>& fl,
+                      std::vector<Geom>& geom, std::vector<Conn>& conn, HostGeometry& g) {
     const int ne = m->ne();
-    g.geom.assign(ne, ElemGeom{});
-    g.conn.assign(ne, ElemConn{});
-    g.slots.clear();
-    g.boundary = g.has_slip_wall = 0;
-    std::vector<ElemGeom>& geom = g.geom;
-    std::vector<ElemConn>& conn = g.conn;
     std::vector<BCSlot>& slots = g.slots;
-    std::vector<double> fn((size_t)ne * 6), fl((size_t)ne * 3);
-    g.xq.resize((size_t)ne * ops.nq * 2);
     for (int e = 0; e < ne; ++e) {
-        double V[6], A[4], det;
-        elem_verts(m, e, V);
-        if (!affine_map(V, A, &det)) {
-            return fail(DGX_ERR_RUNTIME, "Singular Jacobian matrix");
-        }
-        ElemGeom& ge = geom[e];
-        std::memset(&ge, 0, sizeof(ge));
-        for (int k = 0; k < 4; ++k) ge.A[k] = A[k];
-        ge.detJ = std::fabs(det);
-        double h = std::numeric_limits<double>::max();
-        for (int i = 0; i < 3; ++i)
-            for (int j = i + 1; j < 3; ++j)
-                h = std::min(h, std::sqrt((V[2 * i] - V[2 * j]) * (V[2 * i] - V[2 * j]) +
-                                          (V[2 * i + 1] - V[2 * j + 1]) * (V[2 * i + 1] - V[2 * j + 1])));
-        ge.pad[0] = h;
-        for (int f = 0; f < 3; ++f) {
-            if (!face_geom(V, f, &fn[6 * (size_t)e + 2 * f], &fl[3 * (size_t)e + f])) {
-                    return fail(DGX_ERR_RUNTIME, "Degenerate edge detected");
-            }
-            conn[e].nbr[f] = NBR_SKIP;
-        }
+        for (int f = 0; f < NF; ++f) conn[e].nbr[f] = NBR_SKIP;
         conn[e].flags = 0;
-        for (int q = 0; q < ops.nq; ++q) {  // map_to_physical: V^T N
-            const double xi = ops.qp[q][0], eta = ops.qp[q][1];
-            const double N0 = 1.0 - xi - eta;
-            g.xq[((size_t)e * ops.nq + q) * 2] = N0 * V[0] + xi * V[2] + eta * V[4];
-            g.xq[((size_t)e * ops.nq + q) * 2 + 1] = N0 * V[1] + xi * V[3] + eta * V[5];
-        }
     }
-    std::vector<char> taken((size_t)ne * 3, 0);
+    std::vector<char> taken((size_t)ne * NF, 0);
     auto take = [&](int e, int f) {
-        if (taken[3 * (size_t)e + f]) return false;
-        taken[3 * (size_t)e + f] = 1;
+        if (taken[(size_t)NF * e + f]) return false;
+        taken[(size_t)NF * e + f] = 1;
         return true;
     };
     const int nif = (int)m->ifaces.size() / 5;
@@ -631,8 +689,8 @@ int dgx::build_geometry(const dgx_mesh* m, const OpsHost& ops, HostGeometry& g) 
         if (!take(L, fL) || !take(R, fR)) {
             return fail(DGX_ERR_RUNTIME, "unsupported mesh topology: an element face appears in two interior faces");
         }
-        const double* nL = &fn[6 * (size_t)L + 2 * fL];
-        const double hL = fl[3 * (size_t)L + fL];
+        const double* nL = &fn[2 * ((size_t)NF * L + fL)];
+        const double hL = fl[(size_t)NF * L + fL];
         geom[L].n[fL][0] = nL[0];
         geom[L].n[fL][1] = nL[1];
         geom[L].h[fL] = hL;
@@ -648,9 +706,9 @@ int dgx::build_geometry(const dgx_mesh* m, const OpsHost& ops, HostGeometry& g) 
     const int nbf = (int)m->bfaces.size() / 3;
     for (int k = 0; k < nbf; ++k) {
         const int e = m->bfaces[3 * (size_t)k], f = m->bfaces[3 * (size_t)k + 1], tag = m->bfaces[3 * (size_t)k + 2];
-        geom[e].n[f][0] = fn[6 * (size_t)e + 2 * f];
-        geom[e].n[f][1] = fn[6 * (size_t)e + 2 * f + 1];
-        geom[e].h[f] = fl[3 * (size_t)e + f];
+        geom[e].n[f][0] = fn[2 * ((size_t)NF * e + f)];
+        geom[e].n[f][1] = fn[2 * ((size_t)NF * e + f) + 1];
+        geom[e].h[f] = fl[(size_t)NF * e + f];
         auto it = m->bcs.find(tag);
         if (tag < 0 || it == m->bcs.end()) continue;  // no BC: dgfem skips the face
         if (it->second.type == DGX_BC_PERIODIC) {
@@ -677,10 +735,113 @@ int dgx::build_geometry(const dgx_mesh* m, const OpsHost& ops, HostGeometry& g) 
         conn[e].flags |= (1 << 3) << (4 * f);
     }
     for (int e = 0; e < ne && !g.boundary; ++e)
-        for (int f = 0; f < 3; ++f)
+        for (int f = 0; f < NF; ++f)
             if (conn[e].nbr[f] < 0) g.boundary = 1;
     if (slots.empty()) slots.push_back(BCSlot{});
     return DGX_OK;
+}
+
+// compute_max_cfl's h_elem (src/solver/compressible_solver_base.cpp:124-131): the shortest
+// distance between two vertices of the element
+static double shortest_vertex_distance(const double* V, int nv) {
+    double h = std::numeric_limits<double>::max();
+    for (int i = 0; i < nv; ++i)
+        for (int j = i + 1; j < nv; ++j)
+            h = std::min(h, std::sqrt((V[2 * i] - V[2 * j]) * (V[2 * i] - V[2 * j]) +
+                                      (V[2 * i + 1] - V[2 * j + 1]) * (V[2 * i + 1] - V[2 * j + 1])));
+    return h;
+}
+
+// Quadrilateral geometry: the bilinear map's derivative coefficients, faces and slots
+// (DGSpace::compute_element_data / compute_face_data, src/core/space.cpp:69-171, with
+// GeometricMapping::compute_mapping's singular-Jacobian check at the volume and face points).
+static int build_geometry_quad(const dgx_mesh* m, const OpsHost& ops, HostGeometry& g) {
+    const int ne = m->ne();
+    g.qgeom.assign(ne, QuadGeom{});
+    g.qconn.assign(ne, QuadConn{});
+    std::vector<double> fn((size_t)ne * 8), fl((size_t)ne * 4);
+    g.xq.resize((size_t)ne * ops.nq * 2);
+    for (int e = 0; e < ne; ++e) {
+        double V[8];
+        elem_verts(m, e, V);
+        QuadGeom& ge = g.qgeom[e];
+        for (int c = 0; c < 2; ++c) {
+            const double x0 = V[c], x1 = V[2 + c], x2 = V[4 + c], x3 = V[6 + c];
+            double* j = c == 0 ? ge.jx : ge.jy;
+            j[0] = 0.25 * ((x1 - x0) + (x2 - x3));
+            j[1] = 0.25 * ((x3 - x0) + (x2 - x1));
+            j[2] = 0.25 * ((x0 - x1) + (x2 - x3));
+        }
+        auto det_at = [&](double xi, double eta) {
+            const double J00 = ge.jx[0] + ge.jx[2] * eta, J01 = ge.jy[0] + ge.jy[2] * eta;
+            const double J10 = ge.jx[1] + ge.jx[2] * xi, J11 = ge.jy[1] + ge.jy[2] * xi;
+            return J00 * J11 - J10 * J01;
+        };
+        for (int q = 0; q < ops.nq; ++q)
+            if (std::fabs(det_at(ops.qp[q][0], ops.qp[q][1])) < 1e-12)
+                return fail(DGX_ERR_RUNTIME, "Singular Jacobian matrix");
+        for (int f = 0; f < 4; ++f)
+            for (int q = 0; q < ops.nfq; ++q)
+                if (std::fabs(det_at(ops.fxi[f][q][0], ops.fxi[f][q][1])) < 1e-12)
+                    return fail(DGX_ERR_RUNTIME, "Singular Jacobian matrix");
+        ge.hmin = shortest_vertex_distance(V, 4);
+        for (int f = 0; f < 4; ++f)
+            if (!face_geom(V, 4, f, &fn[8 * (size_t)e + 2 * f], &fl[4 * (size_t)e + f]))
+                return fail(DGX_ERR_RUNTIME, "Degenerate edge detected");
+        for (int q = 0; q < ops.nq; ++q) {  // map_to_physical: V^T N (ReferenceQuad shape functions)
+            const double xi = ops.qp[q][0], eta = ops.qp[q][1];
+            const double N[4] = {0.25 * (1.0 - xi) * (1.0 - eta), 0.25 * (1.0 + xi) * (1.0 - eta),
+                                 0.25 * (1.0 + xi) * (1.0 + eta), 0.25 * (1.0 - xi) * (1.0 + eta)};
+            double x = 0.0, y = 0.0;
+            for (int k = 0; k < 4; ++k) {
+                x += N[k] * V[2 * k];
+                y += N[k] * V[2 * k + 1];
+            }
+            g.xq[((size_t)e * ops.nq + q) * 2] = x;
+            g.xq[((size_t)e * ops.nq + q) * 2 + 1] = y;
+        }
+    }
+    return face_slots<4>(m, fn, fl, g.qgeom, g.qconn, g);
+}
+
+// Element geometry, face slots and boundary-condition slots of a mesh:
+// DGSpace::compute_element_data / compute_face_data (src/core/space.cpp:69-171).
+int dgx::build_geometry(const dgx_mesh* m, const OpsHost& ops, HostGeometry& g) {
+    const int ne = m->ne();
+    g.slots.clear();
+    g.boundary = g.has_slip_wall = 0;
+    if ((m->nvpe == 4) != (ops.nf == 4))
+        return fail(DGX_ERR_INVALID, "the space's element type does not match the mesh's");
+    if (m->nvpe == 4) return build_geometry_quad(m, ops, g);
+    g.geom.assign(ne, ElemGeom{});
+    g.conn.assign(ne, ElemConn{});
+    std::vector<ElemGeom>& geom = g.geom;
+    std::vector<double> fn((size_t)ne * 6), fl((size_t)ne * 3);
+    g.xq.resize((size_t)ne * ops.nq * 2);
+    for (int e = 0; e < ne; ++e) {
+        double V[6], A[4], det;
+        elem_verts(m, e, V);
+        if (!affine_map(V, A, &det)) {
+            return fail(DGX_ERR_RUNTIME, "Singular Jacobian matrix");
+        }
+        ElemGeom& ge = geom[e];
+        std::memset(&ge, 0, sizeof(ge));
+        for (int k = 0; k < 4; ++k) ge.A[k] = A[k];
+        ge.detJ = std::fabs(det);
+        ge.pad[0] = shortest_vertex_distance(V, 3);
+        for (int f = 0; f < 3; ++f) {
+            if (!face_geom(V, 3, f, &fn[6 * (size_t)e + 2 * f], &fl[3 * (size_t)e + f])) {
+                    return fail(DGX_ERR_RUNTIME, "Degenerate edge detected");
+            }
+        }
+        for (int q = 0; q < ops.nq; ++q) {  // map_to_physical: V^T N
+            const double xi = ops.qp[q][0], eta = ops.qp[q][1];
+            const double N0 = 1.0 - xi - eta;
+            g.xq[((size_t)e * ops.nq + q) * 2] = N0 * V[0] + xi * V[2] + eta * V[4];
+            g.xq[((size_t)e * ops.nq + q) * 2 + 1] = N0 * V[1] + xi * V[3] + eta * V[5];
+        }
+    }
+    return face_slots<3>(m, fn, fl, geom, g.conn, g);
 }
 
 ElemGeomF dgx::geom_to_f32(const ElemGeom& g, int instance) {
@@ -717,8 +878,16 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
     *out = nullptr;
     if (p->order < 1 || p->order > MAX_P)
         return fail(DGX_ERR_INVALID, "Element order must be between 1 and 4 for the GPU kernels");
-    if (p->basis != DGX_BASIS_MONOMIAL && p->basis != DGX_BASIS_DUBINER)
+    if (p->basis != DGX_BASIS_MONOMIAL && p->basis != DGX_BASIS_DUBINER && p->basis != DGX_BASIS_LEGENDRE)
         return fail(DGX_ERR_INVALID, "unknown basis");
+    const bool quad = m->nvpe == 4;
+    if (quad != (p->basis == DGX_BASIS_LEGENDRE))  // DGSpace::create_basis (src/core/space.cpp:307-319)
+        return fail(DGX_ERR_INVALID, quad ? "quadrilateral meshes use the Legendre basis"
+                                          : "the Legendre basis is for quadrilateral meshes");
+    if (quad && p->order > MAX_P_QUAD)
+        return fail(DGX_ERR_INVALID, "Element order must be between 1 and 3 for the quadrilateral GPU kernels");
+    if (quad && p->precision != DGX_FP64)
+        return fail(DGX_ERR_INVALID, "quadrilateral meshes run in FP64 (DGX_FP64)");
     if (p->physics != DGX_EULER && p->physics != DGX_NAVIER_STOKES)
         return fail(DGX_ERR_INVALID, "unknown physics");
     if (p->precision != DGX_FP64 && p->precision != DGX_MIXED && p->precision != DGX_DF64)
@@ -733,7 +902,8 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
 
     {
         const bool visc = p->physics == DGX_NAVIER_STOKES;
-        int rc = p->precision == DGX_MIXED  ? configure_element_mixed(p->order, visc)
+        int rc = quad                       ? configure_quad_element(p->order, visc)
+                 : p->precision == DGX_MIXED  ? configure_element_mixed(p->order, visc)
                  : p->precision == DGX_DF64 ? configure_element_df64(p->order, visc)
                                             : configure_element_fp64(p->order, visc);
         if (!rc && p->precision == DGX_MIXED && !visc) rc = configure_stage_tc(p->order);
@@ -742,6 +912,7 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
     auto* c = new dgx_ctx;
     c->device = dev;
     c->prm = *p;
+    c->nvpe = m->nvpe;
     if (make_ops(p->order, p->basis, c->ops)) {
         delete c;
         return fail(DGX_ERR_RUNTIME, "could not build reference operators");
@@ -776,7 +947,8 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
         return cudaMalloc(ptr, bytes ? bytes : 16) == cudaSuccess;
     };
     const size_t sb = c->nstate * sizeof(double);
-    if (!alloc((void**)&c->d_geom, sizeof(ElemGeom) * ne) || !alloc((void**)&c->d_conn, sizeof(ElemConn) * ne) ||
+    if ((quad ? !alloc((void**)&c->d_qgeom, sizeof(QuadGeom) * ne) || !alloc((void**)&c->d_qconn, sizeof(QuadConn) * ne)
+              : !alloc((void**)&c->d_geom, sizeof(ElemGeom) * ne) || !alloc((void**)&c->d_conn, sizeof(ElemConn) * ne)) ||
         !alloc((void**)&c->d_bc, sizeof(BCSlot) * slots.size()) || !alloc((void**)&c->d_u1, sb) ||
         !alloc((void**)&c->d_u2, sb) || !alloc((void**)&c->d_mon, 4 * sizeof(double)) ||
         !alloc((void**)&c->d_flag, sizeof(int)) || !alloc((void**)&c->d_status, sizeof(int)) ||
@@ -799,9 +971,12 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
             return fail(DGX_ERR_CUDA, "device upload failed (FP32 geometry)");
         }
     }
-    if (cudaMemset(c->d_status, 0, sizeof(int)) != cudaSuccess ||
-        cudaMemcpy(c->d_geom, geom.data(), sizeof(ElemGeom) * ne, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(c->d_conn, conn.data(), sizeof(ElemConn) * ne, cudaMemcpyHostToDevice) != cudaSuccess ||
+    const bool geom_ok =
+        quad ? cudaMemcpy(c->d_qgeom, hg.qgeom.data(), sizeof(QuadGeom) * ne, cudaMemcpyHostToDevice) == cudaSuccess &&
+                   cudaMemcpy(c->d_qconn, hg.qconn.data(), sizeof(QuadConn) * ne, cudaMemcpyHostToDevice) == cudaSuccess
+             : cudaMemcpy(c->d_geom, geom.data(), sizeof(ElemGeom) * ne, cudaMemcpyHostToDevice) == cudaSuccess &&
+                   cudaMemcpy(c->d_conn, conn.data(), sizeof(ElemConn) * ne, cudaMemcpyHostToDevice) == cudaSuccess;
+    if (cudaMemset(c->d_status, 0, sizeof(int)) != cudaSuccess || !geom_ok ||
         cudaMemcpy(c->d_bc, slots.data(), sizeof(BCSlot) * slots.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->cap, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
@@ -851,8 +1026,9 @@ extern "C" int dgx_rhs(dgx_ctx* c, const double* u, double* du, void* stream) {
 
 extern "C" int dgx_apply_mass_inv(dgx_ctx* c, const double* in, double* out, void* stream) {
     if (!c || (c->ne && (!in || !out))) return fail(DGX_ERR_INVALID, "dgx_apply_mass_inv: null argument");
-    if (launch_mass_inv(c->ne, c->prm.order, c->ops, c->d_geom, in, out, (cudaStream_t)stream))
-        return fail(DGX_ERR_CUDA, "mass inverse launch failed");
+    const int rc = c->nvpe == 4 ? launch_quad_mass_inv(c->ne, c->prm.order, c->ops, c->d_qgeom, in, out, (cudaStream_t)stream)
+                                : launch_mass_inv(c->ne, c->prm.order, c->ops, c->d_geom, in, out, (cudaStream_t)stream);
+    if (rc) return fail(DGX_ERR_CUDA, "mass inverse launch failed");
     return DGX_OK;
 }
 
@@ -997,11 +1173,15 @@ extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void*
     return DGX_OK;
 }
 
+static int monitor(dgx_ctx* c, const double* u, double dt, cudaStream_t s) {
+    return c->nvpe == 4 ? launch_quad_monitor(c->ne, c->prm.order, c->ops, c->d_qgeom, u, dt, c->prm.gamma, c->d_mon, s)
+                        : launch_monitor(c->ne, c->prm.order, c->ops, c->d_geom, u, dt, c->prm.gamma, c->d_mon, s);
+}
+
 extern "C" int dgx_max_cfl(dgx_ctx* c, const double* u, double dt, double* cfl, void* stream) {
     if (!c || !cfl || (c->ne && !u)) return fail(DGX_ERR_INVALID, "dgx_max_cfl: null argument");
     cudaStream_t s = (cudaStream_t)stream;
-    if (launch_monitor(c->ne, c->prm.order, c->ops, c->d_geom, u, dt, c->prm.gamma, c->d_mon, s))
-        return fail(DGX_ERR_CUDA, "monitor launch failed");
+    if (monitor(c, u, dt, s)) return fail(DGX_ERR_CUDA, "monitor launch failed");
     double h[4];
     CUDA_OK(cudaMemcpyAsync(h, c->d_mon, sizeof(h), cudaMemcpyDeviceToHost, s));
     CUDA_OK(cudaStreamSynchronize(s));
@@ -1012,8 +1192,7 @@ extern "C" int dgx_max_cfl(dgx_ctx* c, const double* u, double dt, double* cfl, 
 extern "C" int dgx_density_range(dgx_ctx* c, const double* u, double* rmin, double* rmax, void* stream) {
     if (!c || !rmin || !rmax || (c->ne && !u)) return fail(DGX_ERR_INVALID, "dgx_density_range: null argument");
     cudaStream_t s = (cudaStream_t)stream;
-    if (launch_monitor(c->ne, c->prm.order, c->ops, c->d_geom, u, 0.0, c->prm.gamma, c->d_mon, s))
-        return fail(DGX_ERR_CUDA, "monitor launch failed");
+    if (monitor(c, u, 0.0, s)) return fail(DGX_ERR_CUDA, "monitor launch failed");
     double h[4];
     CUDA_OK(cudaMemcpyAsync(h, c->d_mon, sizeof(h), cudaMemcpyDeviceToHost, s));
     CUDA_OK(cudaStreamSynchronize(s));
@@ -1056,8 +1235,9 @@ extern "C" int dgx_quad_points(const dgx_ctx* c, double* xq) {
 
 extern "C" int dgx_project(dgx_ctx* c, const double* uq, double* u, void* stream) {
     if (!c || (c->ne && (!uq || !u))) return fail(DGX_ERR_INVALID, "dgx_project: null argument");
-    if (launch_project(c->ne, c->prm.order, c->ops, c->d_geom, uq, u, (cudaStream_t)stream))
-        return fail(DGX_ERR_CUDA, "projection launch failed");
+    const int rc = c->nvpe == 4 ? launch_quad_project(c->ne, c->prm.order, c->ops, c->d_qgeom, uq, u, (cudaStream_t)stream)
+                                : launch_project(c->ne, c->prm.order, c->ops, c->d_geom, uq, u, (cudaStream_t)stream);
+    if (rc) return fail(DGX_ERR_CUDA, "projection launch failed");
     return DGX_OK;
 }
 
@@ -1067,7 +1247,7 @@ extern "C" int dgx_eval_points(dgx_ctx* c, int n_points, const double* ref_xy, c
         return fail(DGX_ERR_INVALID, "dgx_eval_points: bad argument");
     if (n_points > EVAL_MAX_POINTS)
         return fail(DGX_ERR_INVALID, "dgx_eval_points: at most " + std::to_string(EVAL_MAX_POINTS) + " points");
-    std::vector<double> phi((size_t)n_points * c->np), grad(2 * 15);
+    std::vector<double> phi((size_t)n_points * c->np), grad(2 * 16);
     for (int k = 0; k < n_points; ++k) basis_eval(c->prm.basis, c->prm.order, ref_xy[2 * k], ref_xy[2 * k + 1],
                                                    &phi[(size_t)k * c->np], grad.data());
     if (launch_eval_points(c->ne, c->np, n_points, phi.data(), u, out, (cudaStream_t)stream))

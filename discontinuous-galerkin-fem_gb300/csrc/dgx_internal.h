@@ -27,6 +27,32 @@ struct alignas(128) ElemGeom {
 };
 static_assert(sizeof(ElemGeom) == 128, "ElemGeom must stay 128 B");
 
+// Quadrilaterals (DGSpace("quad", p), LegendreBasis): orders with compiled kernels,
+// (p+1)^2 modes and (p+1)^2 tensor Gauss-Legendre volume points.
+constexpr int MAX_P_QUAD = 3;
+__host__ __device__ constexpr int n_basis_quad(int p) { return (p + 1) * (p + 1); }
+
+// Per-element geometry of a bilinear quadrilateral, 192 B.  The map is not affine, so
+// the metric terms are evaluated at each point from the shape-function derivatives of
+// ReferenceQuad (src/reference/elements.cpp:92-111):
+//   dx/dxi = jx[0] + jx[2] eta,  dx/deta = jx[1] + jx[2] xi,  and y likewise with jy.
+struct alignas(64) QuadGeom {
+    double jx[3];
+    double jy[3];
+    double h[4];     // face length; the L side's length for interior faces
+    double n[4][2];  // face normal as seen from this element (= +/- the L side's normal)
+    double hmin;     // shortest distance between two vertices (compute_max_cfl's h_elem)
+    double pad[5];
+};
+static_assert(sizeof(QuadGeom) == 192, "QuadGeom must stay 192 B");
+
+// Face connectivity of a quadrilateral, ElemConn's encoding over four faces.
+struct alignas(32) QuadConn {
+    int nbr[4];
+    int flags;
+    int pad[3];
+};
+
 // The same record rounded once to FP32 (64 B) for the mixed-precision stage kernel,
 // whose arithmetic is FP32: it holds exactly the values that kernel would obtain by
 // converting ElemGeom on load.
@@ -74,15 +100,18 @@ struct Ops {
     T minv[NP][NP];       // inverse of the reference mass matrix sum_q w_q phi phi^T
 };
 
-// Host copy of all operators in double precision, sized for MAX_P.
+// Host copy of all operators in double precision, sized for MAX_P triangles and
+// MAX_P_QUAD quadrilaterals.
 struct OpsHost {
     int p, np, nq, nfq;
-    double phi[16][15], dr[16][15], ds[16][15];
-    double phif[3][5][15], drf[3][5][15], dsf[3][5][15];
+    int nf;            // faces per element: 3 (triangles) or 4 (quadrilaterals)
+    double phi[16][16], dr[16][16], ds[16][16];
+    double phif[4][5][16], drf[4][5][16], dsf[4][5][16];
     double wq[16], wf[5];
-    double minv[15][15];
-    double qp[16][2];  // volume points on the reference triangle
-    double fp[5];      // face points on [-1, 1]
+    double minv[16][16];
+    double qp[16][2];     // volume points on the reference element
+    double fp[5];         // face points on [-1, 1]
+    double fxi[4][5][2];  // face points on the reference element, face f, point q
 };
 
 template <int P, typename T>
@@ -185,5 +214,17 @@ int launch_has_nan(size_t n, const double* u, int* d_flag, cudaStream_t s);
 constexpr int EVAL_MAX_POINTS = 128;
 int launch_eval_points(int ne, int np, int npts, const double* phi, const double* u, double* out, cudaStream_t s);
 int launch_f64_to_f32(size_t n, const double* in, float* out, cudaStream_t s);
+
+// Quadrilateral kernels (dgx_quad.cu), FP64, orders 1..MAX_P_QUAD.  StepArgs::geom and
+// StepArgs::conn are not used; the quadrilateral records are passed beside them.
+int launch_quad_element(int p, bool viscous, const StepArgs& a, const QuadGeom* geom, const QuadConn* conn,
+                        const OpsHost& ops, cudaStream_t s);
+int configure_quad_element(int p, bool viscous);
+int launch_quad_mass_inv(int ne, int p, const OpsHost& ops, const QuadGeom* geom, const double* in, double* out,
+                         cudaStream_t s);
+int launch_quad_project(int ne, int p, const OpsHost& ops, const QuadGeom* geom, const double* uq, double* u,
+                        cudaStream_t s);
+int launch_quad_monitor(int ne, int p, const OpsHost& ops, const QuadGeom* geom, const double* u, double dt,
+                        double gamma, double* d_out, cudaStream_t s);
 
 }  // namespace dgx

@@ -51,6 +51,7 @@ int scratch_for_device(int dev, double** out) {
 }  // namespace
 
 extern "C" int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps, void* stream) {
+    if (c && c->nvpe == 4) return dgx::set_error(DGX_ERR_INVALID, "dgx_rk3_step_static: triangle meshes only");
     if (!c || (c->ne && !u) || n_steps < 0) return dgx::set_error(DGX_ERR_INVALID, "dgx_rk3_step_static: bad argument");
     if (c->nstate > (size_t)DGX_STATIC_MAX_STATE)
         return dgx::set_error(DGX_ERR_INVALID,

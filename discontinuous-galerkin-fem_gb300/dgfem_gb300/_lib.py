@@ -16,7 +16,7 @@ LIB_PATH = Path(os.environ.get("DGX_LIBRARY", PKG_ROOT / "libdgx.so"))
 
 OK = 0
 ERR_INVALID, ERR_RUNTIME, ERR_RANGE, ERR_CUDA, ERR_NONFINITE = -1, -2, -3, -4, -5
-BASIS_MONOMIAL, BASIS_DUBINER = 0, 1
+BASIS_MONOMIAL, BASIS_DUBINER, BASIS_LEGENDRE = 0, 1, 2
 EULER, NAVIER_STOKES = 0, 1
 FP64, MIXED, DF64 = 0, 1, 2
 BC_FAR_FIELD, BC_SLIP_WALL, BC_NO_SLIP_WALL, BC_PERIODIC = 0, 1, 2, 3
@@ -36,6 +36,9 @@ SIGNATURES = {
     "dgx_mesh_interior_faces": (C.c_int, [_vp, _ip]),
     "dgx_mesh_boundary_faces": (C.c_int, [_vp, _ip]),
     "dgx_mesh_arrays": (C.c_int, [_vp, _ip, _dp, _ip]),
+    "dgx_mesh_create_nv": (C.c_int, [C.c_int, C.c_int, _dp, C.c_int, _ip, C.c_int, C.POINTER(C.c_char_p), _ip,
+                                     C.c_int, _ip, C.POINTER(_vp)]),
+    "dgx_mesh_vertices_per_element": (C.c_int, [_vp, _ip]),
     "dgx_mesh_destroy": (None, [_vp]),
     "dgx_create": (C.c_int, [_vp, _vp, C.POINTER(_vp)]),
     "dgx_destroy": (None, [_vp]),

@@ -100,7 +100,9 @@ class DGMesh:
             self._h = _handle
         else:
             V = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 2)
-            E = np.ascontiguousarray(elements, dtype=np.int32).reshape(-1, 3)
+            E = np.asarray(elements)
+            nvpe = E.shape[1] if E.ndim == 2 else 3  # 3: triangles, 4: quadrilaterals (mesh.cpp:23-35)
+            E = np.ascontiguousarray(E, dtype=np.int32).reshape(-1, nvpe)
             tags = boundary_tags or {}
             names = (C.c_char_p * max(1, len(tags)))(*[k.encode() for k in tags])
             ids = np.ascontiguousarray(list(tags.values()) or [0], dtype=np.int32)
@@ -109,8 +111,8 @@ class DGMesh:
                 for v1, v2 in boundary_edges[tag]:
                     be.append((tag, v1, v2))
             B = np.ascontiguousarray(be if be else np.zeros((0, 3)), dtype=np.int32).reshape(-1, 3)
-            check(lib.dgx_mesh_create(len(V), _dptr(V), len(E), _iptr(E), len(tags), names,
-                                      _iptr(ids), len(B), _iptr(B), C.byref(self._h)))
+            check(lib.dgx_mesh_create_nv(nvpe, len(V), _dptr(V), len(E), _iptr(E), len(tags), names,
+                                         _iptr(ids), len(B), _iptr(B), C.byref(self._h)))
         self._bc_keep = []
 
     @classmethod
@@ -165,22 +167,38 @@ class DGMesh:
         check(L.load().dgx_mesh_arrays(self._h, None, _dptr(V), None))
         return V
 
+    def get_element_type(self) -> str:
+        """"triangle" or "quad" (DGMesh::get_element_type)."""
+        return "quad" if self.vertices_per_element() == 4 else "triangle"
+
+    def vertices_per_element(self) -> int:
+        n = C.c_int()
+        check(L.load().dgx_mesh_vertices_per_element(self._h, C.byref(n)))
+        return n.value
+
     def get_elements(self) -> np.ndarray:
-        E = np.zeros((self.get_n_elements(), 3), np.int32)
+        E = np.zeros((self.get_n_elements(), self.vertices_per_element()), np.int32)
         check(L.load().dgx_mesh_arrays(self._h, None, None, _iptr(E)))
         return E
 
 
 class DGSpace:
-    """DGSpace("triangle", order) with a basis choice (dgfem's default is monomial)."""
+    """DGSpace("triangle", order) with a basis choice (dgfem's default is monomial), or
+    DGSpace("quad", order), whose basis is LegendreBasis (space.cpp:307-319)."""
 
-    def __init__(self, element_type: str = "triangle", order: int = 1, basis: str = "monomial"):
-        if element_type != "triangle":
+    def __init__(self, element_type: str = "triangle", order: int = 1, basis: Optional[str] = None):
+        if element_type not in ("triangle", "quad"):
             raise ValueError(f"Unknown element type: {element_type}")
         if order < 1 or order > 10:
             raise ValueError(f"Element order must be between 1 and 10, got: {order}")
+        self.element_type = element_type
         self.order = order
-        self.basis = {"monomial": L.BASIS_MONOMIAL, "dubiner": L.BASIS_DUBINER}[basis]
+        if basis is None:
+            basis = "legendre" if element_type == "quad" else "monomial"
+        if (basis == "legendre") != (element_type == "quad"):
+            raise ValueError(f"basis {basis!r} does not apply to {element_type} elements")
+        self.basis = {"monomial": L.BASIS_MONOMIAL, "dubiner": L.BASIS_DUBINER,
+                      "legendre": L.BASIS_LEGENDRE}[basis]
 
     def get_order(self) -> int:
         return self.order

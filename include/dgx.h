@@ -37,7 +37,9 @@ extern "C" {
 #define DGX_ERR_CUDA (-4)      /* CUDA failure or no usable GPU */
 #define DGX_ERR_NONFINITE (-5) /* non-finite or non-positive state detected */
 
-enum { DGX_BASIS_MONOMIAL = 0, DGX_BASIS_DUBINER = 1 };
+/* DGX_BASIS_LEGENDRE: LegendreBasis (src/basis/legendre.cpp), the basis of quadrilateral
+ * meshes (DGSpace::create_basis, src/core/space.cpp:307-319). */
+enum { DGX_BASIS_MONOMIAL = 0, DGX_BASIS_DUBINER = 1, DGX_BASIS_LEGENDRE = 2 };
 enum { DGX_EULER = 0, DGX_NAVIER_STOKES = 1 };
 /* DGX_FP64: FP64 arithmetic and state (the plain form).  DGX_MIXED: FP32 flux and
  * contraction arithmetic, FP64 geometry, M^-1 and RK3 state.  DGX_DF64: the FP64 path's
@@ -56,8 +58,9 @@ typedef struct dgx_ctx dgx_ctx;
  * NavierStokesWeakFormulation(gamma, mu, Pr, sigma0)
  * (include/dgfem/weak_forms/navier_stokes_weak_formulation.hpp:19-20). */
 typedef struct {
-    int order;      /* polynomial order p, 1..4 */
-    int basis;      /* DGX_BASIS_MONOMIAL (dgfem's triangle default) or DGX_BASIS_DUBINER */
+    int order;      /* polynomial order p, 1..4 (quadrilaterals: 1..3) */
+    int basis;      /* triangles: DGX_BASIS_MONOMIAL (dgfem's default) or DGX_BASIS_DUBINER;
+                       quadrilaterals: DGX_BASIS_LEGENDRE */
     int physics;    /* DGX_EULER or DGX_NAVIER_STOKES */
     int precision;  /* DGX_FP64, DGX_MIXED or DGX_DF64 */
     double gamma;   /* 1.4 */
@@ -78,6 +81,14 @@ const char* dgx_version(void);
 int dgx_mesh_create(int n_vertices, const double* vertices, int n_elements, const int* elements,
                     int n_tags, const char* const* tag_names, const int* tag_ids,
                     int n_boundary_edges, const int* boundary_edges, dgx_mesh** out);
+/* The same for vertices_per_element = 3 (triangles) or 4 (bilinear quadrilaterals,
+ * counter-clockwise; DGMesh picks "quad" from the element matrix's 4 columns,
+ * src/core/mesh.cpp:23-35).  elements: [n_elements][vertices_per_element]. */
+int dgx_mesh_create_nv(int vertices_per_element, int n_vertices, const double* vertices, int n_elements,
+                       const int* elements, int n_tags, const char* const* tag_names, const int* tag_ids,
+                       int n_boundary_edges, const int* boundary_edges, dgx_mesh** out);
+/* vertices per element of a mesh: 3 or 4 (DGMesh::get_element_type) */
+int dgx_mesh_vertices_per_element(const dgx_mesh* m, int* vertices_per_element);
 
 /* Structured N_x x N_y quad grid on [x0,x1]x[y0,y1], each quad split along its
  * (i,j)-(i+1,j+1) diagonal into two counter-clockwise triangles, boundary tags
@@ -103,7 +114,8 @@ int dgx_mesh_info(const dgx_mesh* m, int* n_elements, int* n_interior_faces, int
 int dgx_mesh_interior_faces(const dgx_mesh* m, int* out5);
 /* [n][3] = (elem, face, tag id) of boundary faces, in build_precomputed_faces order */
 int dgx_mesh_boundary_faces(const dgx_mesh* m, int* out3);
-/* vertices [n_vertices][2] / elements [n_elements][3]; either pointer may be NULL */
+/* vertices [n_vertices][2] / elements [n_elements][vertices per element]; either
+ * pointer may be NULL */
 int dgx_mesh_arrays(const dgx_mesh* m, int* n_vertices, double* vertices, int* elements);
 void dgx_mesh_destroy(dgx_mesh* m);
 

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from meshes import PERIODIC_PAIRS, TAGS, periodic_rectangle, two_triangle_mesh
+from meshes import PERIODIC_PAIRS, TAGS, periodic_rectangle, quad_rectangle, two_triangle_mesh
 
 ROOT = Path(__file__).resolve().parent.parent
 
@@ -128,3 +128,41 @@ def test_no_gpu_fails_loudly(dg):
     with pytest.raises(dg.DGXError) as ei:
         dg.DGContext(m, dg.DGSpace("triangle", 2), dg.EulerWeakFormulation())
     assert "no CPU fallback" in str(ei.value)
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+@pytest.mark.parametrize("n,nx,distort", [(3, None, 0.0), (5, 4, 0.25), (8, None, 0.2)])
+def test_quad_mesh_faces_match_oracle(dg, n, nx, distort, periodic):
+    """Quadrilateral meshes (4-column element arrays): neighbour pairing, face lists and
+    the reversed flags equal the oracle's restatement of DGMesh."""
+    v, e, b = quad_rectangle(n, nx=nx, distort=distort, seed=n)
+    om = O.OracleMesh(v, e, b, order=2, basis=O.LEGENDRE, periodic=PERIODIC_PAIRS if periodic else ())
+    pm = _product_mesh(dg, v, e, b, periodic=periodic)
+    assert pm.get_element_type() == "quad" and pm.vertices_per_element() == 4
+    assert np.array_equal(pm.get_elements(), e)
+    assert np.array_equal(pm.get_interior_faces(), om.interior_faces())
+    assert np.array_equal(pm.get_boundary_face_data(), om.boundary_faces())
+    if periodic:
+        assert len(pm.get_boundary_face_data()) == 0
+
+
+def test_quad_mesh_permuted_elements_match_oracle(dg):
+    rng = np.random.default_rng(7)
+    v, e, b = quad_rectangle(6, distort=0.2)
+    e = e[rng.permutation(len(e))]
+    om = O.OracleMesh(v, e, b, order=1, basis=O.LEGENDRE)
+    pm = _product_mesh(dg, v, e, b)
+    assert np.array_equal(pm.get_interior_faces(), om.interior_faces())
+    assert np.array_equal(pm.get_boundary_face_data(), om.boundary_faces())
+
+
+def test_element_type_errors(dg):
+    with pytest.raises(ValueError):
+        dg.DGMesh(np.zeros((5, 2)), np.array([[0, 1, 2, 3, 4]]), None, {}, {})
+    with pytest.raises(ValueError):
+        dg.DGSpace("hexagon", 2)
+    with pytest.raises(ValueError):
+        dg.DGSpace("quad", 2, "dubiner")
+    with pytest.raises(ValueError):
+        dg.DGSpace("triangle", 2, "legendre")
+    assert dg.DGSpace("quad", 2).basis == 2
