@@ -338,6 +338,59 @@ def batch_leg(dg, torch, n_inst, steps, seed):
             "fp64_reference_runs_s": t_ref}
 
 
+def quad_leg(dg, torch, cells, steps, order=3):
+    """Bilinear quadrilaterals (DGSpace("quad", 3), Legendre basis): the vortex on a periodic
+    cells x cells mesh whose interior vertices are moved by up to 20 % of the cell size
+    (non-affine elements), FP64, mixed and double-float forms of the quad element kernel,
+    each 3 launches per SSP-RK3 step, and their distance from FP64 after `steps` steps."""
+    n1 = cells + 1
+    xs = np.linspace(-5.0, 5.0, n1)
+    X, Y = np.meshgrid(xs, xs)
+    V = np.stack([X.ravel(), Y.ravel()], axis=1)
+    rng = np.random.default_rng(7)
+    inner = (np.abs(np.abs(V[:, 0]) - 5.0) > 1e-12) & (np.abs(np.abs(V[:, 1]) - 5.0) > 1e-12)
+    V[inner] += 0.2 * (10.0 / cells) * rng.uniform(-1, 1, (int(inner.sum()), 2))
+    vid = lambda i, j: j * n1 + i  # noqa: E731
+    E = np.array([(vid(i, j), vid(i + 1, j), vid(i + 1, j + 1), vid(i, j + 1))
+                  for j in range(cells) for i in range(cells)], dtype=np.int32)
+    edges = {2: [(vid(i, 0), vid(i + 1, 0)) for i in range(cells)],
+             3: [(vid(cells, j), vid(cells, j + 1)) for j in range(cells)],
+             4: [(vid(i, cells), vid(i + 1, cells)) for i in range(cells)],
+             5: [(vid(0, j), vid(0, j + 1)) for j in range(cells)]}
+    mesh = dg.DGMesh(V, E, None, {"Bottom": 2, "Right": 3, "Top": 4, "Left": 5}, edges)
+    mesh.set_periodic_boundaries("Left", "Right")
+    mesh.set_periodic_boundaries("Bottom", "Top")
+    space = dg.DGSpace("quad", order)
+    wf = dg.EulerWeakFormulation(GAMMA)
+    ctxs = {k: dg.DGContext(mesh, space, wf, k) for k in ("fp64", "mixed", "df64")}
+    c64 = ctxs["fp64"]
+    u0 = c64.project(torch.tensor(vortex(c64.quad_points()), device="cuda"))
+    dt = 0.05 / c64.max_cfl(u0, 1.0)
+    dof = c64.n_elements * c64.n_basis * 4
+    out = {"workload": f"euler_vortex_quads_{cells}x{cells}_distorted_p{order}_legendre",
+           "elements": c64.n_elements, "dof": dof, "steps": steps, "dt": dt}
+    ref = None
+    for name, ctx in ctxs.items():
+        u = u0.clone()
+        ctx.rk3_step(u, dt, 2)  # warm-up (graph capture)
+        u = u0.clone()
+        torch.cuda.synchronize()
+        s = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        ctx.rk3_step(u, dt, steps)
+        e1.record(s)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        if ref is None:
+            ref = u
+        out[name] = {"ms_per_step": 1e3 * t / steps, "value": dof * 3 * steps / t,
+                     "vs_fp64_l2_rel": float(torch.linalg.vector_norm(u - ref) / torch.linalg.vector_norm(ref))}
+    out["mixed_vs_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    out["df64_vs_fp64"] = out["fp64"]["ms_per_step"] / out["df64"]["ms_per_step"]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -354,6 +407,8 @@ def main():
     ap.add_argument("--adj-dirs", type=int, default=16, help="finite-difference directions of the adjoint check")
     ap.add_argument("--batch-instances", type=int, default=256, help="instances of the batched leg (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=300, help="SSP-RK3 steps of each batched instance")
+    ap.add_argument("--quad-cells", type=int, default=256, help="quadrilaterals per side of the quad leg (0: skip)")
+    ap.add_argument("--quad-steps", type=int, default=50, help="SSP-RK3 steps of the quad leg")
     args = ap.parse_args()
     rank, ws = dist_init()
     if args.impl == "reference":
@@ -608,6 +663,8 @@ def main():
 
     cfg1 = config1_leg(dg, torch)
 
+    quads = quad_leg(dg, torch, args.quad_cells, args.quad_steps) if args.quad_cells > 0 else None
+
     bat = None
     if args.batch_instances > 0:
         bat = batch_leg(dg, torch, args.batch_instances, args.batch_steps, args.seed)
@@ -641,6 +698,7 @@ def main():
                 "adjoint": adj,
                 "batched": bat,
                 "config1": cfg1,
+                "quadrilaterals": quads,
                 "e2e": {"value": v_e2e, "unit": "DOF*stages/s", "h2d_bytes_per_step": dof * 8,
                         "d2h_bytes_per_step": dof * 8, "steps": ke},
                 "gpu_launches": 3 * args.steps + 1,

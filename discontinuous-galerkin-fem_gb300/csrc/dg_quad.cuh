@@ -22,12 +22,23 @@
 //    the dense per-element inverse dgfem stores
 //    (CompressibleDGSolverBase::compute_mass_matrix_inverse_blocks,
 //    src/solver/compressible_solver_base.cpp:41-61).
+//
+// T is the residual's arithmetic: double (DGX_FP64), float (DGX_MIXED) or f2 (DGX_DF64).
+// The element mass inverse runs in FP64 from FP64 tables (MassOps), except for the RK3
+// stage increment dt M_K^-1 R of the FP32 form, which runs in FP32: an increment of a
+// few percent of the state carries FP32 rounding of a few 1e-9 of the state.  The state
+// and the RK3 combination stay FP64 in every form.
 #pragma once
 
 #include "../../include/dgx.h"
 #include "dg_physics.cuh"
 
 namespace dgx {
+
+template <typename A, typename B>
+struct is_same_type { static constexpr bool value = false; };
+template <typename A>
+struct is_same_type<A, A> { static constexpr bool value = true; };
 
 template <int P, typename T>
 struct QuadOps {
@@ -42,7 +53,7 @@ struct QuadOps {
     T xq[NQ][2];          // volume points (xi, eta)
     T wf[NFQ];            // Gauss-Legendre weights on [-1, 1]
     T xf[4][NFQ][2];      // face points on the reference square
-    double dinv[NP];      // 1 / D_kk, D = sum_q w_q phi phi^T (diagonal)
+    T dinv[NP];           // 1 / D_kk, D = sum_q w_q phi phi^T (diagonal)
 };
 
 template <int P, typename T>
@@ -69,7 +80,28 @@ inline void fill_quad_ops(const OpsHost& h, QuadOps<P, T>& o) {
             o.xf[f][j][1] = (T)h.fxi[f][j][1];
         }
     for (int j = 0; j < Q::NFQ; ++j) o.wf[j] = (T)h.wf[j];
-    for (int i = 0; i < Q::NP; ++i) o.dinv[i] = h.minv[i][i];
+    for (int i = 0; i < Q::NP; ++i) o.dinv[i] = (T)h.minv[i][i];
+}
+
+// FP64 tables of the element mass inverse
+template <int P>
+struct MassOps {
+    static constexpr int NP = (P + 1) * (P + 1), NQ = NP;
+    double phi[NQ][NP];
+    double wq[NQ];
+    double xq[NQ][2];
+    double dinv[NP];
+};
+
+template <int P>
+inline void fill_mass_ops(const OpsHost& h, MassOps<P>& m) {
+    for (int q = 0; q < MassOps<P>::NQ; ++q) {
+        for (int i = 0; i < MassOps<P>::NP; ++i) m.phi[q][i] = h.phi[q][i];
+        m.wq[q] = h.wq[q];
+        m.xq[q][0] = h.qp[q][0];
+        m.xq[q][1] = h.qp[q][1];
+    }
+    for (int i = 0; i < MassOps<P>::NP; ++i) m.dinv[i] = h.minv[i][i];
 }
 
 template <int P, typename T, bool VISC>
@@ -78,6 +110,7 @@ struct QKArgs {
     const QuadGeom* geom;
     const QuadConn* conn;
     QuadOps<P, T> o;
+    MassOps<P> m;
 };
 
 // J_T at (xi, eta): rows (dx/dxi, dy/dxi) and (dx/deta, dy/deta) (mapping.cpp:22-50)
@@ -146,6 +179,8 @@ __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* U
         for (int i = 0; i < NP; ++i)
 #pragma unroll
             for (int v = 0; v < NV; ++v) U[v] = mac(U[v], o.phi[q][i], Ue[i * NV + v]);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) U[v] = settle(U[v]);
         T F[4], Gf[4], uu, vv, pp, ri;
         euler_flux<T>(U, gamma - T(1), F, Gf, uu, vv, pp, ri);
         T J00, J01, J10, J11;
@@ -160,6 +195,11 @@ __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* U
                     gr[v] = mac(gr[v], o.dr[q][i], Ue[i * NV + v]);
                     gs[v] = mac(gs[v], o.ds[q][i], Ue[i * NV + v]);
                 }
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                gr[v] = settle(gr[v]);
+                gs[v] = settle(gs[v]);
+            }
             const T r = rcp_<T>(det);
             const T A0 = J11 * r, A1 = -J01 * r, A2 = -J10 * r, A3 = J00 * r;
             T gx[4], gy[4], Fv[4], Gv[4];
@@ -232,6 +272,8 @@ __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* U
             for (int i = 0; i < NP; ++i)
 #pragma unroll
                 for (int v = 0; v < NV; ++v) Uo[v] = mac(Uo[v], o.phif[f][j][i], Ue[i * NV + v]);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) Uo[v] = settle(Uo[v]);
             T Un[4] = {T(0), T(0), T(0), T(0)};
             const int k = rev ? NFQ - 1 - j : j;
             if (nb >= 0) {
@@ -243,6 +285,8 @@ __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* U
 #pragma unroll
                     for (int v = 0; v < NV; ++v) Un[v] = mac(Un[v], ph, c[v]);
                 }
+#pragma unroll
+                for (int v = 0; v < NV; ++v) Un[v] = settle(Un[v]);
             }
             T H[4] = {T(0), T(0), T(0), T(0)};
             if (nb >= 0) {
@@ -260,6 +304,11 @@ __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* U
                         gr[v] = mac(gr[v], o.drf[f][j][i], Ue[i * NV + v]);
                         gs[v] = mac(gs[v], o.dsf[f][j][i], Ue[i * NV + v]);
                     }
+#pragma unroll
+                for (int v = 0; v < NV; ++v) {
+                    gr[v] = settle(gr[v]);
+                    gs[v] = settle(gs[v]);
+                }
                 T A[4];
                 quad_inverse_map<T>(G, o.xf[f][j][0], o.xf[f][j][1], A);
                 T gx[4], gy[4], Fv[4], Gv[4];
@@ -280,6 +329,11 @@ __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* U
                             nr[v] = mac(nr[v], o.drf[nf][k][i], c[v]);
                             ns[v] = mac(ns[v], o.dsf[nf][k][i], c[v]);
                         }
+                    }
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) {
+                        nr[v] = settle(nr[v]);
+                        ns[v] = settle(ns[v]);
                     }
                     T B[4];
                     quad_inverse_map<T>(geoms[nb], o.xf[nf][k][0], o.xf[nf][k][1], B);
@@ -321,32 +375,35 @@ __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* U
     }
 }
 
-// M_K^-1 applied to the row r (this thread's NP x 4 values in shared memory, overwritten):
-// r <- D^-1 Phi^T diag(w_q / |J_q|) Phi D^-1 r, accumulated in acc (registers).
-template <int P, typename T>
-__device__ __forceinline__ void quad_mass_inv_row(const QuadOps<P, T>& o, const QuadGeom& G, double* r,
-                                                  double acc[n_basis_quad(P)][NV]) {
+// M_K^-1 applied to the row r (this thread's NP x 4 values, overwritten) in arithmetic A
+// from tables of type B: r <- D^-1 Phi^T diag(w_q / |J_q|) Phi D^-1 r, accumulated in acc.
+template <int P, typename A, typename B>
+__device__ __forceinline__ void quad_mass_inv_row(const B (&phi)[n_basis_quad(P)][n_basis_quad(P)],
+                                                  const B (&wq)[n_basis_quad(P)], const B (&xq)[n_basis_quad(P)][2],
+                                                  const B (&dinv)[n_basis_quad(P)], const QuadGeom& G, double* r,
+                                                  A acc[n_basis_quad(P)][NV]) {
     constexpr int NP = n_basis_quad(P), NQ = NP;
 #pragma unroll
     for (int i = 0; i < NP; ++i)
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-            r[i * NV + v] *= o.dinv[i];
-            acc[i][v] = 0.0;
+            r[i * NV + v] = (double)((A)r[i * NV + v] * (A)dinv[i]);
+            acc[i][v] = A(0);
         }
 #pragma unroll 1
     for (int q = 0; q < NQ; ++q) {
-        double y[4] = {0.0, 0.0, 0.0, 0.0};
+        A y[4] = {A(0), A(0), A(0), A(0)};
 #pragma unroll
         for (int k = 0; k < NP; ++k)
 #pragma unroll
-            for (int v = 0; v < NV; ++v) y[v] += (double)o.phi[q][k] * r[k * NV + v];
-        double J00, J01, J10, J11;
-        quad_jacobian<double>(G, (double)o.xq[q][0], (double)o.xq[q][1], J00, J01, J10, J11);
-        const double s = (double)o.wq[q] / fabs(J00 * J11 - J10 * J01);
+            for (int v = 0; v < NV; ++v) y[v] += (A)phi[q][k] * (A)r[k * NV + v];
+        A J00, J01, J10, J11;
+        quad_jacobian<A>(G, (A)xq[q][0], (A)xq[q][1], J00, J01, J10, J11);
+        const A det = J00 * J11 - J10 * J01;
+        const A s = (A)wq[q] / (det < A(0) ? -det : det);
 #pragma unroll
         for (int i = 0; i < NP; ++i) {
-            const double ph = (double)o.phi[q][i] * s;
+            const A ph = (A)phi[q][i] * s;
 #pragma unroll
             for (int v = 0; v < NV; ++v) acc[i][v] += ph * y[v];
         }
@@ -354,7 +411,13 @@ __device__ __forceinline__ void quad_mass_inv_row(const QuadOps<P, T>& o, const 
 #pragma unroll
     for (int i = 0; i < NP; ++i)
 #pragma unroll
-        for (int v = 0; v < NV; ++v) r[i * NV + v] = o.dinv[i] * acc[i][v];
+        for (int v = 0; v < NV; ++v) r[i * NV + v] = (double)((A)dinv[i] * acc[i][v]);
+}
+
+template <int P>
+__device__ __forceinline__ void quad_mass_inv_row64(const MassOps<P>& m, const QuadGeom& G, double* r,
+                                                    double acc[n_basis_quad(P)][NV]) {
+    quad_mass_inv_row<P, double, double>(m.phi, m.wq, m.xq, m.dinv, G, r, acc);
 }
 
 #ifndef DGX_QUAD_MIN_BLOCKS
@@ -404,9 +467,18 @@ __global__ void __launch_bounds__(TILE, DGX_QUAD_MIN_BLOCKS) quad_element_kernel
         for (int i = 0; i < NP; ++i)
 #pragma unroll
             for (int v = 0; v < NV; ++v) sD[tl * STR + i * NV + v] = (double)R[i][v];
-        if (s.mode != MODE_RESIDUAL) {
+        bool done = s.mode == MODE_RESIDUAL;
+        if constexpr (is_same_type<T, float>::value) {
+            if (s.mode == MODE_STAGE) {  // the FP32 form's stage increment: M_K^-1 R in FP32
+                float acc[NP][NV];
+                quad_mass_inv_row<P, float, float>(ka.o.phi, ka.o.wq, ka.o.xq, ka.o.dinv, ka.geom[e], sD + tl * STR,
+                                                   acc);
+                done = true;
+            }
+        }
+        if (!done) {
             double acc[NP][NV];
-            quad_mass_inv_row<P, T>(ka.o, ka.geom[e], sD + tl * STR, acc);
+            quad_mass_inv_row64<P>(ka.m, ka.geom[e], sD + tl * STR, acc);
         }
     }
     __syncthreads();
@@ -436,5 +508,39 @@ template <int P, typename T>
 inline size_t quad_smem_bytes() {
     return (size_t)TILE * (n_basis_quad(P) * NV + 1) * sizeof(double);
 }
+
+template <int P, typename T, bool VISC>
+inline int configure_quad_t() {
+    return cudaFuncSetAttribute(quad_element_kernel<P, T, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)quad_smem_bytes<P, T>()) == cudaSuccess
+               ? 0
+               : -1;
+}
+
+template <int P, typename T, bool VISC>
+inline int launch_quad_t(const StepArgs& a, const QuadGeom* geom, const QuadConn* conn, const OpsHost& oh,
+                         cudaStream_t st) {
+    QKArgs<P, T, VISC> ka;  // by value: operator reads are constant-bank operands
+    ka.s = a;
+    ka.geom = geom;
+    ka.conn = conn;
+    fill_quad_ops<P, T>(oh, ka.o);
+    fill_mass_ops<P>(oh, ka.m);
+    const int grid = (a.ne + TILE - 1) / TILE;
+    if (grid == 0) return 0;
+    quad_element_kernel<P, T, VISC><<<grid, TILE, quad_smem_bytes<P, T>(), st>>>(ka);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+#define DGX_QUAD_DISPATCH(FN, T, ARGS)               \
+    switch (p * 2 + (viscous ? 1 : 0)) {             \
+    case 2: return FN<1, T, false> ARGS;             \
+    case 3: return FN<1, T, true> ARGS;              \
+    case 4: return FN<2, T, false> ARGS;             \
+    case 5: return FN<2, T, true> ARGS;              \
+    case 6: return FN<3, T, false> ARGS;             \
+    case 7: return FN<3, T, true> ARGS;              \
+    default: return -1;                              \
+    }
 
 }  // namespace dgx

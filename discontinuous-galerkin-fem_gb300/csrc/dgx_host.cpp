@@ -526,8 +526,10 @@ extern "C" int dgx_mesh_set_periodic(dgx_mesh* m, const char* t1, const char* t2
     return DGX_OK;
 }
 
-extern "C" int dgx_mesh_create_rectangle(int nx, int ny, double x0, double x1, double y0, double y1,
-                                         int periodic, dgx_mesh** out) {
+// Structured rectangle of nx x ny cells: two triangles per cell (nvpe = 3) or the cell
+// itself (nvpe = 4), boundary tags Bottom=2 Right=3 Top=4 Left=5.
+static int create_rectangle(int nvpe, int nx, int ny, double x0, double x1, double y0, double y1, int periodic,
+                            dgx_mesh** out) {
     if (nx < 1 || ny < 1 || !out || !(x1 > x0) || !(y1 > y0))
         return fail(DGX_ERR_INVALID, "dgx_mesh_create_rectangle: bad arguments");
     const int nvx = nx + 1, nvy = ny + 1;
@@ -540,13 +542,16 @@ extern "C" int dgx_mesh_create_rectangle(int nx, int ny, double x0, double x1, d
             V[2 * ((size_t)j * nvx + i) + 1] = j == ny ? y1 : j * sy + y0;
         }
     auto vid = [&](int i, int j) { return j * nvx + i; };
-    std::vector<int> E((size_t)nx * ny * 6);
-    size_t k = 0;
+    std::vector<int> E;
+    E.reserve((size_t)nx * ny * 6);
     for (int j = 0; j < ny; ++j)
         for (int i = 0; i < nx; ++i) {
             const int a = vid(i, j), b = vid(i + 1, j), c = vid(i + 1, j + 1), d = vid(i, j + 1);
-            const int t[6] = {a, b, c, a, c, d};
-            for (int q = 0; q < 6; ++q) E[k++] = t[q];
+            if (nvpe == 4) {
+                E.insert(E.end(), {a, b, c, d});
+            } else {
+                E.insert(E.end(), {a, b, c, a, c, d});
+            }
         }
     std::vector<int> B;
     for (int i = 0; i < nx; ++i) B.insert(B.end(), {2, vid(i, 0), vid(i + 1, 0)});
@@ -555,14 +560,24 @@ extern "C" int dgx_mesh_create_rectangle(int nx, int ny, double x0, double x1, d
     for (int j = 0; j < ny; ++j) B.insert(B.end(), {5, vid(0, j), vid(0, j + 1)});
     const char* names[4] = {"Bottom", "Right", "Top", "Left"};
     const int ids[4] = {2, 3, 4, 5};
-    int rc = dgx_mesh_create(nvx * nvy, V.data(), nx * ny * 2, E.data(), 4, names, ids,
-                             (int)B.size() / 3, B.data(), out);
+    int rc = dgx_mesh_create_nv(nvpe, nvx * nvy, V.data(), (int)(E.size() / nvpe), E.data(), 4, names, ids,
+                                (int)B.size() / 3, B.data(), out);
     if (rc || !periodic) return rc;
     if ((rc = dgx_mesh_set_periodic(*out, "Left", "Right")) || (rc = dgx_mesh_set_periodic(*out, "Bottom", "Top"))) {
         dgx_mesh_destroy(*out);
         *out = nullptr;
     }
     return rc;
+}
+
+extern "C" int dgx_mesh_create_rectangle(int nx, int ny, double x0, double x1, double y0, double y1,
+                                         int periodic, dgx_mesh** out) {
+    return create_rectangle(3, nx, ny, x0, x1, y0, y1, periodic, out);
+}
+
+extern "C" int dgx_mesh_create_rectangle_quad(int nx, int ny, double x0, double x1, double y0, double y1,
+                                              int periodic, dgx_mesh** out) {
+    return create_rectangle(4, nx, ny, x0, x1, y0, y1, periodic, out);
 }
 
 extern "C" int dgx_mesh_set_bc(dgx_mesh* m, const char* tag, int type, const double* value4) {
@@ -626,7 +641,8 @@ static StepArgs base_args(const dgx_ctx* c) {
 
 static int launch(const dgx_ctx* c, const StepArgs& a, cudaStream_t s) {
     const bool visc = c->prm.physics == DGX_NAVIER_STOKES;
-    const int rc = c->nvpe == 4 ? launch_quad_element(c->prm.order, visc, a, c->d_qgeom, c->d_qconn, c->ops, s)
+    const int rc = c->nvpe == 4 ? launch_quad_element(c->prm.order, visc, c->prm.precision, a, c->d_qgeom,
+                                                      c->d_qconn, c->ops, s)
                    : c->prm.precision == DGX_MIXED  ? launch_element_mixed(c->prm.order, visc, a, c->ops, s)
                    : c->prm.precision == DGX_DF64 ? launch_element_df64(c->prm.order, visc, a, c->ops, s)
                                                   : launch_element_fp64(c->prm.order, visc, a, c->ops, s);
@@ -886,8 +902,6 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
                                           : "the Legendre basis is for quadrilateral meshes");
     if (quad && p->order > MAX_P_QUAD)
         return fail(DGX_ERR_INVALID, "Element order must be between 1 and 3 for the quadrilateral GPU kernels");
-    if (quad && p->precision != DGX_FP64)
-        return fail(DGX_ERR_INVALID, "quadrilateral meshes run in FP64 (DGX_FP64)");
     if (p->physics != DGX_EULER && p->physics != DGX_NAVIER_STOKES)
         return fail(DGX_ERR_INVALID, "unknown physics");
     if (p->precision != DGX_FP64 && p->precision != DGX_MIXED && p->precision != DGX_DF64)
@@ -902,11 +916,11 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
 
     {
         const bool visc = p->physics == DGX_NAVIER_STOKES;
-        int rc = quad                       ? configure_quad_element(p->order, visc)
+        int rc = quad                       ? configure_quad_element(p->order, visc, p->precision)
                  : p->precision == DGX_MIXED  ? configure_element_mixed(p->order, visc)
                  : p->precision == DGX_DF64 ? configure_element_df64(p->order, visc)
                                             : configure_element_fp64(p->order, visc);
-        if (!rc && p->precision == DGX_MIXED && !visc) rc = configure_stage_tc(p->order);
+        if (!rc && p->precision == DGX_MIXED && !visc && !quad) rc = configure_stage_tc(p->order);
         if (rc) return fail(DGX_ERR_CUDA, "could not configure the element kernel");
     }
     auto* c = new dgx_ctx;
@@ -952,7 +966,7 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
         !alloc((void**)&c->d_bc, sizeof(BCSlot) * slots.size()) || !alloc((void**)&c->d_u1, sb) ||
         !alloc((void**)&c->d_u2, sb) || !alloc((void**)&c->d_mon, 4 * sizeof(double)) ||
         !alloc((void**)&c->d_flag, sizeof(int)) || !alloc((void**)&c->d_status, sizeof(int)) ||
-        (p->precision == DGX_MIXED &&
+        (p->precision == DGX_MIXED && !quad &&
          (!alloc((void**)&c->d_uhi[0], c->nstate * sizeof(float)) ||
           !alloc((void**)&c->d_uhi[1], c->nstate * sizeof(float)) ||
           !alloc((void**)&c->d_d1, c->nstate * sizeof(float)) ||
@@ -961,7 +975,7 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
         free_ctx(c);
         return fail(DGX_ERR_CUDA, "cudaMalloc failed for the solver state");
     }
-    if (p->precision == DGX_MIXED) {
+    if (p->precision == DGX_MIXED && !quad) {
         std::vector<ElemGeomF> gf(ne);
         for (int e = 0; e < ne; ++e) gf[e] = geom_to_f32(geom[e], 0);
         if (!alloc((void**)&c->d_geomf, sizeof(ElemGeomF) * ne) ||
@@ -1106,7 +1120,9 @@ extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void*
     if (!c || (c->ne && !u) || n_steps < 0) return fail(DGX_ERR_INVALID, "dgx_rk3_step: bad argument");
     if (c->ne == 0 || n_steps == 0) return DGX_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    const bool mixed = c->prm.precision == DGX_MIXED;
+    // mixed triangles: the increment-form stage kernels.  Mixed quadrilaterals take the
+    // element kernel's three stage launches, as FP64, with FP32 residual arithmetic.
+    const bool mixed = c->prm.precision == DGX_MIXED && c->nvpe == 3;
     // mixed: the FP32 copy of the caller's state, read by the first stage
     if (mixed && launch_f64_to_f32(c->nstate, u, c->d_uhi[0], s)) return fail(DGX_ERR_CUDA, "conversion launch failed");
     if (mixed && c->stage_grid == 0) {

@@ -215,11 +215,16 @@ constexpr int EVAL_MAX_POINTS = 128;
 int launch_eval_points(int ne, int np, int npts, const double* phi, const double* u, double* out, cudaStream_t s);
 int launch_f64_to_f32(size_t n, const double* in, float* out, cudaStream_t s);
 
-// Quadrilateral kernels (dgx_quad.cu), FP64, orders 1..MAX_P_QUAD.  StepArgs::geom and
-// StepArgs::conn are not used; the quadrilateral records are passed beside them.
-int launch_quad_element(int p, bool viscous, const StepArgs& a, const QuadGeom* geom, const QuadConn* conn,
-                        const OpsHost& ops, cudaStream_t s);
-int configure_quad_element(int p, bool viscous);
+// Quadrilateral kernels (dgx_quad.cu; the double-float element kernel in
+// dgx_kernels_df64.cu), orders 1..MAX_P_QUAD, precision DGX_FP64 / DGX_MIXED / DGX_DF64.
+// StepArgs::geom and StepArgs::conn are not used; the quadrilateral records are passed
+// beside them.
+int launch_quad_element(int p, bool viscous, int precision, const StepArgs& a, const QuadGeom* geom,
+                        const QuadConn* conn, const OpsHost& ops, cudaStream_t s);
+int configure_quad_element(int p, bool viscous, int precision);
+int launch_quad_element_df64(int p, bool viscous, const StepArgs& a, const QuadGeom* geom, const QuadConn* conn,
+                             const OpsHost& ops, cudaStream_t s);
+int configure_quad_element_df64(int p, bool viscous);
 int launch_quad_mass_inv(int ne, int p, const OpsHost& ops, const QuadGeom* geom, const double* in, double* out,
                          cudaStream_t s);
 int launch_quad_project(int ne, int p, const OpsHost& ops, const QuadGeom* geom, const double* uq, double* u,

@@ -3,6 +3,7 @@
 // FP32 pipe in pairs of floats.
 #include "df64.cuh"
 #include "dg_element.cuh"
+#include "dg_quad.cuh"
 
 namespace dgx {
 
@@ -16,6 +17,13 @@ int launch_element_df64(int p, bool viscous, const StepArgs& a, const OpsHost& o
     DGX_ELEMENT_DISPATCH(launch_element_t, f2)
 #undef ARGS
 }
+
+int launch_quad_element_df64(int p, bool viscous, const StepArgs& a, const QuadGeom* geom, const QuadConn* conn,
+                             const OpsHost& ops, cudaStream_t s) {
+    DGX_QUAD_DISPATCH(launch_quad_t, f2, (a, geom, conn, ops, s))
+}
+
+int configure_quad_element_df64(int p, bool viscous) { DGX_QUAD_DISPATCH(configure_quad_t, f2, ()) }
 
 int configure_element_df64(int p, bool viscous) {
 #define ARGS ()

@@ -4,44 +4,17 @@
 
 namespace dgx {
 
-template <int P, bool VISC>
-static int configure_quad_t() {
-    return cudaFuncSetAttribute(quad_element_kernel<P, double, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)quad_smem_bytes<P, double>()) == cudaSuccess
-               ? 0
-               : -1;
+int configure_quad_element(int p, bool viscous, int precision) {
+    if (precision == DGX_DF64) return configure_quad_element_df64(p, viscous);
+    if (precision == DGX_MIXED) { DGX_QUAD_DISPATCH(configure_quad_t, float, ()) }
+    DGX_QUAD_DISPATCH(configure_quad_t, double, ())
 }
 
-template <int P, bool VISC>
-static int launch_quad_t(const StepArgs& a, const QuadGeom* geom, const QuadConn* conn, const OpsHost& oh,
-                         cudaStream_t st) {
-    QKArgs<P, double, VISC> ka;  // by value: operator reads are constant-bank operands
-    ka.s = a;
-    ka.geom = geom;
-    ka.conn = conn;
-    fill_quad_ops<P, double>(oh, ka.o);
-    const int grid = (a.ne + TILE - 1) / TILE;
-    if (grid == 0) return 0;
-    quad_element_kernel<P, double, VISC><<<grid, TILE, quad_smem_bytes<P, double>(), st>>>(ka);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
-}
-
-#define DGX_QUAD_DISPATCH(FN, ARGS)                  \
-    switch (p * 2 + (viscous ? 1 : 0)) {             \
-    case 2: return FN<1, false> ARGS;                \
-    case 3: return FN<1, true> ARGS;                 \
-    case 4: return FN<2, false> ARGS;                \
-    case 5: return FN<2, true> ARGS;                 \
-    case 6: return FN<3, false> ARGS;                \
-    case 7: return FN<3, true> ARGS;                 \
-    default: return -1;                              \
-    }
-
-int configure_quad_element(int p, bool viscous) { DGX_QUAD_DISPATCH(configure_quad_t, ()) }
-
-int launch_quad_element(int p, bool viscous, const StepArgs& a, const QuadGeom* geom, const QuadConn* conn,
-                        const OpsHost& ops, cudaStream_t s) {
-    DGX_QUAD_DISPATCH(launch_quad_t, (a, geom, conn, ops, s))
+int launch_quad_element(int p, bool viscous, int precision, const StepArgs& a, const QuadGeom* geom,
+                        const QuadConn* conn, const OpsHost& ops, cudaStream_t s) {
+    if (precision == DGX_DF64) return launch_quad_element_df64(p, viscous, a, geom, conn, ops, s);
+    if (precision == DGX_MIXED) { DGX_QUAD_DISPATCH(launch_quad_t, float, (a, geom, conn, ops, s)) }
+    DGX_QUAD_DISPATCH(launch_quad_t, double, (a, geom, conn, ops, s))
 }
 
 // CompressibleDGSolverBase::apply_mass_inv (src/solver/compressible_solver_base.cpp:54-61)
@@ -55,7 +28,7 @@ __global__ void quad_mass_inv_kernel(const __grid_constant__ QuadOps<P, double> 
     const double* a = in + (size_t)e * NP * NV;
 #pragma unroll
     for (int k = 0; k < NP * NV; ++k) r[k] = a[k];
-    quad_mass_inv_row<P, double>(o, geom[e], r, acc);
+    quad_mass_inv_row<P, double, double>(o.phi, o.wq, o.xq, o.dinv, geom[e], r, acc);
     double* b = out + (size_t)e * NP * NV;
 #pragma unroll
     for (int k = 0; k < NP * NV; ++k) b[k] = r[k];
@@ -85,7 +58,7 @@ __global__ void quad_project_kernel(const __grid_constant__ QuadOps<P, double> o
             for (int v = 0; v < NV; ++v) F[i * NV + v] += s * U[q * NV + v];
         }
     }
-    quad_mass_inv_row<P, double>(o, G, F, acc);
+    quad_mass_inv_row<P, double, double>(o.phi, o.wq, o.xq, o.dinv, G, F, acc);
     double* b = u + (size_t)e * NP * NV;
 #pragma unroll
     for (int k = 0; k < NP * NV; ++k) b[k] = F[k];

@@ -39,6 +39,8 @@ SIGNATURES = {
     "dgx_mesh_create_nv": (C.c_int, [C.c_int, C.c_int, _dp, C.c_int, _ip, C.c_int, C.POINTER(C.c_char_p), _ip,
                                      C.c_int, _ip, C.POINTER(_vp)]),
     "dgx_mesh_vertices_per_element": (C.c_int, [_vp, _ip]),
+    "dgx_mesh_create_rectangle_quad": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                                 C.c_double, C.c_int, C.POINTER(_vp)]),
     "dgx_mesh_destroy": (None, [_vp]),
     "dgx_create": (C.c_int, [_vp, _vp, C.POINTER(_vp)]),
     "dgx_destroy": (None, [_vp]),

@@ -117,10 +117,14 @@ class DGMesh:
 
     @classmethod
     def rectangle(cls, nx: int, ny: int, x0: float, x1: float, y0: float, y1: float,
-                  periodic: bool = True) -> "DGMesh":
-        """Structured triangle mesh of a rectangle (tags Bottom=2 Right=3 Top=4 Left=5)."""
+                  periodic: bool = True, element_type: str = "triangle") -> "DGMesh":
+        """Structured mesh of a rectangle, two triangles per cell or ``element_type="quad"``
+        cells (tags Bottom=2 Right=3 Top=4 Left=5)."""
         h = C.c_void_p()
-        check(L.load().dgx_mesh_create_rectangle(nx, ny, x0, x1, y0, y1, int(periodic), C.byref(h)))
+        if element_type not in ("triangle", "quad"):
+            raise ValueError(f"Unknown element type: {element_type}")
+        fn = L.load().dgx_mesh_create_rectangle_quad if element_type == "quad" else L.load().dgx_mesh_create_rectangle
+        check(fn(nx, ny, x0, x1, y0, y1, int(periodic), C.byref(h)))
         return cls(None, None, _handle=h)
 
     def __del__(self):

@@ -2,7 +2,8 @@
 
 Mirrors dgfem's VTKWriter (include/dgfem/utils/vtk_writer.hpp:29-180,
 src/utils/vtk_writer.cpp): each triangle is subdivided into resolution_factor^2 triangles
-whose vertices are a uniform lattice of the reference triangle; the solution is evaluated
+whose vertices are a uniform lattice of the reference triangle (each quadrilateral into
+resolution_factor^2 quadrilaterals over a lattice of [-1, 1]^2); the solution is evaluated
 at the lattice points (here on the GPU, dgx_eval_points) and written as an ASCII
 UNSTRUCTURED_GRID with one SCALARS block per field.  The lattice order, the sub-triangle
 connectivity, the field names and the number format follow dgfem's writer, so files from
@@ -20,13 +21,20 @@ from . import _lib as L
 from ._lib import check
 
 
-def reference_subdivision(resolution_factor: int) -> Tuple[np.ndarray, np.ndarray]:
-    """Lattice points (xi, eta) of the reference triangle and the sub-triangles over them
+def reference_subdivision(resolution_factor: int, element_type: str = "triangle") -> Tuple[np.ndarray, np.ndarray]:
+    """Lattice points (xi, eta) of the reference element and the sub-cells over them
     (get_reference_subdivision_points / _connectivity, vtk_writer.cpp:325-409)."""
     r = int(resolution_factor)
     if r < 1:
         raise ValueError("resolution_factor must be at least 1")
     n1 = r + 1
+    if element_type == "quad":
+        pts = [(-1.0 + 2.0 * i / r, -1.0 + 2.0 * j / r) for j in range(n1) for i in range(n1)]
+        quads = [(j * n1 + i, j * n1 + i + 1, (j + 1) * n1 + i + 1, (j + 1) * n1 + i)
+                 for j in range(r) for i in range(r)]
+        return np.array(pts, dtype=np.float64), np.array(quads, dtype=np.int64)
+    if element_type != "triangle":
+        raise ValueError(f"Unknown element type: {element_type}")
     pts = [(i / r, j / r) for j in range(n1) for i in range(n1 - j)]
 
     def idx(i, j):
@@ -42,12 +50,16 @@ def reference_subdivision(resolution_factor: int) -> Tuple[np.ndarray, np.ndarra
 
 
 def _points_and_cells(vertices: np.ndarray, elements: np.ndarray, r: int):
-    ref, tri = reference_subdivision(r)
-    V = vertices[elements]  # (E, 3, 2)
+    quad = elements.shape[1] == 4
+    ref, sub = reference_subdivision(r, "quad" if quad else "triangle")
+    V = vertices[elements]  # (E, nv, 2)
     xi, eta = ref[:, 0], ref[:, 1]
-    N = np.stack([1.0 - xi - eta, xi, eta], axis=1)  # (npts, 3): the affine map of the element
+    if quad:  # ReferenceQuad's bilinear shape functions
+        N = 0.25 * np.stack([(1 - xi) * (1 - eta), (1 + xi) * (1 - eta), (1 + xi) * (1 + eta), (1 - xi) * (1 + eta)], axis=1)
+    else:  # the affine map of the triangle
+        N = np.stack([1.0 - xi - eta, xi, eta], axis=1)
     xy = np.einsum("pk,ekd->epd", N, V).reshape(-1, 2)
-    cells = (tri[None, :, :] + (np.arange(len(elements)) * len(ref))[:, None, None]).reshape(-1, 3)
+    cells = (sub[None, :, :] + (np.arange(len(elements)) * len(ref))[:, None, None]).reshape(-1, sub.shape[1])
     return ref, xy, cells
 
 
@@ -56,10 +68,11 @@ def _write(filename: str, title: str, xy: np.ndarray, cells: np.ndarray, fields:
         f.write("# vtk DataFile Version 3.0\n" + title + "\nASCII\nDATASET UNSTRUCTURED_GRID\n")
         f.write(f"POINTS {len(xy)} double\n")
         np.savetxt(f, xy, fmt="%.10e %.10e 0.0")
-        f.write(f"CELLS {len(cells)} {4 * len(cells)}\n")
-        np.savetxt(f, np.column_stack([np.full(len(cells), 3), cells]), fmt="%d")
+        nvc = cells.shape[1]
+        f.write(f"CELLS {len(cells)} {(nvc + 1) * len(cells)}\n")
+        np.savetxt(f, np.column_stack([np.full(len(cells), nvc), cells]), fmt="%d")
         f.write(f"CELL_TYPES {len(cells)}\n")
-        f.write("5\n" * len(cells))
+        f.write(("9\n" if nvc == 4 else "5\n") * len(cells))  # VTK_QUAD / VTK_TRIANGLE
         if fields:
             f.write(f"POINT_DATA {len(xy)}\n")
             for name, values in fields:
@@ -108,5 +121,5 @@ class VTKWriter:
 
     @staticmethod
     def write_mesh(mesh, filename: str):
-        """The mesh's own triangles, no data (write_mesh, vtk_writer.cpp:180-192)."""
+        """The mesh's own cells, no data (write_mesh, vtk_writer.cpp:180-192)."""
         _write(filename, "DGFEM Mesh", mesh.get_vertices(), mesh.get_elements().astype(np.int64), [])

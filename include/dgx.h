@@ -99,6 +99,13 @@ int dgx_mesh_vertices_per_element(const dgx_mesh* m, int* vertices_per_element);
 int dgx_mesh_create_rectangle(int nx, int ny, double x0, double x1, double y0, double y1,
                               int periodic, dgx_mesh** out);
 
+/* The same grid with the N_x x N_y cells themselves as counter-clockwise bilinear
+ * quadrilaterals (vertex ids (i,j), (i+1,j), (i+1,j+1), (i,j+1)); replaces
+ * MeshCreator::create_rectangular_mesh(dx, use_triangles = false, ...)
+ * (include/dgfem/utils/mesh_creation.hpp:36-38) without GMSH. */
+int dgx_mesh_create_rectangle_quad(int nx, int ny, double x0, double x1, double y0, double y1,
+                                   int periodic, dgx_mesh** out);
+
 /* DGMesh::set_periodic_boundaries, include/dgfem/core/mesh.hpp:102, src/core/mesh.cpp:482-588 */
 int dgx_mesh_set_periodic(dgx_mesh* m, const char* tag1, const char* tag2);
 

@@ -37,7 +37,9 @@ inline void check(int rc) {
 }
 
 // DGMesh(vertices, elements, element_tags, boundary_tags, boundary_edges).  VertMat: n x 2,
-// ElemMat: n x 3 (Eigen::MatrixXd / MatrixXi or anything with rows() and operator()).
+// ElemMat: n x 3 triangles or n x 4 quadrilaterals (Eigen::MatrixXd / MatrixXi or anything
+// with rows(), cols() and operator()); the column count picks the element type as in
+// DGMesh's constructor (src/core/mesh.cpp:23-35).
 class Mesh {
 public:
     template <class VertMat, class ElemMat>
@@ -49,9 +51,10 @@ public:
             v[2 * i] = vertices(i, 0);
             v[2 * i + 1] = vertices(i, 1);
         }
-        std::vector<int> e((size_t)elements.rows() * 3);
+        const int nvpe = (int)elements.cols();
+        std::vector<int> e((size_t)elements.rows() * (nvpe > 0 ? nvpe : 1));
         for (long i = 0; i < (long)elements.rows(); ++i)
-            for (int k = 0; k < 3; ++k) e[3 * i + k] = (int)elements(i, k);
+            for (int k = 0; k < nvpe; ++k) e[(size_t)nvpe * i + k] = (int)elements(i, k);
         std::vector<const char*> names;
         std::vector<int> ids;
         for (const auto& t : boundary_tags) {
@@ -65,8 +68,8 @@ public:
                 b.push_back(ed.first);
                 b.push_back(ed.second);
             }
-        check(dgx_mesh_create((int)vertices.rows(), v.data(), (int)elements.rows(), e.data(), (int)names.size(),
-                              names.data(), ids.data(), (int)b.size() / 3, b.data(), &m_));
+        check(dgx_mesh_create_nv(nvpe, (int)vertices.rows(), v.data(), (int)elements.rows(), e.data(),
+                                 (int)names.size(), names.data(), ids.data(), (int)b.size() / 3, b.data(), &m_));
     }
     Mesh(const Mesh&) = delete;
     Mesh& operator=(const Mesh&) = delete;
@@ -78,6 +81,12 @@ public:
     // constant BoundaryConditionEuler (FAR_FIELD: conserved state; NO_SLIP_WALL: primitive)
     void set_boundary_condition_euler(const std::string& tag, int bc_type, const double value[4]) {
         check(dgx_mesh_set_bc(m_, tag.c_str(), bc_type, value));
+    }
+    // "triangle" or "quad" (DGMesh::get_element_type)
+    std::string get_element_type() const {
+        int nvpe = 3;
+        check(dgx_mesh_vertices_per_element(m_, &nvpe));
+        return nvpe == 4 ? "quad" : "triangle";
     }
     int get_n_elements() const {
         int ne = 0;

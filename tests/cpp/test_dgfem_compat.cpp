@@ -51,24 +51,26 @@ int main(int argc, char** argv) {
     const std::vector<int> E = read_all<int>(dir + "/elements.bin");
     const std::vector<int> B = read_all<int>(dir + "/bedges.bin");
     const std::vector<double> U = read_all<double>(dir + "/state.bin");
-    const std::vector<double> P = read_all<double>(dir + "/params.bin");  // order, dt
+    const std::vector<double> P = read_all<double>(dir + "/params.bin");  // order, dt, nvpe, basis
     const int order = (int)P[0];
     const double dt = P[1];
+    const int nvpe = (int)P[2], basis = (int)P[3];
 
     Mat verts((int)V.size() / 2, 2);
     for (int i = 0; i < verts.r; ++i) { verts(i, 0) = V[2 * i]; verts(i, 1) = V[2 * i + 1]; }
-    Mat elems((int)E.size() / 3, 3);
+    Mat elems((int)E.size() / nvpe, nvpe);
     for (int i = 0; i < elems.r; ++i)
-        for (int k = 0; k < 3; ++k) elems(i, k) = E[3 * i + k];
+        for (int k = 0; k < nvpe; ++k) elems(i, k) = E[(size_t)nvpe * i + k];
     std::map<int, std::vector<std::pair<int, int>>> edges;
     for (size_t k = 0; k + 2 < B.size(); k += 3) edges[B[k]].push_back({B[k + 1], B[k + 2]});
     const std::map<std::string, int> tags = {{"Bottom", 2}, {"Right", 3}, {"Top", 4}, {"Left", 5}};
 
     try {
         dgx_dgfem::Mesh mesh(verts, elems, tags, edges);
+        if (mesh.get_element_type() != (nvpe == 4 ? "quad" : "triangle")) return 4;
         mesh.set_periodic_boundaries("Left", "Right");
         mesh.set_periodic_boundaries("Bottom", "Top");
-        dgx_dgfem::EulerDGSolver solver(mesh, order, DGX_BASIS_DUBINER, 1.4);
+        dgx_dgfem::EulerDGSolver solver(mesh, order, basis, 1.4);
         const int ne = solver.n_elements(), np = solver.n_basis();
         std::vector<Mat> u(ne, Mat(np, 4));
         for (int e = 0; e < ne; ++e)

@@ -9,14 +9,15 @@ import numpy as np
 import pytest
 
 import oracle as O
-from meshes import PERIODIC_PAIRS, isentropic_vortex, periodic_rectangle
+from meshes import PERIODIC_PAIRS, isentropic_vortex, periodic_rectangle, quad_rectangle
 
 pytestmark = pytest.mark.gpu
 ROOT = Path(__file__).resolve().parent.parent
 LIBDIR = ROOT / "discontinuous-galerkin-fem_gb300"
 
 
-def test_cpp_layer_matches_oracle(tmp_path):
+@pytest.mark.parametrize("element_type", ["triangle", "quad"])
+def test_cpp_layer_matches_oracle(tmp_path, element_type):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no GPU")
@@ -25,15 +26,17 @@ def test_cpp_layer_matches_oracle(tmp_path):
                     str(ROOT / "tests" / "cpp" / "test_dgfem_compat.cpp"), "-o", str(exe),
                     "-L", str(LIBDIR), "-ldgx", f"-Wl,-rpath,{LIBDIR}"], check=True)
     order = 3
-    v, e, b = periodic_rectangle(10)
-    om = O.OracleMesh(v, e, b, order=order, basis=O.DUBINER, periodic=PERIODIC_PAIRS)
+    quad = element_type == "quad"
+    v, e, b = quad_rectangle(8, distort=0.2) if quad else periodic_rectangle(10)
+    basis = O.LEGENDRE if quad else O.DUBINER
+    om = O.OracleMesh(v, e, b, order=order, basis=basis, periodic=PERIODIC_PAIRS)
     u = om.project(isentropic_vortex(om.quad_points(), beta=5.0, xc=0.4))
     dt = 0.05 / om.max_cfl(1.4, u, 1.0)
     v.astype(np.float64).tofile(tmp_path / "vertices.bin")
     e.astype(np.int32).tofile(tmp_path / "elements.bin")
     b.astype(np.int32).tofile(tmp_path / "bedges.bin")
     u.astype(np.float64).tofile(tmp_path / "state.bin")
-    np.array([order, dt], dtype=np.float64).tofile(tmp_path / "params.bin")
+    np.array([order, dt, e.shape[1], basis], dtype=np.float64).tofile(tmp_path / "params.bin")
     r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
 

@@ -4,7 +4,7 @@ the Euler file's fields at the lattice points."""
 import numpy as np
 import pytest
 
-from meshes import TAGS, periodic_rectangle
+from meshes import TAGS, periodic_rectangle, quad_rectangle
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
@@ -63,3 +63,22 @@ def test_eval_points_then_projection_is_identity(dg, order, basis):
     back = ctx.project(uq.contiguous())
     tol = 1e-12 if basis == "dubiner" else 1e-9  # cond(M) of the monomial basis amplifies rounding
     assert float(torch.linalg.vector_norm(back - u) / torch.linalg.vector_norm(u)) <= tol
+
+
+@pytest.mark.parametrize("order", [1, 3])
+def test_quad_linear_field_at_lattice_points(dg, tmp_path, order):
+    """On bilinear quadrilaterals a linear field lies in the tensor space Q_p (p >= 1), so the
+    projection reproduces it and the sub-quad lattice carries its exact values."""
+    v, e, b = quad_rectangle(4, 0.0, 2.0, 0.0, 1.0, distort=0.2, seed=order)
+    m = dg.DGMesh(v, e, None, dict(TAGS), {})
+    ctx = dg.DGContext(m, dg.DGSpace("quad", order), dg.EulerWeakFormulation(1.4), "fp64")
+    u = ctx.project(torch.tensor(linear(ctx.quad_points()), device="cuda"))
+    dg.VTKWriter.write_euler_solution(ctx, u, str(tmp_path / "qsol"), 1.4, 3)
+    text = (tmp_path / "qsol.vtk").read_text().splitlines()
+    npts = int(text[4].split()[1])
+    assert npts == ctx.n_elements * 16
+    xy = np.array([[float(a) for a in l.split()[:2]] for l in text[5:5 + npts]])
+    i = text.index("SCALARS rho double 1")
+    rho = np.array([float(l) for l in text[i + 2:i + 2 + npts]])
+    assert np.allclose(rho, linear(xy)[:, 0], rtol=1e-10, atol=0)
+    assert text[text.index(f"CELL_TYPES {ctx.n_elements * 9}") + 1] == "9"

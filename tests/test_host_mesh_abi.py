@@ -166,3 +166,15 @@ def test_element_type_errors(dg):
     with pytest.raises(ValueError):
         dg.DGSpace("triangle", 2, "legendre")
     assert dg.DGSpace("quad", 2).basis == 2
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+@pytest.mark.parametrize("n,nx", [(4, None), (3, 5)])
+def test_quad_rectangle_generator(dg, n, nx, periodic):
+    v, e, b = quad_rectangle(n, -5, 5, -5, 5, nx=nx)
+    pm = dg.DGMesh.rectangle(nx or n, n, -5, 5, -5, 5, periodic=periodic, element_type="quad")
+    assert np.array_equal(pm.get_vertices(), v)
+    assert np.array_equal(pm.get_elements(), e)
+    om = O.OracleMesh(v, e, b, order=1, basis=O.LEGENDRE, periodic=PERIODIC_PAIRS if periodic else ())
+    assert np.array_equal(pm.get_interior_faces(), om.interior_faces())
+    assert np.array_equal(pm.get_boundary_face_data(), om.boundary_faces())

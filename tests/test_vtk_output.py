@@ -5,7 +5,7 @@ mesh-only file (no GPU)."""
 import numpy as np
 import pytest
 
-from meshes import TAGS, periodic_rectangle
+from meshes import TAGS, periodic_rectangle, quad_rectangle
 
 
 @pytest.fixture(scope="module")
@@ -56,3 +56,22 @@ def test_euler_fields_order_and_values(dg):
     p = 0.4 * (5.0 - 0.5 * 2.0 * (0.25 + 0.0625))
     assert np.isclose(f["pressure"][0], p) and np.isclose(f["temperature"][0], p / 2.0)
     assert np.isclose(f["mach"][0], np.sqrt(0.3125) / np.sqrt(1.4 * p / 2.0))
+
+
+def test_quad_lattice_and_mesh_file(dg, tmp_path):
+    """[-1, 1]^2 lattice with j outer, i inner and counter-clockwise sub-quads
+    (vtk_writer.cpp:340-347, 394-405); VTK_QUAD = 9 cells (:475-483)."""
+    from dgfem_gb300.vtk import reference_subdivision
+    pts, quads = reference_subdivision(2, "quad")
+    assert np.allclose(pts, [(x, y) for y in (-1, 0, 1) for x in (-1, 0, 1)])
+    assert quads.tolist() == [[0, 1, 4, 3], [1, 2, 5, 4], [3, 4, 7, 6], [4, 5, 8, 7]]
+    with pytest.raises(ValueError):
+        reference_subdivision(2, "hexagon")
+    v, e, b = quad_rectangle(3, distort=0.2)
+    m = dg.DGMesh(v, e, None, dict(TAGS), {})
+    dg.VTKWriter.write_mesh(m, str(tmp_path / "qmesh"))
+    lines = (tmp_path / "qmesh.vtk").read_text().splitlines()
+    k = 5 + len(v)
+    assert lines[k] == f"CELLS {len(e)} {5 * len(e)}"
+    assert lines[k + 1] == "4 " + " ".join(str(x) for x in e[0])
+    assert set(lines[k + 2 + len(e):]) == {"9"}
