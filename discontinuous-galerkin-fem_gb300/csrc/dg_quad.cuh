@@ -265,7 +265,42 @@ __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* U
         };
         // NavierStokesWeakFormulation::compute_penalty_parameter (:275-278)
         const T sigma = VISC ? sigma0 * mu * T((P + 1) * (P + 1)) / (hF > T(1e-12) ? hF : T(1e-12)) : T(0);
-#pragma unroll 1
+        // FP32: the neighbour's traces at all of its face points in one pass over its rows,
+        // put in this face's point order (the face-point loop is then unrolled).  FP64 and
+        // double-float: one pass per point, which keeps the register count (and spills) down.
+        constexpr bool ONEPASS = is_same_type<T, float>::value;
+        constexpr int JUNROLL = ONEPASS ? NFQ : 1;
+        T Ut[ONEPASS ? NFQ : 1][4];
+#pragma unroll
+        for (int k = 0; k < (ONEPASS ? NFQ : 1); ++k)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) Ut[k][v] = T(0);
+        if (ONEPASS && nb >= 0) {
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                T c[4];
+                nrow(i, c);
+#pragma unroll
+                for (int k = 0; k < NFQ; ++k) {
+                    const T ph = o.phif[nf][k][i];
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) Ut[k][v] = mac(Ut[k][v], ph, c[v]);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < NFQ; ++k)
+#pragma unroll
+                for (int v = 0; v < NV; ++v) Ut[k][v] = settle(Ut[k][v]);
+#pragma unroll
+            for (int j = 0; j < NFQ / 2; ++j)
+#pragma unroll
+                for (int v = 0; v < NV; ++v) {
+                    const T a = Ut[j][v], b = Ut[NFQ - 1 - j][v];
+                    Ut[j][v] = rev ? b : a;
+                    Ut[NFQ - 1 - j][v] = rev ? a : b;
+                }
+        }
+#pragma unroll JUNROLL
         for (int j = 0; j < NFQ; ++j) {
             T Uo[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
@@ -274,20 +309,22 @@ __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* U
                 for (int v = 0; v < NV; ++v) Uo[v] = mac(Uo[v], o.phif[f][j][i], Ue[i * NV + v]);
 #pragma unroll
             for (int v = 0; v < NV; ++v) Uo[v] = settle(Uo[v]);
-            T Un[4] = {T(0), T(0), T(0), T(0)};
             const int k = rev ? NFQ - 1 - j : j;
-            if (nb >= 0) {
+            if (!ONEPASS && nb >= 0) {
+#pragma unroll
+                for (int v = 0; v < NV; ++v) Ut[0][v] = T(0);
 #pragma unroll
                 for (int i = 0; i < NP; ++i) {
                     T c[4];
                     nrow(i, c);
                     const T ph = o.phif[nf][k][i];
 #pragma unroll
-                    for (int v = 0; v < NV; ++v) Un[v] = mac(Un[v], ph, c[v]);
+                    for (int v = 0; v < NV; ++v) Ut[0][v] = mac(Ut[0][v], ph, c[v]);
                 }
 #pragma unroll
-                for (int v = 0; v < NV; ++v) Un[v] = settle(Un[v]);
+                for (int v = 0; v < NV; ++v) Ut[0][v] = settle(Ut[0][v]);
             }
+            const T* Un = Ut[ONEPASS ? j : 0];
             T H[4] = {T(0), T(0), T(0), T(0)};
             if (nb >= 0) {
                 rusanov<T>(Uo, Un, nx, ny, gamma, H);
@@ -420,11 +457,15 @@ __device__ __forceinline__ void quad_mass_inv_row64(const MassOps<P>& m, const Q
     quad_mass_inv_row<P, double, double>(m.phi, m.wq, m.xq, m.dinv, G, r, acc);
 }
 
+// CTAs per SM the register allocation must allow for the FP32 stage form (1: unconstrained);
+// DGX_QUAD_MIN_BLOCKS overrides it for experiments.
 #ifndef DGX_QUAD_MIN_BLOCKS
 #define DGX_QUAD_MIN_BLOCKS 1
 #endif
-template <int P, typename T, bool VISC>
-__global__ void __launch_bounds__(TILE, DGX_QUAD_MIN_BLOCKS) quad_element_kernel(const __grid_constant__ QKArgs<P, T, VISC> ka) {
+// MI64: the element mass inverse in FP64 (all modes but the FP32 form's stage increment).
+template <int P, typename T, bool VISC, bool MI64>
+__global__ void __launch_bounds__(TILE, MI64 ? 1 : DGX_QUAD_MIN_BLOCKS)
+    quad_element_kernel(const __grid_constant__ QKArgs<P, T, VISC> ka) {
     constexpr int NP = n_basis_quad(P), NB = NP * NV, STR = NB + 1;
     const StepArgs& s = ka.s;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -467,16 +508,10 @@ __global__ void __launch_bounds__(TILE, DGX_QUAD_MIN_BLOCKS) quad_element_kernel
         for (int i = 0; i < NP; ++i)
 #pragma unroll
             for (int v = 0; v < NV; ++v) sD[tl * STR + i * NV + v] = (double)R[i][v];
-        bool done = s.mode == MODE_RESIDUAL;
-        if constexpr (is_same_type<T, float>::value) {
-            if (s.mode == MODE_STAGE) {  // the FP32 form's stage increment: M_K^-1 R in FP32
-                float acc[NP][NV];
-                quad_mass_inv_row<P, float, float>(ka.o.phi, ka.o.wq, ka.o.xq, ka.o.dinv, ka.geom[e], sD + tl * STR,
-                                                   acc);
-                done = true;
-            }
-        }
-        if (!done) {
+        if constexpr (!MI64) {  // the FP32 form's stage increment: M_K^-1 R in FP32
+            T acc[NP][NV];
+            quad_mass_inv_row<P, T, T>(ka.o.phi, ka.o.wq, ka.o.xq, ka.o.dinv, ka.geom[e], sD + tl * STR, acc);
+        } else if (s.mode != MODE_RESIDUAL) {
             double acc[NP][NV];
             quad_mass_inv_row64<P>(ka.m, ka.geom[e], sD + tl * STR, acc);
         }
@@ -511,10 +546,16 @@ inline size_t quad_smem_bytes() {
 
 template <int P, typename T, bool VISC>
 inline int configure_quad_t() {
-    return cudaFuncSetAttribute(quad_element_kernel<P, T, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)quad_smem_bytes<P, T>()) == cudaSuccess
-               ? 0
-               : -1;
+    const int b = (int)quad_smem_bytes<P, T>();
+    if (cudaFuncSetAttribute(quad_element_kernel<P, T, VISC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) !=
+        cudaSuccess)
+        return -1;
+    if constexpr (is_same_type<T, float>::value) {
+        if (cudaFuncSetAttribute(quad_element_kernel<P, T, VISC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 b) != cudaSuccess)
+            return -1;
+    }
+    return 0;
 }
 
 template <int P, typename T, bool VISC>
@@ -528,7 +569,14 @@ inline int launch_quad_t(const StepArgs& a, const QuadGeom* geom, const QuadConn
     fill_mass_ops<P>(oh, ka.m);
     const int grid = (a.ne + TILE - 1) / TILE;
     if (grid == 0) return 0;
-    quad_element_kernel<P, T, VISC><<<grid, TILE, quad_smem_bytes<P, T>(), st>>>(ka);
+    bool done = false;
+    if constexpr (is_same_type<T, float>::value) {
+        if (a.mode == MODE_STAGE) {
+            quad_element_kernel<P, T, VISC, false><<<grid, TILE, quad_smem_bytes<P, T>(), st>>>(ka);
+            done = true;
+        }
+    }
+    if (!done) quad_element_kernel<P, T, VISC, true><<<grid, TILE, quad_smem_bytes<P, T>(), st>>>(ka);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
