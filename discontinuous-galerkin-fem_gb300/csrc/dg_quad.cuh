@@ -24,14 +24,16 @@
 //    src/solver/compressible_solver_base.cpp:41-61).
 //
 // T is the residual's arithmetic: double (DGX_FP64), float (DGX_MIXED) or f2 (DGX_DF64).
-// The element mass inverse runs in FP64 from FP64 tables (MassOps), except for the RK3
-// stage increment dt M_K^-1 R of the FP32 form, which runs in FP32: an increment of a
-// few percent of the state carries FP32 rounding of a few 1e-9 of the state.  The state
-// and the RK3 combination stay FP64 in every form.
+// The element kernel (residual, rhs and the FP64 / df64 RK3 stages) applies the element
+// mass inverse in FP64 from FP64 tables (MassOps).  The mixed form's RK3 runs in the
+// increment form of the triangle stage kernel (quad_stage_kernel): FP32 copies of u^n plus
+// FP32 increments as the stage state, the increment dt M_K^-1 R in FP32 (a few percent of
+// the state, so its FP32 rounding is a few 1e-9 of the state), and one FP64 add per value
+// and step into the FP64 state.
 #pragma once
 
 #include "../../include/dgx.h"
-#include "dg_physics.cuh"
+#include "dg_stage.cuh"
 
 namespace dgx {
 
@@ -161,14 +163,15 @@ __device__ __forceinline__ bool quad_boundary_state(const BCSlot& bc, const T Uo
     return false;
 }
 
-// Residual of one quadrilateral into R.  Ue: its coefficients (shared memory); sU, e0,
-// nloc: the tile, for in-tile neighbours; others are read from u (FP64) in global memory.
-template <int P, typename T, bool VISC>
+// Residual of one quadrilateral into R.  Ue: its coefficients (shared memory, rows STR
+// apart); sU, e0, nloc: the tile, for in-tile neighbours; getrow(nb, i, c) reads row i of
+// an out-of-tile neighbour from global memory.
+template <int P, typename T, bool VISC, int STR, class GetRow>
 __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* Ue, const T* sU, int e0, int nloc,
-                                              const double* u, const QuadGeom& G, const QuadConn& C,
+                                              const GetRow& getrow, const QuadGeom& G, const QuadConn& C,
                                               const BCSlot* bcs, const QuadGeom* geoms, T gamma, T mu,
                                               T kappa, T sigma0, T R[n_basis_quad(P)][NV]) {
-    constexpr int NP = n_basis_quad(P), NQ = NP, NFQ = P + 1, NB = NP * NV, STR = NB + 1;
+    constexpr int NP = n_basis_quad(P), NQ = NP, NFQ = P + 1;
 
     // ---------------- volume: EulerWeakFormulation::volume_residual (:72-115)
     //                  + NavierStokesWeakFormulation::viscous_volume_residual (:100-140)
@@ -254,13 +257,7 @@ __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* U
 #pragma unroll
                 for (int v = 0; v < NV; ++v) c[v] = Un_s[i * NV + v];
             } else {
-                const double* p = u + (size_t)nb * NB + i * NV;
-                const double2 a = __ldg(reinterpret_cast<const double2*>(p));
-                const double2 b = __ldg(reinterpret_cast<const double2*>(p + 2));
-                c[0] = (T)a.x;
-                c[1] = (T)a.y;
-                c[2] = (T)b.x;
-                c[3] = (T)b.y;
+                getrow(nb, i, c);
             }
         };
         // NavierStokesWeakFormulation::compute_penalty_parameter (:275-278)
@@ -414,17 +411,17 @@ __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* U
 
 // M_K^-1 applied to the row r (this thread's NP x 4 values, overwritten) in arithmetic A
 // from tables of type B: r <- D^-1 Phi^T diag(w_q / |J_q|) Phi D^-1 r, accumulated in acc.
-template <int P, typename A, typename B>
+template <int P, typename A, typename B, typename RT>
 __device__ __forceinline__ void quad_mass_inv_row(const B (&phi)[n_basis_quad(P)][n_basis_quad(P)],
                                                   const B (&wq)[n_basis_quad(P)], const B (&xq)[n_basis_quad(P)][2],
-                                                  const B (&dinv)[n_basis_quad(P)], const QuadGeom& G, double* r,
+                                                  const B (&dinv)[n_basis_quad(P)], const QuadGeom& G, RT* r,
                                                   A acc[n_basis_quad(P)][NV]) {
     constexpr int NP = n_basis_quad(P), NQ = NP;
 #pragma unroll
     for (int i = 0; i < NP; ++i)
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-            r[i * NV + v] = (double)((A)r[i * NV + v] * (A)dinv[i]);
+            r[i * NV + v] = (RT)((A)r[i * NV + v] * (A)dinv[i]);
             acc[i][v] = A(0);
         }
 #pragma unroll 1
@@ -448,24 +445,17 @@ __device__ __forceinline__ void quad_mass_inv_row(const B (&phi)[n_basis_quad(P)
 #pragma unroll
     for (int i = 0; i < NP; ++i)
 #pragma unroll
-        for (int v = 0; v < NV; ++v) r[i * NV + v] = (double)((A)dinv[i] * acc[i][v]);
+        for (int v = 0; v < NV; ++v) r[i * NV + v] = (RT)((A)dinv[i] * acc[i][v]);
 }
 
 template <int P>
 __device__ __forceinline__ void quad_mass_inv_row64(const MassOps<P>& m, const QuadGeom& G, double* r,
                                                     double acc[n_basis_quad(P)][NV]) {
-    quad_mass_inv_row<P, double, double>(m.phi, m.wq, m.xq, m.dinv, G, r, acc);
+    quad_mass_inv_row<P, double, double, double>(m.phi, m.wq, m.xq, m.dinv, G, r, acc);
 }
 
-// CTAs per SM the register allocation must allow for the FP32 stage form (1: unconstrained);
-// DGX_QUAD_MIN_BLOCKS overrides it for experiments.
-#ifndef DGX_QUAD_MIN_BLOCKS
-#define DGX_QUAD_MIN_BLOCKS 1
-#endif
-// MI64: the element mass inverse in FP64 (all modes but the FP32 form's stage increment).
-template <int P, typename T, bool VISC, bool MI64>
-__global__ void __launch_bounds__(TILE, MI64 ? 1 : DGX_QUAD_MIN_BLOCKS)
-    quad_element_kernel(const __grid_constant__ QKArgs<P, T, VISC> ka) {
+template <int P, typename T, bool VISC>
+__global__ void __launch_bounds__(TILE, 1) quad_element_kernel(const __grid_constant__ QKArgs<P, T, VISC> ka) {
     constexpr int NP = n_basis_quad(P), NB = NP * NV, STR = NB + 1;
     const StepArgs& s = ka.s;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -495,8 +485,10 @@ __global__ void __launch_bounds__(TILE, MI64 ? 1 : DGX_QUAD_MIN_BLOCKS)
     if (active) {
         const T mu = (T)s.mu;
         const T kappa = VISC ? (T)(s.mu * s.gamma / (s.prandtl * (s.gamma - 1.0))) : T(0);
-        quad_residual<P, T, VISC>(ka.o, sU + tl * STR, sU, e0, nloc, s.u, ka.geom[e], ka.conn[e], s.bc, ka.geom,
-                                  (T)s.gamma, mu, kappa, (T)s.sigma0, R);
+        const double* ug = s.u;
+        auto getrow = [ug](int nb, int i, T c[4]) { load_row_f64<T, NB>(ug, nb, i, c); };
+        quad_residual<P, T, VISC, STR>(ka.o, sU + tl * STR, sU, e0, nloc, getrow, ka.geom[e], ka.conn[e], s.bc,
+                                       ka.geom, (T)s.gamma, mu, kappa, (T)s.sigma0, R);
     }
     __syncthreads();  // all neighbour reads of sU are done
 
@@ -508,10 +500,7 @@ __global__ void __launch_bounds__(TILE, MI64 ? 1 : DGX_QUAD_MIN_BLOCKS)
         for (int i = 0; i < NP; ++i)
 #pragma unroll
             for (int v = 0; v < NV; ++v) sD[tl * STR + i * NV + v] = (double)R[i][v];
-        if constexpr (!MI64) {  // the FP32 form's stage increment: M_K^-1 R in FP32
-            T acc[NP][NV];
-            quad_mass_inv_row<P, T, T>(ka.o.phi, ka.o.wq, ka.o.xq, ka.o.dinv, ka.geom[e], sD + tl * STR, acc);
-        } else if (s.mode != MODE_RESIDUAL) {
+        if (s.mode != MODE_RESIDUAL) {
             double acc[NP][NV];
             quad_mass_inv_row64<P>(ka.m, ka.geom[e], sD + tl * STR, acc);
         }
@@ -546,16 +535,10 @@ inline size_t quad_smem_bytes() {
 
 template <int P, typename T, bool VISC>
 inline int configure_quad_t() {
-    const int b = (int)quad_smem_bytes<P, T>();
-    if (cudaFuncSetAttribute(quad_element_kernel<P, T, VISC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) !=
-        cudaSuccess)
-        return -1;
-    if constexpr (is_same_type<T, float>::value) {
-        if (cudaFuncSetAttribute(quad_element_kernel<P, T, VISC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 b) != cudaSuccess)
-            return -1;
-    }
-    return 0;
+    return cudaFuncSetAttribute(quad_element_kernel<P, T, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)quad_smem_bytes<P, T>()) == cudaSuccess
+               ? 0
+               : -1;
 }
 
 template <int P, typename T, bool VISC>
@@ -569,14 +552,7 @@ inline int launch_quad_t(const StepArgs& a, const QuadGeom* geom, const QuadConn
     fill_mass_ops<P>(oh, ka.m);
     const int grid = (a.ne + TILE - 1) / TILE;
     if (grid == 0) return 0;
-    bool done = false;
-    if constexpr (is_same_type<T, float>::value) {
-        if (a.mode == MODE_STAGE) {
-            quad_element_kernel<P, T, VISC, false><<<grid, TILE, quad_smem_bytes<P, T>(), st>>>(ka);
-            done = true;
-        }
-    }
-    if (!done) quad_element_kernel<P, T, VISC, true><<<grid, TILE, quad_smem_bytes<P, T>(), st>>>(ka);
+    quad_element_kernel<P, T, VISC><<<grid, TILE, quad_smem_bytes<P, T>(), st>>>(ka);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -590,5 +566,101 @@ inline int launch_quad_t(const StepArgs& a, const QuadGeom* geom, const QuadConn
     case 7: return FN<3, T, true> ARGS;              \
     default: return -1;                              \
     }
+
+// ---------------------------------------------------------------------------------
+// Mixed-precision SSP-RK3 stage on quadrilaterals, the increment form of StageArgs
+// (dgx_internal.h): the stage state is uhi + din in FP32, stages 1 and 2 write FP32
+// increments and stage 3 adds into the FP64 state (stage_combine).  No FP64 arithmetic or
+// FP64 loads in stages 1 and 2: converting FP64 neighbour rows cost the element kernel's
+// FP32 form more FP64-pipe time than its residual took FP32-pipe time.
+template <int P>
+__host__ __device__ constexpr int quad_stage_stride() {  // floats; a 16-byte row count that is odd
+    return ((n_basis_quad(P) * NV / 4) & 1) ? n_basis_quad(P) * NV : n_basis_quad(P) * NV + 4;
+}
+
+template <int P, bool VISC>
+struct QSArgs {
+    StageArgs s;
+    QuadOps<P, float> o;
+};
+
+template <int P, bool VISC>
+__global__ void __launch_bounds__(TILE, 1) quad_stage_kernel(const __grid_constant__ QSArgs<P, VISC> ka) {
+    constexpr int NP = n_basis_quad(P), NB = NP * NV, NB4 = NB / 4, STR = quad_stage_stride<P>();
+    const StageArgs& s = ka.s;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* sU = reinterpret_cast<float*>(smem_raw);  // [TILE][STR]
+    float* sDt = sU + TILE * STR;                     // [TILE] (per-instance dt; unused here)
+
+    const int e0 = blockIdx.x * TILE;
+    const int nloc = min(TILE, s.ne - e0);
+    const int tl = threadIdx.x;
+    const bool active = tl < nloc;
+    const int e = e0 + tl;
+    if (tl == 0 && s.stage == 3)  // the FP64 state is read back in the stage combination
+        prefetch_l2_bulk(s.u64 + (size_t)e0 * NB, (unsigned)(nloc * NB * sizeof(double)));
+    {   // stage state of the tile: uhi + d, 16-byte loads of one contiguous run
+        const float4* uh = reinterpret_cast<const float4*>(s.uhi + (size_t)e0 * NB);
+        const float4* dd = s.din ? reinterpret_cast<const float4*>(s.din + (size_t)e0 * NB) : nullptr;
+        for (int g = tl; g < nloc * NB4; g += TILE) {
+            float4 a = __ldg(uh + g);
+            if (dd) {
+                const float4 b = __ldg(dd + g);
+                a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w;
+            }
+            const int le = g / NB4, k = 4 * (g - le * NB4);
+            *reinterpret_cast<float4*>(sU + le * STR + k) = a;
+        }
+    }
+    __syncthreads();
+
+    float R[NP][NV];
+#pragma unroll
+    for (int i = 0; i < NP; ++i)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) R[i][v] = 0.0f;
+    if (active) {
+        const float* uhi = s.uhi;
+        const float* din = s.din;
+        auto getrow = [uhi, din](int nb, int i, float c[4]) { load_row_f32<NB>(uhi, din, nb, i, c); };
+        quad_residual<P, float, VISC, STR>(ka.o, sU + tl * STR, sU, e0, nloc, getrow, s.qgeom[e], s.qconn[e], s.bc,
+                                           s.qgeom, s.gamma, s.mu, s.kappa, s.sigma0, R);
+    }
+    __syncthreads();  // all neighbour reads of sU are done
+    if (active) {
+#pragma unroll
+        for (int i = 0; i < NP; ++i)
+            *reinterpret_cast<float4*>(sU + tl * STR + i * NV) = make_float4(R[i][0], R[i][1], R[i][2], R[i][3]);
+        float acc[NP][NV];
+        quad_mass_inv_row<P, float, float, float>(ka.o.phi, ka.o.wq, ka.o.xq, ka.o.dinv, s.qgeom[e], sU + tl * STR,
+                                                  acc);
+    }
+    __syncthreads();
+    stage_combine<NB, STR, TILE, 2>(s, sU, sDt, e0, nloc, [](int le) { return le; });
+}
+
+template <int P, bool VISC>
+inline size_t quad_stage_smem_bytes() {
+    return (size_t)(TILE * quad_stage_stride<P>() + TILE) * sizeof(float);
+}
+
+template <int P, bool VISC>
+inline int configure_quad_stage_t() {
+    return cudaFuncSetAttribute(quad_stage_kernel<P, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)quad_stage_smem_bytes<P, VISC>()) == cudaSuccess
+               ? 0
+               : -1;
+}
+
+template <int P, bool VISC>
+inline int launch_quad_stage_t(const StageArgs& a, const OpsHost& oh, cudaStream_t st) {
+    QSArgs<P, VISC> ka;
+    ka.s = a;
+    fill_quad_ops<P, float>(oh, ka.o);
+    const int grid = (a.ne + TILE - 1) / TILE;
+    if (grid == 0) return 0;
+    quad_stage_kernel<P, VISC><<<grid, TILE, quad_stage_smem_bytes<P, VISC>(), st>>>(ka);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
 
 }  // namespace dgx

@@ -921,6 +921,7 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
                  : p->precision == DGX_DF64 ? configure_element_df64(p->order, visc)
                                             : configure_element_fp64(p->order, visc);
         if (!rc && p->precision == DGX_MIXED && !visc && !quad) rc = configure_stage_tc(p->order);
+        if (!rc && p->precision == DGX_MIXED && quad) rc = configure_quad_stage(p->order, visc);
         if (rc) return fail(DGX_ERR_CUDA, "could not configure the element kernel");
     }
     auto* c = new dgx_ctx;
@@ -966,7 +967,7 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
         !alloc((void**)&c->d_bc, sizeof(BCSlot) * slots.size()) || !alloc((void**)&c->d_u1, sb) ||
         !alloc((void**)&c->d_u2, sb) || !alloc((void**)&c->d_mon, 4 * sizeof(double)) ||
         !alloc((void**)&c->d_flag, sizeof(int)) || !alloc((void**)&c->d_status, sizeof(int)) ||
-        (p->precision == DGX_MIXED && !quad &&
+        (p->precision == DGX_MIXED &&
          (!alloc((void**)&c->d_uhi[0], c->nstate * sizeof(float)) ||
           !alloc((void**)&c->d_uhi[1], c->nstate * sizeof(float)) ||
           !alloc((void**)&c->d_d1, c->nstate * sizeof(float)) ||
@@ -1070,6 +1071,8 @@ static StageArgs mixed_stage_args(const dgx_ctx* c, double* u, double dt, int sr
     a.ne = c->ne;
     a.geom = c->d_geomf;
     a.conn = c->d_conn;
+    a.qgeom = c->d_qgeom;  // quadrilaterals (the triangle records are then null)
+    a.qconn = c->d_qconn;
     a.bc = c->d_bc;
     a.dt = (float)dt;
     a.gamma = (float)c->prm.gamma;
@@ -1120,11 +1123,10 @@ extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void*
     if (!c || (c->ne && !u) || n_steps < 0) return fail(DGX_ERR_INVALID, "dgx_rk3_step: bad argument");
     if (c->ne == 0 || n_steps == 0) return DGX_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    // mixed triangles: the increment-form stage kernels.  Mixed quadrilaterals take the
-    // element kernel's three stage launches, as FP64, with FP32 residual arithmetic.
-    const bool mixed = c->prm.precision == DGX_MIXED && c->nvpe == 3;
+    const bool mixed = c->prm.precision == DGX_MIXED;
     // mixed: the FP32 copy of the caller's state, read by the first stage
     if (mixed && launch_f64_to_f32(c->nstate, u, c->d_uhi[0], s)) return fail(DGX_ERR_CUDA, "conversion launch failed");
+    if (mixed && c->stage_grid == 0 && c->nvpe == 4) c->stage_grid = (c->ne + TILE - 1) / TILE;  // one launch shape
     if (mixed && c->stage_grid == 0) {
         // launch shape of the stage kernel: timed on stage 1, which writes only scratch
         const StageArgs a = mixed_stage_args(c, u, dt, 0);

@@ -178,6 +178,8 @@ struct StageArgs {
     const float* dt_inst;  // batched solves: dt per instance, instance id in ElemGeomF::pad (else null)
     int grid;           // persistent grid size (0: one CTA per tile)
     int* status;        // device flag: bit 0 set when stage 3 produced a non-finite value
+    const QuadGeom* qgeom;  // quadrilateral meshes: their records (geom and conn are then null)
+    const QuadConn* qconn;
 };
 
 
@@ -225,6 +227,9 @@ int configure_quad_element(int p, bool viscous, int precision);
 int launch_quad_element_df64(int p, bool viscous, const StepArgs& a, const QuadGeom* geom, const QuadConn* conn,
                              const OpsHost& ops, cudaStream_t s);
 int configure_quad_element_df64(int p, bool viscous);
+// the mixed-precision increment-form stage on quadrilaterals (StageArgs::qgeom / qconn set)
+int launch_quad_stage(int p, bool viscous, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
+int configure_quad_stage(int p, bool viscous);
 int launch_quad_mass_inv(int ne, int p, const OpsHost& ops, const QuadGeom* geom, const double* in, double* out,
                          cudaStream_t s);
 int launch_quad_project(int ne, int p, const OpsHost& ops, const QuadGeom* geom, const double* uq, double* u,

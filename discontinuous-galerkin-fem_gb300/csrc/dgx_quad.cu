@@ -17,6 +17,23 @@ int launch_quad_element(int p, bool viscous, int precision, const StepArgs& a, c
     DGX_QUAD_DISPATCH(launch_quad_t, double, (a, geom, conn, ops, s))
 }
 
+#define DGX_QUAD_STAGE_DISPATCH(FN, ARGS)        \
+    switch (p * 2 + (viscous ? 1 : 0)) {         \
+    case 2: return FN<1, false> ARGS;            \
+    case 3: return FN<1, true> ARGS;             \
+    case 4: return FN<2, false> ARGS;            \
+    case 5: return FN<2, true> ARGS;             \
+    case 6: return FN<3, false> ARGS;            \
+    case 7: return FN<3, true> ARGS;             \
+    default: return -1;                          \
+    }
+
+int configure_quad_stage(int p, bool viscous) { DGX_QUAD_STAGE_DISPATCH(configure_quad_stage_t, ()) }
+
+int launch_quad_stage(int p, bool viscous, const StageArgs& a, const OpsHost& ops, cudaStream_t s) {
+    DGX_QUAD_STAGE_DISPATCH(launch_quad_stage_t, (a, ops, s))
+}
+
 // CompressibleDGSolverBase::apply_mass_inv (src/solver/compressible_solver_base.cpp:54-61)
 template <int P>
 __global__ void quad_mass_inv_kernel(const __grid_constant__ QuadOps<P, double> o, int ne, const QuadGeom* geom,
@@ -28,7 +45,7 @@ __global__ void quad_mass_inv_kernel(const __grid_constant__ QuadOps<P, double> 
     const double* a = in + (size_t)e * NP * NV;
 #pragma unroll
     for (int k = 0; k < NP * NV; ++k) r[k] = a[k];
-    quad_mass_inv_row<P, double, double>(o.phi, o.wq, o.xq, o.dinv, geom[e], r, acc);
+    quad_mass_inv_row<P, double, double, double>(o.phi, o.wq, o.xq, o.dinv, geom[e], r, acc);
     double* b = out + (size_t)e * NP * NV;
 #pragma unroll
     for (int k = 0; k < NP * NV; ++k) b[k] = r[k];
@@ -58,7 +75,7 @@ __global__ void quad_project_kernel(const __grid_constant__ QuadOps<P, double> o
             for (int v = 0; v < NV; ++v) F[i * NV + v] += s * U[q * NV + v];
         }
     }
-    quad_mass_inv_row<P, double, double>(o.phi, o.wq, o.xq, o.dinv, G, F, acc);
+    quad_mass_inv_row<P, double, double, double>(o.phi, o.wq, o.xq, o.dinv, G, F, acc);
     double* b = u + (size_t)e * NP * NV;
 #pragma unroll
     for (int k = 0; k < NP * NV; ++k) b[k] = F[k];
