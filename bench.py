@@ -39,14 +39,22 @@ N_CELLS, ORDER, BASIS = 512, 3, "dubiner"
 GAMMA, CFL, ACC_STEPS = 1.4, 0.05, 500
 # per element per RK stage, p=3, FP64 state: 3*Np*V*8 + 92 bytes of geometry/connectivity
 ALGO_BYTES_PER_ELEM_STAGE = 1052
-# what the mixed stage kernels need per element, averaged over the three stages
-# (stage 1: 400 B, stage 2: 560 B, stage 3: 1200 B; FP32 stage state, FP64 u^n)
-DESIGN_BYTES_PER_ELEM_STAGE = 720
 MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
-# dram__bytes_read.sum + dram__bytes_write.sum per element per launch of the mixed
-# element kernel, from the ncu capture summarised in profiles/element_kernel_mixed_p3.md
-NCU_TRAFFIC_BYTES_PER_ELEM = 518  # stage 2 capture (271.5 MB / 524,288 elements); its design bytes are 560
+# The two CUDA-core forms of the mixed stage (the autotuner picks one), p=3:
+#  design: bytes per element the form needs, averaged over the three stages;
+#  traffic: dram__bytes_read.sum + dram__bytes_write.sum per element of one stage-2 launch
+#           (profiles/stage_kernel_mixed_p3.md, profiles/stage_trace_kernel_p3.md).
+STAGE_FORMS = {
+    # stage 1: 400 B, stage 2: 560 B, stage 3: 1200 B (FP32 stage state, FP64 u^n)
+    "rows": {"kernel": "dgx::stage_kernel<3, Euler, no boundary> (mixed SSP-RK3 stage, neighbour rows)",
+             "design": 720, "traffic": 518,
+             "note": "ncu dram read+write of one stage-2 launch (518 B/element, its design bytes are 560)"},
+    # the rows form's bytes plus the face traces: 192 B written and 192 B read per element
+    "traces": {"kernel": "dgx::stage_trace_kernel<3, no boundary> (mixed SSP-RK3 stage, face traces)",
+               "design": 1104, "traffic": 877,
+               "note": "ncu dram read+write of one stage-2 launch (877 B/element, its design bytes are 944)"},
+}
 
 
 def vortex(xy, t=0.0, beta=5.0, xc=0.0, yc=0.0, uinf=0.5, vinf=0.0, gamma=GAMMA, period=10.0):
@@ -486,6 +494,7 @@ def main():
     clocks = clk.summary()
     t_mx = allreduce_max(t_mx, ws)
     grid, tiles, on_tc = cmx.launch_shape()
+    form = cmx.stage_form()
     # the tensor-core (3xTF32 tcgen05) form of the same stage, forced, timed the same way
     os.environ["DGX_STAGE_KERNEL"] = "tc"
     ctc = dg.DGContext(mesh, space, wf, "mixed")
@@ -545,14 +554,15 @@ def main():
     peak, peak_kind = hbm_peak()
     t_launch = t_mx / (3 * args.steps)
     achieved = ALGO_BYTES_PER_ELEM_STAGE * ne / t_launch / 1e9
+    sf = STAGE_FORMS.get(form, STAGE_FORMS["rows"])
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_kind": peak_kind,
-            "traffic": None if NCU_TRAFFIC_BYTES_PER_ELEM is None else NCU_TRAFFIC_BYTES_PER_ELEM * ne,
-            "kernel": "dgx::stage_kernel<3, Euler, no boundary> (mixed SSP-RK3 stage)",
+            "traffic": sf["traffic"] * ne,
+            "kernel": sf["kernel"],
             "algorithmic_bytes_per_launch": ALGO_BYTES_PER_ELEM_STAGE * ne, "launch_ms": t_launch * 1e3,
-            "design_bytes_per_launch": DESIGN_BYTES_PER_ELEM_STAGE * ne,
-            "achieved_design_bytes": DESIGN_BYTES_PER_ELEM_STAGE * ne / t_launch / 1e9,
-            "traffic_note": "ncu dram read+write of one stage-2 launch (518 B/element, its design bytes are 560)"}
+            "design_bytes_per_launch": sf["design"] * ne,
+            "achieved_design_bytes": sf["design"] * ne / t_launch / 1e9,
+            "traffic_note": sf["note"]}
 
     # ---- Navier-Stokes leg: Taylor-Green-type vortex, [0,2pi]^2, 256x256x2, p=4, Re=1600
     ns = None
@@ -701,7 +711,7 @@ def main():
                 "config": {"workload": f"euler_vortex_{args.cells}x{args.cells}x2_p3_dubiner", "elements": ne, "order": ORDER,
                            "dof": dof, "dt": dt, "cfl": CFL, "l2": "inputs larger than L2 (168 MB state "
                            "+ two 168 MB stage buffers per context)", "parallelism": f"replicas x{ws}"},
-                "stage_kernel": {"form": "tensor cores" if on_tc else "cuda cores", "grid": grid, "tiles": tiles,
+                "stage_kernel": {"form": form, "grid": grid, "tiles": tiles,
                                  "picked_by": "autotuner (timed on the first step)"},
                 "tensor_core_form": tensor_core,
                 "fp64": {"value": v_64, "ms_per_step": 1e3 * t_64 / k64, "steps": k64},

@@ -1,0 +1,357 @@
+// Mixed-precision SSP-RK3 Euler stage with face traces exchanged through HBM.
+//
+// The stage kernel of dg_stage.cuh forms a neighbour's trace on the shared face itself: it
+// reads the neighbour's Np coefficient rows of uhi and of the increment (2 Np 16-byte loads
+// per face) and contracts them with the neighbour-face operators, so every face trace is
+// formed twice per stage (once by each side) and the kernel waits on long chains of
+// neighbour-row loads.  Here each element writes, at the end of a stage, the traces of its
+// next stage state at the points of its three faces:
+//   tr[e][f][j][v], face f, point j (the face's own order), variable v  (3 (p+1) 4 floats),
+// and the next stage reads an element's own traces and its neighbour's (one contiguous
+// 16 (p+1)-byte block per face) instead of coefficient rows.  The traces are formed with the
+// operators and the operation order the face loop of dg_stage.cuh uses, so the two forms give
+// the same numbers bit for bit.  The traces of the state a step starts from are written by
+// trace_init_kernel; stage 3 writes those of the next step's start state (the FP32 copy of
+// u^{n+1}), so the two ping-pong buffers carry the traces from stage to stage and step to step.
+#pragma once
+
+#include "dg_stage.cuh"
+
+namespace dgx {
+
+template <int P>
+__host__ __device__ constexpr int trace_floats() { return 3 * (P + 1) * NV; }
+
+// stage_combine (dg_stage.cuh), which in addition replaces each residual slot of sR with the
+// next stage state: uhi + dout after stages 1 and 2 (what the next stage stages as uhi + din),
+// the FP32 copy of u^{n+1} after stage 3.
+template <int NB, int STR, int THREADS, int CH, typename RowOf>
+__device__ __forceinline__ void stage_combine_next(const StageArgs& s, float* sR, const float* sDt, int e0, int nloc,
+                                                   RowOf rowof) {
+    constexpr int NB4 = NB / 4;
+    const int n4 = nloc * NB4;
+    const size_t b4 = (size_t)e0 * NB4;
+    const int t = threadIdx.x;
+    bool bad = false;
+    for (int g0 = t; g0 < n4; g0 += CH * THREADS) {
+        float4 dv[CH], uh[CH];
+        double2 ua[CH], ub[CH];
+#pragma unroll
+        for (int k = 0; k < CH; ++k) {
+            const int g = g0 + k * THREADS;
+            if (g < n4) {
+                if (s.stage >= 2) dv[k] = __ldg(reinterpret_cast<const float4*>(s.din) + b4 + g);
+                if (s.stage <= 2) uh[k] = __ldg(reinterpret_cast<const float4*>(s.uhi) + b4 + g);
+                if (s.stage == 3) {
+                    ua[k] = reinterpret_cast<const double2*>(s.u64)[2 * (b4 + g)];
+                    ub[k] = reinterpret_cast<const double2*>(s.u64)[2 * (b4 + g) + 1];
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < CH; ++k) {
+            const int g = g0 + k * THREADS;
+            if (g >= n4) break;
+            const int le = g / NB4, c = 4 * (g - le * NB4);
+            const int row = rowof(le);
+            float4* slot = reinterpret_cast<float4*>(sR + row * STR + c);
+            const float4 du = *slot;
+            const float dt = s.dt_inst ? sDt[row] : s.dt;
+            if (s.stage <= 2) {
+                const float4 o = s.stage == 1
+                                     ? make_float4(dt * du.x, dt * du.y, dt * du.z, dt * du.w)
+                                     : make_float4(0.25f * (dv[k].x + dt * du.x), 0.25f * (dv[k].y + dt * du.y),
+                                                   0.25f * (dv[k].z + dt * du.z), 0.25f * (dv[k].w + dt * du.w));
+                reinterpret_cast<float4*>(s.dout)[b4 + g] = o;
+                // rounded add, never contracted with the product above: exactly uhi + din as staged
+                *slot = make_float4(__fadd_rn(uh[k].x, o.x), __fadd_rn(uh[k].y, o.y), __fadd_rn(uh[k].z, o.z),
+                                    __fadd_rn(uh[k].w, o.w));
+            } else {
+                const float d0 = (2.0f / 3.0f) * (dv[k].x + dt * du.x), d1 = (2.0f / 3.0f) * (dv[k].y + dt * du.y);
+                const float d2 = (2.0f / 3.0f) * (dv[k].z + dt * du.z), d3 = (2.0f / 3.0f) * (dv[k].w + dt * du.w);
+                const double2 ra = make_double2(ua[k].x + (double)d0, ua[k].y + (double)d1);
+                const double2 rb = make_double2(ub[k].x + (double)d2, ub[k].y + (double)d3);
+                reinterpret_cast<double2*>(s.u64)[2 * (b4 + g)] = ra;
+                reinterpret_cast<double2*>(s.u64)[2 * (b4 + g) + 1] = rb;
+                const float4 n = make_float4((float)ra.x, (float)ra.y, (float)rb.x, (float)rb.y);
+                reinterpret_cast<float4*>(s.uhi_out)[b4 + g] = n;
+                *slot = n;
+                bad |= !(isfinite(ra.x) && isfinite(ra.y) && isfinite(rb.x) && isfinite(rb.y));
+            }
+        }
+    }
+    if (bad && s.status) atomicOr(s.status, 1);
+}
+
+// traces of the coefficient row block `c` (shared memory, rows NV floats apart) on the three
+// faces, written to tr (global, trace_floats<P>() floats)
+// (one pass over the rows; each trace point still sums i = 0 .. Np-1 in order)
+template <int P>
+__device__ __forceinline__ void write_traces(const Ops<P, float>& o, const float* c, float* tr) {
+    constexpr int NP = n_basis(P), NFQ = P + 1;
+    float U[3][NFQ][4];
+#pragma unroll
+    for (int f = 0; f < 3; ++f)
+#pragma unroll
+        for (int j = 0; j < NFQ; ++j)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) U[f][j][v] = 0.0f;
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+        const float4 c4 = *reinterpret_cast<const float4*>(c + i * NV);
+        const float cc[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+        for (int f = 0; f < 3; ++f)
+#pragma unroll
+            for (int j = 0; j < NFQ; ++j) fma4(o.phif[f][j][i], cc, U[f][j]);
+    }
+#pragma unroll
+    for (int f = 0; f < 3; ++f)
+#pragma unroll
+        for (int j = 0; j < NFQ; ++j)
+            *reinterpret_cast<float4*>(tr + (f * NFQ + j) * NV) = make_float4(U[f][j][0], U[f][j][1], U[f][j][2],
+                                                                              U[f][j][3]);
+}
+
+template <int P, bool BND>
+__device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, float* sU, float* sDt, int tile) {
+    constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1, NB = NP * NV, STR = stage_stride<P>(), NB4 = NB / 4;
+    constexpr int TRF = trace_floats<P>();
+    const StageArgs& s = ka.s;
+    const Ops<P, float>& o = ka.o;
+    const LiftOps<P, float>& L = ka.l;
+
+    const int e0 = tile * TILE;
+    const int nloc = min(TILE, s.ne - e0);
+    const int tl = threadIdx.x;
+    const int el = stage_elem(tl);
+    const bool active = el < nloc;
+    const int e = e0 + el;
+    if (tl == 0 && s.stage == 3)  // the FP64 state is read back in the stage combination
+        prefetch_l2_bulk(s.u64 + (size_t)e0 * NB, (unsigned)(nloc * NB * sizeof(double)));
+    {   // stage state of the tile: uhi + d, 16-byte loads of one contiguous run
+        const float4* uh = reinterpret_cast<const float4*>(s.uhi + (size_t)e0 * NB);
+        const float4* dd = s.din ? reinterpret_cast<const float4*>(s.din + (size_t)e0 * NB) : nullptr;
+        for (int g = tl; g < nloc * NB4; g += TILE) {
+            float4 a = __ldg(uh + g);
+            if (dd) {
+                const float4 b = __ldg(dd + g);
+                a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w;
+            }
+            const int le = g / NB4, k = 4 * (g - le * NB4);
+            *reinterpret_cast<float4*>(sU + stage_row(le) * STR + k) = a;
+        }
+    }
+    __syncthreads();
+
+    float R[NP][NV];
+#pragma unroll
+    for (int i = 0; i < NP; ++i)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) R[i][v] = 0.0f;
+
+    if (active) {
+        const ElemGeomF G = s.geom[e];
+        const float A00 = G.A[0], A01 = G.A[1], A10 = G.A[2], A11 = G.A[3];
+        const float gamma = s.gamma;
+        const float* Ue = sU + tl * STR;
+        if (s.dt_inst) sDt[tl] = s.dt_inst[__float_as_int(G.pad)];
+
+        // ---------------- volume (EulerWeakFormulation::volume_residual :72-115)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            float U[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                const float4 c4 = *reinterpret_cast<const float4*>(Ue + i * NV);
+                const float c[4] = {c4.x, c4.y, c4.z, c4.w};
+                fma4(o.phi[q][i], c, U);
+            }
+            float F[4], Gf[4], u, vv, pp, ri;
+            euler_flux<float>(U, gamma - 1.0f, F, Gf, u, vv, pp, ri);
+            float Fr[4], Fs[4];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                Fr[v] = o.wq[q] * (A00 * F[v] + A10 * Gf[v]);
+                Fs[v] = o.wq[q] * (A01 * F[v] + A11 * Gf[v]);
+            }
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                fma4(L.pr[q][i], Fr, R[i]);
+                fma4(L.ps[q][i], Fs, R[i]);
+            }
+        }
+
+        // ---------------- faces (interior_face_residual :117-175, boundary_face_residual :177-250)
+        const ElemConn C = s.conn[e];
+        const float inv_j = __frcp_rn(G.detJ);
+        const float* own = s.tin + (size_t)e * TRF;
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            const int nb = C.nbr[f];
+            if (BND && nb == NBR_SKIP) continue;
+            const int fl = (C.flags >> (4 * f)) & 15;
+            const int nf = fl & 3;
+            const bool rev = (fl >> 2) & 1;
+            const float nx = G.n[f][0], ny = G.n[f][1], hF = G.h[f];
+            float Uo[NFQ][4], Un[NFQ][4];
+#pragma unroll
+            for (int j = 0; j < NFQ; ++j) {
+                const float4 t = __ldg(reinterpret_cast<const float4*>(own + (f * NFQ + j) * NV));
+                Uo[j][0] = t.x; Uo[j][1] = t.y; Uo[j][2] = t.z; Uo[j][3] = t.w;
+            }
+            BCSlot bc;
+            bc.type = -1;
+            if (!BND || nb >= 0) {
+                const float* nt = s.tin + (size_t)nb * TRF + nf * NFQ * NV;
+#pragma unroll
+                for (int k = 0; k < NFQ; ++k) {
+                    const float4 t = __ldg(reinterpret_cast<const float4*>(nt + k * NV));
+                    Un[k][0] = t.x; Un[k][1] = t.y; Un[k][2] = t.z; Un[k][3] = t.w;
+                }
+#pragma unroll
+                for (int j = 0; j < NFQ / 2; ++j)
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) {
+                        const float a = Un[j][v], b = Un[NFQ - 1 - j][v];
+                        Un[j][v] = rev ? b : a;
+                        Un[NFQ - 1 - j][v] = rev ? a : b;
+                    }
+            } else {
+                bc = s.bc[-1 - nb];
+            }
+#pragma unroll
+            for (int j = 0; j < NFQ; ++j) {
+                float H[4];
+                if (!BND || nb >= 0) {
+                    rusanov<float>(Uo[j], Un[j], nx, ny, gamma, H);
+                } else if (bc.type == DGX_BC_FAR_FIELD || bc.type == DGX_BC_SLIP_WALL ||
+                           bc.type == DGX_BC_NO_SLIP_WALL) {
+                    float Ub[4];
+                    if (bc.type == DGX_BC_FAR_FIELD) {
+#pragma unroll
+                        for (int v = 0; v < 4; ++v) Ub[v] = (float)bc.value[v];
+                    } else if (bc.type == DGX_BC_SLIP_WALL) {
+                        const float rr = __frcp_rn(Uo[j][0]);
+                        const float u = Uo[j][1] * rr, vv = Uo[j][2] * rr;
+                        const float p = (gamma - 1.f) * (Uo[j][3] - 0.5f * Uo[j][0] * (u * u + vv * vv));
+                        const float un = u * nx + vv * ny;
+                        const float W[4] = {Uo[j][0], (u - un * nx) - un * nx, (vv - un * ny) - un * ny, p};
+                        p2c<float>(W, gamma, Ub);
+                    } else {
+                        const float W[4] = {(float)bc.value[0], (float)bc.value[1], (float)bc.value[2],
+                                            (float)bc.value[3]};
+                        p2c<float>(W, gamma, Ub);
+                    }
+                    rusanov<float>(Uo[j], Ub, nx, ny, gamma, H);
+                } else {
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) H[v] = 0.f;
+                }
+                const float w = o.wf[j] * hF * 0.5f * inv_j;
+#pragma unroll
+                for (int i = 0; i < NP; ++i) fma4(-(w * L.pf[f][j][i]), H, R[i]);
+            }
+        }
+    }
+    __syncthreads();  // every read of sU is done
+    if (active) {
+#pragma unroll
+        for (int i = 0; i < NP; ++i)
+            *reinterpret_cast<float4*>(sU + tl * STR + i * NV) = make_float4(R[i][0], R[i][1], R[i][2], R[i][3]);
+    }
+    __syncthreads();
+    // stage combination; the next stage state (uhi + dout, or uhi_out after stage 3) replaces
+    // each residual slot of sU
+    stage_combine_next<NB, STR, TILE, 2>(s, sU, sDt, e0, nloc, [](int le) { return stage_row(le); });
+    __syncthreads();
+    if (active) write_traces<P>(o, sU + tl * STR, s.tout + (size_t)e * TRF);
+    __syncthreads();  // the next tile reuses sU / sDt
+}
+
+// CTAs per SM the register allocation must allow.  Measured on GB300 for p=3 (512x512x2):
+// 3 CTAs (170 registers) 0.656 ms/step; 4 CTAs (128 registers, 588 B of spills) 0.702.
+__host__ __device__ constexpr int trace_min_blocks(int p) {
+#ifdef DGX_TRACE_MIN_BLOCKS
+    return DGX_TRACE_MIN_BLOCKS + 0 * p;
+#else
+    return p <= 3 ? 3 : 2;
+#endif
+}
+
+// Persistent form, grid from the autotuner.
+template <int P, bool BND>
+__global__ void __launch_bounds__(TILE, trace_min_blocks(P))
+    stage_trace_kernel(const __grid_constant__ SArgs<P, false> ka) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* sDt = reinterpret_cast<float*>(smem_raw);
+    float* sU = sDt + TILE;
+    const int ntiles = (ka.s.ne + TILE - 1) / TILE;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) stage_trace_tile<P, BND>(ka, sU, sDt, t);
+}
+
+// The traces of the state u = uhi (+ din) a step starts from: one thread per element.
+template <int P>
+__global__ void __launch_bounds__(TILE) trace_init_kernel(const __grid_constant__ SArgs<P, false> ka) {
+    constexpr int NB = n_basis(P) * NV, STR = stage_stride<P>(), NB4 = NB / 4;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* sU = reinterpret_cast<float*>(smem_raw);
+    const StageArgs& s = ka.s;
+    const int e0 = blockIdx.x * TILE;
+    const int nloc = min(TILE, s.ne - e0);
+    const float4* uh = reinterpret_cast<const float4*>(s.uhi + (size_t)e0 * NB);
+    for (int g = threadIdx.x; g < nloc * NB4; g += TILE) {
+        const int le = g / NB4, k = 4 * (g - le * NB4);
+        *reinterpret_cast<float4*>(sU + le * STR + k) = __ldg(uh + g);
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < nloc)
+        write_traces<P>(ka.o, sU + threadIdx.x * STR, s.tout + (size_t)(e0 + threadIdx.x) * trace_floats<P>());
+}
+
+template <int P>
+inline size_t stage_trace_smem_bytes() {
+    return (size_t)(TILE + TILE * stage_stride<P>()) * sizeof(float);
+}
+
+template <int P>
+inline int configure_stage_trace_t() {
+    const int b = (int)stage_trace_smem_bytes<P>();
+    return cudaFuncSetAttribute(stage_trace_kernel<P, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
+                       cudaSuccess &&
+                   cudaFuncSetAttribute(stage_trace_kernel<P, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        b) == cudaSuccess &&
+                   cudaFuncSetAttribute(trace_init_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
+                       cudaSuccess
+               ? 0
+               : -1;
+}
+
+template <int P>
+inline int launch_stage_trace_t(const StageArgs& a, const OpsHost& oh, int grid, cudaStream_t st) {
+    SArgs<P, false> ka;
+    ka.s = a;
+    fill_ops<P, float>(oh, ka.o);
+    fill_lift<P, float>(oh, ka.l);
+    const int ntiles = (a.ne + TILE - 1) / TILE;
+    if (ntiles == 0) return 0;
+    if (grid <= 0 || grid > ntiles) grid = ntiles;
+    if (a.boundary)
+        stage_trace_kernel<P, true><<<grid, TILE, stage_trace_smem_bytes<P>(), st>>>(ka);
+    else
+        stage_trace_kernel<P, false><<<grid, TILE, stage_trace_smem_bytes<P>(), st>>>(ka);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int P>
+inline int launch_trace_init_t(const StageArgs& a, const OpsHost& oh, cudaStream_t st) {
+    SArgs<P, false> ka;
+    ka.s = a;
+    fill_ops<P, float>(oh, ka.o);
+    const int ntiles = (a.ne + TILE - 1) / TILE;
+    if (ntiles == 0) return 0;
+    trace_init_kernel<P><<<ntiles, TILE, stage_trace_smem_bytes<P>(), st>>>(ka);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace dgx

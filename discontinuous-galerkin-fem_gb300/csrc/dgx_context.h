@@ -32,6 +32,7 @@ struct dgx_ctx {
     int* d_flag = nullptr;
     int* d_status = nullptr;  // bit 0: an RK3 step produced a non-finite value (dgx_step_status)
     float* d_uhi[2] = {nullptr, nullptr};  // FP32 copies of u^n (mixed RK3), ping-ponged
+    float* d_tr[2] = {nullptr, nullptr};    // face traces of the stage states (mixed Euler, trace form)
     float* d_d1 = nullptr;                  // FP32 stage increments (mixed RK3)
     float* d_d2 = nullptr;
     int minv_diag = 0;

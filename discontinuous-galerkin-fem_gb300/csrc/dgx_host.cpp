@@ -662,6 +662,8 @@ static void free_ctx(dgx_ctx* c) {
     cudaFree(c->d_uhi[1]);
     cudaFree(c->d_d1);
     cudaFree(c->d_d2);
+    cudaFree(c->d_tr[0]);
+    cudaFree(c->d_tr[1]);
     if (c->cap) cudaStreamDestroy(c->cap);
     cudaFree(c->d_geom);
     cudaFree(c->d_geomf);
@@ -921,6 +923,7 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
                  : p->precision == DGX_DF64 ? configure_element_df64(p->order, visc)
                                             : configure_element_fp64(p->order, visc);
         if (!rc && p->precision == DGX_MIXED && !visc && !quad) rc = configure_stage_tc(p->order);
+        if (!rc && p->precision == DGX_MIXED && !visc && !quad) rc = configure_stage_trace(p->order);
         if (!rc && p->precision == DGX_MIXED && quad) rc = configure_quad_stage(p->order, visc);
         if (rc) return fail(DGX_ERR_CUDA, "could not configure the element kernel");
     }
@@ -971,7 +974,10 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
          (!alloc((void**)&c->d_uhi[0], c->nstate * sizeof(float)) ||
           !alloc((void**)&c->d_uhi[1], c->nstate * sizeof(float)) ||
           !alloc((void**)&c->d_d1, c->nstate * sizeof(float)) ||
-          !alloc((void**)&c->d_d2, c->nstate * sizeof(float))))) {
+          !alloc((void**)&c->d_d2, c->nstate * sizeof(float)))) ||
+        (p->precision == DGX_MIXED && !quad && p->physics == DGX_EULER &&
+         (!alloc((void**)&c->d_tr[0], (size_t)ne * trace_floats_per_element(p->order) * sizeof(float)) ||
+          !alloc((void**)&c->d_tr[1], (size_t)ne * trace_floats_per_element(p->order) * sizeof(float))))) {
         cudaGetLastError();
         free_ctx(c);
         return fail(DGX_ERR_CUDA, "cudaMalloc failed for the solver state");
@@ -992,6 +998,7 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
              : cudaMemcpy(c->d_geom, geom.data(), sizeof(ElemGeom) * ne, cudaMemcpyHostToDevice) == cudaSuccess &&
                    cudaMemcpy(c->d_conn, conn.data(), sizeof(ElemConn) * ne, cudaMemcpyHostToDevice) == cudaSuccess;
     if (cudaMemset(c->d_status, 0, sizeof(int)) != cudaSuccess || !geom_ok ||
+        (c->d_d1 && cudaMemset(c->d_d1, 0, c->nstate * sizeof(float)) != cudaSuccess) ||
         cudaMemcpy(c->d_bc, slots.data(), sizeof(BCSlot) * slots.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->cap, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
@@ -1002,10 +1009,10 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
     return DGX_OK;
 }
 
-extern "C" int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles, int* tensor_cores) {
+extern "C" int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles, int* form) {
     if (!c) return fail(DGX_ERR_INVALID, "null context");
-    if (grid) *grid = c->stage_grid & ~STAGE_TC;
-    if (tensor_cores) *tensor_cores = (c->stage_grid & STAGE_TC) ? 1 : 0;
+    if (grid) *grid = c->stage_grid & ~(STAGE_TC | STAGE_TRACE);
+    if (form) *form = (c->stage_grid & STAGE_TC) ? 1 : (c->stage_grid & STAGE_TRACE) ? 2 : 0;
     if (tiles) *tiles = (c->ne + TILE - 1) / TILE;
     return DGX_OK;
 }
@@ -1090,12 +1097,17 @@ static StageArgs mixed_stage_args(const dgx_ctx* c, double* u, double dt, int sr
     return a;
 }
 
+// Face-trace form: the stages of a step that starts from uhi[q] read the traces in d_tr[q],
+// d_tr[1-q], d_tr[q] and write d_tr[1-q], d_tr[q], d_tr[1-q]: the next step starts from
+// uhi[1-q] with its traces in d_tr[1-q].
 static int enqueue_rk3_mixed(dgx_ctx* c, double* u, double dt, int src, cudaStream_t s) {
     const StageArgs a = mixed_stage_args(c, u, dt, src);
     const bool visc = c->prm.physics == DGX_NAVIER_STOKES;
-    const StageArgs s1 = [&] { StageArgs t = a; t.stage = 1; t.din = nullptr; t.dout = c->d_d1; return t; }();
-    const StageArgs s2 = [&] { StageArgs t = a; t.stage = 2; t.din = c->d_d1; t.dout = c->d_d2; return t; }();
-    const StageArgs s3 = [&] { StageArgs t = a; t.stage = 3; t.din = c->d_d2; t.dout = nullptr; return t; }();
+    float* const t0 = c->d_tr[src];
+    float* const t1 = c->d_tr[1 - src];
+    const StageArgs s1 = [&] { StageArgs t = a; t.stage = 1; t.din = nullptr; t.dout = c->d_d1; t.tin = t0; t.tout = t1; return t; }();
+    const StageArgs s2 = [&] { StageArgs t = a; t.stage = 2; t.din = c->d_d1; t.dout = c->d_d2; t.tin = t1; t.tout = t0; return t; }();
+    const StageArgs s3 = [&] { StageArgs t = a; t.stage = 3; t.din = c->d_d2; t.dout = nullptr; t.tin = t0; t.tout = t1; return t; }();
     for (const StageArgs* t : {&s1, &s2, &s3})
         if (launch_stage_mixed(c->prm.order, visc, *t, c->ops, s))
             return fail(DGX_ERR_CUDA, std::string("stage kernel launch failed: ") +
@@ -1126,34 +1138,52 @@ extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void*
     const bool mixed = c->prm.precision == DGX_MIXED;
     // mixed: the FP32 copy of the caller's state, read by the first stage
     if (mixed && launch_f64_to_f32(c->nstate, u, c->d_uhi[0], s)) return fail(DGX_ERR_CUDA, "conversion launch failed");
+    // face-trace form: the traces of the state the first step starts from (uhi[0] -> d_tr[0])
+    auto init_traces = [&]() {
+        if (!c->d_tr[0]) return 0;
+        StageArgs t = mixed_stage_args(c, u, dt, 0);
+        t.tout = c->d_tr[0];
+        return launch_trace_init(c->prm.order, t, c->ops, s);
+    };
+    if (mixed && c->d_tr[0] && (c->stage_grid == 0 || (c->stage_grid & STAGE_TRACE)) && init_traces())
+        return fail(DGX_ERR_CUDA, "trace launch failed");
     if (mixed && c->stage_grid == 0 && c->nvpe == 4) c->stage_grid = (c->ne + TILE - 1) / TILE;  // one launch shape
     if (mixed && c->stage_grid == 0) {
-        // launch shape of the stage kernel: timed on stage 1, which writes only scratch
+        // launch shape and form of the stage kernel
         const StageArgs a = mixed_stage_args(c, u, dt, 0);
         const bool visc = c->prm.physics == DGX_NAVIER_STOKES;
-        // candidates: the CUDA-core kernel at each grid; the tensor-core kernel (Euler) only
+        // candidates: both CUDA-core forms (neighbour rows; face traces, Euler) at each grid;
+        // DGX_STAGE_KERNEL=rows / =trace keeps one of them.  The tensor-core kernel (Euler) only
         // when DGX_STAGE_KERNEL asks for it: =tc (alone) or =auto (timed with the others).
         // It is opt-in: at the sizes measured it is slower, and its FP32 accumulation in the
         // tensor cores leaves a larger error over long runs than the CUDA-core FMA chains.
         const int ntiles = (c->ne + TILE - 1) / TILE;
         const char* mode = std::getenv("DGX_STAGE_KERNEL");
         const bool only_tc = mode && std::strcmp(mode, "tc") == 0;
-        const bool only_cuda = !only_tc && (!mode || std::strcmp(mode, "auto") != 0);
+        const bool only_trace = mode && std::strcmp(mode, "trace") == 0;
+        const bool only_rows = mode && std::strcmp(mode, "rows") == 0;
+        const bool with_tc = only_tc || (mode && std::strcmp(mode, "auto") == 0);
         std::vector<int> cands;
-        if (!only_tc || visc) cands = grid_candidates(ntiles);
-        if (!visc && !only_cuda) {
+        const std::vector<int> grids = grid_candidates(ntiles);
+        if (visc || (!only_tc && !only_trace)) cands = grids;  // the neighbour-row form
+        if (!visc && c->d_tr[0] && !only_tc && !only_rows)
+            for (int g : grids) cands.push_back(STAGE_TRACE | g);
+        if (!visc && with_tc) {
             int sms = 152;
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
             cands.push_back(STAGE_TC | std::min(ntiles, sms * stage_tc_ctas_per_sm(c->prm.order)));
         }
         const std::string key = "stage p" + std::to_string(c->prm.order) + (visc ? " ns" : " euler") +
-                                (c->boundary ? " bnd" : "") + " ne" + std::to_string(c->ne) +
-                                (only_tc ? " tc" : only_cuda ? "" : " auto");
+                                (c->boundary ? " bnd" : "") + " ne" + std::to_string(c->ne) + " " + (mode ? mode : "");
+        // timed as stage 2 (state uhi + d1, the increment zeroed at creation), which reads the
+        // increment as stages 2 and 3 do; it writes only scratch (d2 and the traces in d_tr[1])
         int rc = tune_grid(key, cands, [&](int grid, cudaStream_t ts) {
             StageArgs t = a;
-            t.stage = 1;
-            t.din = nullptr;
-            t.dout = c->d_d1;
+            t.stage = 2;
+            t.din = c->d_d1;
+            t.dout = c->d_d2;
+            t.tin = c->d_tr[0];
+            t.tout = c->d_tr[1];
             t.grid = grid;
             return launch_stage_mixed(c->prm.order, visc, t, c->ops, ts);
         }, s, &c->stage_grid);

@@ -180,6 +180,8 @@ struct StageArgs {
     int* status;        // device flag: bit 0 set when stage 3 produced a non-finite value
     const QuadGeom* qgeom;  // quadrilateral meshes: their records (geom and conn are then null)
     const QuadConn* qconn;
+    const float* tin;   // face-trace form: traces of this stage's state (dg_stage_trace.cuh)
+    float* tout;        // face-trace form: traces of the next stage's state
 };
 
 
@@ -197,6 +199,14 @@ int launch_stage_mixed(int p, bool viscous, const StageArgs& a, const OpsHost& o
 constexpr int STAGE_TC = 1 << 30;
 int launch_stage_tc(int p, const StageArgs& a, const OpsHost& ops, int grid, cudaStream_t s);
 int configure_stage_tc(int p);
+// Face-trace form of the mixed Euler stage (dgx_kernels_trace.cu).  A StageArgs::grid with
+// STAGE_TRACE set selects it; the low bits are its grid.  launch_trace_init writes the traces
+// of uhi to tout (the state a step starts from).
+constexpr int STAGE_TRACE = 1 << 28;
+int launch_stage_trace(int p, const StageArgs& a, const OpsHost& ops, int grid, cudaStream_t s);
+int launch_trace_init(int p, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
+int configure_stage_trace(int p);
+size_t trace_floats_per_element(int p);
 int stage_tc_ctas_per_sm(int p);
 // Batched solves (dgx_batch.cu): one launch of the stage over the element ranges of
 // orders 1..MAX_P (per_order[p-1], ne = 0 for an absent order), grid <= 0: one CTA per tile.

@@ -12,6 +12,10 @@ int launch_element_mixed(int p, bool viscous, const StepArgs& a, const OpsHost& 
 
 int launch_stage_mixed(int p, bool viscous, const StageArgs& a, const OpsHost& ops, cudaStream_t s) {
     if (a.qgeom) return launch_quad_stage(p, viscous, a, ops, s);
+    if (a.grid & STAGE_TRACE) {
+        if (viscous) return -1;
+        return launch_stage_trace(p, a, ops, a.grid & ~STAGE_TRACE, s);
+    }
     if (a.grid & STAGE_TC) {
         if (viscous) return -1;
         return launch_stage_tc(p, a, ops, a.grid & ~STAGE_TC, s);

@@ -323,7 +323,14 @@ class DGContext:
         rk3_step; tensor_cores is True for the 3xTF32 tcgen05 form."""
         g, t, k = C.c_int(), C.c_int(), C.c_int()
         check(L.load().dgx_launch_shape(self._h, C.byref(g), C.byref(t), C.byref(k)))
-        return g.value, t.value, bool(k.value)
+        return g.value, t.value, k.value == 1
+
+    def stage_form(self) -> str:
+        """The mixed stage kernel's form: "rows" (neighbour coefficient rows per face),
+        "traces" (face traces through HBM) or "tensor cores"."""
+        k = C.c_int()
+        check(L.load().dgx_launch_shape(self._h, None, None, C.byref(k)))
+        return {0: "rows", 1: "tensor cores", 2: "traces"}[k.value]
 
     def quad_points(self) -> np.ndarray:
         xq = np.zeros((self.n_elements, self.n_quad, 2))

@@ -249,14 +249,16 @@ int dgx_eval_points(dgx_ctx* c, int n_points, const double* ref_xy, const double
 /* ---------------------------------------------------------------- launch shape */
 
 /* The stage kernel the autotuner picked for a mixed-precision context: its grid (CTAs;
- * each walks the 128-element tiles with a grid stride), the number of tiles, and
- * tensor_cores = 1 for the 3xTF32 tcgen05 form (Euler), 0 for the CUDA-core form.  grid is
- * 0 until the first dgx_rk3_step, which times the candidates on its stream: the CUDA-core
- * form at one CTA per tile and at 1..8 CTAs per SM.  Environment: DGX_STAGE_KERNEL=tc takes
- * the tensor-core form, =auto adds it to the timed candidates (it is opt-in: slower at the
- * sizes measured, and its long-run error is larger); DGX_AUTOTUNE=0 skips the timing (one
- * CTA per tile).  No counterpart in dgfem. */
-int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles, int* tensor_cores);
+ * each walks the 128-element tiles with a grid stride), the number of tiles, and its form:
+ * 0 = CUDA cores, neighbour coefficient rows read per face; 2 = CUDA cores, face traces
+ * exchanged through HBM (Euler); 1 = the 3xTF32 tcgen05 form (Euler).  grid is 0 until the
+ * first dgx_rk3_step, which times the candidates on its stream: both CUDA-core forms at one
+ * CTA per tile and at 1..8 CTAs per SM.  Environment: DGX_STAGE_KERNEL=rows or =trace keeps
+ * one CUDA-core form, =tc takes the tensor-core form, =auto adds it to the timed candidates
+ * (it is opt-in: slower at the sizes measured, and its long-run error is larger);
+ * DGX_AUTOTUNE=0 skips the timing (the first candidate: rows, one CTA per tile).
+ * Quadrilateral meshes have one form (grid = tiles).  No counterpart in dgfem. */
+int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles, int* form);
 
 /* ---------------------------------------------------------------- batched solves */
 
