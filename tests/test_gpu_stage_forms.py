@@ -1,0 +1,55 @@
+"""The two CUDA-core forms of the mixed-precision Euler stage, through the C ABI:
+DGX_STAGE_KERNEL=rows (neighbour coefficient rows per face) and =trace (face traces through
+HBM).  They perform the same FP32 operations in the same order, so their states agree bit
+for bit, p = 1..4, periodic and with far-field / no-slip / slip faces, over step counts that
+exercise the one-step and two-step graphs; both stay within the mixed-precision bar of the
+FP64 oracle.  Without the variable the autotuner times both and reports its choice."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from test_gpu_tensor_core import case, rel
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def dg():
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    import dgfem_gb300 as d
+    return d
+
+
+def run(dg, monkeypatch, pm, order, u0, dt, kernel, steps=(3, 2)):
+    if kernel:
+        monkeypatch.setenv("DGX_STAGE_KERNEL", kernel)
+    else:
+        monkeypatch.delenv("DGX_STAGE_KERNEL", raising=False)
+    ctx = dg.DGContext(pm, dg.DGSpace("triangle", order, "dubiner"), dg.EulerWeakFormulation(1.4), "mixed")
+    u = torch.tensor(u0, device="cuda")
+    for n in steps:
+        ctx.rk3_step(u, dt, n)
+    torch.cuda.synchronize()
+    return u.cpu().numpy(), ctx.stage_form()
+
+
+@pytest.mark.parametrize("walls", [False, True])
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_trace_form_equals_row_form(dg, monkeypatch, order, walls):
+    om, pm, u0, dt = case(dg, 9, order, walls)
+    ref = om.rk3_step(O.euler(1.4), u0, dt, 5)
+    rows, f1 = run(dg, monkeypatch, pm, order, u0, dt, "rows")
+    trace, f2 = run(dg, monkeypatch, pm, order, u0, dt, "trace")
+    assert (f1, f2) == ("rows", "traces")
+    assert np.array_equal(rows, trace)
+    assert rel(trace, ref) <= 1e-6
+
+
+def test_autotuner_reports_a_form(dg, monkeypatch):
+    om, pm, u0, dt = case(dg, 24, 3, False)  # 1152 elements, 9 tiles
+    u, form = run(dg, monkeypatch, pm, 3, u0, dt, None, steps=(1,))
+    assert form in ("rows", "traces")
+    assert rel(u, om.rk3_step(O.euler(1.4), u0, dt, 1)) <= 1e-6
