@@ -448,8 +448,8 @@ __global__ void __launch_bounds__(TILE, stage_min_blocks(P, VISC)) stage_kernel(
         for (int k = threadIdx.x; k < OPF; k += TILE) sOp[k] = src[k];
     }
     __syncthreads();
-    const int ntiles = (ka.s.ne + TILE - 1) / TILE;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) stage_tile<P, VISC, BND>(ka, sOp, sU, sDt, t);
+    const int ntiles = ka.s.ntile > 0 ? ka.s.ntile : (ka.s.ne + TILE - 1) / TILE;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) stage_tile<P, VISC, BND>(ka, sOp, sU, sDt, ka.s.tile0 + t);
 }
 
 template <int P, bool VISC>
@@ -475,7 +475,7 @@ inline int launch_stage_t(const StageArgs& a, const OpsHost& oh, cudaStream_t st
     fill_ops<P, float>(oh, ka.o);
     fill_lift<P, float>(oh, ka.l);
     fill_nbr_ops<P>(oh, ka.nb);
-    const int ntiles = (a.ne + TILE - 1) / TILE;
+    const int ntiles = a.ntile > 0 ? a.ntile : (a.ne + TILE - 1) / TILE;
     if (ntiles == 0) return 0;
     const int grid = a.grid > 0 && a.grid < ntiles ? a.grid : ntiles;
     if (a.boundary)

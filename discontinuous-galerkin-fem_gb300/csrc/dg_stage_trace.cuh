@@ -286,8 +286,8 @@ __global__ void __launch_bounds__(TILE, trace_min_blocks(P))
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* sDt = reinterpret_cast<float*>(smem_raw);
     float* sU = sDt + TILE;
-    const int ntiles = (ka.s.ne + TILE - 1) / TILE;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) stage_trace_tile<P, BND>(ka, sU, sDt, t);
+    const int ntiles = ka.s.ntile > 0 ? ka.s.ntile : (ka.s.ne + TILE - 1) / TILE;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) stage_trace_tile<P, BND>(ka, sU, sDt, ka.s.tile0 + t);
 }
 
 // The traces of the state u = uhi (+ din) a step starts from: one thread per element.
@@ -333,7 +333,7 @@ inline int launch_stage_trace_t(const StageArgs& a, const OpsHost& oh, int grid,
     ka.s = a;
     fill_ops<P, float>(oh, ka.o);
     fill_lift<P, float>(oh, ka.l);
-    const int ntiles = (a.ne + TILE - 1) / TILE;
+    const int ntiles = a.ntile > 0 ? a.ntile : (a.ne + TILE - 1) / TILE;
     if (ntiles == 0) return 0;
     if (grid <= 0 || grid > ntiles) grid = ntiles;
     if (a.boundary)

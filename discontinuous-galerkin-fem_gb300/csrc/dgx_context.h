@@ -41,6 +41,8 @@ struct dgx_ctx {
     double* d_adj[3] = {nullptr, nullptr, nullptr};  // adjoint scratch (allocated on first use)
     double* d_kin = nullptr;  // objective partial sums (allocated on first use)
     cudaStream_t cap = nullptr;  // capture stream
+    cudaStream_t host_out = nullptr;          // host-pointer step: copies back (dgx_rk3_step_host)
+    cudaEvent_t host_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaGraphExec_t graph = nullptr;   // one step (FP64) or two steps (mixed)
     cudaGraphExec_t graph1 = nullptr;  // mixed: one step
     int stage_grid = 0;  // mixed: stage-kernel grid picked by the autotuner (0: not yet)

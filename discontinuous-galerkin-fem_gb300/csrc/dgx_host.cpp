@@ -665,6 +665,9 @@ static void free_ctx(dgx_ctx* c) {
     cudaFree(c->d_tr[0]);
     cudaFree(c->d_tr[1]);
     if (c->cap) cudaStreamDestroy(c->cap);
+    if (c->host_out) cudaStreamDestroy(c->host_out);
+    for (cudaEvent_t e : c->host_ev)
+        if (e) cudaEventDestroy(e);
     cudaFree(c->d_geom);
     cudaFree(c->d_geomf);
     cudaFree(c->d_conn);
@@ -1100,18 +1103,26 @@ static StageArgs mixed_stage_args(const dgx_ctx* c, double* u, double dt, int sr
 // Face-trace form: the stages of a step that starts from uhi[q] read the traces in d_tr[q],
 // d_tr[1-q], d_tr[q] and write d_tr[1-q], d_tr[q], d_tr[1-q]: the next step starts from
 // uhi[1-q] with its traces in d_tr[1-q].
-static int enqueue_rk3_mixed(dgx_ctx* c, double* u, double dt, int src, cudaStream_t s) {
+static void mixed_step_args(const dgx_ctx* c, double* u, double dt, int src, StageArgs st[3]) {
     const StageArgs a = mixed_stage_args(c, u, dt, src);
-    const bool visc = c->prm.physics == DGX_NAVIER_STOKES;
     float* const t0 = c->d_tr[src];
     float* const t1 = c->d_tr[1 - src];
-    const StageArgs s1 = [&] { StageArgs t = a; t.stage = 1; t.din = nullptr; t.dout = c->d_d1; t.tin = t0; t.tout = t1; return t; }();
-    const StageArgs s2 = [&] { StageArgs t = a; t.stage = 2; t.din = c->d_d1; t.dout = c->d_d2; t.tin = t1; t.tout = t0; return t; }();
-    const StageArgs s3 = [&] { StageArgs t = a; t.stage = 3; t.din = c->d_d2; t.dout = nullptr; t.tin = t0; t.tout = t1; return t; }();
-    for (const StageArgs* t : {&s1, &s2, &s3})
-        if (launch_stage_mixed(c->prm.order, visc, *t, c->ops, s))
-            return fail(DGX_ERR_CUDA, std::string("stage kernel launch failed: ") +
-                                          cudaGetErrorString(cudaGetLastError()));
+    st[0] = a; st[0].stage = 1; st[0].din = nullptr;   st[0].dout = c->d_d1;  st[0].tin = t0; st[0].tout = t1;
+    st[1] = a; st[1].stage = 2; st[1].din = c->d_d1;   st[1].dout = c->d_d2;  st[1].tin = t1; st[1].tout = t0;
+    st[2] = a; st[2].stage = 3; st[2].din = c->d_d2;   st[2].dout = nullptr;  st[2].tin = t0; st[2].tout = t1;
+}
+
+static int launch_stage(const dgx_ctx* c, const StageArgs& a, cudaStream_t s) {
+    if (launch_stage_mixed(c->prm.order, c->prm.physics == DGX_NAVIER_STOKES, a, c->ops, s))
+        return fail(DGX_ERR_CUDA, std::string("stage kernel launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+    return DGX_OK;
+}
+
+static int enqueue_rk3_mixed(dgx_ctx* c, double* u, double dt, int src, cudaStream_t s) {
+    StageArgs st[3];
+    mixed_step_args(c, u, dt, src, st);
+    for (const StageArgs& t : st)
+        if (int rc = launch_stage(c, t, s)) return rc;
     return DGX_OK;
 }
 
@@ -1131,13 +1142,11 @@ static int capture(dgx_ctx* c, cudaGraphExec_t* out, const std::function<int(cud
     return DGX_OK;
 }
 
-extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void* stream) {
-    if (!c || (c->ne && !u) || n_steps < 0) return fail(DGX_ERR_INVALID, "dgx_rk3_step: bad argument");
-    if (c->ne == 0 || n_steps == 0) return DGX_OK;
-    cudaStream_t s = (cudaStream_t)stream;
-    const bool mixed = c->prm.precision == DGX_MIXED;
-    // mixed: the FP32 copy of the caller's state, read by the first stage
-    if (mixed && launch_f64_to_f32(c->nstate, u, c->d_uhi[0], s)) return fail(DGX_ERR_CUDA, "conversion launch failed");
+// Mixed precision, before the first step of a call: the FP32 copy of the caller's state
+// (read by the first stage), the face traces of that state (trace form), and the stage
+// kernel's launch shape and form (timed the first time).
+static int mixed_prologue(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
+    if (launch_f64_to_f32(c->nstate, u, c->d_uhi[0], s)) return fail(DGX_ERR_CUDA, "conversion launch failed");
     // face-trace form: the traces of the state the first step starts from (uhi[0] -> d_tr[0])
     auto init_traces = [&]() {
         if (!c->d_tr[0]) return 0;
@@ -1145,10 +1154,10 @@ extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void*
         t.tout = c->d_tr[0];
         return launch_trace_init(c->prm.order, t, c->ops, s);
     };
-    if (mixed && c->d_tr[0] && (c->stage_grid == 0 || (c->stage_grid & STAGE_TRACE)) && init_traces())
+    if (c->d_tr[0] && (c->stage_grid == 0 || (c->stage_grid & STAGE_TRACE)) && init_traces())
         return fail(DGX_ERR_CUDA, "trace launch failed");
-    if (mixed && c->stage_grid == 0 && c->nvpe == 4) c->stage_grid = (c->ne + TILE - 1) / TILE;  // one launch shape
-    if (mixed && c->stage_grid == 0) {
+    if (c->stage_grid == 0 && c->nvpe == 4) c->stage_grid = (c->ne + TILE - 1) / TILE;  // one launch shape
+    if (c->stage_grid == 0) {
         // launch shape and form of the stage kernel
         const StageArgs a = mixed_stage_args(c, u, dt, 0);
         const bool visc = c->prm.physics == DGX_NAVIER_STOKES;
@@ -1192,6 +1201,16 @@ extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void*
         if (c->graph1) cudaGraphExecDestroy(c->graph1);
         c->graph = c->graph1 = nullptr;
     }
+    return DGX_OK;
+}
+
+extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void* stream) {
+    if (!c || (c->ne && !u) || n_steps < 0) return fail(DGX_ERR_INVALID, "dgx_rk3_step: bad argument");
+    if (c->ne == 0 || n_steps == 0) return DGX_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool mixed = c->prm.precision == DGX_MIXED;
+    if (mixed)
+        if (int rc = mixed_prologue(c, u, dt, s)) return rc;
     if (!c->graph || c->graph_u != u || c->graph_dt != dt) {
         if (c->graph) cudaGraphExecDestroy(c->graph);
         if (c->graph1) cudaGraphExecDestroy(c->graph1);
@@ -1303,13 +1322,23 @@ extern "C" int dgx_eval_points(dgx_ctx* c, int n_points, const double* ref_xy, c
     return DGX_OK;
 }
 
+// The host-pointer variants run on the context's own stream and share its scratch buffers
+// with calls made on caller streams, so they first wait for all work on the device: a
+// synchronous host call is then ordered after every call made before it.
 static int ensure_host_buffers(dgx_ctx* c) {
+    CUDA_OK(cudaDeviceSynchronize());
     if (c->d_hu) return DGX_OK;
     const size_t sb = (c->nstate ? c->nstate : 1) * sizeof(double);
-    if (cudaMalloc((void**)&c->d_hu, sb) != cudaSuccess || cudaMalloc((void**)&c->d_hr, sb) != cudaSuccess) {
+    if (cudaMalloc((void**)&c->d_hu, sb) != cudaSuccess || cudaMalloc((void**)&c->d_hr, sb) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->host_out, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         return fail(DGX_ERR_CUDA, "cudaMalloc failed for host-variant buffers");
     }
+    for (cudaEvent_t& e : c->host_ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(DGX_ERR_CUDA, "cudaEventCreate failed for host-variant copies");
+        }
     return DGX_OK;
 }
 
@@ -1325,14 +1354,50 @@ extern "C" int dgx_residual_host(dgx_ctx* c, const double* u, double* r) {
     return DGX_OK;
 }
 
+// The host-pointer step is bound by the host link (about 210 GB/s in and 193 GB/s out on
+// GB300 for pinned memory, copy engines and SM copies alike).  For the CUDA-core mixed forms
+// the last step's stage 3, which writes the FP64 state, runs in HOST_CHUNKS tile ranges, and
+// each range is copied back on a second stream as soon as it is written, so the copy back
+// overlaps the rest of stage 3.
+static constexpr int HOST_CHUNKS = 4;
+
 extern "C" int dgx_rk3_step_host(dgx_ctx* c, double* u, double dt, int n_steps) {
     if (!c || (c->ne && !u) || n_steps < 0) return fail(DGX_ERR_INVALID, "dgx_rk3_step_host: bad argument");
     int rc = ensure_host_buffers(c);
     if (rc) return rc;
     const size_t sb = c->nstate * sizeof(double);
     CUDA_OK(cudaMemcpyAsync(c->d_hu, u, sb, cudaMemcpyHostToDevice, c->cap));
-    if ((rc = dgx_rk3_step(c, c->d_hu, dt, n_steps, c->cap))) return rc;
-    CUDA_OK(cudaMemcpyAsync(u, c->d_hu, sb, cudaMemcpyDeviceToHost, c->cap));
+    const bool overlap = c->prm.precision == DGX_MIXED && c->nvpe == 3 && c->ne > 0 && n_steps > 0;
+    if (!overlap) {
+        if ((rc = dgx_rk3_step(c, c->d_hu, dt, n_steps, c->cap))) return rc;
+        CUDA_OK(cudaMemcpyAsync(u, c->d_hu, sb, cudaMemcpyDeviceToHost, c->cap));
+        CUDA_OK(cudaStreamSynchronize(c->cap));
+        return DGX_OK;
+    }
+    if (n_steps > 1 && (rc = dgx_rk3_step(c, c->d_hu, dt, n_steps - 1, c->cap))) return rc;
+    if ((rc = mixed_prologue(c, c->d_hu, dt, c->cap))) return rc;
+    StageArgs st[3];
+    mixed_step_args(c, c->d_hu, dt, 0, st);
+    if ((rc = launch_stage(c, st[0], c->cap)) || (rc = launch_stage(c, st[1], c->cap))) return rc;
+    const int ntiles = (c->ne + TILE - 1) / TILE;
+    const size_t row = (size_t)c->np * NV;  // doubles per element
+    const bool chunked = !(c->stage_grid & STAGE_TC) && ntiles >= HOST_CHUNKS;
+    const int nch = chunked ? HOST_CHUNKS : 1;
+    for (int k = 0; k < nch; ++k) {
+        const int t0 = (int)((long long)ntiles * k / nch), t1 = (int)((long long)ntiles * (k + 1) / nch);
+        StageArgs a = st[2];
+        if (chunked) {
+            a.tile0 = t0;
+            a.ntile = t1 - t0;
+        }
+        if ((rc = launch_stage(c, a, c->cap))) return rc;
+        CUDA_OK(cudaEventRecord(c->host_ev[k], c->cap));
+        CUDA_OK(cudaStreamWaitEvent(c->host_out, c->host_ev[k], 0));
+        const size_t e0 = (size_t)t0 * TILE, e1 = std::min((size_t)t1 * TILE, (size_t)c->ne);
+        CUDA_OK(cudaMemcpyAsync(u + e0 * row, c->d_hu + e0 * row, (e1 - e0) * row * sizeof(double),
+                                cudaMemcpyDeviceToHost, c->host_out));
+    }
+    CUDA_OK(cudaStreamSynchronize(c->host_out));
     CUDA_OK(cudaStreamSynchronize(c->cap));
     return DGX_OK;
 }

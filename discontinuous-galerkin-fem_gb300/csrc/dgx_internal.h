@@ -182,6 +182,7 @@ struct StageArgs {
     const QuadConn* qconn;
     const float* tin;   // face-trace form: traces of this stage's state (dg_stage_trace.cuh)
     float* tout;        // face-trace form: traces of the next stage's state
+    int tile0, ntile;   // CUDA-core forms: the tiles [tile0, tile0 + ntile) only (ntile = 0: all)
 };
 
 

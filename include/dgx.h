@@ -182,10 +182,13 @@ int dgx_quad_points(const dgx_ctx* c, double* xq);
 int dgx_project(dgx_ctx* c, const double* uq, double* u, void* stream);
 
 /* ---------------------------------------------------------------- host-pointer variants */
+/* Synchronous: each first waits for all work on the device (calls made earlier on any
+ * stream), then copies in, computes and copies out on the context's own streams. */
 
 /* assemble_euler_residual on host states (copies in, computes, copies out). */
 int dgx_residual_host(dgx_ctx* c, const double* u, double* r);
-/* time_step_ssp_rk3 on a host state, in place (copies in, n_steps steps, copies out). */
+/* time_step_ssp_rk3 on a host state, in place (copies in, n_steps steps, copies out; in
+ * mixed precision on triangles the copy back overlaps the last stage, range by range). */
 int dgx_rk3_step_host(dgx_ctx* c, double* u, double dt, int n_steps);
 /* apply_mass_inv on host states (copies in, computes, copies out). */
 int dgx_apply_mass_inv_host(dgx_ctx* c, const double* in, double* out);

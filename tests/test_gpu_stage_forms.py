@@ -53,3 +53,18 @@ def test_autotuner_reports_a_form(dg, monkeypatch):
     u, form = run(dg, monkeypatch, pm, 3, u0, dt, None, steps=(1,))
     assert form in ("rows", "traces")
     assert rel(u, om.rk3_step(O.euler(1.4), u0, dt, 1)) <= 1e-6
+
+
+@pytest.mark.parametrize("walls", [False, True])
+@pytest.mark.parametrize("kernel,n", [("rows", 1), ("trace", 1), ("trace", 3)])
+def test_host_pointer_step_equals_device_step(dg, monkeypatch, kernel, n, walls):
+    """dgx_rk3_step_host runs its last step's stage 3 in tile ranges, each copied back to the
+    host while the next range computes; the state equals the device-pointer step's bit for bit."""
+    om, pm, u0, dt = case(dg, 24, 3, walls)  # 1152 elements: 9 tiles, 4 ranges
+    monkeypatch.setenv("DGX_STAGE_KERNEL", kernel)
+    ctx = dg.DGContext(pm, dg.DGSpace("triangle", 3, "dubiner"), dg.EulerWeakFormulation(1.4), "mixed")
+    u = torch.tensor(u0, device="cuda")
+    ctx.rk3_step(u, dt, n)
+    uh = ctx.rk3_step(u0, dt, n)
+    assert np.array_equal(u.cpu().numpy(), uh)
+    assert rel(uh, om.rk3_step(O.euler(1.4), u0, dt, n)) <= 1e-6
