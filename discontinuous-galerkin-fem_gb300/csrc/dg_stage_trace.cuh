@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(TILE) trace_init_kernel(const __grid_constant_
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* sU = reinterpret_cast<float*>(smem_raw);
     const StageArgs& s = ka.s;
-    const int e0 = blockIdx.x * TILE;
+    const int e0 = (s.tile0 + blockIdx.x) * TILE;
     const int nloc = min(TILE, s.ne - e0);
     const float4* uh = reinterpret_cast<const float4*>(s.uhi + (size_t)e0 * NB);
     for (int g = threadIdx.x; g < nloc * NB4; g += TILE) {
@@ -348,7 +348,7 @@ inline int launch_trace_init_t(const StageArgs& a, const OpsHost& oh, cudaStream
     SArgs<P, false> ka;
     ka.s = a;
     fill_ops<P, float>(oh, ka.o);
-    const int ntiles = (a.ne + TILE - 1) / TILE;
+    const int ntiles = a.ntile > 0 ? a.ntile : (a.ne + TILE - 1) / TILE;
     if (ntiles == 0) return 0;
     trace_init_kernel<P><<<ntiles, TILE, stage_trace_smem_bytes<P>(), st>>>(ka);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;

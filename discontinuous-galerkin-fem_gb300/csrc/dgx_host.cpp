@@ -1366,8 +1366,41 @@ extern "C" int dgx_rk3_step_host(dgx_ctx* c, double* u, double dt, int n_steps) 
     int rc = ensure_host_buffers(c);
     if (rc) return rc;
     const size_t sb = c->nstate * sizeof(double);
-    CUDA_OK(cudaMemcpyAsync(c->d_hu, u, sb, cudaMemcpyHostToDevice, c->cap));
     const bool overlap = c->prm.precision == DGX_MIXED && c->nvpe == 3 && c->ne > 0 && n_steps > 0;
+    const int ntiles = (c->ne + TILE - 1) / TILE;
+    const size_t row = (size_t)c->np * NV;  // doubles per element
+    auto tiles_of = [&](int k, int nch, int* t0, int* t1) {
+        *t0 = (int)((long long)ntiles * k / nch);
+        *t1 = (int)((long long)ntiles * (k + 1) / nch);
+    };
+    // A single mixed step on a tuned context: the state comes in range by range on the second
+    // stream, and each range is converted to FP32 (and its face traces formed) on the context
+    // stream while the next range is in flight.
+    const bool chunk_in = overlap && n_steps == 1 && c->stage_grid != 0 && !(c->stage_grid & STAGE_TC) &&
+                          ntiles >= HOST_CHUNKS;
+    if (!chunk_in) {
+        CUDA_OK(cudaMemcpyAsync(c->d_hu, u, sb, cudaMemcpyHostToDevice, c->cap));
+    } else {
+        for (int k = 0; k < HOST_CHUNKS; ++k) {
+            int t0, t1;
+            tiles_of(k, HOST_CHUNKS, &t0, &t1);
+            const size_t e0 = (size_t)t0 * TILE, e1 = std::min((size_t)t1 * TILE, (size_t)c->ne);
+            CUDA_OK(cudaMemcpyAsync(c->d_hu + e0 * row, u + e0 * row, (e1 - e0) * row * sizeof(double),
+                                    cudaMemcpyHostToDevice, c->host_out));
+            CUDA_OK(cudaEventRecord(c->host_ev[k], c->host_out));
+            CUDA_OK(cudaStreamWaitEvent(c->cap, c->host_ev[k], 0));
+            if (launch_f64_to_f32((e1 - e0) * row, c->d_hu + e0 * row, c->d_uhi[0] + e0 * row, c->cap))
+                return fail(DGX_ERR_CUDA, "conversion launch failed");
+            if (c->stage_grid & STAGE_TRACE) {
+                StageArgs t = mixed_stage_args(c, c->d_hu, dt, 0);
+                t.tout = c->d_tr[0];
+                t.tile0 = t0;
+                t.ntile = t1 - t0;
+                if (launch_trace_init(c->prm.order, t, c->ops, c->cap))
+                    return fail(DGX_ERR_CUDA, "trace launch failed");
+            }
+        }
+    }
     if (!overlap) {
         if ((rc = dgx_rk3_step(c, c->d_hu, dt, n_steps, c->cap))) return rc;
         CUDA_OK(cudaMemcpyAsync(u, c->d_hu, sb, cudaMemcpyDeviceToHost, c->cap));
@@ -1375,16 +1408,15 @@ extern "C" int dgx_rk3_step_host(dgx_ctx* c, double* u, double dt, int n_steps) 
         return DGX_OK;
     }
     if (n_steps > 1 && (rc = dgx_rk3_step(c, c->d_hu, dt, n_steps - 1, c->cap))) return rc;
-    if ((rc = mixed_prologue(c, c->d_hu, dt, c->cap))) return rc;
+    if (!chunk_in && (rc = mixed_prologue(c, c->d_hu, dt, c->cap))) return rc;
     StageArgs st[3];
     mixed_step_args(c, c->d_hu, dt, 0, st);
     if ((rc = launch_stage(c, st[0], c->cap)) || (rc = launch_stage(c, st[1], c->cap))) return rc;
-    const int ntiles = (c->ne + TILE - 1) / TILE;
-    const size_t row = (size_t)c->np * NV;  // doubles per element
     const bool chunked = !(c->stage_grid & STAGE_TC) && ntiles >= HOST_CHUNKS;
     const int nch = chunked ? HOST_CHUNKS : 1;
     for (int k = 0; k < nch; ++k) {
-        const int t0 = (int)((long long)ntiles * k / nch), t1 = (int)((long long)ntiles * (k + 1) / nch);
+        int t0, t1;
+        tiles_of(k, nch, &t0, &t1);
         StageArgs a = st[2];
         if (chunked) {
             a.tile0 = t0;
