@@ -649,9 +649,10 @@ def main():
         axq = actx.quad_points()
         for k in range(args.adj_dirs):
             # seeded random smooth direction: a few random Fourier modes per variable,
-            # projected into the DG space (unit-size perturbations of every variable).
-            # Wavenumbers start at 0: the layer varies along y only, so modes with kx >= 1
-            # alone are nearly orthogonal to dJ/du and their derivatives drown in rounding
+            # projected into the DG space and scaled to the norm of u0, so that h is a step
+            # relative to the state.  Wavenumbers start at 0: the layer varies along y only, so
+            # modes with kx >= 1 alone are nearly orthogonal to dJ/du and their derivatives
+            # drown in rounding
             field = np.zeros(axq.shape[:-1] + (4,))
             for var in range(4):
                 for _ in range(3):
@@ -660,6 +661,7 @@ def main():
                     field[..., var] += rng.standard_normal() * np.sin(2 * np.pi * kx * axq[..., 0] + ph_x) * \
                         np.cos(2 * np.pi * ky * axq[..., 1] + ph_y)
             d = actx.project(torch.tensor(field, device="cuda"))
+            d *= torch.linalg.vector_norm(au0) / torch.linalg.vector_norm(d)
             up, um = au0 + h * d, au0 - h * d
             actx.rk3_step(up, adt, na)
             actx.rk3_step(um, adt, na)
@@ -679,7 +681,8 @@ def main():
                "forward_ms_per_step": 1e3 * t_fwd / na, "gradient_s": t_grad,
                "gradient_vs_forward_solve": t_grad / t_fwd,
                "adjoint_step_vs_forward_step": (t_grad - t_fwd) / t_fwd,
-               "fd_directions": args.adj_dirs, "fd_h": h, "fd_max_rel_err": max(fd_err) if fd_err else None,
+               "fd_directions": args.adj_dirs, "fd_h": h, "fd_direction_norm": "||d|| = ||u0|| (h is a relative step)",
+               "fd_max_rel_err": max(fd_err) if fd_err else None,
                "fd_median_rel_err": float(np.median(fd_err)) if fd_err else None,
                "fd_min_abs_derivative": min(fd_abs) if fd_abs else None,
                "fd_max_err_vs_grad_norm": max(fd_cs) if fd_cs else None,
