@@ -69,14 +69,16 @@ __device__ __forceinline__ void stage_combine_next(const StageArgs& s, float* sR
             } else {
                 const float d0 = (2.0f / 3.0f) * (dv[k].x + dt * du.x), d1 = (2.0f / 3.0f) * (dv[k].y + dt * du.y);
                 const float d2 = (2.0f / 3.0f) * (dv[k].z + dt * du.z), d3 = (2.0f / 3.0f) * (dv[k].w + dt * du.w);
-                const double2 ra = make_double2(ua[k].x + (double)d0, ua[k].y + (double)d1);
-                const double2 rb = make_double2(ub[k].x + (double)d2, ub[k].y + (double)d3);
+                // one FP64 add per value; the conversions and the check run on the integer pipe
+                const double2 ra = make_double2(ua[k].x + f32_to_f64_bits(d0), ua[k].y + f32_to_f64_bits(d1));
+                const double2 rb = make_double2(ub[k].x + f32_to_f64_bits(d2), ub[k].y + f32_to_f64_bits(d3));
                 reinterpret_cast<double2*>(s.u64)[2 * (b4 + g)] = ra;
                 reinterpret_cast<double2*>(s.u64)[2 * (b4 + g) + 1] = rb;
-                const float4 n = make_float4((float)ra.x, (float)ra.y, (float)rb.x, (float)rb.y);
+                const float4 n = make_float4(f64_to_f32_bits(ra.x), f64_to_f32_bits(ra.y), f64_to_f32_bits(rb.x),
+                                            f64_to_f32_bits(rb.y));
                 reinterpret_cast<float4*>(s.uhi_out)[b4 + g] = n;
                 *slot = n;
-                bad |= !(isfinite(ra.x) && isfinite(ra.y) && isfinite(rb.x) && isfinite(rb.y));
+                bad |= !(finite_bits(ra.x) && finite_bits(ra.y) && finite_bits(rb.x) && finite_bits(rb.y));
             }
         }
     }

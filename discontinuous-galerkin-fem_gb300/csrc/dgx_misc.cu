@@ -1,6 +1,7 @@
 // FP64 utility kernels around the hot path: standalone inverse mass matrix, L2
 // projection of an initial condition, CFL / density monitors and the NaN scan.
 #include "dgx_internal.h"
+#include "fp_bits.cuh"
 
 namespace dgx {
 
@@ -154,7 +155,7 @@ __global__ void has_nan_kernel(size_t n, const double* u, int* flag) {
 
 __global__ void f64_to_f32_kernel(size_t n, const double* in, float* out) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        out[i] = (float)in[i];
+        out[i] = f64_to_f32_bits(in[i]);  // on the integer pipe (fp_bits.cuh)
 }
 
 #define DGX_DISPATCH_P(p, ...)                                      \
