@@ -405,7 +405,7 @@ __global__ void __launch_bounds__(TILE, DGX_ELEMENT_MIN_BLOCKS) element_kernel(c
 #pragma unroll
             for (int i = 0; i < NP; ++i)
 #pragma unroll
-                for (int v = 0; v < NV; ++v) sD[tl * STR + i * NV + v] = (double)R[i][v];
+                for (int v = 0; v < NV; ++v) sD[tl * STR + i * NV + v] = to_f64(R[i][v]);
         } else {
             const double ij = 1.0 / s.geom[e].detJ;
             if (s.minv_diag) {
@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(TILE, DGX_ELEMENT_MIN_BLOCKS) element_kernel(c
                 for (int i = 0; i < NP; ++i)
 #pragma unroll
                     for (int v = 0; v < NV; ++v)
-                        sD[tl * STR + i * NV + v] = ka.minv64[i][i] * (double)R[i][v] * ij;
+                        sD[tl * STR + i * NV + v] = ka.minv64[i][i] * to_f64(R[i][v]) * ij;
             } else {
 #pragma unroll
                 for (int v = 0; v < NV; ++v) {
@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(TILE, DGX_ELEMENT_MIN_BLOCKS) element_kernel(c
                     for (int i = 0; i < NP; ++i) {
                         double acc = 0.0;
 #pragma unroll
-                        for (int k = 0; k < NP; ++k) acc += ka.minv64[i][k] * (double)R[k][v];
+                        for (int k = 0; k < NP; ++k) acc += ka.minv64[i][k] * to_f64(R[k][v]);
                         col[i] = acc * ij;
                     }
 #pragma unroll

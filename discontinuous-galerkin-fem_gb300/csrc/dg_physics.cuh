@@ -4,6 +4,7 @@
 #pragma once
 
 #include "dgx_internal.h"
+#include "fp_bits.cuh"
 
 namespace dgx {
 
@@ -26,6 +27,12 @@ template <typename C, typename A, typename B>
 __device__ __forceinline__ C mac(C acc, A a, B b) { return acc + a * b; }
 template <typename C>
 __device__ __forceinline__ C settle(C x) { return x; }
+
+// the value as FP64: exact; from FP32 on the integer pipe (fp_bits.cuh)
+__device__ __forceinline__ double to_f64(double x) { return x; }
+__device__ __forceinline__ double to_f64(float x) { return f32_to_f64_bits(x); }
+template <typename T>
+__device__ __forceinline__ double to_f64(T x) { return (double)x; }
 
 // get_fluxes_and_primitive, src/weak_forms/euler_weak_formulation.cpp:27-43
 template <typename T>

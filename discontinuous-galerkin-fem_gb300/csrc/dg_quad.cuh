@@ -499,7 +499,7 @@ __global__ void __launch_bounds__(TILE, 1) quad_element_kernel(const __grid_cons
 #pragma unroll
         for (int i = 0; i < NP; ++i)
 #pragma unroll
-            for (int v = 0; v < NV; ++v) sD[tl * STR + i * NV + v] = (double)R[i][v];
+            for (int v = 0; v < NV; ++v) sD[tl * STR + i * NV + v] = to_f64(R[i][v]);
         if (s.mode != MODE_RESIDUAL) {
             double acc[NP][NV];
             quad_mass_inv_row64<P>(ka.m, ka.geom[e], sD + tl * STR, acc);
