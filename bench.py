@@ -730,7 +730,9 @@ def main():
                 "setup": setup,
                 "e2e": {"value": v_e2e, "unit": "DOF*stages/s", "h2d_bytes_per_step": dof * 8,
                         "d2h_bytes_per_step": dof * 8, "steps": ke},
-                "gpu_launches": 3 * args.steps + 1,
+                # per timed rk3_step call: the FP32 copy of u^n, the face traces of it (trace
+                # form), then three stage launches per step
+                "gpu_launches": 3 * args.steps + (2 if form == "traces" else 1),
                 "roofline": roof, "clocks": clocks, "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
     if ws > 1:
