@@ -116,8 +116,8 @@ struct QKArgs {
 };
 
 // J_T at (xi, eta): rows (dx/dxi, dy/dxi) and (dx/deta, dy/deta) (mapping.cpp:22-50)
-template <typename T>
-__device__ __forceinline__ void quad_jacobian(const QuadGeom& G, T xi, T eta, T& J00, T& J01, T& J10, T& J11) {
+template <typename T, class QG>
+__device__ __forceinline__ void quad_jacobian(const QG& G, T xi, T eta, T& J00, T& J01, T& J10, T& J11) {
     J00 = (T)G.jx[0] + (T)G.jx[2] * eta;
     J01 = (T)G.jy[0] + (T)G.jy[2] * eta;
     J10 = (T)G.jx[1] + (T)G.jx[2] * xi;
@@ -126,8 +126,8 @@ __device__ __forceinline__ void quad_jacobian(const QuadGeom& G, T xi, T eta, T&
 
 // A = inverse(J_T) (mapping.cpp:33-47): dphi/dx = A0 dphi/dxi + A1 dphi/deta,
 // dphi/dy = A2 dphi/dxi + A3 dphi/deta
-template <typename T>
-__device__ __forceinline__ void quad_inverse_map(const QuadGeom& G, T xi, T eta, T A[4]) {
+template <typename T, class QG>
+__device__ __forceinline__ void quad_inverse_map(const QG& G, T xi, T eta, T A[4]) {
     T J00, J01, J10, J11;
     quad_jacobian<T>(G, xi, eta, J00, J01, J10, J11);
     const T r = rcp_<T>(J00 * J11 - J10 * J01);
@@ -166,10 +166,10 @@ __device__ __forceinline__ bool quad_boundary_state(const BCSlot& bc, const T Uo
 // Residual of one quadrilateral into R.  Ue: its coefficients (shared memory, rows STR
 // apart); sU, e0, nloc: the tile, for in-tile neighbours; getrow(nb, i, c) reads row i of
 // an out-of-tile neighbour from global memory.
-template <int P, typename T, bool VISC, int STR, class GetRow>
+template <int P, typename T, bool VISC, int STR, class GetRow, class QG>
 __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* Ue, const T* sU, int e0, int nloc,
-                                              const GetRow& getrow, const QuadGeom& G, const QuadConn& C,
-                                              const BCSlot* bcs, const QuadGeom* geoms, T gamma, T mu,
+                                              const GetRow& getrow, const QG& G, const QuadConn& C,
+                                              const BCSlot* bcs, const QG* geoms, T gamma, T mu,
                                               T kappa, T sigma0, T R[n_basis_quad(P)][NV]) {
     constexpr int NP = n_basis_quad(P), NQ = NP, NFQ = P + 1;
 
@@ -411,10 +411,10 @@ __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* U
 
 // M_K^-1 applied to the row r (this thread's NP x 4 values, overwritten) in arithmetic A
 // from tables of type B: r <- D^-1 Phi^T diag(w_q / |J_q|) Phi D^-1 r, accumulated in acc.
-template <int P, typename A, typename B, typename RT>
+template <int P, typename A, typename B, typename RT, class QG>
 __device__ __forceinline__ void quad_mass_inv_row(const B (&phi)[n_basis_quad(P)][n_basis_quad(P)],
                                                   const B (&wq)[n_basis_quad(P)], const B (&xq)[n_basis_quad(P)][2],
-                                                  const B (&dinv)[n_basis_quad(P)], const QuadGeom& G, RT* r,
+                                                  const B (&dinv)[n_basis_quad(P)], const QG& G, RT* r,
                                                   A acc[n_basis_quad(P)][NV]) {
     constexpr int NP = n_basis_quad(P), NQ = NP;
 #pragma unroll

@@ -23,6 +23,7 @@ struct dgx_ctx {
     int nvpe = 3;                        // 4: quadrilateral mesh (d_qgeom/d_qconn replace d_geom/d_conn)
     dgx::QuadGeom* d_qgeom = nullptr;
     dgx::QuadConn* d_qconn = nullptr;
+    dgx::QuadGeomF* d_qgeomf = nullptr;  // FP32 rounding of d_qgeom (mixed precision)
     dgx::BCSlot* d_bc = nullptr;
     double* d_u1 = nullptr;
     double* d_u2 = nullptr;

@@ -673,6 +673,7 @@ static void free_ctx(dgx_ctx* c) {
     cudaFree(c->d_conn);
     cudaFree(c->d_qgeom);
     cudaFree(c->d_qconn);
+    cudaFree(c->d_qgeomf);
     cudaFree(c->d_bc);
     cudaFree(c->d_u1);
     cudaFree(c->d_u2);
@@ -985,6 +986,30 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
         free_ctx(c);
         return fail(DGX_ERR_CUDA, "cudaMalloc failed for the solver state");
     }
+    if (p->precision == DGX_MIXED && quad) {
+        std::vector<QuadGeomF> gf(ne);
+        for (int e = 0; e < ne; ++e) {
+            const QuadGeom& g = hg.qgeom[e];
+            QuadGeomF& h = gf[e];
+            std::memset(&h, 0, sizeof(h));
+            for (int k = 0; k < 3; ++k) {
+                h.jx[k] = (float)g.jx[k];
+                h.jy[k] = (float)g.jy[k];
+            }
+            for (int f = 0; f < 4; ++f) {
+                h.h[f] = (float)g.h[f];
+                h.n[f][0] = (float)g.n[f][0];
+                h.n[f][1] = (float)g.n[f][1];
+            }
+            h.hmin = (float)g.hmin;
+        }
+        if (!alloc((void**)&c->d_qgeomf, sizeof(QuadGeomF) * (ne ? ne : 1)) ||
+            (ne && cudaMemcpy(c->d_qgeomf, gf.data(), sizeof(QuadGeomF) * ne, cudaMemcpyHostToDevice) != cudaSuccess)) {
+            cudaGetLastError();
+            free_ctx(c);
+            return fail(DGX_ERR_CUDA, "device upload failed (FP32 quadrilateral geometry)");
+        }
+    }
     if (p->precision == DGX_MIXED && !quad) {
         std::vector<ElemGeomF> gf(ne);
         for (int e = 0; e < ne; ++e) gf[e] = geom_to_f32(geom[e], 0);
@@ -1081,7 +1106,7 @@ static StageArgs mixed_stage_args(const dgx_ctx* c, double* u, double dt, int sr
     a.ne = c->ne;
     a.geom = c->d_geomf;
     a.conn = c->d_conn;
-    a.qgeom = c->d_qgeom;  // quadrilaterals (the triangle records are then null)
+    a.qgeom = c->d_qgeomf;  // quadrilaterals (the triangle records are then null)
     a.qconn = c->d_qconn;
     a.bc = c->d_bc;
     a.dt = (float)dt;

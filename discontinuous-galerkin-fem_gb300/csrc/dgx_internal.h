@@ -46,6 +46,18 @@ struct alignas(64) QuadGeom {
 };
 static_assert(sizeof(QuadGeom) == 192, "QuadGeom must stay 192 B");
 
+// The same record rounded once to FP32 (96 B) for the mixed-precision stage on
+// quadrilaterals, whose arithmetic is FP32 (conversions from FP64 would use the FP64 pipe).
+struct alignas(32) QuadGeomF {
+    float jx[3];
+    float jy[3];
+    float h[4];
+    float n[4][2];
+    float hmin;
+    float pad[5];
+};
+static_assert(sizeof(QuadGeomF) == 96, "QuadGeomF must stay 96 B");
+
 // Face connectivity of a quadrilateral, ElemConn's encoding over four faces.
 struct alignas(32) QuadConn {
     int nbr[4];
@@ -178,7 +190,7 @@ struct StageArgs {
     const float* dt_inst;  // batched solves: dt per instance, instance id in ElemGeomF::pad (else null)
     int grid;           // persistent grid size (0: one CTA per tile)
     int* status;        // device flag: bit 0 set when stage 3 produced a non-finite value
-    const QuadGeom* qgeom;  // quadrilateral meshes: their records (geom and conn are then null)
+    const QuadGeomF* qgeom;  // quadrilateral meshes: their records (geom and conn are then null)
     const QuadConn* qconn;
     const float* tin;   // face-trace form: traces of this stage's state (dg_stage_trace.cuh)
     float* tout;        // face-trace form: traces of the next stage's state
