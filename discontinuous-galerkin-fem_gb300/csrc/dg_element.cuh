@@ -244,27 +244,14 @@ __device__ __forceinline__ void element_residual(const Ops<P, OT>& o, const Lift
             T H[4];
             if (nb >= 0) {
                 rusanov<T>(Uo, Un, nx, ny, gamma, H);
-            } else if (bc.type == DGX_BC_FAR_FIELD || bc.type == DGX_BC_SLIP_WALL ||
-                       bc.type == DGX_BC_NO_SLIP_WALL) {
-                T Ub[4];
-                if (bc.type == DGX_BC_FAR_FIELD) {
-#pragma unroll
-                    for (int v = 0; v < 4; ++v) Ub[v] = (T)bc.value[v];
-                } else if (bc.type == DGX_BC_SLIP_WALL) {  // reflect the normal velocity
-                    const T rr = rcp_<T>(Uo[0]);
-                    const T u = Uo[1] * rr, vv = Uo[2] * rr;
-                    const T p = (gamma - T(1)) * (Uo[3] - T(0.5) * Uo[0] * (u * u + vv * vv));
-                    const T un = u * nx + vv * ny;
-                    const T W[4] = {Uo[0], (u - un * nx) - un * nx, (vv - un * ny) - un * ny, p};
-                    p2c<T>(W, gamma, Ub);
-                } else {  // no-slip: primitive wall state
-                    const T W[4] = {(T)bc.value[0], (T)bc.value[1], (T)bc.value[2], (T)bc.value[3]};
-                    p2c<T>(W, gamma, Ub);
-                }
-                rusanov<T>(Uo, Ub, nx, ny, gamma, H);
             } else {
+                T Ub[4];
+                if (inviscid_ghost<T>(bc, Uo, nx, ny, gamma, Ub)) {
+                    rusanov<T>(Uo, Ub, nx, ny, gamma, H);
+                } else {
 #pragma unroll
-                for (int v = 0; v < 4; ++v) H[v] = T(0);
+                    for (int v = 0; v < 4; ++v) H[v] = T(0);
+                }
             }
             if (VISC) {
                 T gr[4] = {T(0), T(0), T(0), T(0)}, gs[4] = {T(0), T(0), T(0), T(0)};
@@ -327,14 +314,8 @@ __device__ __forceinline__ void element_residual(const Ops<P, OT>& o, const Lift
                         H[v] += sideL * jmp - sigma * (Un[v] - Uo[v]);
                     }
                 } else if (bc.type >= 0) {
-                    T Ub[4] = {Uo[0], Uo[1], Uo[2], Uo[3]};
-                    if (bc.type == DGX_BC_NO_SLIP_WALL) {
-                        const T W[4] = {(T)bc.value[0], (T)bc.value[1], (T)bc.value[2], (T)bc.value[3]};
-                        p2c<T>(W, gamma, Ub);
-                    } else {
-#pragma unroll
-                        for (int v = 0; v < 4; ++v) Ub[v] = (T)bc.value[v];
-                    }
+                    T Ub[4];
+                    viscous_ghost<T>(bc, gamma, Ub);
 #pragma unroll
                     for (int v = 0; v < NV; ++v) H[v] += (Fv[v] * nx + Gv[v] * ny) - sigma * (Ub[v] - Uo[v]);
                 }

@@ -115,4 +115,46 @@ __device__ __forceinline__ void p2c(const T W[4], T gamma, T U[4]) {
     U[3] = W[3] / (gamma - T(1)) + T(0.5) * W[0] * (W[1] * W[1] + W[2] * W[2]);
 }
 
+// Exterior state of a boundary face for the inviscid flux (EulerWeakFormulation::
+// boundary_face_residual, src/weak_forms/euler_weak_formulation.cpp:177-250): the far-field
+// state, the interior state with its normal velocity reflected (slip wall), or the no-slip
+// wall's primitive state.  False when the condition contributes no inviscid flux.
+template <typename T>
+__device__ __forceinline__ bool inviscid_ghost(const BCSlot& bc, const T Uo[4], T nx, T ny, T gamma, T Ub[4]) {
+    if (bc.type == DGX_BC_FAR_FIELD) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) Ub[v] = (T)bc.value[v];
+        return true;
+    }
+    if (bc.type == DGX_BC_SLIP_WALL) {
+        const T rr = rcp_<T>(Uo[0]);
+        const T u = Uo[1] * rr, vv = Uo[2] * rr;
+        const T p = (gamma - T(1)) * (Uo[3] - T(0.5) * Uo[0] * (u * u + vv * vv));
+        const T un = u * nx + vv * ny;
+        const T W[4] = {Uo[0], (u - un * nx) - un * nx, (vv - un * ny) - un * ny, p};
+        p2c<T>(W, gamma, Ub);
+        return true;
+    }
+    if (bc.type == DGX_BC_NO_SLIP_WALL) {
+        const T W[4] = {(T)bc.value[0], (T)bc.value[1], (T)bc.value[2], (T)bc.value[3]};
+        p2c<T>(W, gamma, Ub);
+        return true;
+    }
+    return false;
+}
+
+// Boundary state of the viscous penalty term (NavierStokesWeakFormulation::
+// viscous_boundary_face_residual, src/weak_forms/navier_stokes_weak_formulation.cpp:209-273):
+// the no-slip wall's primitive state in conserved form, else the condition's value as given.
+template <typename T>
+__device__ __forceinline__ void viscous_ghost(const BCSlot& bc, T gamma, T Ub[4]) {
+    if (bc.type == DGX_BC_NO_SLIP_WALL) {
+        const T W[4] = {(T)bc.value[0], (T)bc.value[1], (T)bc.value[2], (T)bc.value[3]};
+        p2c<T>(W, gamma, Ub);
+    } else {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) Ub[v] = (T)bc.value[v];
+    }
+}
+
 }  // namespace dgx

@@ -137,32 +137,6 @@ __device__ __forceinline__ void quad_inverse_map(const QG& G, T xi, T eta, T A[4
     A[3] = J00 * r;
 }
 
-// Exterior state of a boundary face (boundary_face_residual, :177-250); false when the
-// face has no condition that contributes an inviscid flux.
-template <typename T>
-__device__ __forceinline__ bool quad_boundary_state(const BCSlot& bc, const T Uo[4], T nx, T ny, T gamma, T Ub[4]) {
-    if (bc.type == DGX_BC_FAR_FIELD) {
-#pragma unroll
-        for (int v = 0; v < 4; ++v) Ub[v] = (T)bc.value[v];
-        return true;
-    }
-    if (bc.type == DGX_BC_SLIP_WALL) {  // reflect the normal velocity
-        const T rr = rcp_<T>(Uo[0]);
-        const T u = Uo[1] * rr, vv = Uo[2] * rr;
-        const T p = (gamma - T(1)) * (Uo[3] - T(0.5) * Uo[0] * (u * u + vv * vv));
-        const T un = u * nx + vv * ny;
-        const T W[4] = {Uo[0], (u - un * nx) - un * nx, (vv - un * ny) - un * ny, p};
-        p2c<T>(W, gamma, Ub);
-        return true;
-    }
-    if (bc.type == DGX_BC_NO_SLIP_WALL) {  // primitive wall state
-        const T W[4] = {(T)bc.value[0], (T)bc.value[1], (T)bc.value[2], (T)bc.value[3]};
-        p2c<T>(W, gamma, Ub);
-        return true;
-    }
-    return false;
-}
-
 // Residual of one quadrilateral into R.  Ue: its coefficients (shared memory, rows STR
 // apart); sU, e0, nloc: the tile, for in-tile neighbours; getrow(nb, i, c) reads row i of
 // an out-of-tile neighbour from global memory.
@@ -327,7 +301,7 @@ __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* U
                 rusanov<T>(Uo, Un, nx, ny, gamma, H);
             } else {
                 T Ub[4];
-                if (quad_boundary_state<T>(bc, Uo, nx, ny, gamma, Ub)) rusanov<T>(Uo, Ub, nx, ny, gamma, H);
+                if (inviscid_ghost<T>(bc, Uo, nx, ny, gamma, Ub)) rusanov<T>(Uo, Ub, nx, ny, gamma, H);
             }
             if (VISC) {
                 T gr[4] = {T(0), T(0), T(0), T(0)}, gs[4] = {T(0), T(0), T(0), T(0)};
@@ -386,14 +360,8 @@ __device__ __forceinline__ void quad_residual(const QuadOps<P, T>& o, const T* U
                         H[v] += sideL * jmp - sigma * (Un[v] - Uo[v]);
                     }
                 } else if (bc.type >= 0) {
-                    T Ub[4] = {Uo[0], Uo[1], Uo[2], Uo[3]};
-                    if (bc.type == DGX_BC_NO_SLIP_WALL) {
-                        const T W[4] = {(T)bc.value[0], (T)bc.value[1], (T)bc.value[2], (T)bc.value[3]};
-                        p2c<T>(W, gamma, Ub);
-                    } else {
-#pragma unroll
-                        for (int v = 0; v < 4; ++v) Ub[v] = (T)bc.value[v];
-                    }
+                    T Ub[4];
+                    viscous_ghost<T>(bc, gamma, Ub);
 #pragma unroll
                     for (int v = 0; v < NV; ++v) H[v] += (Fv[v] * nx + Gv[v] * ny) - sigma * (Ub[v] - Uo[v]);
                 }

@@ -344,28 +344,14 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
                 float H[4];
                 if (!BND || nb >= 0) {
                     rusanov<float>(Uo, Un[j], nx, ny, gamma, H);
-                } else if (bc.type == DGX_BC_FAR_FIELD || bc.type == DGX_BC_SLIP_WALL ||
-                           bc.type == DGX_BC_NO_SLIP_WALL) {
-                    float Ub[4];
-                    if (bc.type == DGX_BC_FAR_FIELD) {
-#pragma unroll
-                        for (int v = 0; v < 4; ++v) Ub[v] = (float)bc.value[v];
-                    } else if (bc.type == DGX_BC_SLIP_WALL) {
-                        const float rr = __frcp_rn(Uo[0]);
-                        const float u = Uo[1] * rr, vv = Uo[2] * rr;
-                        const float p = (gamma - 1.f) * (Uo[3] - 0.5f * Uo[0] * (u * u + vv * vv));
-                        const float un = u * nx + vv * ny;
-                        const float W[4] = {Uo[0], (u - un * nx) - un * nx, (vv - un * ny) - un * ny, p};
-                        p2c<float>(W, gamma, Ub);
-                    } else {
-                        const float W[4] = {(float)bc.value[0], (float)bc.value[1], (float)bc.value[2],
-                                            (float)bc.value[3]};
-                        p2c<float>(W, gamma, Ub);
-                    }
-                    rusanov<float>(Uo, Ub, nx, ny, gamma, H);
                 } else {
+                    float Ub[4];
+                    if (inviscid_ghost<float>(bc, Uo, nx, ny, gamma, Ub)) {
+                        rusanov<float>(Uo, Ub, nx, ny, gamma, H);
+                    } else {
 #pragma unroll
-                    for (int v = 0; v < 4; ++v) H[v] = 0.f;
+                        for (int v = 0; v < 4; ++v) H[v] = 0.f;
+                    }
                 }
                 if (VISC) {
                     float gx[4], gy[4], Fv[4], Gv[4];
@@ -389,15 +375,8 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
                             H[v] += sideL * jmp - sigma * (Un[j][v] - Uo[v]);
                         }
                     } else if (bc.type >= 0) {
-                        float Ub[4] = {Uo[0], Uo[1], Uo[2], Uo[3]};
-                        if (bc.type == DGX_BC_NO_SLIP_WALL) {
-                            const float W[4] = {(float)bc.value[0], (float)bc.value[1], (float)bc.value[2],
-                                                (float)bc.value[3]};
-                            p2c<float>(W, gamma, Ub);
-                        } else {
-#pragma unroll
-                            for (int v = 0; v < 4; ++v) Ub[v] = (float)bc.value[v];
-                        }
+                        float Ub[4];
+                        viscous_ghost<float>(bc, gamma, Ub);
 #pragma unroll
                         for (int v = 0; v < NV; ++v) H[v] += (Fv[v] * nx + Gv[v] * ny) - sigma * (Ub[v] - Uo[v]);
                     }

@@ -139,26 +139,8 @@ __device__ __forceinline__ void tc_face_flux(const TArgs<P>& ka, uint32_t tl, co
             rusanov<float>(Uo[j], Un[j], nx, ny, gamma, H);
         } else if (nb != NBR_SKIP) {
             const BCSlot bc = s.bc[-1 - nb];
-            if (bc.type == DGX_BC_FAR_FIELD || bc.type == DGX_BC_SLIP_WALL || bc.type == DGX_BC_NO_SLIP_WALL) {
-                float Ub[4];
-                if (bc.type == DGX_BC_FAR_FIELD) {
-#pragma unroll
-                    for (int v = 0; v < 4; ++v) Ub[v] = (float)bc.value[v];
-                } else if (bc.type == DGX_BC_SLIP_WALL) {
-                    const float* Ue = Uo[j];
-                    const float rr = __frcp_rn(Ue[0]);
-                    const float u = Ue[1] * rr, vv = Ue[2] * rr;
-                    const float p = (gamma - 1.f) * (Ue[3] - 0.5f * Ue[0] * (u * u + vv * vv));
-                    const float un = u * nx + vv * ny;
-                    const float W[4] = {Ue[0], (u - un * nx) - un * nx, (vv - un * ny) - un * ny, p};
-                    p2c<float>(W, gamma, Ub);
-                } else {
-                    const float W[4] = {(float)bc.value[0], (float)bc.value[1], (float)bc.value[2],
-                                        (float)bc.value[3]};
-                    p2c<float>(W, gamma, Ub);
-                }
-                rusanov<float>(Uo[j], Ub, nx, ny, gamma, H);
-            }
+            float Ub[4];
+            if (inviscid_ghost<float>(bc, Uo[j], nx, ny, gamma, Ub)) rusanov<float>(Uo[j], Ub, nx, ny, gamma, H);
         }
         const float w = -ka.wf[j] * hF * 0.5f * inv_j;
 #pragma unroll

@@ -227,28 +227,14 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
                 float H[4];
                 if (!BND || nb >= 0) {
                     rusanov<float>(Uo[j], Un[j], nx, ny, gamma, H);
-                } else if (bc.type == DGX_BC_FAR_FIELD || bc.type == DGX_BC_SLIP_WALL ||
-                           bc.type == DGX_BC_NO_SLIP_WALL) {
-                    float Ub[4];
-                    if (bc.type == DGX_BC_FAR_FIELD) {
-#pragma unroll
-                        for (int v = 0; v < 4; ++v) Ub[v] = (float)bc.value[v];
-                    } else if (bc.type == DGX_BC_SLIP_WALL) {
-                        const float rr = __frcp_rn(Uo[j][0]);
-                        const float u = Uo[j][1] * rr, vv = Uo[j][2] * rr;
-                        const float p = (gamma - 1.f) * (Uo[j][3] - 0.5f * Uo[j][0] * (u * u + vv * vv));
-                        const float un = u * nx + vv * ny;
-                        const float W[4] = {Uo[j][0], (u - un * nx) - un * nx, (vv - un * ny) - un * ny, p};
-                        p2c<float>(W, gamma, Ub);
-                    } else {
-                        const float W[4] = {(float)bc.value[0], (float)bc.value[1], (float)bc.value[2],
-                                            (float)bc.value[3]};
-                        p2c<float>(W, gamma, Ub);
-                    }
-                    rusanov<float>(Uo[j], Ub, nx, ny, gamma, H);
                 } else {
+                    float Ub[4];
+                    if (inviscid_ghost<float>(bc, Uo[j], nx, ny, gamma, Ub)) {
+                        rusanov<float>(Uo[j], Ub, nx, ny, gamma, H);
+                    } else {
 #pragma unroll
-                    for (int v = 0; v < 4; ++v) H[v] = 0.f;
+                        for (int v = 0; v < 4; ++v) H[v] = 0.f;
+                    }
                 }
                 const float w = o.wf[j] * hF * 0.5f * inv_j;
 #pragma unroll
