@@ -68,3 +68,37 @@ def test_host_pointer_step_equals_device_step(dg, monkeypatch, kernel, n, walls)
     uh = ctx.rk3_step(u0, dt, n)
     assert np.array_equal(u.cpu().numpy(), uh)
     assert rel(uh, om.rk3_step(O.euler(1.4), u0, dt, n)) <= 1e-6
+
+
+@pytest.mark.parametrize("n", [1, 2])
+def test_host_pointer_step_tensor_core_form(dg, monkeypatch, n):
+    """The host-pointer step with the tensor-core form (no range-wise overlap) equals the
+    device-pointer step bit for bit."""
+    om, pm, u0, dt = case(dg, 24, 3, False)
+    monkeypatch.setenv("DGX_STAGE_KERNEL", "tc")
+    ctx = dg.DGContext(pm, dg.DGSpace("triangle", 3, "dubiner"), dg.EulerWeakFormulation(1.4), "mixed")
+    u = torch.tensor(u0, device="cuda")
+    ctx.rk3_step(u, dt, n)
+    assert ctx.stage_form() == "tensor cores"
+    assert np.array_equal(u.cpu().numpy(), ctx.rk3_step(u0, dt, n))
+
+
+def test_host_pointer_step_quadrilaterals(dg):
+    """Mixed quadrilaterals take the host-pointer step without the range-wise overlap; it equals
+    the device-pointer step bit for bit."""
+    from meshes import PERIODIC_PAIRS, TAGS, quad_rectangle
+    v, e, b = quad_rectangle(12, distort=0.2)
+    edges = {}
+    for t, a, c in b:
+        edges.setdefault(int(t), []).append((int(a), int(c)))
+    pm = dg.DGMesh(v, e, None, dict(TAGS), edges)
+    pm.set_periodic_boundaries("Left", "Right")
+    pm.set_periodic_boundaries("Bottom", "Top")
+    om = O.OracleMesh(v, e, b, order=3, basis=O.LEGENDRE, periodic=PERIODIC_PAIRS)
+    from meshes import isentropic_vortex
+    u0 = om.project(isentropic_vortex(om.quad_points(), beta=5.0))
+    dt = 0.05 / om.max_cfl(1.4, u0, 1.0)
+    ctx = dg.DGContext(pm, dg.DGSpace("quad", 3), dg.EulerWeakFormulation(1.4), "mixed")
+    u = torch.tensor(u0, device="cuda")
+    ctx.rk3_step(u, dt, 3)
+    assert np.array_equal(u.cpu().numpy(), ctx.rk3_step(u0, dt, 3))
