@@ -7,9 +7,10 @@
 // neighbour-row loads.  Here each element writes, at the end of a stage, the traces of its
 // next stage state at the points of its three faces:
 //   tr[e][f][j][v], face f, point j (the face's own order), variable v  (3 (p+1) 4 floats),
-// and the next stage reads an element's own traces and its neighbour's (one contiguous
-// 16 (p+1)-byte block per face) instead of coefficient rows.  The traces are formed with the
-// operators and the operation order the face loop of dg_stage.cuh uses, so the two forms give
+// and the next stage reads its neighbour's block (16 (p+1) contiguous bytes per face) instead
+// of the neighbour's coefficient rows; its own traces it still forms from its staged
+// coefficients (measured faster than reading them back).  Every trace is formed with the
+// operators and the operation order of the face loop of dg_stage.cuh, so the two forms give
 // the same numbers bit for bit.  The traces of the state a step starts from are written by
 // trace_init_kernel; stage 3 writes those of the next step's start state (the FP32 copy of
 // u^{n+1}), so the two ping-pong buffers carry the traces from stage to stage and step to step.
@@ -187,7 +188,6 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
         // ---------------- faces (interior_face_residual :117-175, boundary_face_residual :177-250)
         const ElemConn C = s.conn[e];
         const float inv_j = __frcp_rn(G.detJ);
-        const float* own = s.tin + (size_t)e * TRF;
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
             const int nb = C.nbr[f];
@@ -197,10 +197,18 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
             const bool rev = (fl >> 2) & 1;
             const float nx = G.n[f][0], ny = G.n[f][1], hF = G.h[f];
             float Uo[NFQ][4], Un[NFQ][4];
+            // own traces from the staged coefficients: the same sums, in the same order, as the
+            // previous stage's write_traces (the neighbours read those)
 #pragma unroll
-            for (int j = 0; j < NFQ; ++j) {
-                const float4 t = __ldg(reinterpret_cast<const float4*>(own + (f * NFQ + j) * NV));
-                Uo[j][0] = t.x; Uo[j][1] = t.y; Uo[j][2] = t.z; Uo[j][3] = t.w;
+            for (int j = 0; j < NFQ; ++j)
+#pragma unroll
+                for (int v = 0; v < NV; ++v) Uo[j][v] = 0.f;
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                const float4 c4 = *reinterpret_cast<const float4*>(Ue + i * NV);
+                const float cc[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+                for (int j = 0; j < NFQ; ++j) fma4(o.phif[f][j][i], cc, Uo[j]);
             }
             BCSlot bc;
             bc.type = -1;
