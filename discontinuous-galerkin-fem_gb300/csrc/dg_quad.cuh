@@ -554,7 +554,7 @@ struct QSArgs {
 
 template <int P, bool VISC>
 __global__ void __launch_bounds__(TILE, 1) quad_stage_kernel(const __grid_constant__ QSArgs<P, VISC> ka) {
-    constexpr int NP = n_basis_quad(P), NB = NP * NV, NB4 = NB / 4, STR = quad_stage_stride<P>();
+    constexpr int NP = n_basis_quad(P), NB = NP * NV, STR = quad_stage_stride<P>();
     const StageArgs& s = ka.s;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* sU = reinterpret_cast<float*>(smem_raw);  // [TILE][STR]
@@ -567,19 +567,7 @@ __global__ void __launch_bounds__(TILE, 1) quad_stage_kernel(const __grid_consta
     const int e = e0 + tl;
     if (tl == 0 && s.stage == 3)  // the FP64 state is read back in the stage combination
         prefetch_l2_bulk(s.u64 + (size_t)e0 * NB, (unsigned)(nloc * NB * sizeof(double)));
-    {   // stage state of the tile: uhi + d, 16-byte loads of one contiguous run
-        const float4* uh = reinterpret_cast<const float4*>(s.uhi + (size_t)e0 * NB);
-        const float4* dd = s.din ? reinterpret_cast<const float4*>(s.din + (size_t)e0 * NB) : nullptr;
-        for (int g = tl; g < nloc * NB4; g += TILE) {
-            float4 a = __ldg(uh + g);
-            if (dd) {
-                const float4 b = __ldg(dd + g);
-                a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w;
-            }
-            const int le = g / NB4, k = 4 * (g - le * NB4);
-            *reinterpret_cast<float4*>(sU + le * STR + k) = a;
-        }
-    }
+    stage_load_tile<NB, STR>(s.uhi, s.din, sU, e0, nloc, [](int le) { return le; });
     __syncthreads();
 
     float R[NP][NV];

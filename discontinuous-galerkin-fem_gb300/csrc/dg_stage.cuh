@@ -147,6 +147,56 @@ __device__ __forceinline__ void prefetch_l2_bulk(const void* p, unsigned bytes) 
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(bytes) : "memory");
 }
 
+// hint: bring the 128-byte line holding p into L2
+__device__ __forceinline__ void prefetch_l2_line(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// The stage state uhi + din of the tile starting at element e0 into shared memory, element
+// le's row at row_of(le) * STR.  In a full tile a thread issues all of its 16-byte loads
+// before it uses the first, so the tile costs one memory round trip instead of one per pass.
+template <int NB, int STR, typename RowOf>
+__device__ __forceinline__ void stage_load_tile(const float* uhi, const float* din, float* sU, int e0, int nloc,
+                                                RowOf row_of) {
+    constexpr int NB4 = NB / 4;
+    const int tl = threadIdx.x;
+    const float4* uh = reinterpret_cast<const float4*>(uhi + (size_t)e0 * NB);
+    const float4* dd = din ? reinterpret_cast<const float4*>(din + (size_t)e0 * NB) : nullptr;
+    auto put = [&](int g, const float4& a) {
+        const int le = g / NB4, k = 4 * (g - le * NB4);
+        *reinterpret_cast<float4*>(sU + row_of(le) * STR + k) = a;
+    };
+    if (nloc == TILE) {
+        float4 a[NB4];
+        if (dd) {
+            float4 b[NB4];
+#pragma unroll
+            for (int r = 0; r < NB4; ++r) {
+                a[r] = __ldg(uh + tl + r * TILE);
+                b[r] = __ldg(dd + tl + r * TILE);
+            }
+#pragma unroll
+            for (int r = 0; r < NB4; ++r) {
+                a[r].x += b[r].x; a[r].y += b[r].y; a[r].z += b[r].z; a[r].w += b[r].w;
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < NB4; ++r) a[r] = __ldg(uh + tl + r * TILE);
+        }
+#pragma unroll
+        for (int r = 0; r < NB4; ++r) put(tl + r * TILE, a[r]);
+        return;
+    }
+    for (int g = tl; g < nloc * NB4; g += TILE) {
+        float4 a = __ldg(uh + g);
+        if (dd) {
+            const float4 b = __ldg(dd + g);
+            a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w;
+        }
+        put(g, a);
+    }
+}
+
 // Floats of shared memory the neighbour-face operators take (16-byte rows).
 template <int P, bool VISC>
 __host__ __device__ constexpr int stage_op_floats() {
@@ -158,7 +208,7 @@ __host__ __device__ constexpr int stage_op_floats() {
 template <int P, bool VISC, bool BND>
 __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float* sOp, float* sU, float* sDt,
                                            int tile) {
-    constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1, NB = NP * NV, STR = stage_stride<P>(), NB4 = NB / 4;
+    constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1, NB = NP * NV, STR = stage_stride<P>();
     constexpr int NFQP = NbrOps<P>::NFQP;
     const StageArgs& s = ka.s;
     const Ops<P, float>& o = ka.o;
@@ -172,19 +222,7 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
     const int e = e0 + el;
     if (tl == 0 && s.stage == 3)  // the FP64 state is read back in the stage combination
         prefetch_l2_bulk(s.u64 + (size_t)e0 * NB, (unsigned)(nloc * NB * sizeof(double)));
-    {   // stage state of the tile: uhi + d, 16-byte loads of one contiguous run
-        const float4* uh = reinterpret_cast<const float4*>(s.uhi + (size_t)e0 * NB);
-        const float4* dd = s.din ? reinterpret_cast<const float4*>(s.din + (size_t)e0 * NB) : nullptr;
-        for (int g = tl; g < nloc * NB4; g += TILE) {
-            float4 a = __ldg(uh + g);
-            if (dd) {
-                const float4 b = __ldg(dd + g);
-                a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w;
-            }
-            const int le = g / NB4, k = 4 * (g - le * NB4);
-            *reinterpret_cast<float4*>(sU + stage_row(le) * STR + k) = a;
-        }
-    }
+    stage_load_tile<NB, STR>(s.uhi, s.din, sU, e0, nloc, [](int le) { return stage_row(le); });
     __syncthreads();
 
     float R[NP][NV];

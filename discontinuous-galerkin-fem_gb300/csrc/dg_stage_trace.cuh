@@ -23,6 +23,7 @@ namespace dgx {
 template <int P>
 __host__ __device__ constexpr int trace_floats() { return 3 * (P + 1) * NV; }
 
+
 // stage_combine (dg_stage.cuh), which in addition replaces each residual slot of sR with the
 // next stage state: uhi + dout after stages 1 and 2 (what the next stage stages as uhi + din),
 // the FP32 copy of u^{n+1} after stage 3.
@@ -118,7 +119,7 @@ __device__ __forceinline__ void write_traces(const Ops<P, float>& o, const float
 
 template <int P, bool BND>
 __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, float* sU, float* sDt, int tile) {
-    constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1, NB = NP * NV, STR = stage_stride<P>(), NB4 = NB / 4;
+    constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1, NB = NP * NV, STR = stage_stride<P>();
     constexpr int TRF = trace_floats<P>();
     const StageArgs& s = ka.s;
     const Ops<P, float>& o = ka.o;
@@ -132,17 +133,21 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
     const int e = e0 + el;
     if (tl == 0 && s.stage == 3)  // the FP64 state is read back in the stage combination
         prefetch_l2_bulk(s.u64 + (size_t)e0 * NB, (unsigned)(nloc * NB * sizeof(double)));
-    {   // stage state of the tile: uhi + d, 16-byte loads of one contiguous run
-        const float4* uh = reinterpret_cast<const float4*>(s.uhi + (size_t)e0 * NB);
-        const float4* dd = s.din ? reinterpret_cast<const float4*>(s.din + (size_t)e0 * NB) : nullptr;
-        for (int g = tl; g < nloc * NB4; g += TILE) {
-            float4 a = __ldg(uh + g);
-            if (dd) {
-                const float4 b = __ldg(dd + g);
-                a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w;
-            }
-            const int le = g / NB4, k = 4 * (g - le * NB4);
-            *reinterpret_cast<float4*>(sU + stage_row(le) * STR + k) = a;
+    // the element's geometry and connectivity ride in the same round trip as the tile's state
+    ElemGeomF G;
+    ElemConn C;
+    if (active) {
+        G = s.geom[e];
+        C = s.conn[e];
+    }
+    stage_load_tile<NB, STR>(s.uhi, s.din, sU, e0, nloc, [](int le) { return stage_row(le); });
+    if (active) {  // the neighbours' trace blocks (64-byte aligned, one line each), into L2 while
+                   // the volume terms are formed
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            const int nb = C.nbr[f];
+            if (BND && nb < 0) continue;
+            prefetch_l2_line(s.tin + (size_t)nb * TRF + ((C.flags >> (4 * f)) & 3) * NFQ * NV);
         }
     }
     __syncthreads();
@@ -154,7 +159,6 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
         for (int v = 0; v < NV; ++v) R[i][v] = 0.0f;
 
     if (active) {
-        const ElemGeomF G = s.geom[e];
         const float A00 = G.A[0], A01 = G.A[1], A10 = G.A[2], A11 = G.A[3];
         const float gamma = s.gamma;
         const float* Ue = sU + tl * STR;
@@ -186,7 +190,6 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
         }
 
         // ---------------- faces (interior_face_residual :117-175, boundary_face_residual :177-250)
-        const ElemConn C = s.conn[e];
         const float inv_j = __frcp_rn(G.detJ);
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
