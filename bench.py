@@ -52,8 +52,8 @@ STAGE_FORMS = {
              "note": "ncu dram read+write of one stage-2 launch (518 B/element, its design bytes are 560)"},
     # the rows form's bytes plus the face traces: 192 B written and 192 B read per element
     "traces": {"kernel": "dgx::stage_trace_kernel<3, no boundary> (mixed SSP-RK3 stage, face traces)",
-               "design": 1104, "traffic": 877,
-               "note": "ncu dram read+write of one stage-2 launch (877 B/element, its design bytes are 944)"},
+               "design": 1104, "traffic": 881,
+               "note": "ncu dram read+write of one stage-2 launch (881 B/element, its design bytes are 944)"},
 }
 
 
@@ -147,7 +147,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -402,7 +402,7 @@ def quad_leg(dg, torch, cells, steps, order=3):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="dgx", choices=["dgx", "reference"])
     ap.add_argument("--seed", type=int, default=0)

@@ -3,23 +3,37 @@
 // the arithmetic type (double for the FP64 path, float for the mixed path).
 #pragma once
 
+#include "../../include/dgx.h"
 #include "dgx_internal.h"
 #include "fp_bits.cuh"
 
 namespace dgx {
 
+// Reciprocal and square root.  FP64: correctly rounded (the oracle's arithmetic).  FP32 (the
+// mixed path): the hardware approximations rcp.approx.f32 / sqrt.approx.f32 (about one ulp,
+// bounded in tests/cpp/test_fast_math.cu) instead of the correctly rounded sequences, whose
+// extra refinement steps and slow-path branches cost 6 % of the stage; the 500-step error of
+// the mixed path against FP64 stays 4.68e-7 either way (512x512x2 vortex, p=3).
 template <typename T>
 __device__ __forceinline__ T rcp_(T x);
 template <>
 __device__ __forceinline__ double rcp_<double>(double x) { return 1.0 / x; }
 template <>
-__device__ __forceinline__ float rcp_<float>(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ float rcp_<float>(float x) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 template <typename T>
 __device__ __forceinline__ T sqrt_(T x);
 template <>
 __device__ __forceinline__ double sqrt_<double>(double x) { return sqrt(x); }
 template <>
-__device__ __forceinline__ float sqrt_<float>(float x) { return __fsqrt_rn(x); }
+__device__ __forceinline__ float sqrt_<float>(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 
 // acc + a*b (one FMA for float / double); settle(x): x with its representation normalised.
 // Types with their own fused form (double-float) provide overloads.
