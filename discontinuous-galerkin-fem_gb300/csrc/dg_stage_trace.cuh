@@ -87,11 +87,16 @@ __device__ __forceinline__ void stage_combine_next(const StageArgs& s, float* sR
     if (bad && s.status) atomicOr(s.status, 1);
 }
 
-// traces of the coefficient row block `c` (shared memory, rows NV floats apart) on the three
-// faces, written to tr (global, trace_floats<P>() floats)
-// (one pass over the rows; each trace point still sums i = 0 .. Np-1 in order)
-template <int P>
-__device__ __forceinline__ void write_traces(const Ops<P, float>& o, const float* c, float* tr) {
+// traces of the coefficient row block `c` (shared memory, rows NV floats apart) of element e
+// on the three faces, written to tr (global, trace_floats<P>() floats)
+// (one pass over the rows; each trace point still sums i = 0 .. Np-1 in order).  With ghost
+// blocks (s.ghost_bc set, s.conn the trace-form connectivity) a boundary face's block gets the
+// ghost state of each trace point (boundary_face_residual's, from the same trace value and
+// the same operations as the boundary path of the face loop), so the next stage treats the
+// face as an interior one.  GHOST = false leaves the ghost code out.
+template <int P, bool GHOST>
+__device__ __forceinline__ void write_traces(const Ops<P, float>& o, const float* c, float* tr, const StageArgs& s,
+                                             int e) {
     constexpr int NP = n_basis(P), NFQ = P + 1;
     float U[3][NFQ][4];
 #pragma unroll
@@ -115,9 +120,25 @@ __device__ __forceinline__ void write_traces(const Ops<P, float>& o, const float
         for (int j = 0; j < NFQ; ++j)
             *reinterpret_cast<float4*>(tr + (f * NFQ + j) * NV) = make_float4(U[f][j][0], U[f][j][1], U[f][j][2],
                                                                               U[f][j][3]);
+    if (GHOST && s.ghost_bc) {
+        const ElemConn C = s.conn[e];
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            if (C.nbr[f] < s.ne) continue;
+            const BCSlot bc = s.bc[s.ghost_bc[C.nbr[f] - s.ne]];
+            const float nx = s.geom[e].n[f][0], ny = s.geom[e].n[f][1];
+            float* g = s.tout + (size_t)C.nbr[f] * trace_floats<P>();
+#pragma unroll
+            for (int j = 0; j < NFQ; ++j) {
+                float Ub[4];
+                inviscid_ghost<float>(bc, U[f][j], nx, ny, s.gamma, Ub);
+                *reinterpret_cast<float4*>(g + j * NV) = make_float4(Ub[0], Ub[1], Ub[2], Ub[3]);
+            }
+        }
+    }
 }
 
-template <int P, bool BND>
+template <int P, bool BND, bool GHOST>
 __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, float* sU, float* sDt, int tile) {
     constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1, NB = NP * NV, STR = stage_stride<P>();
     constexpr int TRF = trace_floats<P>();
@@ -134,10 +155,11 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
     if (tl == 0 && s.stage == 3)  // the FP64 state is read back in the stage combination
         prefetch_l2_bulk(s.u64 + (size_t)e0 * NB, (unsigned)(nloc * NB * sizeof(double)));
     // the element's geometry and connectivity ride in the same round trip as the tile's state
+    // (the boundary variant, short of registers, loads the geometry after staging)
     ElemGeomF G;
     ElemConn C;
     if (active) {
-        G = s.geom[e];
+        if (!BND) G = s.geom[e];
         C = s.conn[e];
     }
     stage_load_tile<NB, STR>(s.uhi, s.din, sU, e0, nloc, [](int le) { return stage_row(le); });
@@ -159,6 +181,7 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
         for (int v = 0; v < NV; ++v) R[i][v] = 0.0f;
 
     if (active) {
+        if (BND) G = s.geom[e];
         const float A00 = G.A[0], A01 = G.A[1], A10 = G.A[2], A11 = G.A[3];
         const float gamma = s.gamma;
         const float* Ue = sU + tl * STR;
@@ -264,29 +287,32 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
     // each residual slot of sU
     stage_combine_next<NB, STR, TILE, 2>(s, sU, sDt, e0, nloc, [](int le) { return stage_row(le); });
     __syncthreads();
-    if (active) write_traces<P>(o, sU + tl * STR, s.tout + (size_t)e * TRF);
+    if (active) write_traces<P, GHOST>(o, sU + tl * STR, s.tout + (size_t)e * TRF, s, e);
     __syncthreads();  // the next tile reuses sU / sDt
 }
 
 // CTAs per SM the register allocation must allow.  Measured on GB300 for p=3 (512x512x2):
-// 3 CTAs (170 registers) 0.656 ms/step; 4 CTAs (128 registers, 588 B of spills) 0.702.
-__host__ __device__ constexpr int trace_min_blocks(int p) {
+// 3 CTAs (168 registers) 0.527 ms/step, 4 CTAs (128 registers, 588 B of spills) slower; with
+// boundary faces (far field and slip walls) 2 CTAs (255 registers) 0.743 ms/step against 0.769
+// for 3 CTAs (580 B of spills).
+__host__ __device__ constexpr int trace_min_blocks(int p, bool bnd) {
 #ifdef DGX_TRACE_MIN_BLOCKS
-    return DGX_TRACE_MIN_BLOCKS + 0 * p;
+    return DGX_TRACE_MIN_BLOCKS + 0 * p + 0 * bnd;
 #else
-    return p <= 3 ? 3 : 2;
+    return (p <= 3 && !bnd) ? 3 : 2;
 #endif
 }
 
-// Persistent form, grid from the autotuner.
-template <int P, bool BND>
-__global__ void __launch_bounds__(TILE, trace_min_blocks(P))
+// Persistent form, grid from the autotuner.  BND: some faces are boundary or skipped faces
+// (handled in the face loop); GHOST: boundary faces read ghost blocks, which this kernel writes.
+template <int P, bool BND, bool GHOST>
+__global__ void __launch_bounds__(TILE, trace_min_blocks(P, BND))
     stage_trace_kernel(const __grid_constant__ SArgs<P, false> ka) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* sDt = reinterpret_cast<float*>(smem_raw);
     float* sU = sDt + TILE;
     const int ntiles = ka.s.ntile > 0 ? ka.s.ntile : (ka.s.ne + TILE - 1) / TILE;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) stage_trace_tile<P, BND>(ka, sU, sDt, ka.s.tile0 + t);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) stage_trace_tile<P, BND, GHOST>(ka, sU, sDt, ka.s.tile0 + t);
 }
 
 // The traces of the state u = uhi (+ din) a step starts from: one thread per element.
@@ -305,7 +331,8 @@ __global__ void __launch_bounds__(TILE) trace_init_kernel(const __grid_constant_
     }
     __syncthreads();
     if ((int)threadIdx.x < nloc)
-        write_traces<P>(ka.o, sU + threadIdx.x * STR, s.tout + (size_t)(e0 + threadIdx.x) * trace_floats<P>());
+        write_traces<P, true>(ka.o, sU + threadIdx.x * STR, s.tout + (size_t)(e0 + threadIdx.x) * trace_floats<P>(),
+                              s, e0 + threadIdx.x);
 }
 
 template <int P>
@@ -316,10 +343,12 @@ inline size_t stage_trace_smem_bytes() {
 template <int P>
 inline int configure_stage_trace_t() {
     const int b = (int)stage_trace_smem_bytes<P>();
-    return cudaFuncSetAttribute(stage_trace_kernel<P, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
+    return cudaFuncSetAttribute(stage_trace_kernel<P, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
                        cudaSuccess &&
-                   cudaFuncSetAttribute(stage_trace_kernel<P, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        b) == cudaSuccess &&
+                   cudaFuncSetAttribute(stage_trace_kernel<P, false, false>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess &&
+                   cudaFuncSetAttribute(stage_trace_kernel<P, false, true>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess &&
                    cudaFuncSetAttribute(trace_init_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
                        cudaSuccess
                ? 0
@@ -330,15 +359,18 @@ template <int P>
 inline int launch_stage_trace_t(const StageArgs& a, const OpsHost& oh, int grid, cudaStream_t st) {
     SArgs<P, false> ka;
     ka.s = a;
+    if (a.tconn) ka.s.conn = a.tconn;  // boundary faces as interior faces to ghost blocks
     fill_ops<P, float>(oh, ka.o);
     fill_lift<P, float>(oh, ka.l);
     const int ntiles = a.ntile > 0 ? a.ntile : (a.ne + TILE - 1) / TILE;
     if (ntiles == 0) return 0;
     if (grid <= 0 || grid > ntiles) grid = ntiles;
-    if (a.boundary)
-        stage_trace_kernel<P, true><<<grid, TILE, stage_trace_smem_bytes<P>(), st>>>(ka);
+    if (a.tconn)
+        stage_trace_kernel<P, false, true><<<grid, TILE, stage_trace_smem_bytes<P>(), st>>>(ka);
+    else if (a.boundary)
+        stage_trace_kernel<P, true, false><<<grid, TILE, stage_trace_smem_bytes<P>(), st>>>(ka);
     else
-        stage_trace_kernel<P, false><<<grid, TILE, stage_trace_smem_bytes<P>(), st>>>(ka);
+        stage_trace_kernel<P, false, false><<<grid, TILE, stage_trace_smem_bytes<P>(), st>>>(ka);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -346,6 +378,7 @@ template <int P>
 inline int launch_trace_init_t(const StageArgs& a, const OpsHost& oh, cudaStream_t st) {
     SArgs<P, false> ka;
     ka.s = a;
+    if (a.tconn) ka.s.conn = a.tconn;
     fill_ops<P, float>(oh, ka.o);
     const int ntiles = a.ntile > 0 ? a.ntile : (a.ne + TILE - 1) / TILE;
     if (ntiles == 0) return 0;

@@ -34,6 +34,10 @@ struct dgx_ctx {
     int* d_status = nullptr;  // bit 0: an RK3 step produced a non-finite value (dgx_step_status)
     float* d_uhi[2] = {nullptr, nullptr};  // FP32 copies of u^n (mixed RK3), ping-ponged
     float* d_tr[2] = {nullptr, nullptr};    // face traces of the stage states (mixed Euler, trace form)
+    // trace form with ghost blocks (every boundary face has a condition): the connectivity with
+    // boundary face k pointing at block ne + k of d_tr, and each ghost block's condition slot
+    dgx::ElemConn* d_tconn = nullptr;
+    int* d_ghost_bc = nullptr;
     float* d_d1 = nullptr;                  // FP32 stage increments (mixed RK3)
     float* d_d2 = nullptr;
     int minv_diag = 0;

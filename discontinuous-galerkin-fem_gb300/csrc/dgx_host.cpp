@@ -664,6 +664,8 @@ static void free_ctx(dgx_ctx* c) {
     cudaFree(c->d_d2);
     cudaFree(c->d_tr[0]);
     cudaFree(c->d_tr[1]);
+    cudaFree(c->d_tconn);
+    cudaFree(c->d_ghost_bc);
     if (c->cap) cudaStreamDestroy(c->cap);
     if (c->host_out) cudaStreamDestroy(c->host_out);
     for (cudaEvent_t e : c->host_ev)
@@ -969,6 +971,29 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
         return cudaMalloc(ptr, bytes ? bytes : 16) == cudaSuccess;
     };
     const size_t sb = c->nstate * sizeof(double);
+    // Face-trace form on a mesh with boundary faces: when every boundary face has a condition
+    // (no skipped faces), boundary face k becomes an interior face to ghost block ne + k of the
+    // trace buffers, which its owner fills with the ghost states of its traces; the stage then
+    // runs the kernel without the boundary branch.
+    const bool traces = p->precision == DGX_MIXED && !quad && p->physics == DGX_EULER;
+    std::vector<ElemConn> tconn;
+    std::vector<int> ghost_bc;
+    if (traces && hg.boundary) {
+        bool skipped = false;
+        for (int e = 0; e < ne && !skipped; ++e)
+            for (int f = 0; f < 3; ++f) skipped |= conn[e].nbr[f] == NBR_SKIP;
+        if (!skipped) {
+            tconn = conn;
+            for (int e = 0; e < ne; ++e)
+                for (int f = 0; f < 3; ++f)
+                    if (conn[e].nbr[f] < 0) {
+                        tconn[e].nbr[f] = ne + (int)ghost_bc.size();
+                        tconn[e].flags &= ~(7 << (4 * f));  // the block's face 0, points in this face's order
+                        ghost_bc.push_back(-1 - conn[e].nbr[f]);
+                    }
+        }
+    }
+    const size_t trace_blocks = (size_t)ne + ghost_bc.size();
     if ((quad ? !alloc((void**)&c->d_qgeom, sizeof(QuadGeom) * ne) || !alloc((void**)&c->d_qconn, sizeof(QuadConn) * ne)
               : !alloc((void**)&c->d_geom, sizeof(ElemGeom) * ne) || !alloc((void**)&c->d_conn, sizeof(ElemConn) * ne)) ||
         !alloc((void**)&c->d_bc, sizeof(BCSlot) * slots.size()) || !alloc((void**)&c->d_u1, sb) ||
@@ -980,8 +1005,10 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
           !alloc((void**)&c->d_d1, c->nstate * sizeof(float)) ||
           !alloc((void**)&c->d_d2, c->nstate * sizeof(float)))) ||
         (p->precision == DGX_MIXED && !quad && p->physics == DGX_EULER &&
-         (!alloc((void**)&c->d_tr[0], (size_t)ne * trace_floats_per_element(p->order) * sizeof(float)) ||
-          !alloc((void**)&c->d_tr[1], (size_t)ne * trace_floats_per_element(p->order) * sizeof(float))))) {
+         (!alloc((void**)&c->d_tr[0], trace_blocks * trace_floats_per_element(p->order) * sizeof(float)) ||
+          !alloc((void**)&c->d_tr[1], trace_blocks * trace_floats_per_element(p->order) * sizeof(float)))) ||
+        (!ghost_bc.empty() && (!alloc((void**)&c->d_tconn, sizeof(ElemConn) * ne) ||
+                               !alloc((void**)&c->d_ghost_bc, sizeof(int) * ghost_bc.size())))) {
         cudaGetLastError();
         free_ctx(c);
         return fail(DGX_ERR_CUDA, "cudaMalloc failed for the solver state");
@@ -1028,6 +1055,10 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
     if (cudaMemset(c->d_status, 0, sizeof(int)) != cudaSuccess || !geom_ok ||
         (c->d_d1 && cudaMemset(c->d_d1, 0, c->nstate * sizeof(float)) != cudaSuccess) ||
         cudaMemcpy(c->d_bc, slots.data(), sizeof(BCSlot) * slots.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        (c->d_tconn &&
+         (cudaMemcpy(c->d_tconn, tconn.data(), sizeof(ElemConn) * ne, cudaMemcpyHostToDevice) != cudaSuccess ||
+          cudaMemcpy(c->d_ghost_bc, ghost_bc.data(), sizeof(int) * ghost_bc.size(), cudaMemcpyHostToDevice) !=
+              cudaSuccess)) ||
         cudaStreamCreateWithFlags(&c->cap, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         free_ctx(c);
@@ -1122,6 +1153,8 @@ static StageArgs mixed_stage_args(const dgx_ctx* c, double* u, double dt, int sr
     a.uhi_out = c->d_uhi[1 - src];
     a.grid = c->stage_grid;
     a.status = c->d_status;
+    a.tconn = c->d_tconn;
+    a.ghost_bc = c->d_ghost_bc;
     return a;
 }
 

@@ -195,6 +195,11 @@ struct StageArgs {
     const float* tin;   // face-trace form: traces of this stage's state (dg_stage_trace.cuh)
     float* tout;        // face-trace form: traces of the next stage's state
     int tile0, ntile;   // CUDA-core forms: the tiles [tile0, tile0 + ntile) only (ntile = 0: all)
+    // face-trace form on a mesh whose every boundary face has a condition (null otherwise): its
+    // connectivity, in which boundary face k points at the ghost block ne + k of the trace
+    // buffers, and the condition slot of each ghost block
+    const ElemConn* tconn;
+    const int* ghost_bc;
 };
 
 

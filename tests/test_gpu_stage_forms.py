@@ -3,7 +3,10 @@ DGX_STAGE_KERNEL=rows (neighbour coefficient rows per face) and =trace (face tra
 HBM).  They perform the same FP32 operations in the same order, so their states agree bit
 for bit, p = 1..4, periodic and with far-field / no-slip / slip faces, over step counts that
 exercise the one-step and two-step graphs; both stay within the mixed-precision bar of the
-FP64 oracle.  Without the variable the autotuner times both and reports its choice."""
+FP64 oracle.  With a condition on every boundary face the trace form writes ghost blocks and
+runs its kernel without the boundary branch; with faces that have no condition ("skip") it
+runs the kernel with it.  Without the variable the autotuner times both and reports its
+choice."""
 
 import numpy as np
 import pytest
@@ -36,7 +39,7 @@ def run(dg, monkeypatch, pm, order, u0, dt, kernel, steps=(3, 2)):
     return u.cpu().numpy(), ctx.stage_form()
 
 
-@pytest.mark.parametrize("walls", [False, True])
+@pytest.mark.parametrize("walls", [False, True, "skip"])
 @pytest.mark.parametrize("order", [1, 2, 3, 4])
 def test_trace_form_equals_row_form(dg, monkeypatch, order, walls):
     om, pm, u0, dt = case(dg, 9, order, walls)
@@ -55,7 +58,7 @@ def test_autotuner_reports_a_form(dg, monkeypatch):
     assert rel(u, om.rk3_step(O.euler(1.4), u0, dt, 1)) <= 1e-6
 
 
-@pytest.mark.parametrize("walls", [False, True])
+@pytest.mark.parametrize("walls", [False, True, "skip"])
 @pytest.mark.parametrize("kernel,n", [("rows", 1), ("trace", 1), ("trace", 3)])
 def test_host_pointer_step_equals_device_step(dg, monkeypatch, kernel, n, walls):
     """dgx_rk3_step_host runs its last step's stage 3 in tile ranges, each copied back to the
