@@ -289,7 +289,9 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
         //                  :177-250 and the viscous counterparts, NS :142-273)
         const ElemConn C = s.conn[e];
         const float inv_j = __frcp_rn(G.detJ);
-#pragma unroll
+        // one face body, walked three times: unrolled, the code missed the instruction cache and
+        // spilled at the register cap (Euler p=3 0.646 -> 0.594 ms/step, NS p=4 0.676 -> 0.521)
+#pragma unroll 1
         for (int f = 0; f < 3; ++f) {
             const int nb = C.nbr[f];
             if (BND && nb == NBR_SKIP) continue;

@@ -214,7 +214,9 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
 
         // ---------------- faces (interior_face_residual :117-175, boundary_face_residual :177-250)
         const float inv_j = __frcp_rn(G.detJ);
-#pragma unroll
+        // one face body, walked three times (the unrolled form measured 2.7 % slower: its
+        // larger code missed the instruction cache and its registers spilled)
+#pragma unroll 1
         for (int f = 0; f < 3; ++f) {
             const int nb = C.nbr[f];
             if (BND && nb == NBR_SKIP) continue;
