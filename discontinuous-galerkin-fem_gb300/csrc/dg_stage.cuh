@@ -5,8 +5,10 @@
 // Navier-Stokes), M^-1 and the stage combination, one thread per element.  Here:
 //  * arithmetic is FP32 and the stage state is uhi + d (StageArgs, dgx_internal.h);
 //  * M_ref^-1 is folded into the lift operators (precomputed in FP64, rounded once);
-//  * the volume, face and face-point loops are fully unrolled, so every operator of
-//    the element's own faces is an immediate constant-bank operand;
+//  * the volume and face-point loops are fully unrolled, so their operators are
+//    immediate constant-bank operands; the loop over the three faces stays rolled (its
+//    operators are read by face index), which keeps the code small enough for the
+//    instruction cache and the registers within the cap;
 //  * a neighbour's face operators depend on which of its faces is shared, a per-thread
 //    value; they sit in shared memory as [face][basis][point] rows read as 16-byte
 //    vectors.  Lower and upper triangles of a structured mesh share faces in a fixed
@@ -61,9 +63,10 @@ inline void fill_nbr_ops(const OpsHost& h, NbrOps<P>& n) {
 __device__ __forceinline__ int stage_row(int el) { return (el & 1) * (TILE / 2) + (el >> 1); }
 __device__ __forceinline__ int stage_elem(int t) { return 2 * (t & (TILE / 2 - 1)) + t / (TILE / 2); }
 
-// CTAs per SM the register allocation must allow.  Measured on GB300 for p=3 Euler:
-// 4 CTAs (128 registers, 152 B of spills) beats the unconstrained 163 registers / 3 CTAs
-// by 9%.  DGX_STAGE_MIN_BLOCKS overrides it for experiments.
+// CTAs per SM the register allocation must allow.  Measured on GB300 for p=3 Euler (with
+// the face loop unrolled): 4 CTAs (128 registers, 152 B of spills) beat the unconstrained
+// 163 registers / 3 CTAs by 9%; with the rolled face loop 4 CTAs spill 12 B.
+// DGX_STAGE_MIN_BLOCKS overrides it for experiments.
 __host__ __device__ constexpr int stage_min_blocks(int p, bool visc) {
 #ifdef DGX_STAGE_MIN_BLOCKS
     return DGX_STAGE_MIN_BLOCKS + 0 * p * visc;

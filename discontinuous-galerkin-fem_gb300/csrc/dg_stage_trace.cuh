@@ -14,6 +14,10 @@
 // the same numbers bit for bit.  The traces of the state a step starts from are written by
 // trace_init_kernel; stage 3 writes those of the next step's start state (the FP32 copy of
 // u^{n+1}), so the two ping-pong buffers carry the traces from stage to stage and step to step.
+// On a mesh whose boundary faces all have a condition, the buffers hold one ghost block per
+// boundary face after the elements' blocks; the owner fills it with the ghost states of its
+// traces and the face loop reads it like a neighbour's block (GHOST kernels, no boundary
+// branch).  Meshes with faces that take no part keep the boundary branch (BND kernels).
 #pragma once
 
 #include "dg_stage.cuh"
