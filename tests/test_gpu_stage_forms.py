@@ -12,7 +12,8 @@ import numpy as np
 import pytest
 
 import oracle as O
-from test_gpu_tensor_core import case, rel
+from meshes import PERIODIC_PAIRS, TAGS, isentropic_vortex, periodic_rectangle
+from test_gpu_tensor_core import U_INF, case, rel
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
@@ -43,6 +44,31 @@ def run(dg, monkeypatch, pm, order, u0, dt, kernel, steps=(3, 2)):
 @pytest.mark.parametrize("order", [1, 2, 3, 4])
 def test_trace_form_equals_row_form(dg, monkeypatch, order, walls):
     om, pm, u0, dt = case(dg, 9, order, walls)
+    ref = om.rk3_step(O.euler(1.4), u0, dt, 5)
+    rows, f1 = run(dg, monkeypatch, pm, order, u0, dt, "rows")
+    trace, f2 = run(dg, monkeypatch, pm, order, u0, dt, "trace")
+    assert (f1, f2) == ("rows", "traces")
+    assert np.array_equal(rows, trace)
+    assert rel(trace, ref) <= 1e-6
+
+
+@pytest.mark.parametrize("order", [2, 3])
+def test_trace_form_equals_row_form_channel(dg, monkeypatch, order):
+    """Periodic in x, a slip wall below and far field above: periodic pairs and ghost blocks
+    in one mesh."""
+    v, e, b = periodic_rectangle(9)
+    om = O.OracleMesh(v, e, b, order=order, basis=O.DUBINER, periodic=(PERIODIC_PAIRS[0],))
+    om.set_bc(TAGS["Bottom"], O.SLIP_WALL, value=[0.0] * 4)
+    om.set_bc(TAGS["Top"], O.FAR_FIELD, value=U_INF)
+    edges = {}
+    for t, a, c in b:
+        edges.setdefault(int(t), []).append((int(a), int(c)))
+    pm = dg.DGMesh(v, e, None, dict(TAGS), edges)
+    pm.set_periodic_boundaries("Left", "Right")
+    pm.set_boundary_condition_euler("Bottom", dg.BoundaryConditionEuler(O.SLIP_WALL, [0.0] * 4))
+    pm.set_boundary_condition_euler("Top", dg.BoundaryConditionEuler(O.FAR_FIELD, U_INF))
+    u0 = om.project(isentropic_vortex(om.quad_points(), beta=4.0, xc=0.4, yc=-0.3, uinf=0.4))
+    dt = 0.02 / om.max_cfl(1.4, u0, 1.0)
     ref = om.rk3_step(O.euler(1.4), u0, dt, 5)
     rows, f1 = run(dg, monkeypatch, pm, order, u0, dt, "rows")
     trace, f2 = run(dg, monkeypatch, pm, order, u0, dt, "trace")
