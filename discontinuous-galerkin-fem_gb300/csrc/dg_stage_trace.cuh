@@ -27,7 +27,6 @@ namespace dgx {
 template <int P>
 __host__ __device__ constexpr int trace_floats() { return 3 * (P + 1) * NV; }
 
-
 // stage_combine (dg_stage.cuh), which in addition replaces each residual slot of sR with the
 // next stage state: uhi + dout after stages 1 and 2 (what the next stage stages as uhi + din),
 // the FP32 copy of u^{n+1} after stage 3.
@@ -298,9 +297,9 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
 }
 
 // CTAs per SM the register allocation must allow.  Measured on GB300 for p=3 (512x512x2):
-// 3 CTAs (168 registers) 0.527 ms/step, 4 CTAs (128 registers, 588 B of spills) slower; with
-// boundary faces (far field and slip walls) 2 CTAs (255 registers) 0.743 ms/step against 0.769
-// for 3 CTAs (580 B of spills).
+// 3 CTAs (168 registers, no spills) 0.513 ms/step, 4 CTAs (128 registers) 0.544; the
+// boundary-branch kernel, with the face loop still unrolled, ran 0.743 ms/step at 2 CTAs
+// (255 registers) against 0.769 at 3 CTAs (580 B of spills).
 __host__ __device__ constexpr int trace_min_blocks(int p, bool bnd) {
 #ifdef DGX_TRACE_MIN_BLOCKS
     return DGX_TRACE_MIN_BLOCKS + 0 * p + 0 * bnd;
