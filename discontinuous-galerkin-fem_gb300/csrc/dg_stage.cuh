@@ -158,8 +158,7 @@ __device__ __forceinline__ void prefetch_l2_line(const void* p) {
 // The stage state uhi + din of the tile starting at element e0 into shared memory, element
 // le's row at row_of(le) * STR.  In a full tile a thread issues all of its 16-byte loads
 // before it uses the first, so the tile costs one memory round trip instead of one per pass.
-// (BATCH = false: the plain loop, for kernels too short of registers to hold a thread's loads)
-template <int NB, int STR, bool BATCH = true, typename RowOf>
+template <int NB, int STR, typename RowOf>
 __device__ __forceinline__ void stage_load_tile(const float* uhi, const float* din, float* sU, int e0, int nloc,
                                                 RowOf row_of) {
     constexpr int NB4 = NB / 4;
@@ -170,7 +169,7 @@ __device__ __forceinline__ void stage_load_tile(const float* uhi, const float* d
         const int le = g / NB4, k = 4 * (g - le * NB4);
         *reinterpret_cast<float4*>(sU + row_of(le) * STR + k) = a;
     };
-    if (BATCH && nloc == TILE) {
+    if (nloc == TILE) {
         float4 a[NB4];
         if (dd) {
             float4 b[NB4];
@@ -226,8 +225,7 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
     const int e = e0 + el;
     if (tl == 0 && s.stage == 3)  // the FP64 state is read back in the stage combination
         prefetch_l2_bulk(s.u64 + (size_t)e0 * NB, (unsigned)(nloc * NB * sizeof(double)));
-    // with boundary faces the row form has no registers to spare: the plain loop measured faster there
-    stage_load_tile<NB, STR, !BND>(s.uhi, s.din, sU, e0, nloc, [](int le) { return stage_row(le); });
+    stage_load_tile<NB, STR>(s.uhi, s.din, sU, e0, nloc, [](int le) { return stage_row(le); });
     __syncthreads();
 
     float R[NP][NV];
