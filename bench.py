@@ -4,12 +4,16 @@ Workload (one "step" = one SSP-RK3 step = 3 RHS stages over the whole mesh):
   Euler isentropic vortex, periodic [-5,5]^2, 512x512 quads split into 524,288 triangles,
   Dubiner basis p=3 (10 modes x 4 variables = 20,971,520 DOF), gamma=1.4, free stream
   rho=1 u=0.5 v=0 p=1, vortex strength 5 centred at a seeded point of [-2,2]^2,
-  CFL 0.1 (dgfem's convective CFL definition).
+  CFL 0.05 under dgfem's convective CFL definition (0.1, the figure the workload is named
+  with, is unstable for p=3 under that definition; see CFL below).
 
 metric: DOF * RK-stages / s.  `value` is the mixed-precision path with the state resident
 in HBM; the FP64 path, the mixed-vs-FP64 speed-up and the L2/Linf error of the mixed
 path against the FP64 path after 500 steps are reported beside it.  `e2e` times the
 host-pointer C-ABI call (dgx_rk3_step_host) with the state copied in and out each step.
+stdout carries one compact JSON line; the other workloads (Navier-Stokes, batched
+ensemble, adjoint, quadrilaterals, plain-form 16x16x2, set-up times, forms) go to the
+file named by --details.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -44,8 +48,8 @@ MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 # The two CUDA-core forms of the mixed stage (the autotuner picks one), p=3:
 #  design: bytes per element the form needs, averaged over the three stages;
-#  traffic: dram__bytes_read.sum + dram__bytes_write.sum per element of one stage-2 launch
-#           (profiles/stage_kernel_mixed_p3.md, profiles/stage_trace_kernel_p3.md).
+#  traffic: dram__bytes_read.sum + dram__bytes_write.sum per element of one stage-2 launch,
+#           from an ncu capture of that form on the 512x512x2 p=3 workload.
 STAGE_FORMS = {
     # stage 1: 400 B, stage 2: 560 B, stage 3: 1200 B (FP32 stage state, FP64 u^n)
     "rows": {"kernel": "dgx::stage_kernel<3, Euler, no boundary> (mixed SSP-RK3 stage, neighbour rows)",
@@ -207,11 +211,13 @@ class OracleWorkload:
         self.u = self.m.project(vortex(self.m.quad_points(), xc=xc, yc=yc))
         self.ph = O.euler(GAMMA)
         self.dof = self.m.ne * self.m.np * 4
+        # the GPU arm's step: CFL over dgfem's max CFL number of the initial state
+        self.dt = CFL / self.m.max_cfl(GAMMA, self.u, 1.0)
 
-    def run(self, steps, dt=1e-3):
-        """Advance `steps` SSP-RK3 steps; returns (DOF*stages/s, seconds)."""
+    def run(self, steps):
+        """Advance `steps` SSP-RK3 steps of size self.dt; returns (DOF*stages/s, seconds)."""
         t0 = time.perf_counter()
-        self.u = self.m.rk3_step(self.ph, self.u, dt, steps)
+        self.u = self.m.rk3_step(self.ph, self.u, self.dt, steps)
         secs = time.perf_counter() - t0
         return self.dof * 3 * steps / secs, secs
 
@@ -232,8 +238,7 @@ def run_reference(args, rank, ws):
             "steps": k, "warmup": max(1, args.warmup), "ms_per_step": 1e3 * secs / k, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": "euler_vortex_512x512x2_p3_dubiner", "elements": 2 * N_CELLS ** 2,
-                       "order": ORDER, "dof": w.dof},
+            "config": workload_config(N_CELLS, w.dof, w.dt, ws),
             "cpu_baseline": {"value": rate, "unit": "DOF*stages/s", "cores": threads, "kind": "port",
                              "sample": f"each step is one SSP-RK3 step of the full 512x512x2 p=3 mesh "
                                        f"({k} of the {args.steps} asked for timed, at most about "
@@ -241,6 +246,13 @@ def run_reference(args, rank, ws):
                                        f"OpenMP {threads} threads"},
             "e2e": {"value": rate, "unit": "DOF*stages/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def workload_config(cells, dof, dt, ws):
+    """The `config` object of both arms' lines (same keys and values for the same workload)."""
+    return {"workload": f"euler_vortex_{cells}x{cells}x2_p3_dubiner", "elements": 2 * cells * cells, "order": ORDER,
+            "dof": dof, "dt": dt, "cfl": CFL,
+            "l2": "inputs larger than L2 (168 MB FP64 state + stage buffers)", "parallelism": f"replicas x{ws}"}
 
 
 def config1_leg(dg, torch):
@@ -422,6 +434,8 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=300, help="SSP-RK3 steps of each batched instance")
     ap.add_argument("--quad-cells", type=int, default=256, help="quadrilaterals per side of the quad leg (0: skip)")
     ap.add_argument("--quad-steps", type=int, default=50, help="SSP-RK3 steps of the quad leg")
+    ap.add_argument("--details", default="bench_details.json",
+                    help="file for the full results of every leg (stdout carries the compact line)")
     args = ap.parse_args()
     rank, ws = dist_init()
     if args.impl == "reference":
@@ -589,40 +603,48 @@ def main():
         ndt = min(0.025 / n64.max_cfl(nu0, 1.0), 0.05 * h * h * 1600.0)
         ndof = n64.n_elements * n64.n_basis * 4
 
-        def ntimed(ctx, k, chunk=50, keep=100):
-            """k steps in chunks (event-timed on the device), the first step count after
-            which the state is no longer finite, and a copy of the state at step `keep`"""
+        def ntimed(ctx, k, chunk=25, keep=100):
+            """Up to k steps in chunks, event-timed on the device.  Timing stops at the first
+            chunk after which the state is no longer finite (that chunk is not counted), so
+            only steps on finite states are timed.  Returns (seconds, steps timed, first step
+            count with a non-finite state or None, a copy of the state at step `keep`)."""
             u = nu0.clone()
             ctx.rk3_step(u.clone(), ndt, 2)
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            secs, first_bad, kept = 0.0, None, None
+            secs, timed_steps, first_bad, kept = 0.0, 0, None, None
             for done in range(0, k, chunk):
                 n = min(chunk, k - done)
                 e0.record()
                 ctx.rk3_step(u, ndt, n)
                 e1.record()
                 torch.cuda.synchronize()
-                secs += e0.elapsed_time(e1) / 1e3
-                if first_bad is None and not bool(torch.isfinite(u).all()):
+                if not bool(torch.isfinite(u).all()):
                     first_bad = done + n
+                    break
+                secs += e0.elapsed_time(e1) / 1e3
+                timed_steps += n
                 if done + n == keep:
                     kept = u.clone()
-            return secs, first_bad, kept
+            return secs, timed_steps, first_bad, kept
 
-        tn_mx, bad_mx, umx = ntimed(nmx, args.ns_steps)
-        tn_64, bad_64, u64 = ntimed(n64, args.ns_steps)
-        acc100 = None if umx is None else float(torch.linalg.vector_norm(umx - u64) / torch.linalg.vector_norm(u64))
+        tn_mx, kn_mx, bad_mx, umx = ntimed(nmx, args.ns_steps)
+        tn_64, kn_64, bad_64, u64 = ntimed(n64, args.ns_steps)
+        acc100 = None if (umx is None or u64 is None) else \
+            float(torch.linalg.vector_norm(umx - u64) / torch.linalg.vector_norm(u64))
         ns = {"workload": "navier_stokes_taylor_green_256x256x2_p4_dubiner_re1600", "elements": n64.n_elements,
-              "dof": ndof, "dt": ndt, "steps": args.ns_steps,
-              "mixed": {"value": ndof * 3 * args.ns_steps / tn_mx, "ms_per_step": 1e3 * tn_mx / args.ns_steps},
-              "fp64": {"value": ndof * 3 * args.ns_steps / tn_64, "ms_per_step": 1e3 * tn_64 / args.ns_steps},
-              "mixed_vs_fp64": tn_64 / tn_mx,
+              "dof": ndof, "dt": ndt, "steps_asked": args.ns_steps,
+              "mixed": {"value": ndof * 3 * kn_mx / tn_mx if kn_mx else None,
+                        "ms_per_step": 1e3 * tn_mx / kn_mx if kn_mx else None, "steps_timed": kn_mx},
+              "fp64": {"value": ndof * 3 * kn_64 / tn_64 if kn_64 else None,
+                       "ms_per_step": 1e3 * tn_64 / kn_64 if kn_64 else None, "steps_timed": kn_64},
+              "mixed_vs_fp64": (tn_64 / kn_64) / (tn_mx / kn_mx) if kn_mx and kn_64 else None,
               "mixed_vs_fp64_l2_rel_at_step_100": acc100,
               "first_nonfinite_step": {"fp64": bad_64, "mixed": bad_mx},
-              "note": "dgfem's viscous face flux (half jump) grows without bound on this flow at fine "
-                      "resolution; the blow-up time does not depend on dt (oracle, 64x64x2: NaN at t=0.19 "
-                      "with CFL 0.025 and 0.0125), so steps after it are timed on non-finite values"}
+              "note": "only steps on finite states are timed (timing stops at the first 25-step chunk after "
+                      "which the state is not finite).  dgfem's viscous face flux (half jump) grows without "
+                      "bound on this flow at fine resolution; the blow-up time does not depend on dt (oracle, "
+                      "64x64x2: NaN at t=0.19 with CFL 0.025 and 0.0125)"}
         del n64, nmx
 
     # ---- adjoint leg: shear layer 128x128x2, p=3, J = kinetic energy after adj_steps steps,
@@ -707,38 +729,45 @@ def main():
         w = OracleWorkload(1, args.seed)
         rate, secs = w.run(args.cpu_steps)
         cpu = {"value": rate, "unit": "DOF*stages/s", "cores": 1, "kind": "port",
-               "sample": f"{args.cpu_steps} SSP-RK3 steps of the full 512x512x2 p=3 mesh "
+               "sample": f"{args.cpu_steps} SSP-RK3 steps (same dt) of the full 512x512x2 p=3 mesh "
                          f"({secs:.1f} s), FP64 oracle restatement of dgfem's single-threaded path"}
 
     if rank == 0:
+        # compact line: the contract keys and the headline of the metric (mixed vs FP64 at the
+        # stated error, adjoint/forward ratio); every leg in full goes to the details file
         line = {"metric": "DOF*RK-stages/s", "value": v_mx, "unit": "DOF*stages/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_mx / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32 flux/contractions + f64 geometry, mass inverse, RK3 state",
-                "data": "synthetic",
-                "config": {"workload": f"euler_vortex_{args.cells}x{args.cells}x2_p3_dubiner", "elements": ne, "order": ORDER,
-                           "dof": dof, "dt": dt, "cfl": CFL, "l2": "inputs larger than L2 (168 MB state "
-                           "+ two 168 MB stage buffers per context)", "parallelism": f"replicas x{ws}"},
-                "stage_kernel": {"form": form, "grid": grid, "tiles": tiles,
-                                 "picked_by": "autotuner (timed on the first step)"},
-                "tensor_core_form": tensor_core,
-                "fp64": {"value": v_64, "ms_per_step": 1e3 * t_64 / k64, "steps": k64},
-                "df64": df64,
+                "data": "synthetic", "config": workload_config(args.cells, dof, dt, ws),
+                "fp64": {"value": v_64, "ms_per_step": 1e3 * t_64 / k64},
                 "mixed_vs_fp64": v_mx / v_64,
-                "accuracy": acc,
-                "navier_stokes": ns,
+                "accuracy": {k: acc[k] for k in ("steps", "mixed_vs_fp64_l2_rel", "mixed_vs_fp64_linf_rel",
+                                                 "mixed_vs_exact_l2_rel", "fp64_vs_exact_l2_rel") if k in acc},
                 "adjoint_forward_ratio": None if adj is None else adj["adjoint_step_vs_forward_step"],
-                "adjoint": adj,
-                "batched": bat,
-                "config1": cfg1,
-                "quadrilaterals": quads,
-                "setup": setup,
+                "stage_kernel": {"form": form, "grid": grid},
+                "tensor_core_form": {"ms_per_step": tensor_core["ms_per_step"],
+                                     "mixed_vs_fp64_l2_rel": tensor_core["mixed_vs_fp64_l2_rel"]},
                 "e2e": {"value": v_e2e, "unit": "DOF*stages/s", "h2d_bytes_per_step": dof * 8,
-                        "d2h_bytes_per_step": dof * 8, "steps": ke},
+                        "d2h_bytes_per_step": dof * 8},
                 # per timed rk3_step call: the FP32 copy of u^n, the face traces of it (trace
                 # form), then three stage launches per step
                 "gpu_launches": 3 * args.steps + (2 if form == "traces" else 1),
-                "roofline": roof, "clocks": clocks, "cpu_baseline": cpu}
+                "roofline": {k: roof[k] for k in ("bound", "achieved", "peak", "unit", "frac", "traffic",
+                                                  "launch_ms", "peak_kind")},
+                "clocks": clocks,
+                "cpu_baseline": cpu,
+                "details": args.details}
+        details = {"line": line, "roofline": roof, "stage_kernel": {"form": form, "grid": grid, "tiles": tiles,
+                                                                    "picked_by": "autotuner (timed on the first step)"},
+                   "tensor_core_form": tensor_core, "df64": df64, "accuracy": acc, "navier_stokes": ns,
+                   "adjoint": adj, "batched": bat, "config1": cfg1, "quadrilaterals": quads, "setup": setup,
+                   "e2e_steps": ke}
+        try:
+            Path(args.details).parent.mkdir(parents=True, exist_ok=True)
+            Path(args.details).write_text(json.dumps(details, indent=1))
+        except OSError as ex:
+            print(f"bench: could not write {args.details}: {ex}", file=sys.stderr)
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist

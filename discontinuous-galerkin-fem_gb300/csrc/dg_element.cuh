@@ -459,7 +459,7 @@ inline int launch_element_t(const StepArgs& a, const OpsHost& oh, cudaStream_t s
     const int grid = (a.ne + TILE - 1) / TILE;
     if (grid == 0) return 0;
     element_kernel<P, T, VISC><<<grid, TILE, element_smem_bytes<P, T, VISC>(), st>>>(ka);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 #define DGX_ELEMENT_DISPATCH(FN, T)                           \

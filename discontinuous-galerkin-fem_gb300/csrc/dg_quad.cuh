@@ -521,7 +521,7 @@ inline int launch_quad_t(const StepArgs& a, const QuadGeom* geom, const QuadConn
     const int grid = (a.ne + TILE - 1) / TILE;
     if (grid == 0) return 0;
     quad_element_kernel<P, T, VISC><<<grid, TILE, quad_smem_bytes<P, T>(), st>>>(ka);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 #define DGX_QUAD_DISPATCH(FN, T, ARGS)               \
@@ -616,7 +616,7 @@ inline int launch_quad_stage_t(const StageArgs& a, const OpsHost& oh, cudaStream
     const int grid = (a.ne + TILE - 1) / TILE;
     if (grid == 0) return 0;
     quad_stage_kernel<P, VISC><<<grid, TILE, quad_stage_smem_bytes<P, VISC>(), st>>>(ka);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 }  // namespace dgx

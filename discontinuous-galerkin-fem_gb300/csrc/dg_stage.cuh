@@ -507,7 +507,7 @@ inline int launch_stage_t(const StageArgs& a, const OpsHost& oh, cudaStream_t st
         stage_kernel<P, VISC, true><<<grid, TILE, stage_smem_bytes<P, VISC>(), st>>>(ka);
     else
         stage_kernel<P, VISC, false><<<grid, TILE, stage_smem_bytes<P, VISC>(), st>>>(ka);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 }  // namespace dgx

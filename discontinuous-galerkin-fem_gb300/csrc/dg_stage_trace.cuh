@@ -376,7 +376,7 @@ inline int launch_stage_trace_t(const StageArgs& a, const OpsHost& oh, int grid,
         stage_trace_kernel<P, true, false><<<grid, TILE, stage_trace_smem_bytes<P>(), st>>>(ka);
     else
         stage_trace_kernel<P, false, false><<<grid, TILE, stage_trace_smem_bytes<P>(), st>>>(ka);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 template <int P>
@@ -388,7 +388,7 @@ inline int launch_trace_init_t(const StageArgs& a, const OpsHost& oh, cudaStream
     const int ntiles = a.ntile > 0 ? a.ntile : (a.ne + TILE - 1) / TILE;
     if (ntiles == 0) return 0;
     trace_init_kernel<P><<<ntiles, TILE, stage_trace_smem_bytes<P>(), st>>>(ka);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 }  // namespace dgx

@@ -32,7 +32,7 @@ int launch_jvp_t(const AdjArgs& a, const OpsHost& oh, cudaStream_t st) {
         return -1;
     const int grid = (a.ne + TILE - 1) / TILE;
     jvp_kernel<P, VISC><<<grid, TILE, jvp_smem_bytes<P, VISC>(), st>>>(ka);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 template <int P>
@@ -42,7 +42,7 @@ int launch_vjp_t(const AdjArgs& a, const OpsHost& oh, cudaStream_t st) {
     fill_ops<P, double>(oh, ka.o);
     const int grid = (a.ne + TILE - 1) / TILE;
     vjp_kernel<P><<<grid, TILE, vjp_smem_bytes<P>(), st>>>(ka);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 template <int P>
@@ -60,7 +60,7 @@ int launch_kinetic_t(const AdjArgs& a, const OpsHost& oh, double* J, double* gra
     const int grid = (a.ne + 127) / 128;
     kinetic_kernel<P><<<grid, 128, 0, st>>>(ka, J, grad);
     if (J) kinetic_sum_kernel<<<1, 32, 0, st>>>(J, grid, J + grid);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 int launch_jvp(int p, bool visc, const AdjArgs& a, const OpsHost& o, cudaStream_t s) {

@@ -115,7 +115,7 @@ static int launch_batch_t(const BatchArgs& b, bool boundary, int grid, cudaStrea
         batch_stage_kernel<PMAX, true><<<grid, TILE, batch_smem_bytes<PMAX>(), st>>>(b);
     else
         batch_stage_kernel<PMAX, false><<<grid, TILE, batch_smem_bytes<PMAX>(), st>>>(b);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 int batch_tiles(const StageArgs* per_order) {

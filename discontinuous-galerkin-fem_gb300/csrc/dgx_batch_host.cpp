@@ -222,7 +222,7 @@ static int enqueue_batch_step(dgx_batch* b, int src, cudaStream_t s) {
         batch_stage_args(b, src, stage, a);
         if (launch_batch_stage(a, b->ops, b->boundary, b->grid, s))
             return set_error(DGX_ERR_CUDA, std::string("batched stage launch failed: ") +
-                                               cudaGetErrorString(cudaGetLastError()));
+                                               launch_error_text());
     }
     return DGX_OK;
 }

@@ -647,7 +647,7 @@ static int launch(const dgx_ctx* c, const StepArgs& a, cudaStream_t s) {
                    : c->prm.precision == DGX_DF64 ? launch_element_df64(c->prm.order, visc, a, c->ops, s)
                                                   : launch_element_fp64(c->prm.order, visc, a, c->ops, s);
     if (rc) return fail(DGX_ERR_CUDA, std::string("element kernel launch failed: ") +
-                                          cudaGetErrorString(cudaGetLastError()));
+                                          launch_error_text());
     return DGX_OK;
 }
 
@@ -1064,6 +1064,14 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
         free_ctx(c);
         return fail(DGX_ERR_CUDA, "device upload failed");
     }
+    // the allocation-free stepping entry point's scratch array and kernels, loaded here so
+    // that dgx_rk3_step_static itself allocates nothing (triangle meshes only)
+    if (!quad) {
+        if (int rc = static_scratch_setup(dev)) {
+            free_ctx(c);
+            return rc;
+        }
+    }
     *out = c;
     return DGX_OK;
 }
@@ -1172,7 +1180,7 @@ static void mixed_step_args(const dgx_ctx* c, double* u, double dt, int src, Sta
 
 static int launch_stage(const dgx_ctx* c, const StageArgs& a, cudaStream_t s) {
     if (launch_stage_mixed(c->prm.order, c->prm.physics == DGX_NAVIER_STOKES, a, c->ops, s))
-        return fail(DGX_ERR_CUDA, std::string("stage kernel launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+        return fail(DGX_ERR_CUDA, std::string("stage kernel launch failed: ") + launch_error_text());
     return DGX_OK;
 }
 

@@ -7,6 +7,28 @@
 
 namespace dgx {
 
+// Status of the kernel launch just made: 0, or -1 with the CUDA error kept in a thread-local
+// slot, because reading it with cudaGetLastError() also clears it and the caller reports it
+// later (launch_error_text()).
+inline cudaError_t& last_launch_error() {
+    static thread_local cudaError_t e = cudaSuccess;
+    return e;
+}
+inline int launch_status() {
+    const cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) return 0;
+    last_launch_error() = e;
+    return -1;
+}
+// Text of the error behind the last failed launch on this thread (then cleared), or of the
+// pending CUDA error when no launch failed.
+inline const char* launch_error_text() {
+    cudaError_t e = last_launch_error();
+    last_launch_error() = cudaSuccess;
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return cudaGetErrorString(e);
+}
+
 constexpr int NV = 4;      // conserved variables (rho, rho u, rho v, E), assembler.cpp:154
 constexpr int MAX_P = 4;   // orders with compiled kernels
 constexpr int TILE = 128;  // elements per CTA in the element kernels (one per thread)
@@ -244,6 +266,13 @@ int launch_has_nan(size_t n, const double* u, int* d_flag, cudaStream_t s);
 constexpr int EVAL_MAX_POINTS = 128;
 int launch_eval_points(int ne, int np, int npts, const double* phi, const double* u, double* out, cudaStream_t s);
 int launch_f64_to_f32(size_t n, const double* in, float* out, cudaStream_t s);
+// Loads the conversion kernel on the current device (lazy module loading otherwise loads
+// it, and allocates its code, at its first launch).
+int prepare_f64_to_f32();
+// Set-up of the allocation-free stepping entry point (dgx_static.cu) for the current
+// device: looks up, and so loads, the static scratch array and the kernels that entry point
+// launches besides the context's element or stage kernels.  Called by dgx_create.
+int static_scratch_setup(int dev);
 
 // Quadrilateral kernels (dgx_quad.cu; the double-float element kernel in
 // dgx_kernels_df64.cu), orders 1..MAX_P_QUAD, precision DGX_FP64 / DGX_MIXED / DGX_DF64.

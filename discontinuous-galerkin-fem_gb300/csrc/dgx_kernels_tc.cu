@@ -46,7 +46,7 @@ static int launch_tc_t(const StageArgs& a, const OpsHost& oh, int grid, cudaStre
         stage_tc_kernel<P, true><<<grid, TcShape<P>::THREADS, smem, st>>>(k);
     else
         stage_tc_kernel<P, false><<<grid, TcShape<P>::THREADS, smem, st>>>(k);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 int launch_stage_tc(int p, const StageArgs& a, const OpsHost& ops, int grid, cudaStream_t s) {

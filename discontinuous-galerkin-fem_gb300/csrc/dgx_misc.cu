@@ -174,7 +174,7 @@ int launch_mass_inv(int ne, int p, const OpsHost& ops, const ElemGeom* geom, con
     fill_minv(ops, m);
     const int grid = (ne + 127) / 128;
     DGX_DISPATCH_P(p, (void)NQ; mass_inv_kernel<NP><<<grid, 128, 0, s>>>(m, ne, geom, in, out))
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 int launch_project(int ne, int p, const OpsHost& ops, const ElemGeom* geom, const double* uq,
@@ -184,7 +184,7 @@ int launch_project(int ne, int p, const OpsHost& ops, const ElemGeom* geom, cons
     fill_minv(ops, m);
     const int grid = (ne + 127) / 128;
     DGX_DISPATCH_P(p, (project_kernel<NP, NQ><<<grid, 128, 0, s>>>(m, ne, geom, uq, u)))
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 int launch_monitor(int ne, int p, const OpsHost& ops, const ElemGeom* geom, const double* u,
@@ -196,7 +196,7 @@ int launch_monitor(int ne, int p, const OpsHost& ops, const ElemGeom* geom, cons
     if (ne == 0) return 0;
     const int grid = (ne + 127) / 128;
     DGX_DISPATCH_P(p, (monitor_kernel<NP, NQ><<<grid, 128, 0, s>>>(m, ne, geom, u, dt, gamma, d_out)))
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 int launch_has_nan(size_t n, const double* u, int* d_flag, cudaStream_t s) {
@@ -205,7 +205,12 @@ int launch_has_nan(size_t n, const double* u, int* d_flag, cudaStream_t s) {
     size_t blocks = (n + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     has_nan_kernel<<<(unsigned)blocks, 256, 0, s>>>(n, u, d_flag);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
+}
+
+int prepare_f64_to_f32() {
+    cudaFuncAttributes fa;
+    return cudaFuncGetAttributes(&fa, f64_to_f32_kernel) == cudaSuccess ? 0 : -1;
 }
 
 int launch_f64_to_f32(size_t n, const double* in, float* out, cudaStream_t s) {
@@ -213,7 +218,7 @@ int launch_f64_to_f32(size_t n, const double* in, float* out, cudaStream_t s) {
     size_t blocks = (n + 255) / 256;
     if (blocks > 152 * 32) blocks = 152 * 32;
     f64_to_f32_kernel<<<(unsigned)blocks, 256, 0, s>>>(n, in, out);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 
@@ -249,7 +254,7 @@ int launch_eval_points(int ne, int np, int npts, const double* phi, const double
         for (int i = 0; i < np; ++i) a.phi[k][i] = phi[k * np + i];
     const size_t n = (size_t)ne * npts;
     eval_points_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, ne, u, out);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 }  // namespace dgx

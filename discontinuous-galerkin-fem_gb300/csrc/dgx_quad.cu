@@ -159,7 +159,7 @@ int launch_quad_mass_inv(int ne, int p, const OpsHost& ops, const QuadGeom* geom
     const int grid = (ne + 127) / 128;
     DGX_QUAD_P(p, QuadOps<P, double> o; fill_quad_ops<P, double>(ops, o);
                quad_mass_inv_kernel<P><<<grid, 128, 0, s>>>(o, ne, geom, in, out))
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 int launch_quad_project(int ne, int p, const OpsHost& ops, const QuadGeom* geom, const double* uq, double* u,
@@ -168,7 +168,7 @@ int launch_quad_project(int ne, int p, const OpsHost& ops, const QuadGeom* geom,
     const int grid = (ne + 127) / 128;
     DGX_QUAD_P(p, QuadOps<P, double> o; fill_quad_ops<P, double>(ops, o);
                quad_project_kernel<P><<<grid, 128, 0, s>>>(o, ne, geom, uq, u))
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 int launch_quad_monitor(int ne, int p, const OpsHost& ops, const QuadGeom* geom, const double* u, double dt,
@@ -179,7 +179,7 @@ int launch_quad_monitor(int ne, int p, const OpsHost& ops, const QuadGeom* geom,
     const int grid = (ne + 127) / 128;
     DGX_QUAD_P(p, QuadOps<P, double> o; fill_quad_ops<P, double>(ops, o);
                quad_monitor_kernel<P><<<grid, 128, 0, s>>>(o, ne, geom, u, dt, gamma, d_out))
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    return launch_status();
 }
 
 }  // namespace dgx

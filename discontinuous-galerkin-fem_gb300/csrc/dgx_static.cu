@@ -9,13 +9,16 @@
 //
 // Limits and behaviour:
 //  * the scratch is one static __device__ array of 2 * DGX_STATIC_MAX_STATE doubles
-//    (16 MiB); every GPU that loads the library holds it until the process exits;
+//    (16 MiB).  Under lazy module loading (CUDA's default) the array is placed on a device
+//    when its module is loaded there; dgx_create does that for its device (with the device
+//    current), together with the kernels this entry point launches, so the steps themselves
+//    allocate nothing.  A device keeps the array until the process exits;
 //  * states larger than DGX_STATIC_MAX_STATE values are rejected with DGX_ERR_INVALID;
 //  * all calls share the array.  Stage buffers are written in full before they are read,
 //    so nothing has to start at zero, but two calls whose work overlaps on the GPU (other
 //    streams, other host threads) race on it;
-//  * the first call on a device looks the array's device address up (with that device
-//    current) and caches it; make that first call before any stream capture.
+//  * the array's device address is looked up once per device, at dgx_create; creating the
+//    context before any stream capture keeps that lookup out of a capture.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -33,8 +36,9 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 double* g_scratch_ptr[kMaxDevices] = {};
 
-// Device address of g_rk3_scratch on the current device (host code may not use the
-// symbol itself as an address).  Looked up once per device.
+// Device address of g_rk3_scratch on the current device `dev` (host code may not use the
+// symbol itself as an address).  The first lookup on a device loads the array's module
+// there; later calls return the cached address.
 int scratch_for_device(int dev, double** out) {
     if (dev < 0 || dev >= kMaxDevices) return dgx::set_error(DGX_ERR_CUDA, "device index out of range");
     std::lock_guard<std::mutex> lock(g_setup_mutex);
@@ -49,6 +53,15 @@ int scratch_for_device(int dev, double** out) {
     return DGX_OK;
 }
 }  // namespace
+
+int dgx::static_scratch_setup(int dev) {
+    double* p = nullptr;
+    if (int rc = scratch_for_device(dev, &p)) return rc;
+    if (prepare_f64_to_f32())
+        return dgx::set_error(DGX_ERR_CUDA, std::string("loading the FP64->FP32 conversion kernel: ") +
+                                                cudaGetErrorString(cudaGetLastError()));
+    return DGX_OK;
+}
 
 extern "C" int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps, void* stream) {
     if (c && c->nvpe == 4) return dgx::set_error(DGX_ERR_INVALID, "dgx_rk3_step_static: triangle meshes only");
@@ -106,7 +119,8 @@ extern "C" int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps
         float* d1 = f + 2 * c->nstate;
         float* d2 = f + 3 * c->nstate;
         if (launch_f64_to_f32(c->nstate, u, uhi[0], s))
-            return dgx::set_error(DGX_ERR_CUDA, "dgx_rk3_step_static: conversion launch failed");
+            return dgx::set_error(DGX_ERR_CUDA, std::string("dgx_rk3_step_static: conversion launch failed: ") +
+                                                    launch_error_text());
         StageArgs a{};
         a.status = c->d_status;
         a.ne = c->ne;
@@ -132,6 +146,8 @@ extern "C" int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps
             if (!rc) rc = launch_stage_mixed(c->prm.order, visc, a, c->ops, s);
         }
     }
-    if (rc) return dgx::set_error(DGX_ERR_CUDA, "dgx_rk3_step_static: kernel launch failed");
+    if (rc)
+        return dgx::set_error(DGX_ERR_CUDA, std::string("dgx_rk3_step_static: kernel launch failed: ") +
+                                                launch_error_text());
     return DGX_OK;
 }

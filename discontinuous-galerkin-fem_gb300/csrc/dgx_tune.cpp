@@ -74,14 +74,14 @@ int tune_grid(const std::string& key, const std::vector<int>& candidates, const 
     for (int g : candidates) {
         if (launch(g, s)) {
             rc = set_error(DGX_ERR_CUDA, std::string("autotuner: launch failed: ") +
-                                             cudaGetErrorString(cudaGetLastError()));
+                                             launch_error_text());
             break;
         }
         cudaEventRecord(e0, s);
         for (int r = 0; r < REPS && !rc; ++r)
             if (launch(g, s))
                 rc = set_error(DGX_ERR_CUDA, std::string("autotuner: launch failed: ") +
-                                                 cudaGetErrorString(cudaGetLastError()));
+                                                 launch_error_text());
         cudaEventRecord(e1, s);
         float ms = 0.0f;
         if (rc || cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {

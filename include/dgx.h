@@ -230,12 +230,17 @@ int dgx_kinetic_energy_gradient(dgx_ctx* c, const double* u0, double dt, int n_s
  * device state u (in place), with the stage buffers taken from one static device array
  * of the library instead of memory the library allocates.  The call allocates nothing.
  *  - Limit: n_elements * n_basis * 4 <= DGX_STATIC_MAX_STATE; larger states are rejected
- *    with DGX_ERR_INVALID.  The array (2 * DGX_STATIC_MAX_STATE doubles, 16 MiB) is held
- *    by every GPU that loads the library until the process exits.
+ *    with DGX_ERR_INVALID.  The array (2 * DGX_STATIC_MAX_STATE doubles, 16 MiB) is
+ *    reserved on a device when the first triangle-mesh context is created there
+ *    (dgx_create loads it, looks up its device address and loads the kernels this call
+ *    launches, with that device current), and it stays reserved until the process exits.
+ *    Create the context before any stream capture.
  *  - All calls share the array; calls whose GPU work overlaps (other streams or threads)
  *    race on it.  Nothing in it needs to start at zero.
- *  - The first call on a device looks up the array's device address (with the context's
- *    device current); make that first call before any stream capture.
+ *  - Mixed precision runs the stage kernel that reads neighbour coefficient rows, at one CTA
+ *    per 128-element tile, not the form the autotuner picks for dgx_rk3_step (the face-trace
+ *    form needs trace buffers): the results are the same bit for bit, the steps about 15 %
+ *    slower at 524,288 elements.
  *  - The context's device must be current.  Kernels are launched directly on `stream`. */
 #define DGX_STATIC_MAX_STATE (1 << 20)
 int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps, void* stream);

@@ -108,3 +108,16 @@ def quad_rectangle(n, x0=-5.0, x1=5.0, y0=-5.0, y1=5.0, nx=None, distort=0.0, se
     for j in range(ny):
         be.append((LEFT, vid(0, j), vid(0, j + 1)))
     return verts, np.array(elems, dtype=np.int32), np.array(be, dtype=np.int32)
+
+
+def taylor_green(xy, seed=0, gamma=1.4, mach=0.1, noise=1e-3):
+    """Decaying Taylor-Green-type vortex on [0, 2 pi]^2 (conserved variables): rho=1,
+    u=sin x cos y, v=-cos x sin y, p = 1/(gamma M^2) + (cos 2x + cos 2y)/4, plus seeded
+    Gaussian noise of amplitude ``noise`` on both velocity components."""
+    x, y = xy[..., 0], xy[..., 1]
+    rng = np.random.default_rng(seed)
+    u = np.sin(x) * np.cos(y) + noise * rng.standard_normal(x.shape)
+    v = -np.cos(x) * np.sin(y) + noise * rng.standard_normal(x.shape)
+    p = 1.0 / (gamma * mach * mach) + 0.25 * (np.cos(2 * x) + np.cos(2 * y))
+    rho = np.ones_like(x)
+    return primitive_to_conserved(np.stack([rho, u, v, p], axis=-1), gamma)
