@@ -1,408 +1,663 @@
-// Tensor-core form of the mixed-precision SSP-RK3 stage (Euler): the basis<->point
-// contractions run as 3xTF32 tcgen05 GEMMs with FP32 accumulation in TMEM.
+// Tensor-core form of the mixed-precision SSP-RK3 Euler stage: the basis<->point
+// contractions run as 3xTF32 tcgen05 GEMMs with FP32 accumulators in TMEM, in a persistent,
+// warp-specialised pipeline with two tiles in flight per SM.
 //
-// Same discretisation, increment form and stage combination as stage_kernel
-// (dg_stage.cuh); only where the contractions run changes.  Per tile of 128 elements
-// (M = 128 rows, element e = TMEM lane e), for each conserved variable v:
-//   GEMM1  D1_v[e, n] = sum_i U[e, i, v] Psi[n, i]          interpolation to the NQ volume
-//          points and the 3 * NFQ face points of the element's own faces;
-//   GEMM2  D2_v[e, i] = sum_m A2_v[e, m] W[i, m]            projection back to the basis:
-//          A2_v = [Fr(q) | Fs(q) | H'(f, j)], W = [pr | ps | pf] (M_ref^-1 folded in, as
-//          LiftOps), so D2 = M^-1-scaled residual R[e, i, v].
-// Each product is split 3xTF32 (a = a_hi + a_lo; a*b ~ a_hi b_hi + a_hi b_lo + a_lo b_hi),
-// which keeps FP32-level accuracy.  Between the GEMMs, CUDA cores evaluate the Euler
-// fluxes at the points, the neighbour traces and the Rusanov fluxes; they read D1 from
-// TMEM and write A2 to TMEM (tcgen05.ld / tcgen05.st, each thread its element's lane).
+// Same discretisation, increment form and stage combination as the CUDA-core forms
+// (dg_stage.cuh, dg_stage_trace.cuh), and the same face-trace exchange through HBM: every
+// element writes the traces of its next stage state at its face points, and a stage reads its
+// neighbours' trace blocks.  Per tile of 128 elements (M = 128, element e = TMEM lane e):
+//   GEMM1  D1_v[e, n] = sum_{i>=1} S[e, i, v] Psi[n, i]     the stage state at the volume
+//          points and the element's own face points (variable v, slots n);
+//   GEMM2  D2_v[e, i] = sum_m A2_v[e, m] W[i, m]           projection back to the basis,
+//          A2 = [Fr'(q) | Fs'(q) | H'(f, j)], W = [pr | ps | pf] with M_ref^-1 folded in, so D2
+//          is the M^-1-scaled residual;
+//   GEMM3  = GEMM1 on the next stage state; its face columns are the traces written for the
+//          neighbours (the same instructions on the same numbers as the next stage's GEMM1,
+//          so both sides of a face see identical traces).
 //
-// Operands: A1 (the tile's state, split) and the constant B operands sit in shared memory
-// in the K-major no-swizzle layout of tc_ptx.cuh; A2 is read from TMEM.  TMEM holds
-// D1 (4 x N1 columns; D2 reuses them), A2 hi and A2 lo (4 x K2 each): 192 to 512 columns.
+// Two exact rewritings keep the tensor-core rounding away from the large, cancelling terms of
+// the residual of a smooth flow:
+//  * the first basis function is constant (monomial 1, Dubiner sqrt 2), so a point value is
+//    c0 S_0 + sum_{i>=1} Psi_i S_i: the GEMMs interpolate only the modes i >= 1 (a small
+//    deviation) and the FP32 FMA fmaf(c0, S_0, D) adds the mean;
+//  * for a constant flux (F0, G0) the volume and face integrals of every test function cancel
+//    exactly (int_T grad phi = int_dT phi n, with the quadratures exact for these degrees), so
+//    the fluxes enter GEMM2 as deviations from the element's flux at volume point 0:
+//    Fr' = w_q (A00 (F - F0) + A10 (G - G0)), H' = -(w_j h_F / (2|J|)) (H - (F0 nx + G0 ny)).
+// 3xTF32: a b ~ a_hi b_hi + a_hi b_lo + a_lo b_hi, a_hi = tf32(a), a_lo = tf32(a - a_hi).
 //
-// A CTA has 256 threads: two per element (TMEM lane e is reachable from warps e/32 and
-// e/32 + 4).  Half 0 does the volume points and face 0, half 1 faces 1 and 2.  One
-// thread issues the MMAs; completion is tracked by mbarriers whose waits are bounded.
+// Roles (Tc<P>::THREADS = 17 warps; five warps on one SM sub-partition cap a thread at 96
+// registers): 16 compute warps, four threads per element (thread k of
+// element e is in warp 4k + e/32, which reaches e's TMEM lane): thread k takes the volume points
+// q = k mod 4, the face points f*NFQ + j = k mod 4 and the basis functions i = k mod 4.  Warp 16,
+// lane 0, issues the bulk copies (TMA) of each tile's inputs into shared memory and every MMA.
+// Per tile j of a CTA, the compute warps run:
+//   (a) D1(j) -> registers;  (b) volume fluxes -> A2 (TMEM), GEMM2 volume part starts;
+//   (c) face fluxes -> A2, GEMM2 face part;  (d) traces of tile j-1 (GEMM3 output) -> HBM;
+//   (e) split the stage state of tile j+1 -> shared memory, GEMM1(j+1) starts;
+//   (f) D2(j) -> stage combination -> HBM; next stage state split -> shared memory, GEMM3(j).
+// TMEM (columns): A2 hi/lo [0, 8 K2V) (D1 of the next tile lands there once GEMM2 has read A2),
+// D2 [8 K2V, +64), D3 [.., +4 N1V): 512 columns at p = 3, one CTA per SM.
+// Every wait is bounded; on running out the kernel sets bit 1 of the status flag, lets its
+// copies and MMAs drain, frees TMEM and returns.
 #pragma once
 
 #include <cstring>
 
-#include "dg_stage.cuh"
+#include "dg_stage_trace.cuh"
 #include "tc_ptx.cuh"
 
 namespace dgx {
 
 template <int P>
-struct TcShape {
-    static constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1, NB = NP * NV;
-    static constexpr int NQ4 = (NQ + 3) & ~3;             // volume slots, padded to 4
-    static constexpr int FQ = 3 * NFQ;                    // face points of the three faces
-    static constexpr int FQ4 = (FQ + 3) & ~3;
-    static constexpr int KP = (NP + 7) & ~7;              // GEMM1 K (basis)
-    static constexpr int N1 = (NQ4 + FQ4 + 15) & ~15;     // GEMM1 N per variable (points)
-    static constexpr int K2 = (2 * NQ4 + FQ4 + 7) & ~7;   // GEMM2 K per variable (flux slots)
-    static constexpr int N2 = 16;                         // GEMM2 N per variable (basis, padded)
-    static constexpr int A2 = 4 * N1;                     // TMEM column of A2 hi; lo follows at +4*K2
-    static constexpr int COLS_USED = A2 + 8 * K2;
+struct Tc {
+    static constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1, FQ = 3 * NFQ, NB = NP * NV;
+    static constexpr int KT = 4;                          // threads per element
+    static constexpr int KP = 16;                         // GEMM1 K (basis functions, padded)
+    static constexpr int VW = (NQ + KT - 1) / KT;         // volume points per thread
+    static constexpr int VOLK = 2 * KT * VW;              // GEMM2 K, volume part (Fr', Fs')
+    static constexpr int FMAX = (FQ + KT - 1) / KT;
+    static constexpr int FACEK = (KT * FMAX + 7) & ~7;    // GEMM2 K, face part
+    static constexpr int FW = FACEK / KT;                 // face slots per thread (>= its points)
+    static constexpr int K2V = VOLK + FACEK;              // GEMM2 K per variable
+    static constexpr int DW = VW + FW;                    // GEMM1 output slots per thread
+    static constexpr int N1V = (KT * DW + 15) & ~15;      // GEMM1 N per variable
+    static constexpr int BW = (NP + KT - 1) / KT;         // basis functions per thread
+    static constexpr int N2V = 16;                        // GEMM2 N per variable
+    // TMEM columns
+    static constexpr int COL_A2 = 0, COL_D1 = 0, COL_D2 = 8 * K2V, COL_D3 = COL_D2 + 4 * N2V;
+    static constexpr int COLS_USED = COL_D3 + 4 * N1V;
     static constexpr int COLS = COLS_USED <= 256 ? 256 : 512;
-    static constexpr int THREADS = 2 * TILE;
+    // warps
+    static constexpr int CW = 16;
+    static constexpr int THREADS = (CW + 1) * 32;
+    // shared memory (bytes)
+    static constexpr int OFF_A = 0;                               // [8][TILE * KP] floats
+    static constexpr int OFF_B1 = OFF_A + 8 * TILE * KP * 4;      // [2][N1V * KP]
+    static constexpr int OFF_B2 = OFF_B1 + 2 * N1V * KP * 4;      // [2][N2V * K2V]
+    static constexpr int RS = TILE * NB * 8;                      // a tile's u^n (FP64, stage 3) or uhi
+    static constexpr int RD = TILE * NB * 4;                      // its increment
+    static constexpr int RG = TILE * 64, RC = TILE * 16;          // its ElemGeomF, ElemConn
+    static constexpr int RD_OFF = RS, RG_OFF = RS + RD, RC_OFF = RS + RD + RG, RAWB = RS + RD + RG + RC;
+    static constexpr int OFF_RAW = OFF_B2 + 2 * N2V * K2V * 4;    // [2][RAWB]
+    static constexpr int OFF_BAR = OFF_RAW + 2 * RAWB;
+    static constexpr int NBAR = 13;
+    static constexpr int OFF_MISC = OFF_BAR + NBAR * 8;           // TMEM address, abort flag
+    static constexpr int SMEM = OFF_MISC + 16;
+    // barriers
+    static constexpr int G1 = 0, G2 = 1, G3 = 2, A1 = 3, A2V = 4, A2F = 5, A3 = 6, D1RD = 7, FULL = 8, FREE = 10,
+                         DRAIN = 12;
+    __host__ __device__ static constexpr int bar_count(int b) {
+        return (b == G1 || b == G2 || b == G3 || b == DRAIN || b == FULL || b == FULL + 1) ? 1 : CW * 32;
+    }
 };
-static_assert(TcShape<4>::COLS_USED <= 512, "TMEM budget");
-static_assert(TcShape<1>::N2 >= n_basis(1) && TcShape<4>::N2 >= n_basis(4), "GEMM2 N covers the basis");
+static_assert(Tc<3>::COLS_USED <= 512 && Tc<2>::COLS_USED <= 512 && Tc<1>::COLS_USED <= 256, "TMEM budget");
+static_assert(Tc<3>::SMEM <= 227 * 1024, "shared memory budget");
+static_assert(4 * Tc<3>::N1V <= 8 * Tc<3>::K2V && 4 * Tc<1>::N1V <= 8 * Tc<1>::K2V, "D1 inside the A2 region");
+static_assert(Tc<3>::FW >= Tc<3>::FMAX && Tc<2>::FW >= Tc<2>::FMAX && Tc<1>::FW >= Tc<1>::FMAX, "face slots");
+static_assert(4 * Tc<3>::BW <= Tc<3>::N2V, "GEMM2 N covers the basis");
 
 template <int P>
-struct TArgs {
-    using S = TcShape<P>;
+struct TcArgs {
+    using T = Tc<P>;
     StageArgs s;
-    NbrOps<P> nb;
-    float b1[2][S::N1 * S::KP];  // GEMM1 B, hi and lo: row n = point slot, k = basis function
-    float b2[2][S::N2 * S::K2];  // GEMM2 B, hi and lo: row i = basis function, k = flux slot
-    float wq[S::NQ];
-    float wf[S::NFQ];
+    float b1[2][T::N1V * T::KP];   // GEMM1 B, hi and lo: row = point slot, k = basis function
+    float b2[2][T::N2V * T::K2V];  // GEMM2 B, hi and lo: row = basis slot, k = flux slot
+    float wq[T::NQ];
+    float wf[T::NFQ];
+    float c0;                      // the (constant) first basis function
+    long long wait_limit;          // polls of one bounded wait
 };
 
-// shared memory: A1 [2][4][TILE * KP] | B1 [2][N1 * KP] | B2 [2][N2 * K2] | staged inputs
-//                [2][TILE * NB] (uhi, d; bulk-copied) | U tile [TILE][STR] | neighbour-face
-//                operators | dt [TILE] | 3 mbarriers | TMEM address
+// Element row le, basis function i (all four variables) of the stage state in a tile's input
+// buffer: uhi (+ din), or the FP32 rounding of u^n (+ din) in stage 3 -- the same numbers the
+// CUDA-core forms stage.
 template <int P>
-__host__ __device__ constexpr int tc_smem_floats() {
-    using S = TcShape<P>;
-    return 8 * TILE * S::KP + 2 * S::N1 * S::KP + 2 * S::N2 * S::K2 + 2 * TILE * S::NB + TILE * stage_stride<P>() +
-           stage_op_floats<P, false>() + TILE + 8;
-}
-
-static __device__ int g_tc_timeout;  // set when a bounded mbarrier wait gave up (never expected)
-
-// Traces of face f's neighbour at this face's points, from the neighbour's coefficients
-// (independent of GEMM1, so they are formed while it runs).
-template <int P, bool BND>
-__device__ __forceinline__ void tc_face_nbr(const TArgs<P>& ka, const float* sOp, const ElemConn& C, int f,
-                                            float (&Un)[P + 1][4]) {
-    using S = TcShape<P>;
-    constexpr int NP = S::NP, NFQ = S::NFQ, NB = S::NB, NFQP = NbrOps<P>::NFQP;
-    const StageArgs& s = ka.s;
-#pragma unroll
-    for (int k = 0; k < NFQ; ++k)
-#pragma unroll
-        for (int v = 0; v < NV; ++v) Un[k][v] = 0.f;
-    const int nb = C.nbr[f];
-    if (BND && nb < 0) return;
-    const int fl = (C.flags >> (4 * f)) & 15;
-    const int nf = fl & 3;
-    const bool rev = (fl >> 2) & 1;
-    const float* op = sOp + nf * NP * NFQP;
-#pragma unroll
-    for (int i = 0; i < NP; ++i) {
-        float c[4];
-        load_row_f32<NB>(s.uhi, s.din, nb, i, c);
-        float w[NFQP];
-#pragma unroll
-        for (int k4 = 0; k4 < NFQP; k4 += 4) {
-            const float4 t = *reinterpret_cast<const float4*>(op + i * NFQP + k4);
-            w[k4] = t.x; w[k4 + 1] = t.y; w[k4 + 2] = t.z; w[k4 + 3] = t.w;
-        }
-#pragma unroll
-        for (int k = 0; k < NFQ; ++k) fma4(w[k], c, Un[k]);
+__device__ __forceinline__ float4 tc_state(const unsigned char* raw, int stage, bool din, int le, int i) {
+    using T = Tc<P>;
+    const int off = le * T::NB + 4 * i;
+    float4 a;
+    if (stage == 3) {
+        const double2* u = reinterpret_cast<const double2*>(raw) + off / 2;
+        const double2 x = u[0], y = u[1];
+        a = make_float4(f64_to_f32_bits(x.x), f64_to_f32_bits(x.y), f64_to_f32_bits(y.x), f64_to_f32_bits(y.y));
+    } else {
+        a = reinterpret_cast<const float4*>(raw)[off / 4];
     }
-#pragma unroll
-    for (int j = 0; j < NFQ / 2; ++j)
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-            const float a = Un[j][v], b = Un[NFQ - 1 - j][v];
-            Un[j][v] = rev ? b : a;
-            Un[NFQ - 1 - j][v] = rev ? a : b;
-        }
+    if (din) {
+        const float4 d = reinterpret_cast<const float4*>(raw + T::RD_OFF)[off / 4];
+        a = make_float4(__fadd_rn(a.x, d.x), __fadd_rn(a.y, d.y), __fadd_rn(a.z, d.z), __fadd_rn(a.w, d.w));
+    }
+    return a;
 }
 
-// H' = -(w_j h_F / (2|J|)) * numerical flux at the points of face f, written to A2 (hi, lo).
-// Own traces come from D1; Un are the neighbour traces (unused on boundary faces).
-template <int P, bool BND>
-__device__ __forceinline__ void tc_face_flux(const TArgs<P>& ka, uint32_t tl, const ElemGeomF& G, const ElemConn& C,
-                                             int f, const float (&Un)[P + 1][4]) {
-    using S = TcShape<P>;
-    constexpr int NFQ = S::NFQ;
+// x at (row le, basis i) of variable v's GEMM1 A operand, split hi/lo (K-major, no swizzle)
+__device__ __forceinline__ void tc_put_a(float* sA, int v, int le, int i, float x) {
+    float hi, lo;
+    tc::split3(x, hi, lo);
+    const int o = tc::canon_off(le, i, 16);
+    sA[v * TILE * 16 + o] = hi;
+    sA[(4 + v) * TILE * 16 + o] = lo;
+}
+
+// GEMM1 / GEMM3: per variable D[:, v N1V + n] = sum_i A_v[:, i] B1[n, i] (3xTF32).  One routine
+// for both, so that the traces a stage writes equal the next stage's own-face values bit for bit.
+template <int P>
+__device__ __forceinline__ void tc_issue_interp(uint32_t a_smem, uint32_t b1_smem, uint32_t d_tmem) {
+    using T = Tc<P>;
+    constexpr uint32_t id = tc::idesc_tf32(128, T::N1V);
+    constexpr uint32_t SBO = (T::KP / 4) * 128;
+    const uint32_t b_hi = b1_smem, b_lo = b1_smem + T::N1V * T::KP * 4;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        const uint32_t a_hi = a_smem + v * TILE * T::KP * 4, a_lo = a_smem + (4 + v) * TILE * T::KP * 4;
+        const uint32_t d = d_tmem + v * T::N1V;
+#pragma unroll
+        for (int ks = 0; ks < T::KP / 8; ++ks) {
+            tc::mma_ss(d, tc::smem_desc(a_lo + ks * 256, 128, SBO), tc::smem_desc(b_hi + ks * 256, 128, SBO), id, ks > 0);
+            tc::mma_ss(d, tc::smem_desc(a_hi + ks * 256, 128, SBO), tc::smem_desc(b_lo + ks * 256, 128, SBO), id, true);
+            tc::mma_ss(d, tc::smem_desc(a_hi + ks * 256, 128, SBO), tc::smem_desc(b_hi + ks * 256, 128, SBO), id, true);
+        }
+    }
+}
+
+// GEMM2 over the K steps [ks0, ks1) of every variable (A2 from TMEM); ks0 == 0 starts D2.
+template <int P>
+__device__ __forceinline__ void tc_issue_proj(uint32_t tm, uint32_t b2_smem, int ks0, int ks1) {
+    using T = Tc<P>;
+    constexpr uint32_t id = tc::idesc_tf32(128, T::N2V);
+    constexpr uint32_t SBO = (T::K2V / 4) * 128;
+    const uint32_t b_hi = b2_smem, b_lo = b2_smem + T::N2V * T::K2V * 4;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        const uint32_t d = tm + T::COL_D2 + v * T::N2V;
+        for (int ks = ks0; ks < ks1; ++ks) {
+            const uint32_t a_hi = tm + T::COL_A2 + v * T::K2V + ks * 8;
+            const uint32_t a_lo = tm + T::COL_A2 + 4 * T::K2V + v * T::K2V + ks * 8;
+            tc::mma_ts(d, a_lo, tc::smem_desc(b_hi + ks * 256, 128, SBO), id, ks > 0);
+            tc::mma_ts(d, a_hi, tc::smem_desc(b_lo + ks * 256, 128, SBO), id, true);
+            tc::mma_ts(d, a_hi, tc::smem_desc(b_hi + ks * 256, 128, SBO), id, true);
+        }
+    }
+}
+
+// Traces of one tile's next stage state at thread k's face points: fmaf(c0, S_0, D3) (the same
+// operation as the own-face values of the next stage), written to s.tout; with ghost blocks
+// (GHOST), a boundary face's block gets the ghost state of each trace point.  s0: S_0 of the
+// element's next stage state.
+template <int P, bool GHOST>
+__device__ __forceinline__ void tc_traces_out(const TcArgs<P>& ka, uint32_t tl, const float (&s0)[4], int e, bool act,
+                                              int k) {
+    using T = Tc<P>;
+    constexpr int NFQ = T::NFQ, FQ = T::FQ, FW = T::FW, TRF = trace_floats<P>();
     const StageArgs& s = ka.s;
-    float Uo[NFQ][4];
+    float d3[NV][FW];
 #pragma unroll
-    for (int j = 0; j < NFQ; ++j)
-#pragma unroll
-        for (int v = 0; v < NV; ++v) tc::ld1(tl + v * S::N1 + S::NQ4 + f * NFQ + j, Uo[j][v]);
-    const int nb = C.nbr[f];
-    const float nx = G.n[f][0], ny = G.n[f][1], hF = G.h[f];
-    const float gamma = s.gamma;
-    const bool interior = !BND || nb >= 0;
+    for (int v = 0; v < NV; ++v) tc::ldn<FW>(tl + T::COL_D3 + v * T::N1V + k * T::DW + T::VW, d3[v]);
     tc::wait_ld();
-    const float inv_j = __frcp_rn(G.detJ);
-    float Hh[NFQ][4], Hl[NFQ][4];
+    if (!act) return;
 #pragma unroll
-    for (int j = 0; j < NFQ; ++j) {
-        float H[4] = {0.f, 0.f, 0.f, 0.f};
-        if (interior) {
-            rusanov<float>(Uo[j], Un[j], nx, ny, gamma, H);
-        } else if (nb != NBR_SKIP) {
-            const BCSlot bc = s.bc[-1 - nb];
-            float Ub[4];
-            if (inviscid_ghost<float>(bc, Uo[j], nx, ny, gamma, Ub)) rusanov<float>(Uo[j], Ub, nx, ny, gamma, H);
+    for (int r = 0; r < FW; ++r) {
+        const int fp = k + T::KT * r;
+        if (fp >= FQ) break;
+        float U[4] = {fmaf(ka.c0, s0[0], d3[0][r]), fmaf(ka.c0, s0[1], d3[1][r]), fmaf(ka.c0, s0[2], d3[2][r]),
+                      fmaf(ka.c0, s0[3], d3[3][r])};
+        *reinterpret_cast<float4*>(s.tout + (size_t)e * TRF + fp * NV) = make_float4(U[0], U[1], U[2], U[3]);
+        if (GHOST && s.ghost_bc) {
+            const int f = fp / NFQ, jp = fp - f * NFQ;
+            const int nb = s.conn[e].nbr[f];
+            if (nb >= s.ne) {
+                const BCSlot bc = s.bc[s.ghost_bc[nb - s.ne]];
+                const float nx = s.geom[e].n[f][0], ny = s.geom[e].n[f][1];
+                float Ub[4];
+                inviscid_ghost<float>(bc, U, nx, ny, s.gamma, Ub);
+                *reinterpret_cast<float4*>(s.tout + (size_t)nb * TRF + jp * NV) = make_float4(Ub[0], Ub[1], Ub[2], Ub[3]);
+            }
         }
-        const float w = -ka.wf[j] * hF * 0.5f * inv_j;
-#pragma unroll
-        for (int v = 0; v < NV; ++v) tc::split3(w * H[v], Hh[j][v], Hl[j][v]);
     }
-    __syncwarp();
-#pragma unroll
-    for (int j = 0; j < NFQ; ++j)
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-            const uint32_t col = 2 * S::NQ4 + f * NFQ + j;
-            tc::st1(tl + S::A2 + v * S::K2 + col, Hh[j][v]);
-            tc::st1(tl + S::A2 + (4 + v) * S::K2 + col, Hl[j][v]);
-        }
 }
 
-template <int P, bool BND>
-__global__ void __launch_bounds__(2 * TILE, 1) stage_tc_kernel(const __grid_constant__ TArgs<P> ka) {
-    using S = TcShape<P>;
-    constexpr int NP = S::NP, NQ = S::NQ, NB = S::NB, KP = S::KP, STR = stage_stride<P>(), NB4 = NB / 4;
-    constexpr int OPF = stage_op_floats<P, false>();
-    constexpr long WAIT_LIMIT = 1L << 24;
-    const StageArgs& s = ka.s;
-    extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
-    float* sA1 = reinterpret_cast<float*>(tc_smem_raw);
-    float* sB1 = sA1 + 8 * TILE * KP;
-    float* sB2 = sB1 + 2 * S::N1 * KP;
-    float* sIn = sB2 + 2 * S::N2 * S::K2;  // [2][TILE * NB]: the next tile's uhi and d, bulk-copied
-    float* sU = sIn + 2 * TILE * NB;
-    float* sOp = sU + TILE * STR;
-    float* sDt = sOp + OPF;
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(sDt + TILE);  // GEMM1, GEMM2, input copy
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 3);
-
-    const int t = threadIdx.x, warp = t >> 5;
-    const int e = t & (TILE - 1), half = t >> 7;  // element (= TMEM lane), half
-    for (int k = t; k < 2 * S::N1 * KP; k += S::THREADS) sB1[k] = (&ka.b1[0][0])[k];
-    for (int k = t; k < 2 * S::N2 * S::K2; k += S::THREADS) sB2[k] = (&ka.b2[0][0])[k];
-    for (int k = t; k < OPF; k += S::THREADS) sOp[k] = (&ka.nb.phi[0][0][0])[k];
+// Shared set-up of both kernels: operands B into shared memory, A zeroed (its columns i = 0
+// and i >= NP stay zero), barriers, TMEM.  Returns the TMEM base address.
+template <int P>
+__device__ __forceinline__ uint32_t tc_setup(const TcArgs<P>& ka, unsigned char* smem) {
+    using T = Tc<P>;
+    const int t = threadIdx.x;
+    float* sA = reinterpret_cast<float*>(smem + T::OFF_A);
+    float* sB1 = reinterpret_cast<float*>(smem + T::OFF_B1);
+    float* sB2 = reinterpret_cast<float*>(smem + T::OFF_B2);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::OFF_BAR);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + T::OFF_MISC);
+    for (int x = t; x < 8 * TILE * T::KP; x += T::THREADS) sA[x] = 0.f;
+    for (int x = t; x < 2 * T::N1V * T::KP; x += T::THREADS) sB1[x] = (&ka.b1[0][0])[x];
+    for (int x = t; x < 2 * T::N2V * T::K2V; x += T::THREADS) sB2[x] = (&ka.b2[0][0])[x];
     if (t == 0) {
-        tc::mbar_init(&mbar[0], 1);
-        tc::mbar_init(&mbar[1], 1);
-        tc::mbar_init(&mbar[2], 1);
+        for (int b = 0; b < T::NBAR; ++b) tc::mbar_init(&bar[b], T::bar_count(b));
+        *reinterpret_cast<volatile int*>(smem + T::OFF_MISC + 4) = 0;
     }
-    if (warp == 0) tc::tmem_alloc(tslot, S::COLS);
+    if ((t >> 5) == T::CW) tc::tmem_alloc(tslot, T::COLS);
+    tc::fence_async_smem();  // A and B as written here, for the tensor cores
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
-    const uint32_t tm = *tslot;
-    const uint32_t tl = tm + ((uint32_t)(32 * (warp & 3)) << 16);  // this warp's lane quadrant
-    // A2 columns past the last flux slot are read by GEMM2 and never written per tile
-    for (int c = 2 * S::NQ4 + S::FQ + half; c < S::K2; c += 2)
-#pragma unroll
-        for (int v = 0; v < 8; ++v) tc::st1(tl + S::A2 + v * S::K2 + c, 0.f);
-    tc::wait_st();
+    return *tslot;
+}
 
-    uint32_t phase = 0;
-    bool failed = false;
-    const int ntiles = (s.ne + TILE - 1) / TILE;
-    // bulk copy of a tile's inputs into sIn, completing on mbar[2]
-    auto stage_in = [&](int tile) {
-        const int n0 = tile * TILE, nn = min(TILE, s.ne - n0);
-        const uint32_t bytes = (uint32_t)(nn * NB * sizeof(float));
-        tc::mbar_expect_tx(&mbar[2], s.din ? 2 * bytes : bytes);
-        tc::bulk_g2s(sIn, s.uhi + (size_t)n0 * NB, bytes, &mbar[2]);
-        if (s.din) tc::bulk_g2s(sIn + TILE * NB, s.din + (size_t)n0 * NB, bytes, &mbar[2]);
-    };
-    if (t == 0 && (int)blockIdx.x < ntiles) stage_in(blockIdx.x);
-    bool copy_pending = (int)blockIdx.x < ntiles;
-    uint32_t copy_parity = 0;  // the phase of mbar[2] the pending copy completes
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, phase ^= 1) {
-        const int e0 = tile * TILE;
-        const int nloc = min(TILE, s.ne - e0);
-        const bool active = e < nloc;
-        const int ee = active ? e0 + e : e0;  // inactive lanes work on a valid element; results unused
-        if (t == 0 && s.stage == 3)  // this tile's FP64 state, read in the stage combination
-            tc::prefetch_l2(s.u64 + (size_t)e0 * NB, (uint32_t)(nloc * NB * sizeof(double)));
-        // the tile's inputs, bulk-copied into sIn while the previous tile was computed
-        const bool okin = tc::mbar_wait(&mbar[2], phase, WAIT_LIMIT);
-        if (__syncthreads_or(!okin)) {
-            failed = true;
-            break;
-        }
-        copy_pending = false;
-        {   // stage state of the tile, rows = elements
-            const float4* uh = reinterpret_cast<const float4*>(sIn);
-            const float4* dd = s.din ? reinterpret_cast<const float4*>(sIn + TILE * NB) : nullptr;
-            for (int g = t; g < nloc * NB4; g += S::THREADS) {
-                float4 a = uh[g];
-                if (dd) {
-                    const float4 b = dd[g];
-                    a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w;
-                }
-                const int le = g / NB4, k = 4 * (g - le * NB4);
-                *reinterpret_cast<float4*>(sU + le * STR + k) = a;
-            }
-        }
-        __syncthreads();
-        if (tile + (int)gridDim.x < ntiles) {  // sIn is free: start the next tile's copy
-            if (t == 0) {
-                tc::fence_async_smem();
-                stage_in(tile + gridDim.x);
-            }
-            copy_pending = true;
-            copy_parity = phase ^ 1;
-        }
-        // A1: the split state in the K-major operand layout, variables 2*half and 2*half + 1
-#pragma unroll
-        for (int vv = 0; vv < 2; ++vv) {
-            const int v = 2 * half + vv;
-#pragma unroll
-            for (int k4 = 0; k4 < KP; k4 += 4) {
-                float hi[4], lo[4];
-#pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    const int i = k4 + c;
-                    const float x = (i < NP && active) ? sU[e * STR + i * NV + v] : 0.f;
-                    tc::split3(x, hi[c], lo[c]);
-                }
-                const int off = tc::canon_off(e, k4, KP);
-                *reinterpret_cast<float4*>(sA1 + v * TILE * KP + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-                *reinterpret_cast<float4*>(sA1 + (4 + v) * TILE * KP + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
-            }
-        }
-        tc::fence_async_smem();
-        tc::fence_before();
-        __syncthreads();
-        if (t == 0) {  // GEMM1: per variable, KP/8 steps of three TF32 products
-            tc::fence_after();
-            constexpr uint32_t id = tc::idesc_tf32(128, S::N1);
-            constexpr uint32_t SBO = (KP / 4) * 128;
-            const uint32_t b_hi = tc::smem_u32(sB1), b_lo = tc::smem_u32(sB1 + S::N1 * KP);
-#pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                const uint32_t a_hi = tc::smem_u32(sA1 + v * TILE * KP), a_lo = tc::smem_u32(sA1 + (4 + v) * TILE * KP);
-#pragma unroll
-                for (int ks = 0; ks < KP / 8; ++ks) {
-                    const uint32_t d = tm + v * S::N1;
-                    tc::mma_ss(d, tc::smem_desc(a_lo + ks * 256, 128, SBO), tc::smem_desc(b_hi + ks * 256, 128, SBO), id, ks > 0);
-                    tc::mma_ss(d, tc::smem_desc(a_hi + ks * 256, 128, SBO), tc::smem_desc(b_lo + ks * 256, 128, SBO), id, true);
-                    tc::mma_ss(d, tc::smem_desc(a_hi + ks * 256, 128, SBO), tc::smem_desc(b_hi + ks * 256, 128, SBO), id, true);
-                }
-            }
-            tc::commit(&mbar[0]);
-        }
-        // neighbour traces while GEMM1 runs: half 0 face 0, half 1 faces 1 and 2
-        const ElemGeomF G = s.geom[ee];
-        const ElemConn C = s.conn[ee];
-        float UnA[P + 1][4], UnB[P + 1][4];
-        if (half == 0) {
-            tc_face_nbr<P, BND>(ka, sOp, C, 0, UnA);
-        } else {
-            tc_face_nbr<P, BND>(ka, sOp, C, 1, UnA);
-            tc_face_nbr<P, BND>(ka, sOp, C, 2, UnB);
-        }
-        const bool ok1 = tc::mbar_wait(&mbar[0], phase, WAIT_LIMIT);
-        if (__syncthreads_or(!ok1)) {
-            failed = true;
-            break;
-        }
+// Teardown: every thread arrives here; then TMEM is freed.
+template <int P>
+__device__ __forceinline__ void tc_teardown(uint32_t tm) {
+    using T = Tc<P>;
+    tc::fence_before();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == T::CW) {
         tc::fence_after();
+        tc::tmem_dealloc(tm, T::COLS);
+    }
+}
 
-        // ---- fluxes between the GEMMs
-        if (half == 0) {
-            if (active && s.dt_inst) sDt[e] = s.dt_inst[__float_as_int(G.pad)];
-            __syncwarp();
-            const float A00 = G.A[0], A01 = G.A[1], A10 = G.A[2], A11 = G.A[3];
+// Bulk copy of tile `tile`'s inputs into input buffer b (issuing thread only).
+template <int P>
+__device__ __forceinline__ void tc_load_tile(const StageArgs& s, unsigned char* raw, uint64_t* full, int tile,
+                                             bool state_only) {
+    using T = Tc<P>;
+    const int e0 = tile * TILE, nloc = min(TILE, s.ne - e0);
+    const uint32_t bs = (uint32_t)nloc * T::NB * (s.stage == 3 ? 8u : 4u);
+    const uint32_t bd = (s.din && !state_only) ? (uint32_t)nloc * T::NB * 4u : 0u;
+    const uint32_t bg = state_only ? 0u : (uint32_t)nloc * 64u, bc = state_only ? 0u : (uint32_t)nloc * 16u;
+    tc::mbar_expect_tx(full, bs + bd + bg + bc);
+    if (s.stage == 3) tc::bulk_g2s(raw, s.u64 + (size_t)e0 * T::NB, bs, full);
+    else tc::bulk_g2s(raw, s.uhi + (size_t)e0 * T::NB, bs, full);
+    if (bd) tc::bulk_g2s(raw + T::RD_OFF, s.din + (size_t)e0 * T::NB, bd, full);
+    if (bg) tc::bulk_g2s(raw + T::RG_OFF, s.geom + e0, bg, full);
+    if (bc) tc::bulk_g2s(raw + T::RC_OFF, s.conn + e0, bc, full);
+}
+
+template <int P, bool GHOST>
+__global__ void __launch_bounds__(Tc<P>::THREADS, 1) stage_tc_kernel(const __grid_constant__ TcArgs<P> ka) {
+    using T = Tc<P>;
+    constexpr int NP = T::NP, NQ = T::NQ, NFQ = T::NFQ, FQ = T::FQ, NB = T::NB, KT = T::KT;
+    constexpr int VW = T::VW, FW = T::FW, DW = T::DW, BW = T::BW, N1V = T::N1V, K2V = T::K2V;
+    constexpr int TRF = trace_floats<P>();
+    constexpr long long DRAIN_LIMIT = 1LL << 26;
+    const StageArgs& s = ka.s;
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    float* sA = reinterpret_cast<float*>(tc_smem + T::OFF_A);
+    unsigned char* sRaw = tc_smem + T::OFF_RAW;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(tc_smem + T::OFF_BAR);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tc_smem + T::OFF_MISC + 4);
+
+    const uint32_t tm = tc_setup<P>(ka, tc_smem);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int all_tiles = s.ntile > 0 ? s.ntile : (s.ne + TILE - 1) / TILE;
+    const int n = (int)blockIdx.x < all_tiles ? (all_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+    auto tile_of = [&](int j) { return s.tile0 + (int)blockIdx.x + j * (int)gridDim.x; };
+    const long long LIM = ka.wait_limit;
+    auto wait = [&](int b, int parity) {
+        const bool ok = tc::mbar_wait_or_abort(&bar[b], (uint32_t)(parity & 1), (long)LIM, abort_flag);
+        if (!ok && s.status) atomicOr(s.status, 2);
+        return ok;
+    };
+    const uint32_t sA_u = tc::smem_u32(sA), sB1_u = tc::smem_u32(tc_smem + T::OFF_B1),
+                   sB2_u = tc::smem_u32(tc_smem + T::OFF_B2);
+
+    if (warp == T::CW) {
+        // ------------------------------------------------ copies and MMAs (one thread)
+        if (lane == 0) {
+            int issued[2] = {0, 0};
+            auto load = [&](int j) {
+                tc_load_tile<P>(s, sRaw + (j & 1) * T::RAWB, &bar[T::FULL + (j & 1)], tile_of(j), false);
+                ++issued[j & 1];
+            };
+            if (n > 0) load(0);
+            if (n > 1) load(1);
+            bool ok = n > 0 && wait(T::A1, 0);
+            if (ok) {
+                tc::fence_after();
+                tc_issue_interp<P>(sA_u, sB1_u, tm + T::COL_D1);
+                tc::commit(&bar[T::G1]);
+            }
+            for (int j = 0; ok && j < n; ++j) {
+                if (!(ok = wait(T::A2V, j))) break;
+                tc::fence_after();
+                tc_issue_proj<P>(tm, sB2_u, 0, T::VOLK / 8);
+                if (!(ok = wait(T::A2F, j))) break;
+                tc::fence_after();
+                tc_issue_proj<P>(tm, sB2_u, T::VOLK / 8, K2V / 8);
+                tc::commit(&bar[T::G2]);
+                if (j + 1 < n) {  // GEMM1 of the next tile, into the A2 region once GEMM2 has read it
+                    if (!(ok = wait(T::A1, j + 1) && wait(T::G2, j))) break;
+                    tc::fence_after();
+                    tc_issue_interp<P>(sA_u, sB1_u, tm + T::COL_D1);
+                    tc::commit(&bar[T::G1]);
+                }
+                if (!(ok = wait(T::A3, j))) break;
+                tc::fence_after();
+                tc_issue_interp<P>(sA_u, sB1_u, tm + T::COL_D3);
+                tc::commit(&bar[T::G3]);
+                if (j + 2 < n) {  // the input buffer of tile j is free once its stage combination is done
+                    if (!(ok = wait(T::FREE + (j & 1), j >> 1))) break;
+                    tc::fence_async_smem();
+                    load(j + 2);
+                }
+            }
+            // drain: every MMA and every bulk copy issued has completed before TMEM is freed
+            tc::commit(&bar[T::DRAIN]);
+            tc::mbar_wait(&bar[T::DRAIN], 0, (long)DRAIN_LIMIT);
+            for (int b = 0; b < 2; ++b)
+                if (issued[b]) tc::mbar_wait(&bar[T::FULL + b], (uint32_t)((issued[b] - 1) & 1), (long)DRAIN_LIMIT);
+        }
+        __syncwarp();
+    } else {
+        // ------------------------------------------------ compute warps
+        const int qd = warp & 3, k = warp >> 2, le = 32 * qd + lane;
+        const uint32_t tl = tm + ((uint32_t)(32 * qd) << 16);  // this warp's TMEM lane quadrant
+        const float c0 = ka.c0, gamma = s.gamma;
+        const bool has_din = s.din != nullptr;
+        auto arrive = [&](int b) { tc::mbar_arrive(&bar[b]); };
+        // the stage state of tile j (input buffer j & 1), split into the GEMM1 operand
+        auto split_state = [&](int j) {
+            const unsigned char* raw = sRaw + (j & 1) * T::RAWB;
 #pragma unroll
-            for (int q0 = 0; q0 < S::NQ4; q0 += 4) {
-                float Uv[4][4];
+            for (int r = 0; r < BW; ++r) {
+                const int i = k + KT * r;
+                if (i >= 1 && i < NP) {
+                    const float4 a = tc_state<P>(raw, s.stage, has_din, le, i);
+                    tc_put_a(sA, 0, le, i, a.x);
+                    tc_put_a(sA, 1, le, i, a.y);
+                    tc_put_a(sA, 2, le, i, a.z);
+                    tc_put_a(sA, 3, le, i, a.w);
+                }
+            }
+            tc::fence_async_smem();
+        };
+        bool ok = true;
+        float sn0[4] = {0.f, 0.f, 0.f, 0.f};  // S_0 of the previous tile's next stage state (its traces)
+        if (n > 0 && (ok = wait(T::FULL, 0))) {
+            split_state(0);
+            arrive(T::A1);
+        }
+        for (int j = 0; ok && j < n; ++j) {
+            const int e0 = tile_of(j) * TILE, nloc = min(TILE, s.ne - e0);
+            const bool act = le < nloc;
+            const int e = e0 + le;
+            const unsigned char* raw = sRaw + (j & 1) * T::RAWB;
+            const ElemGeomF* G = reinterpret_cast<const ElemGeomF*>(raw + T::RG_OFF) + le;
+            const ElemConn C = reinterpret_cast<const ElemConn*>(raw + T::RC_OFF)[le];
+            const float4 s0 = tc_state<P>(raw, s.stage, has_din, le, 0);
+            const float S0[4] = {s0.x, s0.y, s0.z, s0.w};
+            // the neighbour trace blocks this thread reads in (c): into L2 now
+            auto nbr_trace = [&](int r) -> const float* {
+                const int fp = k + KT * r, f = fp / NFQ, jp = fp - f * NFQ;
+                const int fl = (C.flags >> (4 * f)) & 15;
+                const int pt = ((fl >> 2) & 1) ? NFQ - 1 - jp : jp;
+                return s.tin + (size_t)C.nbr[f] * TRF + ((fl & 3) * NFQ + pt) * NV;
+            };
 #pragma unroll
-                for (int v = 0; v < NV; ++v) tc::ld4(tl + v * S::N1 + q0, Uv[v]);
-                tc::wait_ld();
-                float rh[4][4], rl[4][4], sh[4][4], sl[4][4];  // [variable][point]
+            for (int r = 0; r < FW; ++r)
+                if (act && k + KT * r < FQ) prefetch_l2_line(nbr_trace(r));
+            // (a) D1(j): the stage state at this thread's points (fluctuation part)
+            if (!(ok = wait(T::G1, j))) break;
+            tc::fence_after();
+            float d1[NV][DW], q0[NV];
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int q = q0 + j;
-                    if (q < NQ) {
-                        const float U[4] = {Uv[0][j], Uv[1][j], Uv[2][j], Uv[3][j]};
-                        float F[4], Gf[4], u, vv, pp, ri;
-                        euler_flux<float>(U, s.gamma - 1.0f, F, Gf, u, vv, pp, ri);
+            for (int v = 0; v < NV; ++v) {
+                tc::ldn<DW>(tl + T::COL_D1 + v * N1V + k * DW, d1[v]);
+                tc::ld1(tl + T::COL_D1 + v * N1V, q0[v]);  // volume point 0 (thread 0's first slot)
+            }
+            tc::wait_ld();
+            tc::fence_before();
+            arrive(T::D1RD);  // the A2 region (where D1 lies) may be overwritten once all have read it
+            const float A00 = G->A[0], A01 = G->A[1], A10 = G->A[2], A11 = G->A[3];
+            float Fb[4], Gb[4];  // the flux at volume point 0: the constant the fluxes deviate from
+            {
+                const float U[4] = {fmaf(c0, S0[0], q0[0]), fmaf(c0, S0[1], q0[1]), fmaf(c0, S0[2], q0[2]),
+                                    fmaf(c0, S0[3], q0[3])};
+                float u, vv, pp, ri;
+                euler_flux<float>(U, gamma - 1.0f, Fb, Gb, u, vv, pp, ri);
+            }
+            if (!(ok = wait(T::D1RD, j))) break;
+            tc::fence_after();
+            // (b) volume fluxes -> A2 volume columns k 2VW + 2r (Fr') and k 2VW + 2r + 1 (Fs') of each
+            //     variable, stored point by point
 #pragma unroll
-                        for (int v = 0; v < NV; ++v) {
-                            tc::split3(ka.wq[q] * (A00 * F[v] + A10 * Gf[v]), rh[v][j], rl[v][j]);
-                            tc::split3(ka.wq[q] * (A01 * F[v] + A11 * Gf[v]), sh[v][j], sl[v][j]);
-                        }
-                    } else {
+            for (int r = 0; r < VW; ++r) {
+                const int q = k + KT * r;
+                float fr[4] = {0.f, 0.f, 0.f, 0.f}, fs[4] = {0.f, 0.f, 0.f, 0.f};
+                if (q < NQ) {
+                    const float U[4] = {fmaf(c0, S0[0], d1[0][r]), fmaf(c0, S0[1], d1[1][r]),
+                                        fmaf(c0, S0[2], d1[2][r]), fmaf(c0, S0[3], d1[3][r])};
+                    float F[4], Gf[4], u, vv, pp, ri;
+                    euler_flux<float>(U, gamma - 1.0f, F, Gf, u, vv, pp, ri);
+                    const float w = ka.wq[q];
 #pragma unroll
-                        for (int v = 0; v < NV; ++v) rh[v][j] = rl[v][j] = sh[v][j] = sl[v][j] = 0.f;
+                    for (int v = 0; v < NV; ++v) {
+                        const float dF = F[v] - Fb[v], dG = Gf[v] - Gb[v];
+                        fr[v] = w * (A00 * dF + A10 * dG);
+                        fs[v] = w * (A01 * dF + A11 * dG);
                     }
                 }
 #pragma unroll
                 for (int v = 0; v < NV; ++v) {
-                    tc::st4(tl + S::A2 + v * S::K2 + q0, rh[v]);
-                    tc::st4(tl + S::A2 + (4 + v) * S::K2 + q0, rl[v]);
-                    tc::st4(tl + S::A2 + v * S::K2 + S::NQ4 + q0, sh[v]);
-                    tc::st4(tl + S::A2 + (4 + v) * S::K2 + S::NQ4 + q0, sl[v]);
+                    float hi[2], lo[2];
+                    tc::split3(fr[v], hi[0], lo[0]);
+                    tc::split3(fs[v], hi[1], lo[1]);
+                    tc::st2(tl + T::COL_A2 + v * K2V + k * 2 * VW + 2 * r, hi);
+                    tc::st2(tl + T::COL_A2 + 4 * K2V + v * K2V + k * 2 * VW + 2 * r, lo);
                 }
             }
-            tc_face_flux<P, BND>(ka, tl, G, C, 0, UnA);
-        } else {
-            tc_face_flux<P, BND>(ka, tl, G, C, 1, UnA);
-            tc_face_flux<P, BND>(ka, tl, G, C, 2, UnB);
+            tc::wait_st();
+            tc::fence_before();
+            arrive(T::A2V);
+            // (c) face fluxes -> A2 face columns VOLK + k FW + r, stored point by point
+            {
+                float4 un[FW];
+#pragma unroll
+                for (int r = 0; r < FW; ++r)
+                    un[r] = (act && k + KT * r < FQ) ? __ldg(reinterpret_cast<const float4*>(nbr_trace(r)))
+                                                     : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float inv_j = __frcp_rn(G->detJ);
+#pragma unroll
+                for (int r = 0; r < FW; ++r) {
+                    const int fp = k + KT * r;
+                    float Hd[4] = {0.f, 0.f, 0.f, 0.f};
+                    if (fp < FQ) {
+                        const int f = fp / NFQ, jp = fp - f * NFQ;
+                        const float nx = G->n[f][0], ny = G->n[f][1], hF = G->h[f];
+                        const float Uo[4] = {fmaf(c0, S0[0], d1[0][VW + r]), fmaf(c0, S0[1], d1[1][VW + r]),
+                                             fmaf(c0, S0[2], d1[2][VW + r]), fmaf(c0, S0[3], d1[3][VW + r])};
+                        const float Un[4] = {un[r].x, un[r].y, un[r].z, un[r].w};
+                        float H[4];
+                        rusanov<float>(Uo, Un, nx, ny, gamma, H);
+                        const float w = ka.wf[jp] * hF * 0.5f * inv_j;
+#pragma unroll
+                        for (int v = 0; v < NV; ++v) Hd[v] = -(w * (H[v] - (Fb[v] * nx + Gb[v] * ny)));
+                    }
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) {
+                        float hi, lo;
+                        tc::split3(Hd[v], hi, lo);
+                        tc::st1(tl + T::COL_A2 + v * K2V + T::VOLK + k * FW + r, hi);
+                        tc::st1(tl + T::COL_A2 + 4 * K2V + v * K2V + T::VOLK + k * FW + r, lo);
+                    }
+                }
+                tc::wait_st();
+                tc::fence_before();
+                arrive(T::A2F);
+            }
+            // (d) the traces of tile j - 1 (GEMM3, issued at the end of its iteration)
+            if (j > 0) {
+                if (!(ok = wait(T::G3, j - 1))) break;
+                tc::fence_after();
+                const int ep = tile_of(j - 1) * TILE;
+                tc_traces_out<P, GHOST>(ka, tl, sn0, ep + le, le < min(TILE, s.ne - ep), k);
+            }
+            // (e) the stage state of tile j + 1 into the GEMM1 operand
+            if (j + 1 < n) {
+                if (!(ok = wait(T::FULL + ((j + 1) & 1), (j + 1) >> 1))) break;
+                split_state(j + 1);
+                tc::fence_before();
+                arrive(T::A1);
+            }
+            // (f) the M^-1-scaled residual, the stage combination and the next stage state
+            if (!(ok = wait(T::G2, j))) break;
+            tc::fence_after();
+            float d2[NV][BW], r0[NV];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                tc::ldn<BW>(tl + T::COL_D2 + v * T::N2V + k * BW, d2[v]);
+                tc::ld1(tl + T::COL_D2 + v * T::N2V, r0[v]);  // basis function 0 (thread 0's first slot)
+            }
+            tc::wait_ld();
+            bool bad = false;
+            const float dt = s.dt;
+            // stage combination of basis function i (residual R): the next stage state into Sn; the
+            // outputs are written when `write` (stage_combine_next's arithmetic)
+            auto combine = [&](int i, const float (&R)[4], bool write, float (&Sn)[4]) {
+                const int off = le * NB + 4 * i;             // value index in the tile buffers
+                const size_t g = (size_t)e * NB + 4 * i;     // and in the global arrays
+                float4 dv = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (has_din) dv = reinterpret_cast<const float4*>(raw + T::RD_OFF)[off / 4];
+                if (s.stage <= 2) {
+                    const float4 uh = reinterpret_cast<const float4*>(raw)[off / 4];
+                    const float4 o = s.stage == 1
+                                         ? make_float4(dt * R[0], dt * R[1], dt * R[2], dt * R[3])
+                                         : make_float4(0.25f * (dv.x + dt * R[0]), 0.25f * (dv.y + dt * R[1]),
+                                                       0.25f * (dv.z + dt * R[2]), 0.25f * (dv.w + dt * R[3]));
+                    if (write) *reinterpret_cast<float4*>(s.dout + g) = o;
+                    Sn[0] = __fadd_rn(uh.x, o.x);
+                    Sn[1] = __fadd_rn(uh.y, o.y);
+                    Sn[2] = __fadd_rn(uh.z, o.z);
+                    Sn[3] = __fadd_rn(uh.w, o.w);
+                } else {
+                    const double2* ur = reinterpret_cast<const double2*>(raw) + off / 2;
+                    const double2 ua = ur[0], ub = ur[1];
+                    const float d0 = (2.0f / 3.0f) * (dv.x + dt * R[0]), dd1 = (2.0f / 3.0f) * (dv.y + dt * R[1]);
+                    const float dd2 = (2.0f / 3.0f) * (dv.z + dt * R[2]), dd3 = (2.0f / 3.0f) * (dv.w + dt * R[3]);
+                    const double2 ra = make_double2(ua.x + f32_to_f64_bits(d0), ua.y + f32_to_f64_bits(dd1));
+                    const double2 rb = make_double2(ub.x + f32_to_f64_bits(dd2), ub.y + f32_to_f64_bits(dd3));
+                    Sn[0] = f64_to_f32_bits(ra.x);
+                    Sn[1] = f64_to_f32_bits(ra.y);
+                    Sn[2] = f64_to_f32_bits(rb.x);
+                    Sn[3] = f64_to_f32_bits(rb.y);
+                    if (write) {
+                        reinterpret_cast<double2*>(s.u64 + g)[0] = ra;
+                        reinterpret_cast<double2*>(s.u64 + g)[1] = rb;
+                        *reinterpret_cast<float4*>(s.uhi_out + g) = make_float4(Sn[0], Sn[1], Sn[2], Sn[3]);
+                        bad |= !(finite_bits(ra.x) && finite_bits(ra.y) && finite_bits(rb.x) && finite_bits(rb.y));
+                    }
+                }
+            };
+            // every thread forms S_0 of the next state (the traces need it); thread 0 writes it
+            combine(0, r0, act && k == 0, sn0);
+            float Sn[BW][4];
+#pragma unroll
+            for (int r = 0; r < BW; ++r) {
+                const int i = k + KT * r;
+                if (i >= 1 && i < NP) {
+                    const float R[4] = {d2[0][r], d2[1][r], d2[2][r], d2[3][r]};
+                    combine(i, R, act, Sn[r]);
+                }
+            }
+            if (bad && s.status) atomicOr(s.status, 1);
+            tc::fence_before();
+            arrive(T::FREE + (j & 1));  // this tile's input buffer is no longer read
+            if (j + 1 < n) {  // the GEMM1 operand buffer is free once GEMM1(j + 1) is done
+                if (!(ok = wait(T::G1, j + 1))) break;
+            }
+#pragma unroll
+            for (int r = 0; r < BW; ++r) {
+                const int i = k + KT * r;
+                if (i >= 1 && i < NP) {
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) tc_put_a(sA, v, le, i, Sn[r][v]);
+                }
+            }
+            tc::fence_async_smem();
+            tc::fence_before();
+            arrive(T::A3);
+        }
+        // the traces of the last tile
+        if (ok && n > 0 && (ok = wait(T::G3, n - 1))) {
+            tc::fence_after();
+            const int ep = tile_of(n - 1) * TILE;
+            tc_traces_out<P, GHOST>(ka, tl, sn0, ep + le, le < min(TILE, s.ne - ep), k);
+        }
+    }
+    tc_teardown<P>(tm);
+}
+
+// The traces of the state a step starts from (uhi), with the tensor-core operations of the
+// stage kernel (so that they equal the first stage's own-face values bit for bit).  One tile
+// at a time per CTA: copy, split, GEMM3, traces.
+template <int P, bool GHOST>
+__global__ void __launch_bounds__(Tc<P>::THREADS, 1) tc_trace_init_kernel(const __grid_constant__ TcArgs<P> ka) {
+    using T = Tc<P>;
+    constexpr int NP = T::NP, KT = T::KT, BW = T::BW;
+    const StageArgs& s = ka.s;
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    float* sA = reinterpret_cast<float*>(tc_smem + T::OFF_A);
+    unsigned char* sRaw = tc_smem + T::OFF_RAW;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(tc_smem + T::OFF_BAR);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tc_smem + T::OFF_MISC + 4);
+    const uint32_t tm = tc_setup<P>(ka, tc_smem);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int all_tiles = s.ntile > 0 ? s.ntile : (s.ne + TILE - 1) / TILE;
+    const int n = (int)blockIdx.x < all_tiles ? (all_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+    auto tile_of = [&](int j) { return s.tile0 + (int)blockIdx.x + j * (int)gridDim.x; };
+    auto wait = [&](int b, int parity) {
+        const bool ok = tc::mbar_wait_or_abort(&bar[b], (uint32_t)(parity & 1), (long)ka.wait_limit, abort_flag);
+        if (!ok && s.status) atomicOr(s.status, 2);
+        return ok;
+    };
+    if (warp == T::CW) {
+        if (lane == 0) {
+            int issued = 0;
+            bool ok = true;
+            for (int j = 0; ok && j < n; ++j) {
+                if (j > 0 && !(ok = wait(T::FREE, j - 1))) break;  // the previous tile is done with the buffers
+                tc::fence_async_smem();
+                tc_load_tile<P>(s, sRaw, &bar[T::FULL], tile_of(j), true);
+                ++issued;
+                if (!(ok = wait(T::A3, j))) break;
+                tc::fence_after();
+                tc_issue_interp<P>(tc::smem_u32(sA), tc::smem_u32(tc_smem + T::OFF_B1), tm + T::COL_D3);
+                tc::commit(&bar[T::G3]);
+            }
+            tc::commit(&bar[T::DRAIN]);
+            tc::mbar_wait(&bar[T::DRAIN], 0, 1L << 26);
+            if (issued) tc::mbar_wait(&bar[T::FULL], (uint32_t)((issued - 1) & 1), 1L << 26);
         }
         __syncwarp();
-        tc::wait_st();
-        tc::fence_before();
-        __syncthreads();
-        if (t == 0) {  // GEMM2: A from TMEM, per variable, K2/8 steps of three TF32 products
-            tc::fence_after();
-            constexpr uint32_t id = tc::idesc_tf32(128, S::N2);
-            constexpr uint32_t SBO = (S::K2 / 4) * 128;
-            const uint32_t b_hi = tc::smem_u32(sB2), b_lo = tc::smem_u32(sB2 + S::N2 * S::K2);
+    } else {
+        const int qd = warp & 3, k = warp >> 2, le = 32 * qd + lane;
+        const uint32_t tl = tm + ((uint32_t)(32 * qd) << 16);
+        for (int j = 0; j < n; ++j) {
+            if (!wait(T::FULL, j)) break;
+            const int e0 = tile_of(j) * TILE, nloc = min(TILE, s.ne - e0);
 #pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                const uint32_t d = tm + v * S::N2;
-#pragma unroll
-                for (int ks = 0; ks < S::K2 / 8; ++ks) {
-                    const uint32_t a_hi = tm + S::A2 + v * S::K2 + ks * 8, a_lo = tm + S::A2 + (4 + v) * S::K2 + ks * 8;
-                    tc::mma_ts(d, a_lo, tc::smem_desc(b_hi + ks * 256, 128, SBO), id, ks > 0);
-                    tc::mma_ts(d, a_hi, tc::smem_desc(b_lo + ks * 256, 128, SBO), id, true);
-                    tc::mma_ts(d, a_hi, tc::smem_desc(b_hi + ks * 256, 128, SBO), id, true);
+            for (int r = 0; r < BW; ++r) {
+                const int i = k + KT * r;
+                if (i >= 1 && i < NP) {
+                    const float4 a = tc_state<P>(sRaw, s.stage, false, le, i);
+                    tc_put_a(sA, 0, le, i, a.x);
+                    tc_put_a(sA, 1, le, i, a.y);
+                    tc_put_a(sA, 2, le, i, a.z);
+                    tc_put_a(sA, 3, le, i, a.w);
                 }
             }
-            tc::commit(&mbar[1]);
+            tc::fence_async_smem();
+            tc::fence_before();
+            tc::mbar_arrive(&bar[T::A3]);
+            if (!wait(T::G3, j)) break;
+            tc::fence_after();
+            const float4 z = tc_state<P>(sRaw, s.stage, false, le, 0);
+            const float s0[4] = {z.x, z.y, z.z, z.w};
+            tc_traces_out<P, GHOST>(ka, tl, s0, e0 + le, le < nloc, k);
+            tc::fence_before();
+            tc::mbar_arrive(&bar[T::FREE]);
         }
-        const bool ok2 = tc::mbar_wait(&mbar[1], phase, WAIT_LIMIT);
-        if (__syncthreads_or(!ok2)) {
-            failed = true;
-            break;
-        }
-        tc::fence_after();
-        {   // residual (M^-1 applied) of variables 2*half, 2*half + 1 into the tile rows
-            float r0[16], r1[16];
-            __syncwarp();
-            tc::ld16(tl + (2 * half) * S::N2, r0);
-            tc::ld16(tl + (2 * half + 1) * S::N2, r1);
-            tc::wait_ld();
-            if (active) {
-#pragma unroll
-                for (int i = 0; i < NP; ++i)
-                    *reinterpret_cast<float2*>(sU + e * STR + i * NV + 2 * half) = make_float2(r0[i], r1[i]);
-            }
-        }
-        tc::fence_before();
-        __syncthreads();
-        stage_combine<NB, STR, S::THREADS, (TILE * NB4 + S::THREADS - 1) / S::THREADS>(s, sU, sDt, e0, nloc,
-                                                                                       [](int le) { return le; });
-        __syncthreads();
     }
-    if (failed) {  // a wait gave up: flag it, let outstanding MMAs and copies drain
-        if (t == 0) atomicExch(&g_tc_timeout, 1);
-        tc::mbar_wait(&mbar[0], phase, WAIT_LIMIT);
-        tc::mbar_wait(&mbar[1], phase, WAIT_LIMIT);
-    }
-    if (copy_pending) tc::mbar_wait(&mbar[2], copy_parity, WAIT_LIMIT);
-    tc::fence_before();
-    __syncthreads();
-    if (warp == 0) {
-        tc::fence_after();
-        tc::tmem_dealloc(tm, S::COLS);
-    }
+    tc_teardown<P>(tm);
 }
 
 // host: tf32 rounding (nearest, ties to even) of a finite float
@@ -420,48 +675,65 @@ inline void split3_host(double x, float& hi, float& lo) {
     lo = tf32_round_host((float)(x - (double)hi));
 }
 
+// Host-side operands.  Returns false when the first basis function is not constant (the
+// fluctuation form needs it to be).
 template <int P>
-inline void fill_tc_ops(const OpsHost& h, TArgs<P>& k) {
-    using S = TcShape<P>;
-    constexpr int NP = S::NP, NQ = S::NQ, NFQ = S::NFQ;
-    fill_nbr_ops<P>(h, k.nb);
-    for (int n = 0; n < S::N1; ++n)
-        for (int i = 0; i < S::KP; ++i) {
+inline bool fill_tc_ops(const OpsHost& h, TcArgs<P>& k) {
+    using T = Tc<P>;
+    constexpr int NP = T::NP, NQ = T::NQ, NFQ = T::NFQ, FQ = T::FQ, KT = T::KT;
+    const double c0 = h.phi[0][0];
+    for (int q = 0; q < NQ; ++q)
+        if (std::fabs(h.phi[q][0] - c0) > 1e-14 * std::fabs(c0)) return false;
+    for (int f = 0; f < 3; ++f)
+        for (int j = 0; j < NFQ; ++j)
+            if (std::fabs(h.phif[f][j][0] - c0) > 1e-14 * std::fabs(c0)) return false;
+    k.c0 = (float)c0;
+    // GEMM1 B: row = thread k's slot r (k DW + r): volume point k + 4r (r < VW), face point
+    // k + 4 (r - VW) (r >= VW); column = basis function i >= 1
+    for (int n = 0; n < T::N1V; ++n)
+        for (int i = 0; i < T::KP; ++i) {
             double x = 0.0;
-            if (i < NP) {
-                if (n < NQ) x = h.phi[n][i];
-                else if (n >= S::NQ4 && n < S::NQ4 + S::FQ) x = h.phif[(n - S::NQ4) / NFQ][(n - S::NQ4) % NFQ][i];
+            const int kk = n / T::DW, r = n % T::DW;
+            if (kk < KT && i >= 1 && i < NP) {
+                if (r < T::VW) {
+                    const int q = kk + KT * r;
+                    if (q < NQ) x = h.phi[q][i];
+                } else {
+                    const int fp = kk + KT * (r - T::VW);
+                    if (fp < FQ) x = h.phif[fp / NFQ][fp % NFQ][i];
+                }
             }
-            const int off = tc::canon_off(n, i, S::KP);
+            const int off = tc::canon_off(n, i, T::KP);
             split3_host(x, k.b1[0][off], k.b1[1][off]);
         }
-    for (int i = 0; i < S::N2; ++i)
-        for (int m = 0; m < S::K2; ++m) {
+    // GEMM2 B: row = thread k's basis slot r (k BW + r): basis function k + 4r; column = flux
+    // slot: volume k 2VW + 2r: Fr'(k + 4r), k 2VW + 2r + 1: Fs'(k + 4r); face VOLK + k FW + r
+    for (int pos = 0; pos < T::N2V; ++pos)
+        for (int m = 0; m < T::K2V; ++m) {
             double x = 0.0;
-            if (i < NP) {
+            const int kb = pos / T::BW, rb = pos % T::BW, i = kb + KT * rb;
+            if (kb < KT && i < NP) {
                 auto lift = [&](const double* op) {  // (M_ref^-1 op)_i for an operator row over the basis
                     double a = 0.0;
                     for (int kk = 0; kk < NP; ++kk) a += h.minv[i][kk] * op[kk];
                     return a;
                 };
-                if (m < NQ) x = lift(h.dr[m]);
-                else if (m >= S::NQ4 && m < S::NQ4 + NQ) x = lift(h.ds[m - S::NQ4]);
-                else if (m >= 2 * S::NQ4 && m < 2 * S::NQ4 + S::FQ)
-                    x = lift(h.phif[(m - 2 * S::NQ4) / NFQ][(m - 2 * S::NQ4) % NFQ]);
+                if (m < T::VOLK) {
+                    const int kk = m / (2 * T::VW), r = (m % (2 * T::VW)) / 2, is_s = m & 1;
+                    const int q = kk + KT * r;
+                    if (q < NQ) x = is_s ? lift(h.ds[q]) : lift(h.dr[q]);
+                } else {
+                    const int kk = (m - T::VOLK) / T::FW, r = (m - T::VOLK) % T::FW;
+                    const int fp = kk + KT * r;
+                    if (fp < FQ) x = lift(h.phif[fp / NFQ][fp % NFQ]);
+                }
             }
-            const int off = tc::canon_off(i, m, S::K2);
+            const int off = tc::canon_off(pos, m, T::K2V);
             split3_host(x, k.b2[0][off], k.b2[1][off]);
         }
     for (int q = 0; q < NQ; ++q) k.wq[q] = (float)h.wq[q];
     for (int j = 0; j < NFQ; ++j) k.wf[j] = (float)h.wf[j];
-}
-
-template <int P>
-inline size_t stage_tc_smem_bytes() {
-    const size_t b = (size_t)tc_smem_floats<P>() * sizeof(float);
-    // TMEM bounds the CTAs per SM (512 columns: one, 256: two); shared memory enforces it
-    const size_t floor = TcShape<P>::COLS == 512 ? 120 * 1024 : 80 * 1024;
-    return b < floor ? floor : b;
+    return true;
 }
 
 }  // namespace dgx

@@ -1212,42 +1212,44 @@ static int capture(dgx_ctx* c, cudaGraphExec_t* out, const std::function<int(cud
 // (read by the first stage), the face traces of that state (trace form), and the stage
 // kernel's launch shape and form (timed the first time).
 static int mixed_prologue(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
-    if (launch_f64_to_f32(c->nstate, u, c->d_uhi[0], s)) return fail(DGX_ERR_CUDA, "conversion launch failed");
-    // face-trace form: the traces of the state the first step starts from (uhi[0] -> d_tr[0])
-    auto init_traces = [&]() {
-        if (!c->d_tr[0]) return 0;
+    if (launch_f64_to_f32(c->nstate, u, c->d_uhi[0], s))
+        return fail(DGX_ERR_CUDA, std::string("conversion launch failed: ") + launch_error_text());
+    // face-trace and tensor-core forms: the traces of the state the first step starts from
+    // (uhi[0] -> d_tr[0]), each form with its own operations
+    auto init_traces = [&](bool tc) {
         StageArgs t = mixed_stage_args(c, u, dt, 0);
         t.tout = c->d_tr[0];
-        return launch_trace_init(c->prm.order, t, c->ops, s);
+        const int rc = tc ? launch_tc_trace_init(c->prm.order, t, c->ops, c->stage_grid & ~STAGE_TC, s)
+                          : launch_trace_init(c->prm.order, t, c->ops, s);
+        return rc ? fail(DGX_ERR_CUDA, std::string("trace launch failed: ") + launch_error_text()) : DGX_OK;
     };
-    if (c->d_tr[0] && (c->stage_grid == 0 || (c->stage_grid & STAGE_TRACE)) && init_traces())
-        return fail(DGX_ERR_CUDA, "trace launch failed");
     if (c->stage_grid == 0 && c->nvpe == 4) c->stage_grid = (c->ne + TILE - 1) / TILE;  // one launch shape
     if (c->stage_grid == 0) {
         // launch shape and form of the stage kernel
         const StageArgs a = mixed_stage_args(c, u, dt, 0);
         const bool visc = c->prm.physics == DGX_NAVIER_STOKES;
-        // candidates: both CUDA-core forms (neighbour rows; face traces, Euler) at each grid;
-        // DGX_STAGE_KERNEL=rows / =trace keeps one of them.  The tensor-core kernel (Euler) only
-        // when DGX_STAGE_KERNEL asks for it: =tc (alone) or =auto (timed with the others).
-        // It is opt-in: at the sizes measured it is slower, and its FP32 accumulation in the
-        // tensor cores leaves a larger error over long runs than the CUDA-core FMA chains.
+        // candidates: the neighbour-row form at each grid; for Euler the face-trace form at each
+        // grid and the tensor-core form (orders 1-3, meshes whose faces are all interior or ghost
+        // faces) at one CTA per SM.  DGX_STAGE_KERNEL=rows / =trace / =tc keeps one form.
         const int ntiles = (c->ne + TILE - 1) / TILE;
         const char* mode = std::getenv("DGX_STAGE_KERNEL");
         const bool only_tc = mode && std::strcmp(mode, "tc") == 0;
         const bool only_trace = mode && std::strcmp(mode, "trace") == 0;
         const bool only_rows = mode && std::strcmp(mode, "rows") == 0;
-        const bool with_tc = only_tc || (mode && std::strcmp(mode, "auto") == 0);
+        const bool tc_ok = !visc && c->d_tr[0] && stage_tc_supported(c->prm.order) && (!c->boundary || c->d_tconn);
         std::vector<int> cands;
         const std::vector<int> grids = grid_candidates(ntiles);
-        if (visc || (!only_tc && !only_trace)) cands = grids;  // the neighbour-row form
+        if (visc || (!only_tc && !only_trace) || (only_tc && !tc_ok)) cands = grids;  // the neighbour-row form
         if (!visc && c->d_tr[0] && !only_tc && !only_rows)
             for (int g : grids) cands.push_back(STAGE_TRACE | g);
-        if (!visc && with_tc) {
+        if (tc_ok && !only_trace && !only_rows) {
             int sms = 152;
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
             cands.push_back(STAGE_TC | std::min(ntiles, sms * stage_tc_ctas_per_sm(c->prm.order)));
         }
+        // the traces the timed launches read (their rounding does not matter for the timing)
+        if (c->d_tr[0])
+            if (int rc = init_traces(false)) return rc;
         const std::string key = "stage p" + std::to_string(c->prm.order) + (visc ? " ns" : " euler") +
                                 (c->boundary ? " bnd" : "") + " ne" + std::to_string(c->ne) + " " + (mode ? mode : "");
         // timed as stage 2 (state uhi + d1, the increment zeroed at creation), which reads the
@@ -1267,6 +1269,8 @@ static int mixed_prologue(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
         if (c->graph1) cudaGraphExecDestroy(c->graph1);
         c->graph = c->graph1 = nullptr;
     }
+    if (c->d_tr[0] && (c->stage_grid & (STAGE_TRACE | STAGE_TC)))
+        if (int rc = init_traces((c->stage_grid & STAGE_TC) != 0)) return rc;
     return DGX_OK;
 }
 
@@ -1275,6 +1279,8 @@ extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void*
     if (c->ne == 0 || n_steps == 0) return DGX_OK;
     cudaStream_t s = (cudaStream_t)stream;
     const bool mixed = c->prm.precision == DGX_MIXED;
+    if (mixed && (reinterpret_cast<uintptr_t>(u) & 15))  // the stage kernels move the state in 16-byte pieces
+        return fail(DGX_ERR_INVALID, "dgx_rk3_step: a mixed-precision state must be 16-byte aligned");
     if (mixed)
         if (int rc = mixed_prologue(c, u, dt, s)) return rc;
     if (!c->graph || c->graph_u != u || c->graph_dt != dt) {
@@ -1357,6 +1363,9 @@ extern "C" int dgx_step_status(dgx_ctx* c, int* nonfinite, void* stream) {
     CUDA_OK(cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
     CUDA_OK(cudaStreamSynchronize(s));
     if (nonfinite) *nonfinite = f & 1;
+    if (f & 2)
+        return fail(DGX_ERR_TIMEOUT, "a bounded wait inside the tensor-core stage kernel gave up; the step's "
+                                     "results are not valid");
     return (f & 1) ? fail(DGX_ERR_NONFINITE, "an SSP-RK3 step produced a non-finite value") : DGX_OK;
 }
 
@@ -1442,8 +1451,7 @@ extern "C" int dgx_rk3_step_host(dgx_ctx* c, double* u, double dt, int n_steps) 
     // A single mixed step on a tuned context: the state comes in range by range on the second
     // stream, and each range is converted to FP32 (and its face traces formed) on the context
     // stream while the next range is in flight.
-    const bool chunk_in = overlap && n_steps == 1 && c->stage_grid != 0 && !(c->stage_grid & STAGE_TC) &&
-                          ntiles >= HOST_CHUNKS;
+    const bool chunk_in = overlap && n_steps == 1 && c->stage_grid != 0 && ntiles >= HOST_CHUNKS;
     if (!chunk_in) {
         CUDA_OK(cudaMemcpyAsync(c->d_hu, u, sb, cudaMemcpyHostToDevice, c->cap));
     } else {
@@ -1457,13 +1465,15 @@ extern "C" int dgx_rk3_step_host(dgx_ctx* c, double* u, double dt, int n_steps) 
             CUDA_OK(cudaStreamWaitEvent(c->cap, c->host_ev[k], 0));
             if (launch_f64_to_f32((e1 - e0) * row, c->d_hu + e0 * row, c->d_uhi[0] + e0 * row, c->cap))
                 return fail(DGX_ERR_CUDA, "conversion launch failed");
-            if (c->stage_grid & STAGE_TRACE) {
+            if (c->stage_grid & (STAGE_TRACE | STAGE_TC)) {
                 StageArgs t = mixed_stage_args(c, c->d_hu, dt, 0);
                 t.tout = c->d_tr[0];
                 t.tile0 = t0;
                 t.ntile = t1 - t0;
-                if (launch_trace_init(c->prm.order, t, c->ops, c->cap))
-                    return fail(DGX_ERR_CUDA, "trace launch failed");
+                const int lrc = (c->stage_grid & STAGE_TC)
+                                    ? launch_tc_trace_init(c->prm.order, t, c->ops, c->stage_grid & ~STAGE_TC, c->cap)
+                                    : launch_trace_init(c->prm.order, t, c->ops, c->cap);
+                if (lrc) return fail(DGX_ERR_CUDA, std::string("trace launch failed: ") + launch_error_text());
             }
         }
     }
@@ -1478,7 +1488,7 @@ extern "C" int dgx_rk3_step_host(dgx_ctx* c, double* u, double dt, int n_steps) 
     StageArgs st[3];
     mixed_step_args(c, c->d_hu, dt, 0, st);
     if ((rc = launch_stage(c, st[0], c->cap)) || (rc = launch_stage(c, st[1], c->cap))) return rc;
-    const bool chunked = !(c->stage_grid & STAGE_TC) && ntiles >= HOST_CHUNKS;
+    const bool chunked = ntiles >= HOST_CHUNKS;
     const int nch = chunked ? HOST_CHUNKS : 1;
     for (int k = 0; k < nch; ++k) {
         int t0, t1;

@@ -234,11 +234,16 @@ int configure_element_mixed(int p, bool viscous);
 int launch_element_df64(int p, bool viscous, const StepArgs& a, const OpsHost& ops, cudaStream_t s);
 int configure_element_df64(int p, bool viscous);
 int launch_stage_mixed(int p, bool viscous, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
-// Tensor-core form of the mixed Euler stage (dgx_kernels_tc.cu).  A StageArgs::grid with
-// STAGE_TC set selects it; the low bits are its grid (<= 0: one CTA per tile).
+// Tensor-core form of the mixed Euler stage (dgx_kernels_tc.cu), orders 1..3, meshes whose
+// faces are all interior or ghost faces (StageArgs::tconn).  A StageArgs::grid with STAGE_TC
+// set selects it; the low bits are its grid (<= 0: one CTA per tile).  It exchanges face
+// traces like the face-trace form (tin / tout), and launch_tc_trace_init writes the traces of
+// uhi with its own operations (the CUDA-core trace kernel's would differ in rounding).
 constexpr int STAGE_TC = 1 << 30;
 int launch_stage_tc(int p, const StageArgs& a, const OpsHost& ops, int grid, cudaStream_t s);
+int launch_tc_trace_init(int p, const StageArgs& a, const OpsHost& ops, int grid, cudaStream_t s);
 int configure_stage_tc(int p);
+bool stage_tc_supported(int p);
 // Face-trace form of the mixed Euler stage (dgx_kernels_trace.cu).  A StageArgs::grid with
 // STAGE_TRACE set selects it; the low bits are its grid.  launch_trace_init writes the traces
 // of uhi to tout (the state a step starts from).

@@ -1,62 +1,86 @@
-// Launchers of the tensor-core (3xTF32 tcgen05) form of the mixed-precision Euler stage.
+// Launchers of the tensor-core (3xTF32 tcgen05) form of the mixed-precision Euler stage,
+// orders 1..3 (dg_stage_tc.cuh).
+#include <cstdlib>
+
 #include "dg_stage_tc.cuh"
 
 namespace dgx {
 
+// Polls of one bounded wait inside the kernels.  DGX_TC_WAIT_LIMIT overrides it (a test makes
+// the waits run out on purpose and checks the status the kernels report).
+static long long tc_wait_limit() {
+    const char* v = std::getenv("DGX_TC_WAIT_LIMIT");
+    if (v && *v) {
+        const long long x = std::atoll(v);
+        if (x > 0) return x;
+    }
+    return 1LL << 24;
+}
+
 template <int P>
 static int configure_tc_t() {
-    const int b = (int)stage_tc_smem_bytes<P>();
-    return cudaFuncSetAttribute(stage_tc_kernel<P, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
-                       cudaSuccess &&
-                   cudaFuncSetAttribute(stage_tc_kernel<P, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
-                       cudaSuccess
+    const int b = Tc<P>::SMEM;
+    const auto set = [b](const void* f) {
+        return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess;
+    };
+    return set((const void*)stage_tc_kernel<P, false>) && set((const void*)stage_tc_kernel<P, true>) &&
+                   set((const void*)tc_trace_init_kernel<P, false>) && set((const void*)tc_trace_init_kernel<P, true>)
                ? 0
                : -1;
 }
+
+bool stage_tc_supported(int p) { return p >= 1 && p <= 3; }
 
 int configure_stage_tc(int p) {
     switch (p) {
     case 1: return configure_tc_t<1>();
     case 2: return configure_tc_t<2>();
     case 3: return configure_tc_t<3>();
-    case 4: return configure_tc_t<4>();
-    default: return -1;
+    default: return 0;  // no tensor-core form at this order; nothing to configure
     }
 }
 
-int stage_tc_ctas_per_sm(int p) {
-    switch (p) {
-    case 1: return TcShape<1>::COLS == 512 ? 1 : 2;
-    case 2: return TcShape<2>::COLS == 512 ? 1 : 2;
-    case 3: return TcShape<3>::COLS == 512 ? 1 : 2;
-    default: return TcShape<4>::COLS == 512 ? 1 : 2;
-    }
-}
+int stage_tc_ctas_per_sm(int) { return 1; }
 
 template <int P>
-static int launch_tc_t(const StageArgs& a, const OpsHost& oh, int grid, cudaStream_t st) {
-    TArgs<P> k;
+static int launch_tc_t(const StageArgs& a, const OpsHost& oh, int grid, bool init, cudaStream_t st) {
+    TcArgs<P> k;
+    std::memset(&k, 0, sizeof(k));
     k.s = a;
-    fill_tc_ops<P>(oh, k);
-    const int ntiles = (a.ne + TILE - 1) / TILE;
+    if (a.tconn) k.s.conn = a.tconn;  // boundary faces as interior faces to ghost blocks
+    if (!fill_tc_ops<P>(oh, k)) return -1;
+    k.wait_limit = tc_wait_limit();
+    const int ntiles = a.ntile > 0 ? a.ntile : (a.ne + TILE - 1) / TILE;
     if (ntiles == 0) return 0;
     if (grid <= 0 || grid > ntiles) grid = ntiles;
-    const size_t smem = stage_tc_smem_bytes<P>();
-    if (a.boundary)
-        stage_tc_kernel<P, true><<<grid, TcShape<P>::THREADS, smem, st>>>(k);
-    else
-        stage_tc_kernel<P, false><<<grid, TcShape<P>::THREADS, smem, st>>>(k);
+    const bool ghost = a.tconn != nullptr;
+    if (init) {
+        if (ghost) tc_trace_init_kernel<P, true><<<grid, Tc<P>::THREADS, Tc<P>::SMEM, st>>>(k);
+        else tc_trace_init_kernel<P, false><<<grid, Tc<P>::THREADS, Tc<P>::SMEM, st>>>(k);
+    } else {
+        if (ghost) stage_tc_kernel<P, true><<<grid, Tc<P>::THREADS, Tc<P>::SMEM, st>>>(k);
+        else stage_tc_kernel<P, false><<<grid, Tc<P>::THREADS, Tc<P>::SMEM, st>>>(k);
+    }
     return launch_status();
 }
 
-int launch_stage_tc(int p, const StageArgs& a, const OpsHost& ops, int grid, cudaStream_t s) {
+static int dispatch(int p, const StageArgs& a, const OpsHost& ops, int grid, bool init, cudaStream_t s) {
+    // the tensor-core form covers meshes whose faces are all interior or ghost faces
+    if (a.boundary && !a.tconn) return -1;
     switch (p) {
-    case 1: return launch_tc_t<1>(a, ops, grid, s);
-    case 2: return launch_tc_t<2>(a, ops, grid, s);
-    case 3: return launch_tc_t<3>(a, ops, grid, s);
-    case 4: return launch_tc_t<4>(a, ops, grid, s);
+    case 1: return launch_tc_t<1>(a, ops, grid, init, s);
+    case 2: return launch_tc_t<2>(a, ops, grid, init, s);
+    case 3: return launch_tc_t<3>(a, ops, grid, init, s);
     default: return -1;
     }
+}
+
+int launch_stage_tc(int p, const StageArgs& a, const OpsHost& ops, int grid, cudaStream_t s) {
+    return dispatch(p, a, ops, grid, false, s);
+}
+
+int launch_tc_trace_init(int p, const StageArgs& a, const OpsHost& ops, int grid, cudaStream_t s) {
+    return dispatch(p, a, ops, grid, true, s);
 }
 
 }  // namespace dgx

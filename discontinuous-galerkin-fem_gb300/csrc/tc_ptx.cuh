@@ -56,15 +56,33 @@ __device__ __forceinline__ void mbar_init(uint64_t* mbar, int count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(mbar)), "r"(count));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
+// One poll: true once the phase with the given parity has completed.
+__device__ __forceinline__ bool mbar_test(uint64_t* mbar, uint32_t parity) {
+    uint32_t done = 0;
+    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done) : "r"(smem_u32(mbar)), "r"(parity) : "memory");
+    return done != 0;
+}
 // Waits for the phase with the given parity; gives up after `limit` polls and returns false.
 __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, long limit) {
-    uint32_t done = 0;
-    for (long it = 0; it < limit; ++it) {
-        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-                     : "=r"(done) : "r"(smem_u32(mbar)), "r"(parity) : "memory");
-        if (done) return true;
-    }
+    for (long it = 0; it < limit; ++it)
+        if (mbar_test(mbar, parity)) return true;
     return false;
+}
+// The same, also giving up (false) as soon as *abort is set; on running out of polls it sets
+// *abort itself, so that every other waiter of the CTA gives up too.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* mbar, uint32_t parity, long limit, volatile int* abort) {
+    for (long it = 0; it < limit; ++it) {
+        if (mbar_test(mbar, parity)) return true;
+        if (*abort) return false;
+    }
+    *abort = 1;
+    return false;
+}
+// Arrival of the calling thread (release semantics: its earlier shared-memory writes are
+// visible to threads that observe the phase complete).
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_u32(mbar)) : "memory");
 }
 
 // TMEM allocation by one full warp; the base address is written to *slot (shared memory)
@@ -80,6 +98,14 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t base, uint32_t ncols) {
 __device__ __forceinline__ void ld1(uint32_t a, float& x) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];" : "=f"(x) : "r"(a));
 }
+__device__ __forceinline__ void ld2(uint32_t a, float* x) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];" : "=f"(x[0]), "=f"(x[1]) : "r"(a));
+}
+__device__ __forceinline__ void ld8(uint32_t a, float* x) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(x[0]), "=f"(x[1]), "=f"(x[2]), "=f"(x[3]), "=f"(x[4]), "=f"(x[5]), "=f"(x[6]), "=f"(x[7])
+                 : "r"(a));
+}
 __device__ __forceinline__ void ld4(uint32_t a, float* x) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
                  : "=f"(x[0]), "=f"(x[1]), "=f"(x[2]), "=f"(x[3]) : "r"(a));
@@ -94,11 +120,34 @@ __device__ __forceinline__ void wait_ld() { asm volatile("tcgen05.wait::ld.sync.
 __device__ __forceinline__ void st1(uint32_t a, float x) {
     asm volatile("tcgen05.st.sync.aligned.32x32b.x1.b32 [%0], {%1};" :: "r"(a), "f"(x));
 }
+__device__ __forceinline__ void st2(uint32_t a, const float* x) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1,%2};" :: "r"(a), "f"(x[0]), "f"(x[1]));
+}
+__device__ __forceinline__ void st8(uint32_t a, const float* x) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
+                 :: "r"(a), "f"(x[0]), "f"(x[1]), "f"(x[2]), "f"(x[3]), "f"(x[4]), "f"(x[5]), "f"(x[6]), "f"(x[7]));
+}
 __device__ __forceinline__ void st4(uint32_t a, const float* x) {
     asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};"
                  :: "r"(a), "f"(x[0]), "f"(x[1]), "f"(x[2]), "f"(x[3]));
 }
 __device__ __forceinline__ void wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// N consecutive columns of this thread's lane (N known at compile time), in x8/x4/x2/x1 pieces
+template <int N>
+__device__ __forceinline__ void ldn(uint32_t a, float* x) {
+    if constexpr (N >= 8) { ld8(a, x); ldn<N - 8>(a + 8, x + 8); }
+    else if constexpr (N >= 4) { ld4(a, x); ldn<N - 4>(a + 4, x + 4); }
+    else if constexpr (N >= 2) { ld2(a, x); ldn<N - 2>(a + 2, x + 2); }
+    else if constexpr (N == 1) { ld1(a, x[0]); }
+}
+template <int N>
+__device__ __forceinline__ void stn(uint32_t a, const float* x) {
+    if constexpr (N >= 8) { st8(a, x); stn<N - 8>(a + 8, x + 8); }
+    else if constexpr (N >= 4) { st4(a, x); stn<N - 4>(a + 4, x + 4); }
+    else if constexpr (N >= 2) { st2(a, x); stn<N - 2>(a + 2, x + 2); }
+    else if constexpr (N == 1) { st1(a, x[0]); }
+}
 
 // Bulk (TMA) copy of `bytes` contiguous bytes global -> shared, completing on `mbar` as a
 // transaction count; the issuing thread first arms the barrier with the expected bytes.

@@ -15,7 +15,7 @@ PKG_ROOT = Path(__file__).resolve().parent.parent
 LIB_PATH = Path(os.environ.get("DGX_LIBRARY", PKG_ROOT / "libdgx.so"))
 
 OK = 0
-ERR_INVALID, ERR_RUNTIME, ERR_RANGE, ERR_CUDA, ERR_NONFINITE = -1, -2, -3, -4, -5
+ERR_INVALID, ERR_RUNTIME, ERR_RANGE, ERR_CUDA, ERR_NONFINITE, ERR_TIMEOUT = -1, -2, -3, -4, -5, -6
 BASIS_MONOMIAL, BASIS_DUBINER, BASIS_LEGENDRE = 0, 1, 2
 EULER, NAVIER_STOKES = 0, 1
 FP64, MIXED, DF64 = 0, 1, 2

@@ -356,7 +356,8 @@ class DGContext:
 
     def step_nonfinite(self) -> bool:
         """True when an RK3 step since the last call produced a NaN or Inf (device flag, read
-        and cleared on torch's current stream)."""
+        and cleared on torch's current stream).  Raises DGXError (DGX_ERR_TIMEOUT) when a
+        bounded wait inside the tensor-core stage kernel gave up."""
         import torch
         f = C.c_int()
         rc = L.load().dgx_step_status(self._h, C.byref(f), C.c_void_p(torch.cuda.current_stream().cuda_stream))

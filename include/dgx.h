@@ -36,6 +36,7 @@ extern "C" {
 #define DGX_ERR_RANGE (-3)     /* std::out_of_range in dgfem */
 #define DGX_ERR_CUDA (-4)      /* CUDA failure or no usable GPU */
 #define DGX_ERR_NONFINITE (-5) /* non-finite or non-positive state detected */
+#define DGX_ERR_TIMEOUT (-6)   /* a bounded wait inside a kernel gave up (dgx_step_status) */
 
 /* DGX_BASIS_LEGENDRE: LegendreBasis (src/basis/legendre.cpp), the basis of quadrilateral
  * meshes (DGSpace::create_basis, src/core/space.cpp:307-319). */
@@ -171,7 +172,9 @@ int dgx_has_nan(dgx_ctx* c, const double* u, int* has_nan, void* stream);
  * allocation-free variants) produced a NaN or Inf since the last call.  The stage kernels set
  * a device flag as they write u^{n+1}; this call reads and clears it (synchronising with
  * `stream`).  Returns DGX_ERR_NONFINITE with *nonfinite = 1, or DGX_OK with 0.  dgfem scans
- * the state after each step and stops the run (compressible_solver_base.cpp:290-301). */
+ * the state after each step and stops the run (compressible_solver_base.cpp:290-301).
+ * Returns DGX_ERR_TIMEOUT when a bounded wait inside the tensor-core stage kernel gave up
+ * (its results are then not valid; the kernel returned and the context stays usable). */
 int dgx_step_status(dgx_ctx* c, int* nonfinite, void* stream);
 
 /* Physical coordinates of every volume quadrature point, [n_elements][n_quad][2] (host),
@@ -259,13 +262,13 @@ int dgx_eval_points(dgx_ctx* c, int n_points, const double* ref_xy, const double
 /* The stage kernel the autotuner picked for a mixed-precision context: its grid (CTAs;
  * each walks the 128-element tiles with a grid stride), the number of tiles, and its form:
  * 0 = CUDA cores, neighbour coefficient rows read per face; 2 = CUDA cores, face traces
- * exchanged through HBM (Euler); 1 = the 3xTF32 tcgen05 form (Euler).  grid is 0 until the
- * first dgx_rk3_step, which times the candidates on its stream: both CUDA-core forms at one
- * CTA per tile and at 1..8 CTAs per SM.  Environment: DGX_STAGE_KERNEL=rows or =trace keeps
- * one CUDA-core form, =tc takes the tensor-core form, =auto adds it to the timed candidates
- * (it is opt-in: slower at the sizes measured, and its long-run error is larger);
- * DGX_AUTOTUNE=0 skips the timing (the first candidate: rows, one CTA per tile).
- * Quadrilateral meshes have one form (grid = tiles).  No counterpart in dgfem. */
+ * exchanged through HBM (Euler); 1 = the 3xTF32 tcgen05 tensor-core form (Euler, orders 1-3,
+ * meshes whose boundary faces all have a condition; one CTA per SM).  grid is 0 until the
+ * first dgx_rk3_step, which times the candidates on its stream: the CUDA-core forms at one
+ * CTA per tile and at 1..8 CTAs per SM, and the tensor-core form.  Environment:
+ * DGX_STAGE_KERNEL=rows, =trace or =tc keeps one form; DGX_AUTOTUNE=0 skips the timing (the
+ * first candidate).  Quadrilateral meshes have one form (grid = tiles).  A mixed-precision
+ * state passed to dgx_rk3_step must be 16-byte aligned.  No counterpart in dgfem. */
 int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles, int* form);
 
 /* ---------------------------------------------------------------- batched solves */

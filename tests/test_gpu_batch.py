@@ -86,7 +86,10 @@ def single(dg, om, pm, u0, dt, order, steps=(3, 2)):
 
 
 @pytest.mark.parametrize("walls", [(), (1, 4, 6)])
-def test_batch_matches_single_solves_and_oracle(dg, walls):
+def test_batch_matches_single_solves_and_oracle(dg, monkeypatch, walls):
+    # the single solves run a CUDA-core form, which the batched kernel equals bit for bit (the
+    # tensor-core form rounds differently)
+    monkeypatch.setenv("DGX_STAGE_KERNEL", "trace")
     insts, orders = build(dg, SPECS, walls)
     batch, outs = run_batch(dg, insts, orders)
     for k, ((om, pm, u0, dt), order) in enumerate(zip(insts, orders)):

@@ -85,7 +85,7 @@ def test_autotuner_reports_a_form(dg, monkeypatch):
 
 
 @pytest.mark.parametrize("walls", [False, True, "skip"])
-@pytest.mark.parametrize("kernel,n", [("rows", 1), ("trace", 1), ("trace", 3)])
+@pytest.mark.parametrize("kernel,n", [("rows", 1), ("trace", 1), ("trace", 3), ("tc", 1), ("tc", 3)])
 def test_host_pointer_step_equals_device_step(dg, monkeypatch, kernel, n, walls):
     """dgx_rk3_step_host runs its last step's stage 3 in tile ranges, each copied back to the
     host while the next range computes; the state equals the device-pointer step's bit for bit."""
@@ -101,8 +101,8 @@ def test_host_pointer_step_equals_device_step(dg, monkeypatch, kernel, n, walls)
 
 @pytest.mark.parametrize("n", [1, 2])
 def test_host_pointer_step_tensor_core_form(dg, monkeypatch, n):
-    """The host-pointer step with the tensor-core form (no range-wise overlap) equals the
-    device-pointer step bit for bit."""
+    """The host-pointer step with the tensor-core form (stage 3 in tile ranges, each copied
+    back while the next computes) equals the device-pointer step bit for bit."""
     om, pm, u0, dt = case(dg, 24, 3, False)
     monkeypatch.setenv("DGX_STAGE_KERNEL", "tc")
     ctx = dg.DGContext(pm, dg.DGSpace("triangle", 3, "dubiner"), dg.EulerWeakFormulation(1.4), "mixed")
