@@ -87,8 +87,9 @@ struct Tc {
     // barriers
     static constexpr int G1 = 0, G2 = 1, G3 = 2, A1 = 3, A2V = 4, A2F = 5, A3 = 6, D1RD = 7, FULL = 8, FREE = 10,
                          DRAIN = 12;
+    // barriers the compute warps complete take one arrival per warp (lane 0, after __syncwarp)
     __host__ __device__ static constexpr int bar_count(int b) {
-        return (b == G1 || b == G2 || b == G3 || b == DRAIN || b == FULL || b == FULL + 1) ? 1 : CW * 32;
+        return (b == G1 || b == G2 || b == G3 || b == DRAIN || b == FULL || b == FULL + 1) ? 1 : CW;
     }
 };
 static_assert(Tc<3>::COLS_USED <= 512 && Tc<2>::COLS_USED <= 512 && Tc<1>::COLS_USED <= 256, "TMEM budget");
@@ -107,6 +108,7 @@ struct TcArgs {
     float wf[T::NFQ];
     float c0;                      // the (constant) first basis function
     long long wait_limit;          // polls of one bounded wait
+    unsigned wait_hint_ns;         // each poll may sleep up to this long (0: plain polls)
 };
 
 // Element row le, basis function i (all four variables) of the stage state in a tile's input
@@ -142,23 +144,24 @@ __device__ __forceinline__ void tc_put_a(float* sA, int v, int le, int i, float 
 
 // GEMM1 / GEMM3: per variable D[:, v N1V + n] = sum_i A_v[:, i] B1[n, i] (3xTF32).  One routine
 // for both, so that the traces a stage writes equal the next stage's own-face values bit for bit.
+// Every accumulator receives its products in the same order (K step, then lo*hi, hi*lo, hi*hi);
+// the four variables' independent chains are interleaved.  Descriptors are formed once and
+// advanced by their 16-byte address field (all operands lie in the first 256 KB of the window).
 template <int P>
 __device__ __forceinline__ void tc_issue_interp(uint32_t a_smem, uint32_t b1_smem, uint32_t d_tmem) {
     using T = Tc<P>;
     constexpr uint32_t id = tc::idesc_tf32(128, T::N1V);
     constexpr uint32_t SBO = (T::KP / 4) * 128;
-    const uint32_t b_hi = b1_smem, b_lo = b1_smem + T::N1V * T::KP * 4;
+    constexpr uint64_t A_V = (TILE * T::KP * 4) >> 4, A_LO = 4 * A_V, B_LO = (T::N1V * T::KP * 4) >> 4, KS = 256 >> 4;
+    const uint64_t da = tc::smem_desc(a_smem, 128, SBO), db = tc::smem_desc(b1_smem, 128, SBO);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) {
-        const uint32_t a_hi = a_smem + v * TILE * T::KP * 4, a_lo = a_smem + (4 + v) * TILE * T::KP * 4;
-        const uint32_t d = d_tmem + v * T::N1V;
+    for (int ks = 0; ks < T::KP / 8; ++ks)
 #pragma unroll
-        for (int ks = 0; ks < T::KP / 8; ++ks) {
-            tc::mma_ss(d, tc::smem_desc(a_lo + ks * 256, 128, SBO), tc::smem_desc(b_hi + ks * 256, 128, SBO), id, ks > 0);
-            tc::mma_ss(d, tc::smem_desc(a_hi + ks * 256, 128, SBO), tc::smem_desc(b_lo + ks * 256, 128, SBO), id, true);
-            tc::mma_ss(d, tc::smem_desc(a_hi + ks * 256, 128, SBO), tc::smem_desc(b_hi + ks * 256, 128, SBO), id, true);
-        }
-    }
+        for (int pr = 0; pr < 3; ++pr)  // a_lo b_hi, a_hi b_lo, a_hi b_hi
+#pragma unroll
+            for (int v = 0; v < NV; ++v)
+                tc::mma_ss(d_tmem + v * T::N1V, da + v * A_V + ks * KS + (pr == 0 ? A_LO : 0),
+                           db + ks * KS + (pr == 1 ? B_LO : 0), id, ks > 0 || pr > 0);
 }
 
 // GEMM2 over the K steps [ks0, ks1) of every variable (A2 from TMEM); ks0 == 0 starts D2.
@@ -167,18 +170,16 @@ __device__ __forceinline__ void tc_issue_proj(uint32_t tm, uint32_t b2_smem, int
     using T = Tc<P>;
     constexpr uint32_t id = tc::idesc_tf32(128, T::N2V);
     constexpr uint32_t SBO = (T::K2V / 4) * 128;
-    const uint32_t b_hi = b2_smem, b_lo = b2_smem + T::N2V * T::K2V * 4;
+    constexpr uint64_t B_LO = (T::N2V * T::K2V * 4) >> 4, KS = 256 >> 4;
+    const uint64_t db = tc::smem_desc(b2_smem, 128, SBO);
+    for (int ks = ks0; ks < ks1; ++ks)
 #pragma unroll
-    for (int v = 0; v < NV; ++v) {
-        const uint32_t d = tm + T::COL_D2 + v * T::N2V;
-        for (int ks = ks0; ks < ks1; ++ks) {
-            const uint32_t a_hi = tm + T::COL_A2 + v * T::K2V + ks * 8;
-            const uint32_t a_lo = tm + T::COL_A2 + 4 * T::K2V + v * T::K2V + ks * 8;
-            tc::mma_ts(d, a_lo, tc::smem_desc(b_hi + ks * 256, 128, SBO), id, ks > 0);
-            tc::mma_ts(d, a_hi, tc::smem_desc(b_lo + ks * 256, 128, SBO), id, true);
-            tc::mma_ts(d, a_hi, tc::smem_desc(b_hi + ks * 256, 128, SBO), id, true);
-        }
-    }
+        for (int pr = 0; pr < 3; ++pr)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                const uint32_t a = tm + T::COL_A2 + (pr == 0 ? 4 * T::K2V : 0) + v * T::K2V + ks * 8;
+                tc::mma_ts(tm + T::COL_D2 + v * T::N2V, a, db + ks * KS + (pr == 1 ? B_LO : 0), id, ks > 0 || pr > 0);
+            }
 }
 
 // Traces of one tile's next stage state at thread k's face points: fmaf(c0, S_0, D3) (the same
@@ -293,7 +294,7 @@ __global__ void __launch_bounds__(Tc<P>::THREADS, 1) stage_tc_kernel(const __gri
     auto tile_of = [&](int j) { return s.tile0 + (int)blockIdx.x + j * (int)gridDim.x; };
     const long long LIM = ka.wait_limit;
     auto wait = [&](int b, int parity) {
-        const bool ok = tc::mbar_wait_or_abort(&bar[b], (uint32_t)(parity & 1), (long)LIM, abort_flag);
+        const bool ok = tc::mbar_wait_or_abort(&bar[b], (uint32_t)(parity & 1), (long)LIM, abort_flag, ka.wait_hint_ns);
         if (!ok && s.status) atomicOr(s.status, 2);
         return ok;
     };
@@ -353,7 +354,12 @@ __global__ void __launch_bounds__(Tc<P>::THREADS, 1) stage_tc_kernel(const __gri
         const uint32_t tl = tm + ((uint32_t)(32 * qd) << 16);  // this warp's TMEM lane quadrant
         const float c0 = ka.c0, gamma = s.gamma;
         const bool has_din = s.din != nullptr;
-        auto arrive = [&](int b) { tc::mbar_arrive(&bar[b]); };
+        // every lane's shared-memory / TMEM writes (fenced by the caller) are ordered before lane
+        // 0's release-arrival by the warp barrier
+        auto arrive = [&](int b) {
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&bar[b]);
+        };
         // the stage state of tile j (input buffer j & 1), split into the GEMM1 operand
         auto split_state = [&](int j) {
             const unsigned char* raw = sRaw + (j & 1) * T::RAWB;
@@ -382,15 +388,15 @@ __global__ void __launch_bounds__(Tc<P>::THREADS, 1) stage_tc_kernel(const __gri
             const int e = e0 + le;
             const unsigned char* raw = sRaw + (j & 1) * T::RAWB;
             const ElemGeomF* G = reinterpret_cast<const ElemGeomF*>(raw + T::RG_OFF) + le;
-            const ElemConn C = reinterpret_cast<const ElemConn*>(raw + T::RC_OFF)[le];
+            const ElemConn* C = reinterpret_cast<const ElemConn*>(raw + T::RC_OFF) + le;
             const float4 s0 = tc_state<P>(raw, s.stage, has_din, le, 0);
             const float S0[4] = {s0.x, s0.y, s0.z, s0.w};
             // the neighbour trace blocks this thread reads in (c): into L2 now
             auto nbr_trace = [&](int r) -> const float* {
                 const int fp = k + KT * r, f = fp / NFQ, jp = fp - f * NFQ;
-                const int fl = (C.flags >> (4 * f)) & 15;
+                const int fl = (C->flags >> (4 * f)) & 15;
                 const int pt = ((fl >> 2) & 1) ? NFQ - 1 - jp : jp;
-                return s.tin + (size_t)C.nbr[f] * TRF + ((fl & 3) * NFQ + pt) * NV;
+                return s.tin + (size_t)C->nbr[f] * TRF + ((fl & 3) * NFQ + pt) * NV;
             };
 #pragma unroll
             for (int r = 0; r < FW; ++r)
@@ -417,6 +423,11 @@ __global__ void __launch_bounds__(Tc<P>::THREADS, 1) stage_tc_kernel(const __gri
             }
             if (!(ok = wait(T::D1RD, j))) break;
             tc::fence_after();
+            float4 un[FW];  // neighbour traces at this thread's face points, used in (c)
+#pragma unroll
+            for (int r = 0; r < FW; ++r)
+                un[r] = (act && k + KT * r < FQ) ? __ldg(reinterpret_cast<const float4*>(nbr_trace(r)))
+                                                 : make_float4(0.f, 0.f, 0.f, 0.f);
             // (b) volume fluxes -> A2 volume columns k 2VW + 2r (Fr') and k 2VW + 2r + 1 (Fs') of each
             //     variable, stored point by point
 #pragma unroll
@@ -450,11 +461,6 @@ __global__ void __launch_bounds__(Tc<P>::THREADS, 1) stage_tc_kernel(const __gri
             arrive(T::A2V);
             // (c) face fluxes -> A2 face columns VOLK + k FW + r, stored point by point
             {
-                float4 un[FW];
-#pragma unroll
-                for (int r = 0; r < FW; ++r)
-                    un[r] = (act && k + KT * r < FQ) ? __ldg(reinterpret_cast<const float4*>(nbr_trace(r)))
-                                                     : make_float4(0.f, 0.f, 0.f, 0.f);
                 const float inv_j = __frcp_rn(G->detJ);
 #pragma unroll
                 for (int r = 0; r < FW; ++r) {
@@ -605,7 +611,8 @@ __global__ void __launch_bounds__(Tc<P>::THREADS, 1) tc_trace_init_kernel(const 
     const int n = (int)blockIdx.x < all_tiles ? (all_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
     auto tile_of = [&](int j) { return s.tile0 + (int)blockIdx.x + j * (int)gridDim.x; };
     auto wait = [&](int b, int parity) {
-        const bool ok = tc::mbar_wait_or_abort(&bar[b], (uint32_t)(parity & 1), (long)ka.wait_limit, abort_flag);
+        const bool ok = tc::mbar_wait_or_abort(&bar[b], (uint32_t)(parity & 1), (long)ka.wait_limit, abort_flag,
+                                               ka.wait_hint_ns);
         if (!ok && s.status) atomicOr(s.status, 2);
         return ok;
     };
@@ -647,14 +654,16 @@ __global__ void __launch_bounds__(Tc<P>::THREADS, 1) tc_trace_init_kernel(const 
             }
             tc::fence_async_smem();
             tc::fence_before();
-            tc::mbar_arrive(&bar[T::A3]);
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&bar[T::A3]);
             if (!wait(T::G3, j)) break;
             tc::fence_after();
             const float4 z = tc_state<P>(sRaw, s.stage, false, le, 0);
             const float s0[4] = {z.x, z.y, z.z, z.w};
             tc_traces_out<P, GHOST>(ka, tl, s0, e0 + le, le < nloc, k);
             tc::fence_before();
-            tc::mbar_arrive(&bar[T::FREE]);
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&bar[T::FREE]);
         }
     }
     tc_teardown<P>(tm);

@@ -6,15 +6,21 @@
 
 namespace dgx {
 
-// Polls of one bounded wait inside the kernels.  DGX_TC_WAIT_LIMIT overrides it (a test makes
-// the waits run out on purpose and checks the status the kernels report).
-static long long tc_wait_limit() {
+// Bounded waits inside the kernels: by default up to 2^16 polls that may each sleep up to 20 us
+// (about 1.3 s in all, far beyond any wait in a healthy launch).  DGX_TC_WAIT_LIMIT=n makes it n
+// plain polls (a test makes the waits run out on purpose and checks the status the kernels
+// report).
+static void tc_wait_bounds(long long* limit, unsigned* hint_ns) {
+    *limit = 1LL << 16;
+    *hint_ns = 20000;
     const char* v = std::getenv("DGX_TC_WAIT_LIMIT");
     if (v && *v) {
         const long long x = std::atoll(v);
-        if (x > 0) return x;
+        if (x > 0) {
+            *limit = x;
+            *hint_ns = 0;
+        }
     }
-    return 1LL << 24;
 }
 
 template <int P>
@@ -49,7 +55,7 @@ static int launch_tc_t(const StageArgs& a, const OpsHost& oh, int grid, bool ini
     k.s = a;
     if (a.tconn) k.s.conn = a.tconn;  // boundary faces as interior faces to ghost blocks
     if (!fill_tc_ops<P>(oh, k)) return -1;
-    k.wait_limit = tc_wait_limit();
+    tc_wait_bounds(&k.wait_limit, &k.wait_hint_ns);
     const int ntiles = a.ntile > 0 ? a.ntile : (a.ne + TILE - 1) / TILE;
     if (ntiles == 0) return 0;
     if (grid <= 0 || grid > ntiles) grid = ntiles;
