@@ -1510,6 +1510,51 @@ extern "C" int dgx_rk3_step_host(dgx_ctx* c, double* u, double dt, int n_steps) 
     return DGX_OK;
 }
 
+extern "C" int dgx_state_alloc(const dgx_ctx* c, double** u) {
+    if (!c || !u) return fail(DGX_ERR_INVALID, "dgx_state_alloc: null argument");
+    *u = nullptr;
+    int dev = -1;
+    CUDA_OK(cudaGetDevice(&dev));
+    if (dev != c->device) CUDA_OK(cudaSetDevice(c->device));
+    const cudaError_t e = cudaMalloc(u, c->nstate ? c->nstate * sizeof(double) : 16);
+    if (dev != c->device) cudaSetDevice(dev);
+    if (e != cudaSuccess) {
+        *u = nullptr;
+        return fail(DGX_ERR_CUDA, std::string("dgx_state_alloc: ") + cudaGetErrorString(e));
+    }
+    return DGX_OK;
+}
+
+extern "C" void dgx_state_free(double* u) {
+    if (u) cudaFree(u);
+}
+
+extern "C" int dgx_state_copy(const dgx_ctx* c, double* dst, const double* src, int to_device) {
+    if (!c || (c->nstate && (!dst || !src))) return fail(DGX_ERR_INVALID, "dgx_state_copy: bad argument");
+    if (c->nstate == 0) return DGX_OK;
+    CUDA_OK(cudaMemcpy(dst, src, c->nstate * sizeof(double), to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost));
+    return DGX_OK;
+}
+
+extern "C" int dgx_project_host(dgx_ctx* c, const double* uq, double* u) {
+    if (!c || (c->ne && (!uq || !u))) return fail(DGX_ERR_INVALID, "dgx_project_host: bad argument");
+    if (c->ne == 0) return DGX_OK;
+    int rc = ensure_host_buffers(c);
+    if (rc) return rc;
+    const size_t nq = (size_t)c->ne * c->nq * NV;
+    double* d_uq = nullptr;
+    CUDA_OK(cudaMalloc(&d_uq, nq * sizeof(double)));
+    rc = [&]() -> int {
+        CUDA_OK(cudaMemcpyAsync(d_uq, uq, nq * sizeof(double), cudaMemcpyHostToDevice, c->cap));
+        if (int r = dgx_project(c, d_uq, c->d_hu, c->cap)) return r;
+        CUDA_OK(cudaMemcpyAsync(u, c->d_hu, c->nstate * sizeof(double), cudaMemcpyDeviceToHost, c->cap));
+        CUDA_OK(cudaStreamSynchronize(c->cap));
+        return DGX_OK;
+    }();
+    cudaFree(d_uq);
+    return rc;
+}
+
 extern "C" int dgx_apply_mass_inv_host(dgx_ctx* c, const double* in, double* out) {
     if (!c || (c->ne && (!in || !out))) return fail(DGX_ERR_INVALID, "dgx_apply_mass_inv_host: null argument");
     int rc = ensure_host_buffers(c);

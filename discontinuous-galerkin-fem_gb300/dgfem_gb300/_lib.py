@@ -58,6 +58,10 @@ SIGNATURES = {
     "dgx_rk3_step_host": (C.c_int, [_vp, _dp, C.c_double, C.c_int]),
     "dgx_rk3_step_static": (C.c_int, [_vp, _vp, C.c_double, C.c_int, _vp]),
     "dgx_apply_mass_inv_host": (C.c_int, [_vp, _dp, _dp]),
+    "dgx_project_host": (C.c_int, [_vp, _dp, _dp]),
+    "dgx_state_alloc": (C.c_int, [_vp, C.POINTER(_vp)]),
+    "dgx_state_free": (None, [_vp]),
+    "dgx_state_copy": (C.c_int, [_vp, _vp, _vp, C.c_int]),
     "dgx_monitor_host": (C.c_int, [_vp, _dp, C.c_double, _dp, _dp, _dp, _ip]),
     "dgx_residual_jvp": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "dgx_residual_vjp": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),

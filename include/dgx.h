@@ -184,6 +184,16 @@ int dgx_quad_points(const dgx_ctx* c, double* xq);
  * uq = the initial condition at dgx_quad_points, [n_elements][n_quad][4] (device). */
 int dgx_project(dgx_ctx* c, const double* uq, double* u, void* stream);
 
+/* ---------------------------------------------------------------- device states for callers without CUDA */
+/* A device buffer for one state of this context (n_elements * n_basis * 4 doubles) on the
+ * context's device, for callers that do not link the CUDA runtime themselves (the C++ layer's
+ * solve() keeps its state there between steps).  Free it with dgx_state_free. */
+int dgx_state_alloc(const dgx_ctx* c, double** u);
+void dgx_state_free(double* u);
+/* Copies one state: to_device != 0: host src -> device dst, else device src -> host dst.
+ * Synchronous. */
+int dgx_state_copy(const dgx_ctx* c, double* dst, const double* src, int to_device);
+
 /* ---------------------------------------------------------------- host-pointer variants */
 /* Synchronous: each first waits for all work on the device (calls made earlier on any
  * stream), then copies in, computes and copies out on the context's own streams. */
@@ -195,6 +205,9 @@ int dgx_residual_host(dgx_ctx* c, const double* u, double* r);
 int dgx_rk3_step_host(dgx_ctx* c, double* u, double dt, int n_steps);
 /* apply_mass_inv on host states (copies in, computes, copies out). */
 int dgx_apply_mass_inv_host(dgx_ctx* c, const double* in, double* out);
+/* project_initial_condition on host arrays: uq [n_elements][n_quad][4] (the initial condition
+ * at dgx_quad_points), u the projected state. */
+int dgx_project_host(dgx_ctx* c, const double* uq, double* u);
 /* compute_max_cfl, compute_density_range and the NaN scan of run_time_integration on a host
  * state; any output pointer may be NULL. */
 int dgx_monitor_host(dgx_ctx* c, const double* u, double dt, double* cfl, double* rho_min,

@@ -1,6 +1,7 @@
-// Drives include/dgx_dgfem.hpp the way dgfem's own code would: a DGMesh built from
-// vertex/element arrays and boundary edges, periodic pairing, an assembler, and states
-// held as std::vector of Np x 4 matrices.  Reads its inputs from files written by
+// Drives include/dgx_dgfem.hpp the way dgfem's own code would: a shared DGMesh built from
+// vertex/element arrays and boundary edges, periodic pairing, a DG space, a solver built from
+// (mesh, gamma), and states held as std::vector of Np x 4 matrices (the layer's own dense type
+// here; dgfem's Eigen::MatrixXd when Eigen is on the include path).  Reads its inputs from files written by
 // tests/test_gpu_cpp_layer.py and writes the results next to them as raw doubles.
 //   usage: test_dgfem_compat <dir>
 #include <dgx_dgfem.hpp>
@@ -11,17 +12,7 @@
 #include <string>
 #include <vector>
 
-struct Mat {  // the minimal matrix interface the layer needs (Eigen::MatrixXd has it too)
-    int r = 0, c = 0;
-    std::vector<double> a;
-    Mat() = default;
-    Mat(int rr, int cc) { resize(rr, cc); }
-    long rows() const { return r; }
-    long cols() const { return c; }
-    void resize(int rr, int cc) { r = rr; c = cc; a.assign((size_t)rr * cc, 0.0); }
-    double& operator()(long i, long j) { return a[(size_t)j * r + i]; }  // column-major, as Eigen
-    double operator()(long i, long j) const { return a[(size_t)j * r + i]; }
-};
+using Mat = dgx_dgfem::MatrixXd;
 
 template <class T>
 static std::vector<T> read_all(const std::string& path) {
@@ -57,29 +48,35 @@ int main(int argc, char** argv) {
     const int nvpe = (int)P[2], basis = (int)P[3];
 
     Mat verts((int)V.size() / 2, 2);
-    for (int i = 0; i < verts.r; ++i) { verts(i, 0) = V[2 * i]; verts(i, 1) = V[2 * i + 1]; }
-    Mat elems((int)E.size() / nvpe, nvpe);
-    for (int i = 0; i < elems.r; ++i)
+    for (long i = 0; i < verts.rows(); ++i) { verts(i, 0) = V[2 * i]; verts(i, 1) = V[2 * i + 1]; }
+    dgx_dgfem::MatrixXi elems((int)E.size() / nvpe, nvpe);
+    for (long i = 0; i < elems.rows(); ++i)
         for (int k = 0; k < nvpe; ++k) elems(i, k) = E[(size_t)nvpe * i + k];
     std::map<int, std::vector<std::pair<int, int>>> edges;
     for (size_t k = 0; k + 2 < B.size(); k += 3) edges[B[k]].push_back({B[k + 1], B[k + 2]});
     const std::map<std::string, int> tags = {{"Bottom", 2}, {"Right", 3}, {"Top", 4}, {"Left", 5}};
 
     try {
-        dgx_dgfem::Mesh mesh(verts, elems, tags, edges);
-        if (mesh.get_element_type() != (nvpe == 4 ? "quad" : "triangle")) return 4;
-        mesh.set_periodic_boundaries("Left", "Right");
-        mesh.set_periodic_boundaries("Bottom", "Top");
-        dgx_dgfem::EulerDGSolver solver(mesh, order, basis, 1.4);
+        auto mesh = std::make_shared<dgx_dgfem::DGMesh>(verts, elems, dgx_dgfem::VectorXi(elems.rows()), tags, edges);
+        const std::string type = nvpe == 4 ? "quad" : "triangle";
+        if (mesh->get_element_type() != type) return 4;
+        mesh->set_periodic_boundaries("Left", "Right");
+        mesh->set_periodic_boundaries("Bottom", "Top");
+        mesh->initialize_dg_space(std::make_shared<dgx_dgfem::DGSpace>(type, order, basis), 4);
+        dgx_dgfem::EulerDGSolver solver(mesh, 1.4);
+        // the assembler on its own, as DGAssembler(mesh, weak_form)
+        dgx_dgfem::DGAssembler assembler(mesh, std::make_shared<dgx_dgfem::EulerWeakFormulation>(1.4));
         const int ne = solver.n_elements(), np = solver.n_basis();
         std::vector<Mat> u(ne, Mat(np, 4));
         for (int e = 0; e < ne; ++e)
             for (int i = 0; i < np; ++i)
                 for (int v = 0; v < 4; ++v) u[e](i, v) = U[((size_t)e * np + i) * 4 + v];
 
-        std::vector<Mat> R;
+        std::vector<Mat> R, R2;
         solver.assemble_euler_residual(u, R);
+        assembler.assemble_euler_residual(u, R2);
         write_state(dir + "/residual.bin", R);
+        write_state(dir + "/residual_assembler.bin", R2);
         write_state(dir + "/minv.bin", solver.apply_mass_inv(R));
         write_state(dir + "/rk3.bin", solver.time_step_ssp_rk3(u, dt));
         const double cfl = solver.compute_max_cfl(u, dt);
