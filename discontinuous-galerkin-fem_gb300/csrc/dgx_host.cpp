@@ -1138,6 +1138,26 @@ static int enqueue_rk3(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
     return launch(c, a, s);
 }
 
+extern "C" int dgx_rk3_stage(dgx_ctx* c, const double* u_n, const double* u_s, double* out, double dt, int stage,
+                             void* stream) {
+    if (!c || stage < 1 || stage > 3 || (c->ne && (!u_n || !u_s || !out)) || (c->ne && out == u_s))
+        return fail(DGX_ERR_INVALID, "dgx_rk3_stage: bad argument");
+    if (c->prm.precision == DGX_MIXED)
+        return fail(DGX_ERR_INVALID, "dgx_rk3_stage: FP64 and double-float contexts only");
+    if (c->ne == 0) return DGX_OK;
+    static const double A[3] = {0.0, 0.75, 1.0 / 3.0}, B[3] = {1.0, 0.25, 2.0 / 3.0};
+    StepArgs a = base_args(c);
+    a.mode = MODE_STAGE;
+    a.status = c->d_status;
+    a.dt = dt;
+    a.u = u_s;
+    a.un = stage == 1 ? nullptr : u_n;
+    a.out = out;
+    a.a = A[stage - 1];
+    a.b = B[stage - 1];
+    return launch(c, a, (cudaStream_t)stream);
+}
+
 // Mixed precision: the three stages of one step, reading the FP32 copy uhi[src] of u^n
 // and writing the FP32 copy of u^{n+1} to uhi[1 - src] (see StageArgs).
 static StageArgs mixed_stage_args(const dgx_ctx* c, double* u, double dt, int src) {

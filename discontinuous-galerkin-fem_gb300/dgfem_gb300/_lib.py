@@ -49,6 +49,7 @@ SIGNATURES = {
     "dgx_apply_mass_inv": (C.c_int, [_vp, _vp, _vp, _vp]),
     "dgx_rhs": (C.c_int, [_vp, _vp, _vp, _vp]),
     "dgx_rk3_step": (C.c_int, [_vp, _vp, C.c_double, C.c_int, _vp]),
+    "dgx_rk3_stage": (C.c_int, [_vp, _vp, _vp, _vp, C.c_double, C.c_int, _vp]),
     "dgx_max_cfl": (C.c_int, [_vp, _vp, C.c_double, _dp, _vp]),
     "dgx_density_range": (C.c_int, [_vp, _vp, _dp, _dp, _vp]),
     "dgx_has_nan": (C.c_int, [_vp, _vp, _ip, _vp]),

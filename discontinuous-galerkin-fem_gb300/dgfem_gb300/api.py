@@ -318,6 +318,13 @@ class DGContext:
         check(lib.dgx_rk3_step_host(self._h, _dptr(u), float(dt), int(n_steps)))
         return u
 
+    def rk3_stage(self, u_n, u_s, out, dt: float, stage: int):
+        """One SSP-RK3 stage on CUDA tensors (dgx_rk3_stage; FP64 and df64 contexts): the stage
+        the step makes, for drivers that exchange data between stages (dgfem_gb300.partition)."""
+        check(L.load().dgx_rk3_stage(self._h, self._dev(u_n), self._dev(u_s), self._dev(out), float(dt), int(stage),
+                                     _stream_of(out)))
+        return out
+
     def launch_shape(self) -> Tuple[int, int, bool]:
         """(grid, tiles, tensor_cores) of the mixed stage kernel; grid is 0 until the first
         rk3_step; tensor_cores is True for the 3xTF32 tcgen05 form."""

@@ -159,6 +159,15 @@ int dgx_rhs(dgx_ctx* c, const double* u, double* du, void* stream);
  * of a step are captured once into a CUDA graph and replayed. */
 int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void* stream);
 
+/* One stage of time_step_ssp_rk3 (include/dgfem/solver/time_stepping.hpp:39-55) on device
+ * states, for drivers that exchange data between stages (element partitions with a halo
+ * exchange): stage 1: out = u_s + dt L(u_s) (u_s = u_n); stage 2: out = 3/4 u_n + 1/4 (u_s +
+ * dt L(u_s)); stage 3: out = 1/3 u_n + 2/3 (u_s + dt L(u_s)), L = M^-1 R.  Each stage is the
+ * launch dgx_rk3_step makes for it, so three calls equal one step bit for bit.  FP64 and
+ * double-float contexts; out may alias u_n but not u_s. */
+int dgx_rk3_stage(dgx_ctx* c, const double* u_n, const double* u_s, double* out, double dt, int stage,
+                  void* stream);
+
 /* CompressibleDGSolverBase::compute_max_cfl / compute_density_range,
  * src/solver/compressible_solver_base.cpp:114-199.  Results are written to host memory
  * (the call synchronises the stream).  CFL is +inf when rho<=0 or p<=0 anywhere. */
