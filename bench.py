@@ -76,6 +76,21 @@ def vortex(xy, t=0.0, beta=5.0, xc=0.0, yc=0.0, uinf=0.5, vinf=0.0, gamma=GAMMA,
     return np.stack([rho, rho * u, rho * v, p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v)], -1)
 
 
+def vortex_device(xy, t=0.0, beta=5.0, xc=0.0, yc=0.0, uinf=0.5, vinf=0.0, gamma=GAMMA, period=10.0):
+    """vortex() on a CUDA tensor of points (the initial condition evaluated on the GPU)."""
+    import torch
+    x = xy[..., 0] - (xc + uinf * t)
+    y = xy[..., 1] - (yc + vinf * t)
+    x = torch.remainder(x + period / 2, period) - period / 2
+    y = torch.remainder(y + period / 2, period) - period / 2
+    g = beta / (2.0 * np.pi) * torch.exp(0.5 * (1.0 - (x * x + y * y)))
+    u, v = uinf - y * g, vinf + x * g
+    T = 1.0 - (gamma - 1.0) / (2.0 * gamma) * g * g
+    rho = T ** (1.0 / (gamma - 1.0))
+    p = rho * T
+    return torch.stack([rho, rho * u, rho * v, p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v)], -1)
+
+
 def taylor_green(xy, seed=0, gamma=GAMMA, mach=0.1, noise=1e-3):
     """Decaying Taylor-Green-type vortex on [0, 2 pi]^2 (conserved variables): rho=1,
     u=sin x cos y, v=-cos x sin y, p = 1/(gamma M^2) + (cos 2x + cos 2y)/4, plus seeded
@@ -463,9 +478,11 @@ def main():
     ne, nb = c64.n_elements, c64.n_basis
     dof = ne * nb * 4
     xc, yc = vortex_centre(args.seed)
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    xq = c64.quad_points()
-    uq = torch.tensor(vortex(xq, xc=xc, yc=yc), device="cuda")
+    xq_dev = c64.quad_points_device()
+    uq = vortex_device(xq_dev, xc=xc, yc=yc)
+    torch.cuda.synchronize()
     t_ic = time.perf_counter() - t0
     t0 = time.perf_counter()
     u0 = c64.project(uq)
@@ -473,7 +490,7 @@ def main():
     t_proj = time.perf_counter() - t0
     del uq
     setup = {"elements": ne, "mesh_and_periodic_pairing_s": t_mesh, "context_fp64_s": t_ctx,
-             "initial_condition_on_host_s": t_ic, "l2_projection_gpu_s": t_proj}
+             "initial_condition_on_gpu_s": t_ic, "l2_projection_gpu_s": t_proj}
     dt = CFL / c64.max_cfl(u0, 1.0)
 
     # ---- accuracy at t_final: mixed vs FP64 (the FP64 path matches the oracle to 1e-12 per RHS)
@@ -484,7 +501,7 @@ def main():
         c64.rk3_step(u64, dt, args.acc_steps)
         cmx.rk3_step(umx, dt, args.acc_steps)
         torch.cuda.synchronize()
-        exact = c64.project(torch.tensor(vortex(xq, t=dt * args.acc_steps, xc=xc, yc=yc), device="cuda"))
+        exact = c64.project(vortex_device(xq_dev, t=dt * args.acc_steps, xc=xc, yc=yc))
         d = (umx - u64)
         acc = {"steps": args.acc_steps, "t_final": dt * args.acc_steps,
                "mixed_vs_fp64_l2_rel": float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(u64)),

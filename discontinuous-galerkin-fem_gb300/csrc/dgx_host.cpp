@@ -361,17 +361,20 @@ static void rebuild_faces(dgx_mesh* m) {
     const int ne = m->ne(), K = m->nvpe;
     m->ifaces.clear();
     m->bfaces.clear();
-    std::unordered_set<unsigned long long> seen;
-    seen.reserve((size_t)ne * 2);
+    m->ifaces.reserve((size_t)ne * K / 2 * 5 + 16);
     double VL[8], VR[8];
     for (int L = 0; L < ne; ++L) {
         elem_verts(m, L, VL);
+        const int* nb = &m->nbr[2 * (size_t)K * L];
         for (int fL = 0; fL < K; ++fL) {
-            const int R = m->nbr[2 * ((size_t)K * L + fL)], fR = m->nbr[2 * ((size_t)K * L + fL) + 1];
+            const int R = nb[2 * fL], fR = nb[2 * fL + 1];
             if (R >= 0) {
-                const unsigned long long key =
-                    ((unsigned long long)std::min(L, R) << 32) | (unsigned)std::max(L, R);
-                if (!seen.insert(key).second) continue;
+                // one face per element pair, at its first occurrence in element order (dgfem keys
+                // its face set by the pair): met here when R >= L and no earlier face of L has R
+                if (R < L) continue;
+                bool earlier = false;
+                for (int g = 0; g < fL; ++g) earlier |= nb[2 * g] == R;
+                if (earlier) continue;
                 elem_verts(m, R, VR);
                 const int rec[5] = {L, R, fL, fR, face_reversed(K, VL, fL, VR, fR) ? 1 : 0};
                 m->ifaces.insert(m->ifaces.end(), rec, rec + 5);
@@ -382,27 +385,40 @@ static void rebuild_faces(dgx_mesh* m) {
         }
     }
 }
-
-// DGMesh ctor, build_face_connectivity and identify_boundary_faces
-// (src/core/mesh.cpp:18-51, 312-402) with a sort instead of dgfem's O(E*F) map scan.
 static int build_connectivity(dgx_mesh* m, int nbe, const int* bedges) {
     const int ne = m->ne(), K = m->nvpe;
-    struct Rec { int a, b, ord; };
-    std::vector<Rec> r((size_t)ne * K);
+    // face slots keyed by their vertex pair (min, max): a stable radix sort of the packed keys
+    // keeps equal pairs in slot order (the first two slots of a pair become neighbours)
+    const size_t ns = (size_t)ne * K;
+    const uint64_t nv = (uint64_t)(m->verts.size() / 2);
+    std::vector<uint64_t> key(ns), key2(ns);
+    std::vector<int> ord(ns), ord2(ns);
     for (int e = 0; e < ne; ++e)
         for (int f = 0; f < K; ++f) {
             const int v1 = m->elems[(size_t)K * e + f], v2 = m->elems[(size_t)K * e + (f + 1) % K];
-            r[(size_t)K * e + f] = {std::min(v1, v2), std::max(v1, v2), K * e + f};
+            key[(size_t)K * e + f] = (uint64_t)std::min(v1, v2) * nv + (uint64_t)std::max(v1, v2);
+            ord[(size_t)K * e + f] = K * e + f;
         }
-    std::sort(r.begin(), r.end(), [](const Rec& x, const Rec& y) {
-        return x.a != y.a ? x.a < y.a : x.b != y.b ? x.b < y.b : x.ord < y.ord;
-    });
+    uint64_t kmax = 0;
+    for (uint64_t k : key) kmax = std::max(kmax, k);
+    for (int shift = 0; shift < 64 && (kmax >> shift) != 0; shift += 16) {
+        std::vector<size_t> count(65537, 0);
+        for (uint64_t k : key) ++count[((k >> shift) & 0xFFFF) + 1];
+        for (int d = 0; d < 65536; ++d) count[d + 1] += count[d];
+        for (size_t i = 0; i < ns; ++i) {
+            const size_t pos = count[(key[i] >> shift) & 0xFFFF]++;
+            key2[pos] = key[i];
+            ord2[pos] = ord[i];
+        }
+        key.swap(key2);
+        ord.swap(ord2);
+    }
     m->nbr.assign((size_t)ne * 2 * K, -1);
-    for (size_t i = 0; i < r.size();) {
+    for (size_t i = 0; i < ns;) {
         size_t j = i;
-        while (j < r.size() && r[j].a == r[i].a && r[j].b == r[i].b) ++j;
+        while (j < ns && key[j] == key[i]) ++j;
         if (j - i >= 2) {  // the first two faces of a vertex pair become neighbours
-            const int e1 = r[i].ord / K, f1 = r[i].ord % K, e2 = r[i + 1].ord / K, f2 = r[i + 1].ord % K;
+            const int e1 = ord[i] / K, f1 = ord[i] % K, e2 = ord[i + 1] / K, f2 = ord[i + 1] % K;
             m->nbr[2 * ((size_t)K * e1 + f1)] = e2;
             m->nbr[2 * ((size_t)K * e1 + f1) + 1] = f2;
             m->nbr[2 * ((size_t)K * e2 + f2)] = e1;
@@ -1392,6 +1408,14 @@ extern "C" int dgx_step_status(dgx_ctx* c, int* nonfinite, void* stream) {
 extern "C" int dgx_quad_points(const dgx_ctx* c, double* xq) {
     if (!c || !xq) return fail(DGX_ERR_INVALID, "dgx_quad_points: null argument");
     std::copy(c->xq.begin(), c->xq.end(), xq);
+    return DGX_OK;
+}
+
+extern "C" int dgx_quad_points_device(const dgx_ctx* c, double* xq, void* stream) {
+    if (!c || (c->ne && !xq)) return fail(DGX_ERR_INVALID, "dgx_quad_points_device: bad argument");
+    if (c->xq.empty()) return DGX_OK;
+    CUDA_OK(cudaMemcpyAsync(xq, c->xq.data(), c->xq.size() * sizeof(double), cudaMemcpyHostToDevice,
+                            (cudaStream_t)stream));
     return DGX_OK;
 }
 

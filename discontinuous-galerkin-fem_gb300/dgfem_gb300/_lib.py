@@ -54,6 +54,7 @@ SIGNATURES = {
     "dgx_density_range": (C.c_int, [_vp, _vp, _dp, _dp, _vp]),
     "dgx_has_nan": (C.c_int, [_vp, _vp, _ip, _vp]),
     "dgx_quad_points": (C.c_int, [_vp, _dp]),
+    "dgx_quad_points_device": (C.c_int, [_vp, _vp, _vp]),
     "dgx_project": (C.c_int, [_vp, _vp, _vp, _vp]),
     "dgx_residual_host": (C.c_int, [_vp, _dp, _dp]),
     "dgx_rk3_step_host": (C.c_int, [_vp, _dp, C.c_double, C.c_int]),

@@ -344,6 +344,14 @@ class DGContext:
         check(L.load().dgx_quad_points(self._h, _dptr(xq)))
         return xq
 
+    def quad_points_device(self):
+        """quad_points() as a CUDA tensor, for evaluating an initial condition on the GPU."""
+        import torch
+        xq = torch.empty((self.n_elements, self.n_quad, 2), dtype=torch.float64, device="cuda")
+        check(L.load().dgx_quad_points_device(self._h, C.c_void_p(xq.data_ptr()),
+                                              C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        return xq
+
     def project(self, uq):
         """L2 projection of values at quad_points() (device tensor in, device tensor out)."""
         import torch

@@ -189,6 +189,9 @@ int dgx_step_status(dgx_ctx* c, int* nonfinite, void* stream);
 /* Physical coordinates of every volume quadrature point, [n_elements][n_quad][2] (host),
  * GeometricMapping::map_to_physical at the points project_initial_condition uses. */
 int dgx_quad_points(const dgx_ctx* c, double* xq);
+/* The same points written to device memory xq (n_elements * n_quad * 2 doubles), stream-ordered,
+ * for evaluating an initial condition on the GPU before dgx_project. */
+int dgx_quad_points_device(const dgx_ctx* c, double* xq, void* stream);
 /* CompressibleDGSolverBase::project_initial_condition, src/solver/compressible_solver_base.cpp:63-104:
  * uq = the initial condition at dgx_quad_points, [n_elements][n_quad][4] (device). */
 int dgx_project(dgx_ctx* c, const double* uq, double* u, void* stream);

@@ -238,3 +238,13 @@ def test_config1_vortex_200_steps_fp64(dg):
     exact = om.project(isentropic_vortex(om.quad_points(), t=200 * dt, beta=5.0))
     assert abs(rel(out, exact) - rel(ref, exact)) <= 1e-8
     assert rel(out, exact) < 2e-3
+
+
+def test_quad_points_on_device_equal_host_points(dg):
+    """dgx_quad_points_device writes the points dgx_quad_points returns (the initial condition
+    can then be evaluated on the GPU before dgx_project)."""
+    m = dg.DGMesh.rectangle(9, 7, -5.0, 5.0, -3.0, 4.0, periodic=True)
+    ctx = dg.DGContext(m, dg.DGSpace("triangle", 3, "dubiner"), dg.EulerWeakFormulation(1.4), "fp64")
+    xd = ctx.quad_points_device()
+    torch.cuda.synchronize()
+    assert np.array_equal(xd.cpu().numpy(), ctx.quad_points())
