@@ -445,6 +445,7 @@ def main():
     ap.add_argument("--ns-steps", type=int, default=1000, help="steps of the Navier-Stokes leg (0: skip)")
     ap.add_argument("--adj-steps", type=int, default=1000, help="steps of the adjoint leg (0: skip)")
     ap.add_argument("--adj-dirs", type=int, default=16, help="finite-difference directions of the adjoint check")
+    ap.add_argument("--adj-snapshots", type=int, default=20, help="snapshots of the binomial-checkpointing gradient")
     ap.add_argument("--batch-instances", type=int, default=256, help="instances of the batched leg (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=300, help="SSP-RK3 steps of each batched instance")
     ap.add_argument("--quad-cells", type=int, default=256, help="quadrilaterals per side of the quad leg (0: skip)")
@@ -665,7 +666,8 @@ def main():
         del n64, nmx
 
     # ---- adjoint leg: shear layer 128x128x2, p=3, J = kinetic energy after adj_steps steps,
-    #      checkpoints every 50 steps; adjoint/forward time ratio and FD / tangent-linear checks
+    #      checkpoints every 50 steps, and again with binomial checkpointing (memory held and
+    #      forward steps recomputed by each); adjoint/forward time ratio and FD / tangent-linear checks
     adj = None
     if args.adj_steps > 0:
         amesh = dg.DGMesh.rectangle(128, 128, 0.0, 1.0, 0.0, 1.0, periodic=True)
@@ -687,6 +689,19 @@ def main():
         Jv, grad = actx.kinetic_energy_gradient(au0, adt, na, ce)
         torch.cuda.synchronize()
         t_grad = time.perf_counter() - t0
+        # binomial checkpointing: adj_snapshots states instead of the uniform scheme's
+        # (na / ce + 1) checkpoints and 3 ce + 1 segment states, at the price of recomputed steps
+        nsnap = args.adj_snapshots
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Jb, gradb, bst = actx.kinetic_energy_gradient_binomial(au0, adt, na, nsnap)
+        torch.cuda.synchronize()
+        t_bin = time.perf_counter() - t0
+        binomial = dict(bst, snapshots=nsnap, gradient_s=t_bin, gradient_vs_forward_solve=t_bin / t_fwd,
+                        equals_uniform_bitwise=bool(Jb == Jv and torch.equal(gradb, grad)),
+                        state_mb=bst["states_held"] * au0.numel() * 8 / 1e6)
+        del gradb
+        uniform_states = (na + ce - 1) // ce + 1 + 3 * min(ce, na) + 1
         rng = np.random.default_rng(1234)
         h = 1e-6
         fd_err, tlm_err, fd_abs, fd_cs = [], [], [], []
@@ -725,6 +740,8 @@ def main():
                "forward_ms_per_step": 1e3 * t_fwd / na, "gradient_s": t_grad,
                "gradient_vs_forward_solve": t_grad / t_fwd,
                "adjoint_step_vs_forward_step": (t_grad - t_fwd) / t_fwd,
+               "uniform_states_held": uniform_states, "uniform_recomputed_steps": na,
+               "uniform_state_mb": uniform_states * au0.numel() * 8 / 1e6, "binomial": binomial,
                "fd_directions": args.adj_dirs, "fd_h": h, "fd_direction_norm": "||d|| = ||u0|| (h is a relative step)",
                "fd_max_rel_err": max(fd_err) if fd_err else None,
                "fd_median_rel_err": float(np.median(fd_err)) if fd_err else None,

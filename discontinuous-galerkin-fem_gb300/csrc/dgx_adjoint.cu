@@ -355,3 +355,140 @@ extern "C" int dgx_kinetic_energy_gradient(dgx_ctx* c, const double* u0, double 
     if (rc == DGX_ERR_CUDA && std::string(dgx_last_error()).empty()) dgx::set_error(rc, "gradient sweep failed");
     return rc;
 }
+
+// ---------------------------------------------------------------- binomial checkpointing
+// The reverse sweep of n SSP-RK3 steps with s snapshot states beside the stored start state:
+// F(n, s) = the fewest forward steps it recomputes, F(1, s) = 0 (one adjoint step recomputes
+// its own two stages), F(n, 0) = n (n - 1) / 2 (every step re-advanced from the start), and
+// F(n, s) = min over k of k + F(n - k, s - 1) + F(k, s): advance k steps into a snapshot, reverse
+// the n - k steps after it with one snapshot fewer, then the k steps before it.  Solved exactly
+// by dynamic programming; its minima are the binomial schedules of Griewank's revolve.
+namespace {
+struct BinomialSchedule {
+    int N = 0, S = 0;
+    std::vector<long long> F;
+    std::vector<int> K;
+    size_t at(int n, int s) const { return (size_t)n * (S + 1) + s; }
+    void build(int n_steps, int snaps) {
+        N = n_steps;
+        S = snaps;
+        F.assign((size_t)(N + 1) * (S + 1), 0);
+        K.assign(F.size(), 1);
+        for (int n = 1; n <= N; ++n) F[at(n, 0)] = (long long)n * (n - 1) / 2;
+        for (int sn = 1; sn <= S; ++sn)
+            for (int n = 2; n <= N; ++n) {
+                long long best = -1;
+                int bk = 1;
+                for (int k = 1; k < n; ++k) {
+                    const long long v = k + F[at(n - k, sn - 1)] + F[at(k, sn)];
+                    if (best < 0 || v < best) {
+                        best = v;
+                        bk = k;
+                    }
+                }
+                F[at(n, sn)] = best;
+                K[at(n, sn)] = bk;
+            }
+    }
+};
+
+struct BinomialRun {
+    dgx_ctx* c;
+    double dt;
+    cudaStream_t st;
+    const BinomialSchedule* plan;
+    std::vector<double*> snap;  // snap[l - 1]: the snapshot of recursion level l
+    double* work;               // the re-advanced state of the levels without snapshots
+    double* grad;
+    long long recomputed = 0;
+
+    int step(double* x) {  // one SSP-RK3 step in place
+        int rc = fwd_stage(c, x, nullptr, c->d_u1, 0.0, 1.0, dt, st);
+        if (!rc) rc = fwd_stage(c, c->d_u1, x, c->d_u2, 0.75, 0.25, dt, st);
+        if (!rc) rc = fwd_stage(c, c->d_u2, x, x, 1.0 / 3.0, 2.0 / 3.0, dt, st);
+        return rc;
+    }
+    int adjoint_at(const double* x) {  // the cotangent across the step that starts at x
+        int rc = fwd_stage(c, x, nullptr, c->d_u1, 0.0, 1.0, dt, st);
+        if (!rc) rc = fwd_stage(c, c->d_u1, x, c->d_u2, 0.75, 0.25, dt, st);
+        if (!rc) rc = adjoint_step(c, x, c->d_u1, c->d_u2, grad, dt, st);
+        return rc;
+    }
+    int copy(double* dst, const double* src) {
+        return cudaMemcpyAsync(dst, src, c->nstate * sizeof(double), cudaMemcpyDeviceToDevice, st) == cudaSuccess
+                   ? DGX_OK
+                   : dgx::set_error(DGX_ERR_CUDA, "state copy failed");
+    }
+    // reverses the n steps after state ua (left unchanged) with sn snapshots
+    int reverse(const double* ua, int n, int sn) {
+        if (n == 1) return adjoint_at(ua);
+        if (sn == 0) {
+            for (int j = n - 1; j >= 0; --j) {
+                if (int rc = copy(work, ua)) return rc;
+                for (int t = 0; t < j; ++t)
+                    if (int rc = step(work)) return rc;
+                recomputed += j;
+                if (int rc = adjoint_at(work)) return rc;
+            }
+            return DGX_OK;
+        }
+        const int k = plan->K[plan->at(n, sn)];
+        double* sp = snap[sn - 1];
+        if (int rc = copy(sp, ua)) return rc;
+        for (int t = 0; t < k; ++t)
+            if (int rc = step(sp)) return rc;
+        recomputed += k;
+        if (int rc = reverse(sp, n - k, sn - 1)) return rc;
+        return reverse(ua, k, sn);
+    }
+};
+}  // namespace
+
+extern "C" int dgx_kinetic_energy_gradient_binomial(dgx_ctx* c, const double* u0, double dt, int n_steps,
+                                                    int n_snapshots, double* J, double* grad, long long* stats,
+                                                    void* stream) {
+    if (c && c->nvpe == 4)
+        return dgx::set_error(DGX_ERR_INVALID, "dgx_kinetic_energy_gradient_binomial: triangle meshes only");
+    if (!c || (c->ne && (!u0 || !grad)) || n_steps < 0 || n_snapshots < 0)
+        return dgx::set_error(DGX_ERR_INVALID, "dgx_kinetic_energy_gradient_binomial: bad argument");
+    // the schedule costs O(n_steps^2 n_snapshots) host operations
+    if ((double)n_steps * n_steps * (n_snapshots + 1) > 4.0e9)
+        return dgx::set_error(DGX_ERR_INVALID,
+                              "dgx_kinetic_energy_gradient_binomial: n_steps^2 * (n_snapshots + 1) above 4e9; "
+                              "use dgx_kinetic_energy_gradient's uniform checkpoints");
+    if (int rc = need_adjoint(c, "dgx_kinetic_energy_gradient_binomial")) return rc;
+    if (c->ne == 0) return DGX_OK;
+    if (int rc = ensure_adjoint_buffers(c)) return rc;
+    const int snaps = std::min(n_snapshots, std::max(n_steps - 1, 0));
+    BinomialSchedule plan;
+    plan.build(n_steps, snaps);
+    BinomialRun run{c, dt, (cudaStream_t)stream, &plan, std::vector<double*>(snaps, nullptr), nullptr, grad};
+    const size_t sb = c->nstate * sizeof(double);
+    auto release = [&]() {
+        for (double* p : run.snap) cudaFree(p);
+        cudaFree(run.work);
+    };
+    if (cudaMalloc((void**)&run.work, sb) != cudaSuccess) {
+        cudaGetLastError();
+        return dgx::set_error(DGX_ERR_CUDA, "cudaMalloc failed for the work state");
+    }
+    for (auto& p : run.snap)
+        if (cudaMalloc((void**)&p, sb) != cudaSuccess) {
+            cudaGetLastError();
+            release();
+            return dgx::set_error(DGX_ERR_CUDA, "cudaMalloc failed for snapshots");
+        }
+    // forward sweep to u(T) for the objective and its gradient, then the reverse sweep
+    int rc = run.copy(run.work, u0);
+    for (int n = 0; n < n_steps && !rc; ++n) rc = run.step(run.work);
+    if (!rc) rc = dgx_kinetic_energy(c, run.work, J, grad, stream);
+    if (!rc && n_steps > 0) rc = run.reverse(u0, n_steps, snaps);
+    if (!rc && cudaStreamSynchronize(run.st) != cudaSuccess) rc = dgx::set_error(DGX_ERR_CUDA, "gradient sweep failed");
+    release();
+    if (stats) {
+        stats[0] = run.recomputed;                                   // forward steps of the reverse sweep
+        stats[1] = snaps + 1;                                        // states held besides u0 and the stages
+        stats[2] = n_steps > 0 ? plan.F[plan.at(n_steps, snaps)] : 0;  // the schedule's optimum
+    }
+    return rc;
+}

@@ -71,6 +71,8 @@ SIGNATURES = {
     "dgx_rk3_step_adjoint": (C.c_int, [_vp, _vp, _vp, C.c_double, _vp]),
     "dgx_kinetic_energy": (C.c_int, [_vp, _vp, _dp, _vp, _vp]),
     "dgx_kinetic_energy_gradient": (C.c_int, [_vp, _vp, C.c_double, C.c_int, C.c_int, _dp, _vp, _vp]),
+    "dgx_kinetic_energy_gradient_binomial": (C.c_int, [_vp, _vp, C.c_double, C.c_int, C.c_int, _dp, _vp,
+                                                       C.POINTER(C.c_longlong), _vp]),
     "dgx_launch_shape": (C.c_int, [_vp, _ip, _ip, _ip]),
     "dgx_eval_points": (C.c_int, [_vp, C.c_int, _dp, _vp, _vp, _vp]),
     "dgx_step_status": (C.c_int, [_vp, _ip, _vp]),

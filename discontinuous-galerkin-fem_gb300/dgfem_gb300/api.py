@@ -430,6 +430,19 @@ class DGContext:
                                                    _stream_of(u0)))
         return J.value, g
 
+    def kinetic_energy_gradient_binomial(self, u0, dt: float, n_steps: int, n_snapshots: int):
+        """(J(u(T)), dJ/du0, stats) by binomial checkpointing with n_snapshots device states;
+        stats = {"recomputed_steps", "states_held", "optimal_recomputed_steps"}."""
+        import torch
+        J = C.c_double()
+        g = torch.empty_like(u0)
+        st = (C.c_longlong * 3)()
+        check(L.load().dgx_kinetic_energy_gradient_binomial(self._h, self._dev(u0), float(dt), int(n_steps),
+                                                            int(n_snapshots), C.byref(J), self._dev(g), st,
+                                                            _stream_of(u0)))
+        return J.value, g, {"recomputed_steps": int(st[0]), "states_held": int(st[1]),
+                            "optimal_recomputed_steps": int(st[2])}
+
 
 class _DeviceArray:
     """CUDA array interface over float64 device memory owned by a DGBatch (torch.as_tensor

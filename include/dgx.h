@@ -249,6 +249,17 @@ int dgx_kinetic_energy(dgx_ctx* c, const double* u, double* J, double* grad, voi
  * grad (device state) are outputs.  Allocates its checkpoint storage for the call.  Euler only. */
 int dgx_kinetic_energy_gradient(dgx_ctx* c, const double* u0, double dt, int n_steps, int checkpoint_every,
                                 double* J, double* grad, void* stream);
+/* The same gradient with binomial checkpointing (the schedules of Griewank's revolve, found by
+ * dynamic programming): n_snapshots device states beside u0 and one work state, and the fewest
+ * recomputed forward steps any schedule with that memory needs: with c = n_snapshots + 1
+ * checkpoints (u0 included), t n - C(c + t, t - 1) for C(c + t - 1, t - 1) < n <= C(c + t, t)
+ * (Griewank and Walther, ACM TOMS 26 (2000)).  The gradient equals
+ * dgx_kinetic_energy_gradient's bit for bit.
+ * stats (may be NULL): [0] forward steps recomputed in the reverse sweep, [1] states held
+ * (snapshots + the work state), [2] the schedule's optimum.  Rejects n_steps^2 (n_snapshots + 1)
+ * > 4e9 (the schedule's host cost).  Euler only; no counterpart in dgfem. */
+int dgx_kinetic_energy_gradient_binomial(dgx_ctx* c, const double* u0, double dt, int n_steps, int n_snapshots,
+                                         double* J, double* grad, long long* stats, void* stream);
 
 /* ---------------------------------------------------------------- allocation-free stepping */
 

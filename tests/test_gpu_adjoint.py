@@ -159,3 +159,46 @@ def test_adjoint_rejects_unsupported_contexts(dg):
     ns = dg.DGContext(m, dg.DGSpace("triangle", 2, "dubiner"), dg.NavierStokesWeakFormulation(), "fp64")
     with pytest.raises(ValueError):
         ns.residual_vjp(u, u)
+
+
+def binomial_optimum(n, snapshots):
+    """Griewank and Walther's minimal forward-step count for reversing n steps with c = snapshots + 1
+    checkpoints (the start state included): t n - C(c + t, t - 1), C(c + t - 1, t - 1) < n <= C(c + t, t)."""
+    from math import comb
+    if n <= 1:
+        return 0
+    c = snapshots + 1
+    t = 0
+    while comb(c + t, t) < n:
+        t += 1
+    return t * n - comb(c + t, t - 1)
+
+
+@pytest.mark.parametrize("n,snapshots", [(1, 3), (2, 0), (9, 0), (20, 1), (20, 3), (33, 2), (20, 40)])
+def test_binomial_checkpointing_equals_uniform(dg, n, snapshots):
+    """The gradient with binomial checkpointing equals the uniform-checkpoint gradient bit for bit
+    (the same forward states, the same adjoint steps in the same order); the forward steps it
+    recomputes are the published optimum for its memory."""
+    om, ctx, ph, u = make(dg, n=6, order=3)
+    dt = 0.05 / om.max_cfl(1.4, u, 1.0)
+    J1, g1 = ctx.kinetic_energy_gradient(T(u), dt, n, 7)
+    J2, g2, st = ctx.kinetic_energy_gradient_binomial(T(u), dt, n, snapshots)
+    assert J1 == J2
+    assert torch.equal(g1, g2)
+    s = min(snapshots, n - 1)
+    assert st["states_held"] == s + 1
+    assert st["recomputed_steps"] == st["optimal_recomputed_steps"]
+    want = n * (n - 1) // 2 if s == 0 else binomial_optimum(n, s)
+    assert st["optimal_recomputed_steps"] == want
+
+
+def test_binomial_checkpointing_long_run(dg):
+    """500 steps with 10 snapshots: 11 states instead of the uniform scheme's ~70, the gradient
+    still equal bit for bit."""
+    om, ctx, ph, u = make(dg, n=4, order=2)
+    dt = 0.05 / om.max_cfl(1.4, u, 1.0)
+    J1, g1 = ctx.kinetic_energy_gradient(T(u), dt, 500, 23)
+    J2, g2, st = ctx.kinetic_energy_gradient_binomial(T(u), dt, 500, 10)
+    assert J1 == J2 and torch.equal(g1, g2)
+    assert st["recomputed_steps"] == binomial_optimum(500, 10)
+    assert st["recomputed_steps"] <= 4 * 500
