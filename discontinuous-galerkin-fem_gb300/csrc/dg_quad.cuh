@@ -32,6 +32,8 @@
 // and step into the FP64 state.
 #pragma once
 
+#include <memory>
+
 #include "../../include/dgx.h"
 #include "dg_stage.cuh"
 
@@ -114,6 +116,25 @@ struct QKArgs {
     QuadOps<P, T> o;
     MassOps<P> m;
 };
+
+// Order 4: the operators (28 KB in FP64) and the FP64 mass-inverse tables (6 KB) exceed the
+// 32 KB of kernel parameters together, so the mass-inverse tables live in constant memory.
+// They depend on the order only (tensor Gauss-Legendre rule, Legendre basis), so one copy per
+// device and translation unit, written when the kernel is configured, serves every context.
+template <typename T, bool VISC>
+struct QKArgs<4, T, VISC> {
+    StepArgs s;
+    const QuadGeom* geom;
+    const QuadConn* conn;
+    QuadOps<4, T> o;
+};
+static __constant__ MassOps<4> c_quad_mass4;
+
+template <int P, typename T, bool VISC>
+__device__ __forceinline__ const MassOps<P>& qk_mass(const QKArgs<P, T, VISC>& ka) {
+    if constexpr (P == 4) return c_quad_mass4;
+    else return ka.m;
+}
 
 // J_T at (xi, eta): rows (dx/dxi, dy/dxi) and (dx/deta, dy/deta) (mapping.cpp:22-50)
 template <typename T, class QG>
@@ -470,7 +491,7 @@ __global__ void __launch_bounds__(TILE, 1) quad_element_kernel(const __grid_cons
             for (int v = 0; v < NV; ++v) sD[tl * STR + i * NV + v] = to_f64(R[i][v]);
         if (s.mode != MODE_RESIDUAL) {
             double acc[NP][NV];
-            quad_mass_inv_row64<P>(ka.m, ka.geom[e], sD + tl * STR, acc);
+            quad_mass_inv_row64<P>(qk_mass(ka), ka.geom[e], sD + tl * STR, acc);
         }
     }
     __syncthreads();
@@ -503,21 +524,29 @@ inline size_t quad_smem_bytes() {
 
 template <int P, typename T, bool VISC>
 inline int configure_quad_t() {
-    return cudaFuncSetAttribute(quad_element_kernel<P, T, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)quad_smem_bytes<P, T>()) == cudaSuccess
-               ? 0
-               : -1;
+    if (cudaFuncSetAttribute(quad_element_kernel<P, T, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)quad_smem_bytes<P, T>()) != cudaSuccess)
+        return -1;
+    if constexpr (P == 4) {
+        auto h = std::make_unique<OpsHost>();
+        auto m = std::make_unique<MassOps<4>>();
+        if (make_ops(4, DGX_BASIS_LEGENDRE, *h)) return -1;
+        fill_mass_ops<4>(*h, *m);
+        if (cudaMemcpyToSymbol(c_quad_mass4, m.get(), sizeof(MassOps<4>)) != cudaSuccess) return -1;
+    }
+    return 0;
 }
 
 template <int P, typename T, bool VISC>
 inline int launch_quad_t(const StepArgs& a, const QuadGeom* geom, const QuadConn* conn, const OpsHost& oh,
                          cudaStream_t st) {
+    static_assert(sizeof(QKArgs<P, T, VISC>) <= 32764, "quadrilateral kernel arguments exceed the parameter limit");
     QKArgs<P, T, VISC> ka;  // by value: operator reads are constant-bank operands
     ka.s = a;
     ka.geom = geom;
     ka.conn = conn;
     fill_quad_ops<P, T>(oh, ka.o);
-    fill_mass_ops<P>(oh, ka.m);
+    if constexpr (P < 4) fill_mass_ops<P>(oh, ka.m);
     const int grid = (a.ne + TILE - 1) / TILE;
     if (grid == 0) return 0;
     quad_element_kernel<P, T, VISC><<<grid, TILE, quad_smem_bytes<P, T>(), st>>>(ka);
@@ -532,6 +561,8 @@ inline int launch_quad_t(const StepArgs& a, const QuadGeom* geom, const QuadConn
     case 5: return FN<2, T, true> ARGS;              \
     case 6: return FN<3, T, false> ARGS;             \
     case 7: return FN<3, T, true> ARGS;              \
+    case 8: return FN<4, T, false> ARGS;             \
+    case 9: return FN<4, T, true> ARGS;              \
     default: return -1;                              \
     }
 
@@ -610,6 +641,7 @@ inline int configure_quad_stage_t() {
 
 template <int P, bool VISC>
 inline int launch_quad_stage_t(const StageArgs& a, const OpsHost& oh, cudaStream_t st) {
+    static_assert(sizeof(QSArgs<P, VISC>) <= 32764, "quadrilateral stage arguments exceed the parameter limit");
     QSArgs<P, VISC> ka;
     ka.s = a;
     fill_quad_ops<P, float>(oh, ka.o);

@@ -1,29 +1,32 @@
-// Batched mixed-precision SSP-RK3 stage kernel: many independent Euler solves, of uneven
-// sizes and orders 1..4, advanced by one persistent launch per stage.
+// Batched mixed-precision SSP-RK3 stage kernel: many independent Euler or Navier-Stokes
+// solves, of uneven sizes and orders 1..4, advanced by one persistent launch per stage.
 //
 // The instances of one order are concatenated into one element range (their own
 // connectivity, offset into the range), so a tile of 128 elements holds one order only.
 // Tiles of order 1 come first, then order 2, ...; each CTA loads the neighbour-face
 // operators of every order once, then walks the tiles with a grid stride and runs the
 // order's tile body (dg_stage.cuh) on each.  Each element carries its instance number in
-// ElemGeomF::pad and takes its time step from a per-instance table.
+// ElemGeomF::pad and takes its time step from a per-instance table.  The physics (and its
+// parameters) is the batch's: VISC selects the Navier-Stokes tile body for every order.
 #include <cstring>
 
 #include "dg_stage.cuh"
 
 namespace dgx {
 
+template <bool VISC>
 struct BatchArgs {
-    SArgs<1, false> a1;
-    SArgs<2, false> a2;
-    SArgs<3, false> a3;
-    SArgs<4, false> a4;
+    SArgs<1, VISC> a1;
+    SArgs<2, VISC> a2;
+    SArgs<3, VISC> a3;
+    SArgs<4, VISC> a4;
     int tile_end[MAX_P];  // tiles of orders 1..p, cumulative
 };
-static_assert(sizeof(BatchArgs) <= 32764, "batched stage arguments exceed the kernel parameter limit");
+static_assert(sizeof(BatchArgs<false>) <= 32764 && sizeof(BatchArgs<true>) <= 32764,
+              "batched stage arguments exceed the kernel parameter limit");
 
-template <int P>
-__device__ __forceinline__ const SArgs<P, false>& batch_order(const BatchArgs& b) {
+template <int P, bool VISC>
+__device__ __forceinline__ const SArgs<P, VISC>& batch_order(const BatchArgs<VISC>& b) {
     if constexpr (P == 1) return b.a1;
     else if constexpr (P == 2) return b.a2;
     else if constexpr (P == 3) return b.a3;
@@ -31,77 +34,83 @@ __device__ __forceinline__ const SArgs<P, false>& batch_order(const BatchArgs& b
 }
 
 // first shared-memory float of order p's neighbour-face operators (16-byte aligned)
+template <bool VISC>
 __host__ __device__ constexpr int batch_op_off(int p) {
     int s = 0;
-    for (int q = 1; q < p; ++q) s += 3 * n_basis(q) * ((q + 1 + 3) & ~3);
+    for (int q = 1; q < p; ++q) s += (VISC ? 3 : 1) * 3 * n_basis(q) * ((q + 1 + 3) & ~3);
     return s;
 }
 
-template <int P, int PMAX, bool BND>
-__device__ __forceinline__ void batch_tile(const BatchArgs& ka, const float* sOp, float* sU, float* sDt, int t) {
+template <int P, int PMAX, bool VISC, bool BND>
+__device__ __forceinline__ void batch_tile(const BatchArgs<VISC>& ka, const float* sOp, float* sU, float* sDt, int t) {
     if constexpr (P < PMAX) {
         if (t >= ka.tile_end[P - 1]) {
-            batch_tile<P + 1, PMAX, BND>(ka, sOp, sU, sDt, t);
+            batch_tile<P + 1, PMAX, VISC, BND>(ka, sOp, sU, sDt, t);
             return;
         }
     }
     const int t0 = P > 1 ? ka.tile_end[P - 2] : 0;
-    stage_tile<P, false, BND>(batch_order<P>(ka), sOp + batch_op_off(P), sU, sDt, t - t0);
+    stage_tile<P, VISC, BND>(batch_order<P>(ka), sOp + batch_op_off<VISC>(P), sU, sDt, t - t0);
 }
 
-template <int P, int PMAX>
-__device__ __forceinline__ void batch_load_ops(const BatchArgs& ka, float* sOp) {
-    constexpr int OPF = stage_op_floats<P, false>();
+template <int P, int PMAX, bool VISC>
+__device__ __forceinline__ void batch_load_ops(const BatchArgs<VISC>& ka, float* sOp) {
+    constexpr int OPF = stage_op_floats<P, VISC>();
     const float* src = &batch_order<P>(ka).nb.phi[0][0][0];
-    for (int k = threadIdx.x; k < OPF; k += TILE) sOp[batch_op_off(P) + k] = src[k];
+    for (int k = threadIdx.x; k < OPF; k += TILE) sOp[batch_op_off<VISC>(P) + k] = src[k];
     if constexpr (P < PMAX) batch_load_ops<P + 1, PMAX>(ka, sOp);
 }
 
-template <int PMAX, bool BND>
-__global__ void __launch_bounds__(TILE, stage_min_blocks(PMAX, false))
-    batch_stage_kernel(const __grid_constant__ BatchArgs ka) {
+template <int PMAX, bool VISC, bool BND>
+__global__ void __launch_bounds__(TILE, stage_min_blocks(PMAX, VISC))
+    batch_stage_kernel(const __grid_constant__ BatchArgs<VISC> ka) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* sOp = reinterpret_cast<float*>(smem_raw);
-    float* sDt = sOp + batch_op_off(PMAX + 1);
+    float* sDt = sOp + batch_op_off<VISC>(PMAX + 1);
     float* sU = sDt + TILE;
     batch_load_ops<1, PMAX>(ka, sOp);
     __syncthreads();
     const int ntiles = ka.tile_end[PMAX - 1];
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) batch_tile<1, PMAX, BND>(ka, sOp, sU, sDt, t);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) batch_tile<1, PMAX, VISC, BND>(ka, sOp, sU, sDt, t);
 }
 
-template <int PMAX>
+template <int PMAX, bool VISC>
 constexpr size_t batch_smem_bytes() {
-    return (size_t)(batch_op_off(PMAX + 1) + TILE + TILE * stage_stride<PMAX>()) * sizeof(float);
+    return (size_t)(batch_op_off<VISC>(PMAX + 1) + TILE + TILE * stage_stride<PMAX>()) * sizeof(float);
 }
 
-template <int PMAX>
+template <int PMAX, bool VISC>
 static int configure_batch_t() {
-    const int b = (int)batch_smem_bytes<PMAX>();
-    return cudaFuncSetAttribute(batch_stage_kernel<PMAX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
-                       cudaSuccess &&
-                   cudaFuncSetAttribute(batch_stage_kernel<PMAX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        b) == cudaSuccess
+    const int b = (int)batch_smem_bytes<PMAX, VISC>();
+    return cudaFuncSetAttribute(batch_stage_kernel<PMAX, VISC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                b) == cudaSuccess &&
+                   cudaFuncSetAttribute(batch_stage_kernel<PMAX, VISC, false>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess
                ? 0
                : -1;
 }
 
-int configure_batch_stage() {
-    return configure_batch_t<1>() || configure_batch_t<2>() || configure_batch_t<3>() || configure_batch_t<4>() ? -1
-                                                                                                                : 0;
+template <bool VISC>
+static int configure_batch_v() {
+    return configure_batch_t<1, VISC>() || configure_batch_t<2, VISC>() || configure_batch_t<3, VISC>() ||
+                   configure_batch_t<4, VISC>()
+               ? -1
+               : 0;
 }
 
-template <int P>
-static SArgs<P, false>& order_slot(BatchArgs& b) {
+int configure_batch_stage(bool visc) { return visc ? configure_batch_v<true>() : configure_batch_v<false>(); }
+
+template <int P, bool VISC>
+static SArgs<P, VISC>& order_slot(BatchArgs<VISC>& b) {
     if constexpr (P == 1) return b.a1;
     else if constexpr (P == 2) return b.a2;
     else if constexpr (P == 3) return b.a3;
     else return b.a4;
 }
 
-template <int P>
-static void fill_order(BatchArgs& b, const StageArgs& a, const OpsHost& oh) {
-    SArgs<P, false>& k = order_slot<P>(b);
+template <int P, bool VISC>
+static void fill_order(BatchArgs<VISC>& b, const StageArgs& a, const OpsHost& oh) {
+    SArgs<P, VISC>& k = order_slot<P>(b);
     k.s = a;
     if (a.ne == 0) return;
     fill_ops<P, float>(oh, k.o);
@@ -109,12 +118,12 @@ static void fill_order(BatchArgs& b, const StageArgs& a, const OpsHost& oh) {
     fill_nbr_ops<P>(oh, k.nb);
 }
 
-template <int PMAX>
-static int launch_batch_t(const BatchArgs& b, bool boundary, int grid, cudaStream_t st) {
+template <int PMAX, bool VISC>
+static int launch_batch_t(const BatchArgs<VISC>& b, bool boundary, int grid, cudaStream_t st) {
     if (boundary)
-        batch_stage_kernel<PMAX, true><<<grid, TILE, batch_smem_bytes<PMAX>(), st>>>(b);
+        batch_stage_kernel<PMAX, VISC, true><<<grid, TILE, batch_smem_bytes<PMAX, VISC>(), st>>>(b);
     else
-        batch_stage_kernel<PMAX, false><<<grid, TILE, batch_smem_bytes<PMAX>(), st>>>(b);
+        batch_stage_kernel<PMAX, VISC, false><<<grid, TILE, batch_smem_bytes<PMAX, VISC>(), st>>>(b);
     return launch_status();
 }
 
@@ -124,9 +133,10 @@ int batch_tiles(const StageArgs* per_order) {
     return n;
 }
 
-int launch_batch_stage(const StageArgs* per_order, const OpsHost* ops, int boundary, int grid, cudaStream_t s) {
+template <bool VISC>
+static int launch_batch_v(const StageArgs* per_order, const OpsHost* ops, int boundary, int grid, cudaStream_t s) {
     static_assert(MAX_P == 4, "batched stage kernel covers orders 1..4");
-    BatchArgs b;
+    BatchArgs<VISC> b;
     std::memset(&b, 0, sizeof(b));
     fill_order<1>(b, per_order[0], ops[0]);
     fill_order<2>(b, per_order[1], ops[1]);
@@ -146,6 +156,12 @@ int launch_batch_stage(const StageArgs* per_order, const OpsHost* ops, int bound
     case 3: return launch_batch_t<3>(b, boundary != 0, grid, s);
     default: return launch_batch_t<4>(b, boundary != 0, grid, s);
     }
+}
+
+int launch_batch_stage(const StageArgs* per_order, const OpsHost* ops, int boundary, bool visc, int grid,
+                       cudaStream_t s) {
+    return visc ? launch_batch_v<true>(per_order, ops, boundary, grid, s)
+                : launch_batch_v<false>(per_order, ops, boundary, grid, s);
 }
 
 }  // namespace dgx

@@ -2,7 +2,8 @@
 //
 // dgfem advances one mesh per solver object (CompressibleDGSolverBase::solve,
 // src/solver/compressible_solver_base.cpp:236-312); an ensemble is a loop over solver
-// objects.  Here an ensemble of mixed-precision Euler solves shares one device layout:
+// objects.  Here an ensemble of mixed-precision Euler (or Navier-Stokes) solves shares one
+// device layout:
 // the instances of each order are concatenated into one element range (geometry in FP32
 // with the instance number in the spare slot, connectivity and boundary slots offset into
 // the range), every RK3 stage of every instance is one launch of the batched stage kernel
@@ -77,20 +78,34 @@ extern "C" int dgx_batch_create(int n_inst, const dgx_mesh* const* meshes, const
         const dgx_params& p = params[i];
         const std::string at = " (instance " + std::to_string(i) + ")";
         if (!meshes[i]) return set_error(DGX_ERR_INVALID, "dgx_batch_create: null mesh" + at);
+        int nvpe = 0;
+        if (dgx_mesh_vertices_per_element(meshes[i], &nvpe) != DGX_OK || nvpe != 3)
+            return set_error(DGX_ERR_INVALID, "batched solves run on triangle meshes" + at);
         if (p.order < 1 || p.order > MAX_P)
             return set_error(DGX_ERR_INVALID, "Element order must be between 1 and 4 for the GPU kernels" + at);
-        if (p.physics != DGX_EULER)
-            return set_error(DGX_ERR_INVALID, "batched solves cover the Euler equations" + at);
+        if (p.physics != DGX_EULER && p.physics != DGX_NAVIER_STOKES)
+            return set_error(DGX_ERR_INVALID, "unknown physics" + at);
         if (p.precision != DGX_MIXED)
             return set_error(DGX_ERR_INVALID, "batched solves run in mixed precision" + at);
-        if (p.basis != p0.basis || p.gamma != p0.gamma)
-            return set_error(DGX_ERR_INVALID, "batched instances must share the basis and gamma" + at);
+        if (p.basis != p0.basis || p.gamma != p0.gamma || p.physics != p0.physics)
+            return set_error(DGX_ERR_INVALID, "batched instances must share the basis, gamma and physics" + at);
+        if (p.physics == DGX_NAVIER_STOKES) {  // NavierStokesWeakFormulation ctor checks (:22-33)
+            if (p.mu != p0.mu || p.prandtl != p0.prandtl || p.sigma0 != p0.sigma0)
+                return set_error(DGX_ERR_INVALID, "batched Navier-Stokes instances must share mu, Prandtl and sigma0" + at);
+            if (!(p.mu > 0.0))
+                return set_error(DGX_ERR_INVALID, "Dynamic viscosity must be positive for Navier-Stokes weak formulation" + at);
+            if (!(p.prandtl > 0.0))
+                return set_error(DGX_ERR_INVALID, "Prandtl number must be positive for Navier-Stokes weak formulation" + at);
+            if (!(p.sigma0 > 0.0))
+                return set_error(DGX_ERR_INVALID, "Penalty prefactor must be positive for Navier-Stokes weak formulation" + at);
+        }
         if (p.basis != DGX_BASIS_MONOMIAL && p.basis != DGX_BASIS_DUBINER)
             return set_error(DGX_ERR_INVALID, "unknown basis" + at);
     }
     int dev = 0;
     if (int rc = check_device(&dev)) return rc;
-    if (configure_batch_stage()) return set_error(DGX_ERR_CUDA, "could not configure the batched stage kernel");
+    const bool visc = p0.physics == DGX_NAVIER_STOKES;
+    if (configure_batch_stage(visc)) return set_error(DGX_ERR_CUDA, "could not configure the batched stage kernel");
 
     auto* b = new dgx_batch;
     b->device = dev;
@@ -210,6 +225,11 @@ static void batch_stage_args(const dgx_batch* b, int src, int stage, StageArgs* 
         s.bc = g.bc;
         s.dt = 0.0f;
         s.gamma = (float)b->prm.gamma;
+        if (b->prm.physics == DGX_NAVIER_STOKES) {
+            s.mu = (float)b->prm.mu;
+            s.kappa = (float)(b->prm.mu * b->prm.gamma / (b->prm.prandtl * (b->prm.gamma - 1.0)));
+            s.sigma0 = (float)b->prm.sigma0;
+        }
         s.boundary = b->boundary;
         s.dt_inst = b->d_dt;
         s.grid = b->grid;
@@ -220,7 +240,7 @@ static int enqueue_batch_step(dgx_batch* b, int src, cudaStream_t s) {
     for (int stage = 1; stage <= 3; ++stage) {
         StageArgs a[MAX_P];
         batch_stage_args(b, src, stage, a);
-        if (launch_batch_stage(a, b->ops, b->boundary, b->grid, s))
+        if (launch_batch_stage(a, b->ops, b->boundary, b->prm.physics == DGX_NAVIER_STOKES, b->grid, s))
             return set_error(DGX_ERR_CUDA, std::string("batched stage launch failed: ") +
                                                launch_error_text());
     }
@@ -268,12 +288,14 @@ extern "C" int dgx_batch_rk3_step(dgx_batch* b, const double* dt, int n_steps, v
         std::string key = "batch";
         for (int p = 0; p < MAX_P; ++p) key += " p" + std::to_string(p + 1) + ":" + std::to_string(b->grp[p].ne);
         if (b->boundary) key += " bnd";
+        const bool visc = b->prm.physics == DGX_NAVIER_STOKES;
+        if (visc) key += " ns";
         StageArgs a[MAX_P];
         batch_stage_args(b, 0, 1, a);
         const OpsHost* ops = b->ops;
         int grid = 0;
         const int rc = tune_grid(key, grid_candidates(batch_tiles(a)), [&](int g, cudaStream_t ts) {
-            return launch_batch_stage(a, ops, b->boundary, g, ts);
+            return launch_batch_stage(a, ops, b->boundary, visc, g, ts);
         }, s, &grid);
         if (rc) return rc;
         b->grid = grid;

@@ -59,9 +59,6 @@ namespace dgx {
 // Records the message returned by dgx_last_error() on this thread and returns `code`.
 int set_error(int code, const std::string& msg);
 
-// Reference operators of order p in the given basis (returns nonzero on failure).
-int make_ops(int p, int basis, OpsHost& o);
-
 // Host copy of a mesh's device geometry: per-element affine map, face normals and lengths,
 // face connectivity, boundary-condition slots and the physical volume quadrature points.
 struct HostGeometry {

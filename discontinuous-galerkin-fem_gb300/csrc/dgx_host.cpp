@@ -233,7 +233,7 @@ int dgx::make_ops(int p, int basis, OpsHost& o) {
         std::copy(dgx_tri_rule_weights + dgx_tri_rule_offset[order],
                   dgx_tri_rule_weights + dgx_tri_rule_offset[order] + o.nq, qw.begin());
     }
-    double phi[16], g[32];
+    double phi[OPS_MAX_NP], g[2 * OPS_MAX_NP];
     for (int q = 0; q < o.nq; ++q) {
         o.qp[q][0] = qp[2 * q];
         o.qp[q][1] = qp[2 * q + 1];
@@ -925,7 +925,7 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
         return fail(DGX_ERR_INVALID, quad ? "quadrilateral meshes use the Legendre basis"
                                           : "the Legendre basis is for quadrilateral meshes");
     if (quad && p->order > MAX_P_QUAD)
-        return fail(DGX_ERR_INVALID, "Element order must be between 1 and 3 for the quadrilateral GPU kernels");
+        return fail(DGX_ERR_INVALID, "Element order must be between 1 and 4 for the quadrilateral GPU kernels");
     if (p->physics != DGX_EULER && p->physics != DGX_NAVIER_STOKES)
         return fail(DGX_ERR_INVALID, "unknown physics");
     if (p->precision != DGX_FP64 && p->precision != DGX_MIXED && p->precision != DGX_DF64)
@@ -1433,7 +1433,7 @@ extern "C" int dgx_eval_points(dgx_ctx* c, int n_points, const double* ref_xy, c
         return fail(DGX_ERR_INVALID, "dgx_eval_points: bad argument");
     if (n_points > EVAL_MAX_POINTS)
         return fail(DGX_ERR_INVALID, "dgx_eval_points: at most " + std::to_string(EVAL_MAX_POINTS) + " points");
-    std::vector<double> phi((size_t)n_points * c->np), grad(2 * 16);
+    std::vector<double> phi((size_t)n_points * c->np), grad(2 * OPS_MAX_NP);
     for (int k = 0; k < n_points; ++k) basis_eval(c->prm.basis, c->prm.order, ref_xy[2 * k], ref_xy[2 * k + 1],
                                                    &phi[(size_t)k * c->np], grad.data());
     if (launch_eval_points(c->ne, c->np, n_points, phi.data(), u, out, (cudaStream_t)stream))

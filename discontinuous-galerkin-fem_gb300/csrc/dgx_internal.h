@@ -51,7 +51,7 @@ static_assert(sizeof(ElemGeom) == 128, "ElemGeom must stay 128 B");
 
 // Quadrilaterals (DGSpace("quad", p), LegendreBasis): orders with compiled kernels,
 // (p+1)^2 modes and (p+1)^2 tensor Gauss-Legendre volume points.
-constexpr int MAX_P_QUAD = 3;
+constexpr int MAX_P_QUAD = 4;
 __host__ __device__ constexpr int n_basis_quad(int p) { return (p + 1) * (p + 1); }
 
 // Per-element geometry of a bilinear quadrilateral, 192 B.  The map is not affine, so
@@ -134,19 +134,23 @@ struct Ops {
     T minv[NP][NP];       // inverse of the reference mass matrix sum_q w_q phi phi^T
 };
 
-// Host copy of all operators in double precision, sized for MAX_P triangles and
-// MAX_P_QUAD quadrilaterals.
+// Host copy of all operators in double precision, sized for MAX_P triangles (15 modes, 16
+// points) and MAX_P_QUAD quadrilaterals (25 modes, 25 points).
+constexpr int OPS_MAX_NP = 25, OPS_MAX_NQ = 25, OPS_MAX_NFQ = 5;
 struct OpsHost {
     int p, np, nq, nfq;
     int nf;            // faces per element: 3 (triangles) or 4 (quadrilaterals)
-    double phi[16][16], dr[16][16], ds[16][16];
-    double phif[4][5][16], drf[4][5][16], dsf[4][5][16];
-    double wq[16], wf[5];
-    double minv[16][16];
-    double qp[16][2];     // volume points on the reference element
-    double fp[5];         // face points on [-1, 1]
-    double fxi[4][5][2];  // face points on the reference element, face f, point q
+    double phi[OPS_MAX_NQ][OPS_MAX_NP], dr[OPS_MAX_NQ][OPS_MAX_NP], ds[OPS_MAX_NQ][OPS_MAX_NP];
+    double phif[4][OPS_MAX_NFQ][OPS_MAX_NP], drf[4][OPS_MAX_NFQ][OPS_MAX_NP], dsf[4][OPS_MAX_NFQ][OPS_MAX_NP];
+    double wq[OPS_MAX_NQ], wf[OPS_MAX_NFQ];
+    double minv[OPS_MAX_NP][OPS_MAX_NP];
+    double qp[OPS_MAX_NQ][2];         // volume points on the reference element
+    double fp[OPS_MAX_NFQ];           // face points on [-1, 1]
+    double fxi[4][OPS_MAX_NFQ][2];    // face points on the reference element, face f, point q
 };
+
+// Reference operators of order p in the given basis (returns nonzero on failure; dgx_host.cpp).
+int make_ops(int p, int basis, OpsHost& o);
 
 template <int P, typename T>
 inline void fill_ops(const OpsHost& h, Ops<P, T>& o) {
@@ -255,9 +259,10 @@ size_t trace_floats_per_element(int p);
 int stage_tc_ctas_per_sm(int p);
 // Batched solves (dgx_batch.cu): one launch of the stage over the element ranges of
 // orders 1..MAX_P (per_order[p-1], ne = 0 for an absent order), grid <= 0: one CTA per tile.
-int launch_batch_stage(const StageArgs* per_order, const OpsHost* ops, int boundary, int grid, cudaStream_t s);
+int launch_batch_stage(const StageArgs* per_order, const OpsHost* ops, int boundary, bool visc, int grid,
+                       cudaStream_t s);
 int batch_tiles(const StageArgs* per_order);
-int configure_batch_stage();
+int configure_batch_stage(bool visc);
 
 // Small FP64 utility kernels (dgx_misc.cu).
 int launch_mass_inv(int ne, int p, const OpsHost& ops, const ElemGeom* geom, const double* in,

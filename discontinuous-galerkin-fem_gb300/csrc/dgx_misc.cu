@@ -226,7 +226,7 @@ int launch_f64_to_f32(size_t n, const double* in, float* out, cudaStream_t s) {
 // one thread per (element, point).  phi holds the basis at reference points (host-built).
 struct EvalArgs {
     int npts, np;
-    double phi[EVAL_MAX_POINTS][16];  // up to 16 modes (p=4 triangles, p=3 quadrilaterals)
+    double phi[EVAL_MAX_POINTS][OPS_MAX_NP];  // up to 25 modes (p=4 quadrilaterals)
 };
 
 __global__ void eval_points_kernel(const __grid_constant__ EvalArgs a, int ne, const double* u, double* out) {
@@ -246,7 +246,7 @@ __global__ void eval_points_kernel(const __grid_constant__ EvalArgs a, int ne, c
 
 int launch_eval_points(int ne, int np, int npts, const double* phi, const double* u, double* out, cudaStream_t s) {
     if (ne == 0 || npts == 0) return 0;
-    if (npts > EVAL_MAX_POINTS || np > 16) return -1;
+    if (npts > EVAL_MAX_POINTS || np > OPS_MAX_NP) return -1;
     EvalArgs a;
     a.npts = npts;
     a.np = np;

@@ -25,6 +25,8 @@ int launch_quad_element(int p, bool viscous, int precision, const StepArgs& a, c
     case 5: return FN<2, true> ARGS;             \
     case 6: return FN<3, false> ARGS;            \
     case 7: return FN<3, true> ARGS;             \
+    case 8: return FN<4, false> ARGS;            \
+    case 9: return FN<4, true> ARGS;             \
     default: return -1;                          \
     }
 
@@ -150,6 +152,7 @@ __global__ void quad_monitor_kernel(const __grid_constant__ QuadOps<P, double> o
     case 1: { constexpr int P = 1; __VA_ARGS__; break; } \
     case 2: { constexpr int P = 2; __VA_ARGS__; break; } \
     case 3: { constexpr int P = 3; __VA_ARGS__; break; } \
+    case 4: { constexpr int P = 4; __VA_ARGS__; break; } \
     default: return -1;                                \
     }
 

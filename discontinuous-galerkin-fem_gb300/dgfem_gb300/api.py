@@ -455,10 +455,12 @@ class _DeviceArray:
 
 
 class DGBatch:
-    """Independent mixed-precision Euler solves advanced together (include/dgx.h dgx_batch_*).
+    """Independent mixed-precision Euler or Navier-Stokes solves advanced together
+    (include/dgx.h dgx_batch_*).
 
-    ``meshes[i]`` and ``spaces[i]`` (order 1..4, one basis for all) define instance i; every
-    RK3 stage of every instance is one persistent kernel launch.  ``state(i)`` is a CUDA
+    ``meshes[i]`` and ``spaces[i]`` (order 1..4, one basis for all) define instance i; the
+    weak form (its physics and parameters) is shared; every RK3 stage of every instance is
+    one persistent kernel launch.  ``state(i)`` is a CUDA
     float64 tensor view of instance i's state, shape (n_elements, n_basis, 4), owned by the
     batch.  No counterpart in dgfem, where an ensemble is a loop over solver objects."""
 
@@ -467,12 +469,11 @@ class DGBatch:
         if len(meshes) != len(spaces) or not meshes:
             raise ValueError("DGBatch needs one space per mesh and at least one instance")
         wf = weak_form or EulerWeakFormulation()
-        if wf.has_viscous_terms():
-            raise ValueError("batched solves cover the Euler equations")
+        visc = wf.has_viscous_terms()
+        phys = (L.NAVIER_STOKES, wf.mu, wf.prandtl, wf.sigma0) if visc else (L.EULER, 0.0, 0.0, 0.0)
         lib = L.load()
         n = len(meshes)
-        prm = (L.Params * n)(*[L.Params(s.order, s.basis, L.EULER, L.MIXED, wf.gamma, 0.0, 0.0, 0.0)
-                                for s in spaces])
+        prm = (L.Params * n)(*[L.Params(s.order, s.basis, phys[0], L.MIXED, wf.gamma, *phys[1:]) for s in spaces])
         hs = (C.c_void_p * n)(*[m._h.value for m in meshes])
         self._h = C.c_void_p()
         check(lib.dgx_batch_create(n, hs, C.cast(prm, C.c_void_p), C.byref(self._h)))

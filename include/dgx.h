@@ -59,7 +59,7 @@ typedef struct dgx_ctx dgx_ctx;
  * NavierStokesWeakFormulation(gamma, mu, Pr, sigma0)
  * (include/dgfem/weak_forms/navier_stokes_weak_formulation.hpp:19-20). */
 typedef struct {
-    int order;      /* polynomial order p, 1..4 (quadrilaterals: 1..3) */
+    int order;      /* polynomial order p, 1..4 (triangles and quadrilaterals) */
     int basis;      /* triangles: DGX_BASIS_MONOMIAL (dgfem's default) or DGX_BASIS_DUBINER;
                        quadrilaterals: DGX_BASIS_LEGENDRE */
     int physics;    /* DGX_EULER or DGX_NAVIER_STOKES */
@@ -310,10 +310,11 @@ int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles, int* form);
 /* ---------------------------------------------------------------- batched solves */
 
 /* No counterpart in dgfem, where an ensemble is a loop over solver objects.  n_inst
- * independent mixed-precision Euler solves, each on its own mesh and order (1..4, params[i]
- * .order), advanced together: every SSP-RK3 stage of every instance is one persistent
- * kernel launch, and dgx_batch_rk3_step replays CUDA graphs of those launches.  All
- * instances share the basis and gamma (params[0]); other precisions and physics are
+ * independent mixed-precision Euler or Navier-Stokes solves on triangle meshes, each on its
+ * own mesh and order (1..4, params[i].order), advanced together: every SSP-RK3 stage of
+ * every instance is one persistent kernel launch, and dgx_batch_rk3_step replays CUDA graphs
+ * of those launches.  All instances share the basis, gamma and physics, and Navier-Stokes
+ * instances mu, Prandtl and sigma0 (params[0]); anything else, and other precisions, are
  * rejected with DGX_ERR_INVALID.  Meshes are read at creation only. */
 typedef struct dgx_batch dgx_batch;
 int dgx_batch_create(int n_inst, const dgx_mesh* const* meshes, const dgx_params* params, dgx_batch** out);

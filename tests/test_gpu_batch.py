@@ -4,6 +4,7 @@
   same instance run alone through a mixed-precision context ends (same FP32 stage code,
   same rounding: <= 1e-12 relative), and within the mixed tolerance of the FP64 oracle;
 * batches with boundary faces (far-field / no-slip next to periodic instances);
+* Navier-Stokes batches (shared viscous parameters) against single viscous solves;
 * the grid the autotuner picks is one of its candidates; DGX_AUTOTUNE=0 keeps one CTA per
   tile.
 """
@@ -66,8 +67,8 @@ def build(dg, specs, walls=()):
     return [instance(dg, *sp, walls=(k in walls)) for k, sp in enumerate(specs)], [sp[1] for sp in specs]
 
 
-def run_batch(dg, insts, orders, steps=(3, 2)):
-    batch = dg.DGBatch([i[1] for i in insts], [dg.DGSpace("triangle", p, "dubiner") for p in orders])
+def run_batch(dg, insts, orders, steps=(3, 2), wf=None):
+    batch = dg.DGBatch([i[1] for i in insts], [dg.DGSpace("triangle", p, "dubiner") for p in orders], wf)
     for k, (om, pm, u0, dt) in enumerate(insts):
         batch.state(k).copy_(torch.tensor(u0, device="cuda"))
     dts = [i[3] for i in insts]
@@ -77,8 +78,8 @@ def run_batch(dg, insts, orders, steps=(3, 2)):
     return batch, [batch.state(k).cpu().numpy() for k in range(len(insts))]
 
 
-def single(dg, om, pm, u0, dt, order, steps=(3, 2)):
-    ctx = dg.DGContext(pm, dg.DGSpace("triangle", order, "dubiner"), dg.EulerWeakFormulation(1.4), "mixed")
+def single(dg, om, pm, u0, dt, order, steps=(3, 2), wf=None):
+    ctx = dg.DGContext(pm, dg.DGSpace("triangle", order, "dubiner"), wf or dg.EulerWeakFormulation(1.4), "mixed")
     u = torch.tensor(u0, device="cuda")
     for n in steps:
         ctx.rk3_step(u, dt, n)
@@ -96,6 +97,26 @@ def test_batch_matches_single_solves_and_oracle(dg, monkeypatch, walls):
         alone = single(dg, om, pm, u0, dt, order)
         assert rel(outs[k], alone) <= 1e-12, (k, rel(outs[k], alone))
         ref = om.rk3_step(O.euler(1.4), u0, dt, 5)
+        assert np.isfinite(ref).all()
+        assert rel(outs[k], ref) <= 1e-6, (k, rel(outs[k], ref))
+        assert rel(outs[k] - u0, ref - u0) <= 1e-4
+
+
+@pytest.mark.parametrize("walls", [(), (0, 3)])
+def test_batch_navier_stokes_matches_single_solves_and_oracle(dg, walls):
+    """Navier-Stokes instances (shared mu, Prandtl, sigma0) of orders 1..4: each equals its
+    mixed-precision context run alone (the same viscous stage code) and stays within the mixed
+    tolerance of the FP64 oracle."""
+    mu, pr, s0 = 0.01, 0.72, 5.0
+    wf = dg.NavierStokesWeakFormulation(1.4, mu, pr, s0)
+    specs = [(5, 1, 2.0, 0.5, -1.0, 0.3), (6, 2, 3.0, -1.0, 0.2, 0.5), (4, 3, 2.5, 1.0, 1.0, 0.2),
+             (3, 4, 2.0, -0.5, 0.5, 0.4), (7, 3, 4.0, 0.3, -0.6, 0.6)]
+    insts, orders = build(dg, specs, walls)
+    batch, outs = run_batch(dg, insts, orders, wf=wf)
+    for k, ((om, pm, u0, dt), order) in enumerate(zip(insts, orders)):
+        alone = single(dg, om, pm, u0, dt, order, wf=wf)
+        assert rel(outs[k], alone) <= 1e-12, (k, rel(outs[k], alone))
+        ref = om.rk3_step(O.navier_stokes(1.4, mu, pr, s0), u0, dt, 5)
         assert np.isfinite(ref).all()
         assert rel(outs[k], ref) <= 1e-6, (k, rel(outs[k], ref))
         assert rel(outs[k] - u0, ref - u0) <= 1e-4

@@ -65,7 +65,7 @@ def vortex_state(om, seed=0, noise=1e-3):
 
 @pytest.mark.parametrize("visc", [False, True])
 @pytest.mark.parametrize("distort", [0.0, 0.2])
-@pytest.mark.parametrize("order", [1, 2, 3])
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
 def test_quad_residual_fp64_periodic(dg, order, distort, visc):
     v, e, b = quad_rectangle(6, distort=distort, seed=order)
     om, pm = make_pair(dg, v, e, b, order, True)
@@ -79,8 +79,9 @@ def test_quad_residual_fp64_periodic(dg, order, distort, visc):
     assert rel(ctx.residual(u), R_orc) <= 1e-12  # host-pointer entry point
 
 
+@pytest.mark.parametrize("order", [3, 4])
 @pytest.mark.parametrize("visc", [False, True])
-def test_quad_residual_fp64_boundaries(dg, visc):
+def test_quad_residual_fp64_boundaries(dg, visc, order):
     """Slip wall, far field and no-slip wall faces on a distorted, element-permuted mesh."""
     rng = np.random.default_rng(5)
     v, e, b = quad_rectangle(7, 0.0, 1.0, 0.0, 1.0, distort=0.2, seed=3)
@@ -90,16 +91,16 @@ def test_quad_residual_fp64_boundaries(dg, visc):
            ("Right", 3, O.FAR_FIELD, U_inf),
            ("Top", 4, O.NO_SLIP_WALL, [1.0, 0.0, 0.0, 1.0]),
            ("Left", 5, O.FAR_FIELD, U_inf)]
-    om, pm = make_pair(dg, v, e, b, 3, False, bcs=bcs)
+    om, pm = make_pair(dg, v, e, b, order, False, bcs=bcs)
     oph, wf = physics(dg, visc)
     u = om.project(np.broadcast_to(U_inf, om.quad_points().shape[:-1] + (4,)).copy())
     u = u + 1e-2 * np.random.default_rng(1).standard_normal(u.shape) * np.abs(u).max()
-    ctx = dg.DGContext(pm, dg.DGSpace("quad", 3), wf, "fp64")
+    ctx = dg.DGContext(pm, dg.DGSpace("quad", order), wf, "fp64")
     R_gpu = ctx.residual(torch.tensor(u, device="cuda")).cpu().numpy()
     assert rel(R_gpu, om.residual(oph, u)) <= 1e-12
 
 
-@pytest.mark.parametrize("order", [1, 2, 3])
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
 def test_quad_rhs_and_mass_inverse_fp64(dg, order):
     v, e, b = quad_rectangle(5, distort=0.25, seed=11)
     om, pm = make_pair(dg, v, e, b, order, True)
@@ -113,7 +114,7 @@ def test_quad_rhs_and_mass_inverse_fp64(dg, order):
 
 
 @pytest.mark.parametrize("visc", [False, True])
-@pytest.mark.parametrize("order", [2, 3])
+@pytest.mark.parametrize("order", [2, 3, 4])
 def test_quad_rk3_steps_fp64(dg, order, visc):
     v, e, b = quad_rectangle(6, distort=0.15, seed=2)
     om, pm = make_pair(dg, v, e, b, order, True)
@@ -129,10 +130,11 @@ def test_quad_rk3_steps_fp64(dg, order, visc):
     assert rel(ctx.rk3_step(u0, dt, 4), ref) <= 1e-11
 
 
-def test_quad_monitors_and_projection(dg):
+@pytest.mark.parametrize("order", [3, 4])
+def test_quad_monitors_and_projection(dg, order):
     v, e, b = quad_rectangle(8, distort=0.2, seed=4)
-    om, pm = make_pair(dg, v, e, b, 3, True)
-    ctx = dg.DGContext(pm, dg.DGSpace("quad", 3), dg.EulerWeakFormulation(), "fp64")
+    om, pm = make_pair(dg, v, e, b, order, True)
+    ctx = dg.DGContext(pm, dg.DGSpace("quad", order), dg.EulerWeakFormulation(), "fp64")
     xq = ctx.quad_points()
     assert rel(xq, om.quad_points()) <= 1e-15
     uq = isentropic_vortex(xq, beta=5.0)
@@ -170,7 +172,7 @@ def test_quad_unsupported_forms_fail_loudly(dg):
     v, e, b = quad_rectangle(3)
     m = dg.DGMesh(v, e, None, dict(TAGS), {})
     with pytest.raises(dg.DGXError):
-        dg.DGContext(m, dg.DGSpace("quad", 4), dg.EulerWeakFormulation(), "fp64")
+        dg.DGContext(m, dg.DGSpace("quad", 5), dg.EulerWeakFormulation(), "fp64")
     tri = dg.DGMesh.rectangle(2, 2, 0, 1, 0, 1)
     with pytest.raises(dg.DGXError):
         dg.DGContext(tri, dg.DGSpace("quad", 2), dg.EulerWeakFormulation(), "fp64")
@@ -181,7 +183,7 @@ def test_quad_unsupported_forms_fail_loudly(dg):
 
 
 @pytest.mark.parametrize("visc", [False, True])
-@pytest.mark.parametrize("order", [1, 2, 3])
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
 def test_quad_residual_mixed_and_df64(dg, order, visc):
     v, e, b = quad_rectangle(6, distort=0.2, seed=order)
     om, pm = make_pair(dg, v, e, b, order, True)
@@ -198,7 +200,7 @@ def test_quad_residual_mixed_and_df64(dg, order, visc):
 
 
 @pytest.mark.parametrize("visc", [False, True])
-@pytest.mark.parametrize("order", [2, 3])
+@pytest.mark.parametrize("order", [2, 3, 4])
 def test_quad_rk3_mixed_precision_vs_oracle(dg, order, visc):
     """FP32 residual and stage increment, FP64 state and RK3 combination: after 5 steps
     within 1e-6 relative L2 of the FP64 oracle; the update itself to FP32 level."""
