@@ -569,7 +569,7 @@ inline int launch_quad_t(const StepArgs& a, const QuadGeom* geom, const QuadConn
 // ---------------------------------------------------------------------------------
 // Mixed-precision SSP-RK3 stage on quadrilaterals, the increment form of StageArgs
 // (dgx_internal.h): the stage state is uhi + din in FP32, stages 1 and 2 write FP32
-// increments and stage 3 adds into the FP64 state (stage_combine).  No FP64 arithmetic or
+// increments and stage 3 adds into the state (stage_combine, rk3_next).  No FP64 arithmetic or
 // FP64 loads in stages 1 and 2: converting FP64 neighbour rows cost the element kernel's
 // FP32 form more FP64-pipe time than its residual took FP32-pipe time.
 template <int P>
@@ -596,8 +596,8 @@ __global__ void __launch_bounds__(TILE, 1) quad_stage_kernel(const __grid_consta
     const int tl = threadIdx.x;
     const bool active = tl < nloc;
     const int e = e0 + tl;
-    if (tl == 0 && s.stage == 3)  // the FP64 state is read back in the stage combination
-        prefetch_l2_bulk(s.u64 + (size_t)e0 * NB, (unsigned)(nloc * NB * sizeof(double)));
+    if (tl == 0 && s.stage == 3)  // u^n is read back in the stage combination
+        rk3_prefetch(s, (size_t)e0 * NB, nloc * NB);
     stage_load_tile<NB, STR>(s.uhi, s.din, sU, e0, nloc, [](int le) { return le; });
     __syncthreads();
 

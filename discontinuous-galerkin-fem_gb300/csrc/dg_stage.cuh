@@ -87,9 +87,82 @@ __device__ __forceinline__ void fma4(float s, const float (&c)[4], float (&acc)[
     acc[3] = b.y;
 }
 
+// Double-float addition (hi, lo) + d -> (oh, ol), |lo| <= ulp(hi) / 2: Knuth's TwoSum of hi and
+// d (exact), the low parts added, and a second TwoSum that renormalises, so oh is the FP32
+// rounding of oh + ol and the result is within 2^-48 of the exact sum (relative).  Every
+// operation is a rounded FP32 add (never contracted or reassociated).
+__device__ __forceinline__ void df_add(float hi, float lo, float d, float& oh, float& ol) {
+    const float s = __fadd_rn(hi, d);
+    const float bp = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(d, bp));
+    const float t = __fadd_rn(lo, e);
+    oh = __fadd_rn(s, t);
+    const float bq = __fsub_rn(oh, s);
+    ol = __fadd_rn(__fsub_rn(s, __fsub_rn(oh, bq)), __fsub_rn(t, bq));
+}
+
+__device__ __forceinline__ bool finite_f32(float x) { return (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u; }
+
+// Stage 3 of one value: u^{n+1} = u^n + d.  u^n is un64 (s.u64_in: the caller's FP64 state, first
+// step of a call) or the double-float pair hi + lo; u^{n+1} goes to r64 (s.u64_out: last step of
+// a call; written by the caller) or to the pair (returned hi, lo_out).  A call of one step adds
+// in FP64 exactly as before; the steps between the first and the last of a call add on the FP32
+// pipe (GB300's FP64 pipe runs at a small fraction of its FP32 rate).  Returns the FP32 rounding
+// of u^{n+1}; the conversions run on the integer pipe (fp_bits.cuh).
+__device__ __forceinline__ float rk3_next(const StageArgs& s, double un64, float hi, float lo, float d, float& lo_out,
+                                          double& r64, bool& bad) {
+    if (s.u64_in) {
+        const double r = un64 + f32_to_f64_bits(d);
+        const float h = f64_to_f32_bits(r);
+        if (s.u64_out) r64 = r;
+        else lo_out = f64_to_f32_bits(r - f32_to_f64_bits(h));  // the difference is exact in FP64
+        bad |= !finite_bits(r);
+        return h;
+    }
+    float h, l;
+    df_add(hi, lo, d, h, l);
+    if (s.u64_out) r64 = f32_to_f64_bits(h) + f32_to_f64_bits(l);  // exact: l lies below h's last bit
+    else lo_out = l;
+    bad |= !finite_f32(h);
+    return h;
+}
+
+// Stage 3 of four consecutive values at float4 index i4 of the state arrays: reads u^n (u64 or
+// the pair, loaded by the caller into un / hi / lo), writes u64 or ulo, and uhi_out; returns the
+// FP32 rounding of u^{n+1}.
+__device__ __forceinline__ float4 rk3_next4(const StageArgs& s, size_t i4, const double2 (&un)[2], float4 hi,
+                                            float4 lo, const float (&d)[4], bool& bad) {
+    const double u0[4] = {un[0].x, un[0].y, un[1].x, un[1].y};
+    const float h0[4] = {hi.x, hi.y, hi.z, hi.w}, l0[4] = {lo.x, lo.y, lo.z, lo.w};
+    float h[4], l[4];
+    double r[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) h[v] = rk3_next(s, u0[v], h0[v], l0[v], d[v], l[v], r[v], bad);
+    if (s.u64_out) {
+        reinterpret_cast<double2*>(s.u64)[2 * i4] = make_double2(r[0], r[1]);
+        reinterpret_cast<double2*>(s.u64)[2 * i4 + 1] = make_double2(r[2], r[3]);
+    } else {
+        reinterpret_cast<float4*>(s.ulo)[i4] = make_float4(l[0], l[1], l[2], l[3]);
+    }
+    const float4 o = make_float4(h[0], h[1], h[2], h[3]);
+    reinterpret_cast<float4*>(s.uhi_out)[i4] = o;
+    return o;
+}
+
+// The stage-3 inputs of four values at float4 index i4: u64 (u64_in) or the pair uhi + ulo.
+__device__ __forceinline__ void rk3_load4(const StageArgs& s, size_t i4, double2 (&un)[2], float4& hi, float4& lo) {
+    if (s.u64_in) {
+        un[0] = reinterpret_cast<const double2*>(s.u64)[2 * i4];
+        un[1] = reinterpret_cast<const double2*>(s.u64)[2 * i4 + 1];
+    } else {
+        hi = __ldg(reinterpret_cast<const float4*>(s.uhi) + i4);
+        lo = reinterpret_cast<const float4*>(s.ulo)[i4];
+    }
+}
+
 // Stage combination of one tile in the increment form, 16-byte accesses:
 //   stage 1: dout = dt R;  stage 2: dout = (din + dt R) / 4;
-//   stage 3: u64 += 2/3 (din + dt R) (FP64), uhi_out = (float)u64.
+//   stage 3: u^{n+1} = u^n + 2/3 (din + dt R) (rk3_next), uhi_out = its FP32 rounding.
 // R (M^-1-scaled residual) of local element le is row rowof(le) of sR; the loads of CH
 // consecutive float4 slots of a thread are issued before any of them is used.
 template <int NB, int STR, int THREADS, int CH, typename RowOf>
@@ -101,17 +174,14 @@ __device__ __forceinline__ void stage_combine(const StageArgs& s, const float* s
     const int t = threadIdx.x;
     bool bad = false;
     for (int g0 = t; g0 < n4; g0 += CH * THREADS) {
-        float4 dv[CH];
-        double2 ua[CH], ub[CH];
+        float4 dv[CH], hi[CH], lo[CH];
+        double2 un[CH][2];
 #pragma unroll
         for (int k = 0; k < CH; ++k) {
             const int g = g0 + k * THREADS;
             if (g < n4) {
                 if (s.stage >= 2) dv[k] = __ldg(reinterpret_cast<const float4*>(s.din) + b4 + g);
-                if (s.stage == 3) {
-                    ua[k] = reinterpret_cast<const double2*>(s.u64)[2 * (b4 + g)];
-                    ub[k] = reinterpret_cast<const double2*>(s.u64)[2 * (b4 + g) + 1];
-                }
+                if (s.stage == 3) rk3_load4(s, b4 + g, un[k], hi[k], lo[k]);
             }
         }
 #pragma unroll
@@ -129,16 +199,9 @@ __device__ __forceinline__ void stage_combine(const StageArgs& s, const float* s
                     make_float4(0.25f * (dv[k].x + dt * du.x), 0.25f * (dv[k].y + dt * du.y),
                                 0.25f * (dv[k].z + dt * du.z), 0.25f * (dv[k].w + dt * du.w));
             } else {
-                const float d0 = (2.0f / 3.0f) * (dv[k].x + dt * du.x), d1 = (2.0f / 3.0f) * (dv[k].y + dt * du.y);
-                const float d2 = (2.0f / 3.0f) * (dv[k].z + dt * du.z), d3 = (2.0f / 3.0f) * (dv[k].w + dt * du.w);
-                // one FP64 add per value; the conversions and the check run on the integer pipe
-                const double2 ra = make_double2(ua[k].x + f32_to_f64_bits(d0), ua[k].y + f32_to_f64_bits(d1));
-                const double2 rb = make_double2(ub[k].x + f32_to_f64_bits(d2), ub[k].y + f32_to_f64_bits(d3));
-                reinterpret_cast<double2*>(s.u64)[2 * (b4 + g)] = ra;
-                reinterpret_cast<double2*>(s.u64)[2 * (b4 + g) + 1] = rb;
-                reinterpret_cast<float4*>(s.uhi_out)[b4 + g] = make_float4(f64_to_f32_bits(ra.x), f64_to_f32_bits(ra.y), f64_to_f32_bits(rb.x),
-                                            f64_to_f32_bits(rb.y));
-                bad |= !(finite_bits(ra.x) && finite_bits(ra.y) && finite_bits(rb.x) && finite_bits(rb.y));
+                const float d[4] = {(2.0f / 3.0f) * (dv[k].x + dt * du.x), (2.0f / 3.0f) * (dv[k].y + dt * du.y),
+                                    (2.0f / 3.0f) * (dv[k].z + dt * du.z), (2.0f / 3.0f) * (dv[k].w + dt * du.w)};
+                rk3_next4(s, b4 + g, un[k], hi[k], lo[k], d, bad);
             }
         }
     }
@@ -148,6 +211,12 @@ __device__ __forceinline__ void stage_combine(const StageArgs& s, const float* s
 // hint: bring [p, p + bytes) into L2 (bulk async prefetch; 16-byte aligned, bytes % 16 == 0)
 __device__ __forceinline__ void prefetch_l2_bulk(const void* p, unsigned bytes) {
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(bytes) : "memory");
+}
+
+// hint for stage 3: bring the tile's u^n (u64, or the low parts ulo) into L2
+__device__ __forceinline__ void rk3_prefetch(const StageArgs& s, size_t v0, int nvals) {
+    if (s.u64_in) prefetch_l2_bulk(s.u64 + v0, (unsigned)(nvals * sizeof(double)));
+    else prefetch_l2_bulk(s.ulo + v0, (unsigned)(nvals * sizeof(float)));
 }
 
 // hint: bring the 128-byte line holding p into L2
@@ -223,8 +292,8 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
     const int el = stage_elem(tl);
     const bool active = el < nloc;
     const int e = e0 + el;
-    if (tl == 0 && s.stage == 3)  // the FP64 state is read back in the stage combination
-        prefetch_l2_bulk(s.u64 + (size_t)e0 * NB, (unsigned)(nloc * NB * sizeof(double)));
+    if (tl == 0 && s.stage == 3)  // u^n is read back in the stage combination
+        rk3_prefetch(s, (size_t)e0 * NB, nloc * NB);
     stage_load_tile<NB, STR>(s.uhi, s.din, sU, e0, nloc, [](int le) { return stage_row(le); });
     __syncthreads();
 
@@ -449,10 +518,14 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
             s.dout[base + g] = 0.25f * (__ldg(s.din + base + g) + dt * du);
         } else {
             const float delta = (2.0f / 3.0f) * (__ldg(s.din + base + g) + dt * du);
-            const double r = s.u64[base + g] + f32_to_f64_bits(delta);
-            s.u64[base + g] = r;
-            s.uhi_out[base + g] = f64_to_f32_bits(r);
-            bad |= !finite_bits(r);
+            const size_t i = base + g;
+            double r = 0.0;
+            float lo = 0.0f;
+            const float h = s.u64_in ? rk3_next(s, s.u64[i], 0.0f, 0.0f, delta, lo, r, bad)
+                                     : rk3_next(s, 0.0, __ldg(s.uhi + i), s.ulo[i], delta, lo, r, bad);
+            if (s.u64_out) s.u64[i] = r;
+            else s.ulo[i] = lo;
+            s.uhi_out[i] = h;
         }
     }
     if (bad && s.status) atomicOr(s.status, 1);

@@ -75,7 +75,8 @@ struct Tc {
     static constexpr int OFF_A = 0;                               // [8][TILE * KP] floats
     static constexpr int OFF_B1 = OFF_A + 8 * TILE * KP * 4;      // [2][N1V * KP]
     static constexpr int OFF_B2 = OFF_B1 + 2 * N1V * KP * 4;      // [2][N2V * K2V]
-    static constexpr int RS = TILE * NB * 8;                      // a tile's u^n (FP64, stage 3) or uhi
+    // a tile's u^n in stage 3 (FP64, or uhi then ulo: RL_OFF) or uhi
+    static constexpr int RS = TILE * NB * 8, RL_OFF = TILE * NB * 4;
     static constexpr int RD = TILE * NB * 4;                      // its increment
     static constexpr int RG = TILE * 64, RC = TILE * 16;          // its ElemGeomF, ElemConn
     static constexpr int RD_OFF = RS, RG_OFF = RS + RD, RC_OFF = RS + RD + RG, RAWB = RS + RD + RG + RC;
@@ -112,14 +113,14 @@ struct TcArgs {
 };
 
 // Element row le, basis function i (all four variables) of the stage state in a tile's input
-// buffer: uhi (+ din), or the FP32 rounding of u^n (+ din) in stage 3 -- the same numbers the
-// CUDA-core forms stage.
+// buffer: uhi (+ din), or the FP32 rounding of the FP64 u^n (+ din) in the first step's stage 3
+// -- the same numbers the CUDA-core forms stage.
 template <int P>
-__device__ __forceinline__ float4 tc_state(const unsigned char* raw, int stage, bool din, int le, int i) {
+__device__ __forceinline__ float4 tc_state(const unsigned char* raw, int stage, bool in64, bool din, int le, int i) {
     using T = Tc<P>;
     const int off = le * T::NB + 4 * i;
     float4 a;
-    if (stage == 3) {
+    if (stage == 3 && in64) {
         const double2* u = reinterpret_cast<const double2*>(raw) + off / 2;
         const double2 x = u[0], y = u[1];
         a = make_float4(f64_to_f32_bits(x.x), f64_to_f32_bits(x.y), f64_to_f32_bits(y.x), f64_to_f32_bits(y.y));
@@ -266,8 +267,14 @@ __device__ __forceinline__ void tc_load_tile(const StageArgs& s, unsigned char* 
     const uint32_t bd = (s.din && !state_only) ? (uint32_t)nloc * T::NB * 4u : 0u;
     const uint32_t bg = state_only ? 0u : (uint32_t)nloc * 64u, bc = state_only ? 0u : (uint32_t)nloc * 16u;
     tc::mbar_expect_tx(full, bs + bd + bg + bc);
-    if (s.stage == 3) tc::bulk_g2s(raw, s.u64 + (size_t)e0 * T::NB, bs, full);
-    else tc::bulk_g2s(raw, s.uhi + (size_t)e0 * T::NB, bs, full);
+    if (s.stage == 3 && s.u64_in) {
+        tc::bulk_g2s(raw, s.u64 + (size_t)e0 * T::NB, bs, full);
+    } else if (s.stage == 3) {  // the double-float pair: uhi, then ulo at RL_OFF
+        tc::bulk_g2s(raw, s.uhi + (size_t)e0 * T::NB, bs / 2, full);
+        tc::bulk_g2s(raw + T::RL_OFF, s.ulo + (size_t)e0 * T::NB, bs / 2, full);
+    } else {
+        tc::bulk_g2s(raw, s.uhi + (size_t)e0 * T::NB, bs, full);
+    }
     if (bd) tc::bulk_g2s(raw + T::RD_OFF, s.din + (size_t)e0 * T::NB, bd, full);
     if (bg) tc::bulk_g2s(raw + T::RG_OFF, s.geom + e0, bg, full);
     if (bc) tc::bulk_g2s(raw + T::RC_OFF, s.conn + e0, bc, full);
@@ -367,7 +374,7 @@ __global__ void __launch_bounds__(Tc<P>::THREADS, 1) stage_tc_kernel(const __gri
             for (int r = 0; r < BW; ++r) {
                 const int i = k + KT * r;
                 if (i >= 1 && i < NP) {
-                    const float4 a = tc_state<P>(raw, s.stage, has_din, le, i);
+                    const float4 a = tc_state<P>(raw, s.stage, s.u64_in != 0, has_din, le, i);
                     tc_put_a(sA, 0, le, i, a.x);
                     tc_put_a(sA, 1, le, i, a.y);
                     tc_put_a(sA, 2, le, i, a.z);
@@ -389,7 +396,7 @@ __global__ void __launch_bounds__(Tc<P>::THREADS, 1) stage_tc_kernel(const __gri
             const unsigned char* raw = sRaw + (j & 1) * T::RAWB;
             const ElemGeomF* G = reinterpret_cast<const ElemGeomF*>(raw + T::RG_OFF) + le;
             const ElemConn* C = reinterpret_cast<const ElemConn*>(raw + T::RC_OFF) + le;
-            const float4 s0 = tc_state<P>(raw, s.stage, has_din, le, 0);
+            const float4 s0 = tc_state<P>(raw, s.stage, s.u64_in != 0, has_din, le, 0);
             const float S0[4] = {s0.x, s0.y, s0.z, s0.w};
             // the neighbour trace blocks this thread reads in (c): into L2 now
             auto nbr_trace = [&](int r) -> const float* {
@@ -535,21 +542,33 @@ __global__ void __launch_bounds__(Tc<P>::THREADS, 1) stage_tc_kernel(const __gri
                     Sn[2] = __fadd_rn(uh.z, o.z);
                     Sn[3] = __fadd_rn(uh.w, o.w);
                 } else {
-                    const double2* ur = reinterpret_cast<const double2*>(raw) + off / 2;
-                    const double2 ua = ur[0], ub = ur[1];
-                    const float d0 = (2.0f / 3.0f) * (dv.x + dt * R[0]), dd1 = (2.0f / 3.0f) * (dv.y + dt * R[1]);
-                    const float dd2 = (2.0f / 3.0f) * (dv.z + dt * R[2]), dd3 = (2.0f / 3.0f) * (dv.w + dt * R[3]);
-                    const double2 ra = make_double2(ua.x + f32_to_f64_bits(d0), ua.y + f32_to_f64_bits(dd1));
-                    const double2 rb = make_double2(ub.x + f32_to_f64_bits(dd2), ub.y + f32_to_f64_bits(dd3));
-                    Sn[0] = f64_to_f32_bits(ra.x);
-                    Sn[1] = f64_to_f32_bits(ra.y);
-                    Sn[2] = f64_to_f32_bits(rb.x);
-                    Sn[3] = f64_to_f32_bits(rb.y);
+                    double un[4] = {0.0, 0.0, 0.0, 0.0};
+                    float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+                    if (s.u64_in) {
+                        const double2* ur = reinterpret_cast<const double2*>(raw) + off / 2;
+                        un[0] = ur[0].x; un[1] = ur[0].y; un[2] = ur[1].x; un[3] = ur[1].y;
+                    } else {
+                        hi = reinterpret_cast<const float4*>(raw)[off / 4];
+                        lo = reinterpret_cast<const float4*>(raw + T::RL_OFF)[off / 4];
+                    }
+                    const float h0[4] = {hi.x, hi.y, hi.z, hi.w}, l0[4] = {lo.x, lo.y, lo.z, lo.w};
+                    const float dva[4] = {dv.x, dv.y, dv.z, dv.w};
+                    float l[4];
+                    double r[4];
+                    bool bad_here = false;
+#pragma unroll
+                    for (int v = 0; v < 4; ++v)
+                        Sn[v] = rk3_next(s, un[v], h0[v], l0[v], (2.0f / 3.0f) * (dva[v] + dt * R[v]), l[v], r[v],
+                                         bad_here);
                     if (write) {
-                        reinterpret_cast<double2*>(s.u64 + g)[0] = ra;
-                        reinterpret_cast<double2*>(s.u64 + g)[1] = rb;
+                        if (s.u64_out) {
+                            reinterpret_cast<double2*>(s.u64 + g)[0] = make_double2(r[0], r[1]);
+                            reinterpret_cast<double2*>(s.u64 + g)[1] = make_double2(r[2], r[3]);
+                        } else {
+                            *reinterpret_cast<float4*>(s.ulo + g) = make_float4(l[0], l[1], l[2], l[3]);
+                        }
                         *reinterpret_cast<float4*>(s.uhi_out + g) = make_float4(Sn[0], Sn[1], Sn[2], Sn[3]);
-                        bad |= !(finite_bits(ra.x) && finite_bits(ra.y) && finite_bits(rb.x) && finite_bits(rb.y));
+                        bad |= bad_here;
                     }
                 }
             };
@@ -645,7 +664,7 @@ __global__ void __launch_bounds__(Tc<P>::THREADS, 1) tc_trace_init_kernel(const 
             for (int r = 0; r < BW; ++r) {
                 const int i = k + KT * r;
                 if (i >= 1 && i < NP) {
-                    const float4 a = tc_state<P>(sRaw, s.stage, false, le, i);
+                    const float4 a = tc_state<P>(sRaw, s.stage, s.u64_in != 0, false, le, i);
                     tc_put_a(sA, 0, le, i, a.x);
                     tc_put_a(sA, 1, le, i, a.y);
                     tc_put_a(sA, 2, le, i, a.z);
@@ -658,7 +677,7 @@ __global__ void __launch_bounds__(Tc<P>::THREADS, 1) tc_trace_init_kernel(const 
             if (lane == 0) tc::mbar_arrive(&bar[T::A3]);
             if (!wait(T::G3, j)) break;
             tc::fence_after();
-            const float4 z = tc_state<P>(sRaw, s.stage, false, le, 0);
+            const float4 z = tc_state<P>(sRaw, s.stage, s.u64_in != 0, false, le, 0);
             const float s0[4] = {z.x, z.y, z.z, z.w};
             tc_traces_out<P, GHOST>(ka, tl, s0, e0 + le, le < nloc, k);
             tc::fence_before();

@@ -39,18 +39,15 @@ __device__ __forceinline__ void stage_combine_next(const StageArgs& s, float* sR
     const int t = threadIdx.x;
     bool bad = false;
     for (int g0 = t; g0 < n4; g0 += CH * THREADS) {
-        float4 dv[CH], uh[CH];
-        double2 ua[CH], ub[CH];
+        float4 dv[CH], uh[CH], lo[CH];
+        double2 un[CH][2];
 #pragma unroll
         for (int k = 0; k < CH; ++k) {
             const int g = g0 + k * THREADS;
             if (g < n4) {
                 if (s.stage >= 2) dv[k] = __ldg(reinterpret_cast<const float4*>(s.din) + b4 + g);
                 if (s.stage <= 2) uh[k] = __ldg(reinterpret_cast<const float4*>(s.uhi) + b4 + g);
-                if (s.stage == 3) {
-                    ua[k] = reinterpret_cast<const double2*>(s.u64)[2 * (b4 + g)];
-                    ub[k] = reinterpret_cast<const double2*>(s.u64)[2 * (b4 + g) + 1];
-                }
+                else rk3_load4(s, b4 + g, un[k], uh[k], lo[k]);
             }
         }
 #pragma unroll
@@ -72,18 +69,9 @@ __device__ __forceinline__ void stage_combine_next(const StageArgs& s, float* sR
                 *slot = make_float4(__fadd_rn(uh[k].x, o.x), __fadd_rn(uh[k].y, o.y), __fadd_rn(uh[k].z, o.z),
                                     __fadd_rn(uh[k].w, o.w));
             } else {
-                const float d0 = (2.0f / 3.0f) * (dv[k].x + dt * du.x), d1 = (2.0f / 3.0f) * (dv[k].y + dt * du.y);
-                const float d2 = (2.0f / 3.0f) * (dv[k].z + dt * du.z), d3 = (2.0f / 3.0f) * (dv[k].w + dt * du.w);
-                // one FP64 add per value; the conversions and the check run on the integer pipe
-                const double2 ra = make_double2(ua[k].x + f32_to_f64_bits(d0), ua[k].y + f32_to_f64_bits(d1));
-                const double2 rb = make_double2(ub[k].x + f32_to_f64_bits(d2), ub[k].y + f32_to_f64_bits(d3));
-                reinterpret_cast<double2*>(s.u64)[2 * (b4 + g)] = ra;
-                reinterpret_cast<double2*>(s.u64)[2 * (b4 + g) + 1] = rb;
-                const float4 n = make_float4(f64_to_f32_bits(ra.x), f64_to_f32_bits(ra.y), f64_to_f32_bits(rb.x),
-                                            f64_to_f32_bits(rb.y));
-                reinterpret_cast<float4*>(s.uhi_out)[b4 + g] = n;
-                *slot = n;
-                bad |= !(finite_bits(ra.x) && finite_bits(ra.y) && finite_bits(rb.x) && finite_bits(rb.y));
+                const float d[4] = {(2.0f / 3.0f) * (dv[k].x + dt * du.x), (2.0f / 3.0f) * (dv[k].y + dt * du.y),
+                                    (2.0f / 3.0f) * (dv[k].z + dt * du.z), (2.0f / 3.0f) * (dv[k].w + dt * du.w)};
+                *slot = rk3_next4(s, b4 + g, un[k], uh[k], lo[k], d, bad);
             }
         }
     }
@@ -155,8 +143,8 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
     const int el = stage_elem(tl);
     const bool active = el < nloc;
     const int e = e0 + el;
-    if (tl == 0 && s.stage == 3)  // the FP64 state is read back in the stage combination
-        prefetch_l2_bulk(s.u64 + (size_t)e0 * NB, (unsigned)(nloc * NB * sizeof(double)));
+    if (tl == 0 && s.stage == 3)  // u^n is read back in the stage combination
+        rk3_prefetch(s, (size_t)e0 * NB, nloc * NB);
     // the element's geometry and connectivity ride in the same round trip as the tile's state
     // (the boundary variant, short of registers, loads the geometry after staging)
     ElemGeomF G;

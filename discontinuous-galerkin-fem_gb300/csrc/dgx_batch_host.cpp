@@ -26,6 +26,7 @@ struct Group {  // the instances of one order, concatenated
     BCSlot* bc = nullptr;
     double* u = nullptr;                  // FP64 state of every instance of this order
     float* uhi[2] = {nullptr, nullptr};   // FP32 copies of u^n, ping-ponged
+    float* ulo = nullptr;                 // low parts of the double-float state
     float* d1 = nullptr;                  // FP32 stage increments
     float* d2 = nullptr;
 };
@@ -43,15 +44,14 @@ struct dgx_batch {
     int boundary = 0;
     int grid = 0;  // stage-kernel grid picked by the autotuner (0: not yet)
     cudaStream_t cap = nullptr;
-    cudaGraphExec_t graph = nullptr;   // two steps
-    cudaGraphExec_t graph1 = nullptr;  // one step
+    cudaGraphExec_t graph[N_STEP_GRAPHS] = {};  // the StepGraph replays (dgx_internal.h)
 };
 
 static void free_batch(dgx_batch* b) {
     if (!b) return;
     cudaSetDevice(b->device);
-    if (b->graph) cudaGraphExecDestroy(b->graph);
-    if (b->graph1) cudaGraphExecDestroy(b->graph1);
+    for (cudaGraphExec_t g : b->graph)
+        if (g) cudaGraphExecDestroy(g);
     for (Group& g : b->grp) {
         cudaFree(g.geomf);
         cudaFree(g.conn);
@@ -59,6 +59,7 @@ static void free_batch(dgx_batch* b) {
         cudaFree(g.u);
         cudaFree(g.uhi[0]);
         cudaFree(g.uhi[1]);
+        cudaFree(g.ulo);
         cudaFree(g.d1);
         cudaFree(g.d2);
     }
@@ -168,6 +169,7 @@ extern "C" int dgx_batch_create(int n_inst, const dgx_mesh* const* meshes, const
             cudaMemset(g.u, 0, g.nstate * sizeof(double)) != cudaSuccess ||
             cudaMalloc((void**)&g.uhi[0], g.nstate * sizeof(float)) != cudaSuccess ||
             cudaMalloc((void**)&g.uhi[1], g.nstate * sizeof(float)) != cudaSuccess ||
+            cudaMalloc((void**)&g.ulo, g.nstate * sizeof(float)) != cudaSuccess ||
             cudaMalloc((void**)&g.d1, g.nstate * sizeof(float)) != cudaSuccess ||
             cudaMalloc((void**)&g.d2, g.nstate * sizeof(float)) != cudaSuccess) {
             cudaGetLastError();
@@ -206,8 +208,8 @@ extern "C" int dgx_batch_launch_shape(const dgx_batch* b, int* grid, int* tiles)
     return DGX_OK;
 }
 
-// Stage arguments of every order for one step reading uhi[src].
-static void batch_stage_args(const dgx_batch* b, int src, int stage, StageArgs* a) {
+// Stage arguments of every order for one step reading uhi[src], in place `kind` of its call.
+static void batch_stage_args(const dgx_batch* b, int src, int stage, StepKind kind, StageArgs* a) {
     for (int p = 0; p < MAX_P; ++p) {
         const Group& g = b->grp[p];
         StageArgs& s = a[p];
@@ -219,6 +221,8 @@ static void batch_stage_args(const dgx_batch* b, int src, int stage, StageArgs* 
         s.din = stage == 1 ? nullptr : stage == 2 ? g.d1 : g.d2;
         s.dout = stage == 1 ? g.d1 : stage == 2 ? g.d2 : nullptr;
         s.u64 = g.u;
+        s.ulo = g.ulo;
+        set_step_kind(s, kind);
         s.uhi_out = g.uhi[1 - src];
         s.geom = g.geomf;
         s.conn = g.conn;
@@ -236,10 +240,10 @@ static void batch_stage_args(const dgx_batch* b, int src, int stage, StageArgs* 
     }
 }
 
-static int enqueue_batch_step(dgx_batch* b, int src, cudaStream_t s) {
+static int enqueue_batch_step(dgx_batch* b, int src, StepKind kind, cudaStream_t s) {
     for (int stage = 1; stage <= 3; ++stage) {
         StageArgs a[MAX_P];
-        batch_stage_args(b, src, stage, a);
+        batch_stage_args(b, src, stage, kind, a);
         if (launch_batch_stage(a, b->ops, b->boundary, b->prm.physics == DGX_NAVIER_STOKES, b->grid, s))
             return set_error(DGX_ERR_CUDA, std::string("batched stage launch failed: ") +
                                                launch_error_text());
@@ -247,12 +251,14 @@ static int enqueue_batch_step(dgx_batch* b, int src, cudaStream_t s) {
     return DGX_OK;
 }
 
-static int capture_batch(dgx_batch* b, cudaGraphExec_t* out, int steps) {
+static int capture_batch(dgx_batch* b, cudaGraphExec_t* out, int which) {
     cudaGraph_t g;
+    GraphStep gs[2];
+    const int steps = graph_steps(which, gs);
     if (cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         return set_error(DGX_ERR_CUDA, "graph capture could not start");
     int rc = DGX_OK;
-    for (int k = 0; k < steps && !rc; ++k) rc = enqueue_batch_step(b, k & 1, b->cap);
+    for (int k = 0; k < steps && !rc; ++k) rc = enqueue_batch_step(b, gs[k].src, gs[k].kind, b->cap);
     const cudaError_t ec = cudaStreamEndCapture(b->cap, &g);
     if (rc) return rc;
     if (ec != cudaSuccess) return set_error(DGX_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
@@ -291,7 +297,7 @@ extern "C" int dgx_batch_rk3_step(dgx_batch* b, const double* dt, int n_steps, v
         const bool visc = b->prm.physics == DGX_NAVIER_STOKES;
         if (visc) key += " ns";
         StageArgs a[MAX_P];
-        batch_stage_args(b, 0, 1, a);
+        batch_stage_args(b, 0, 1, STEP_ONLY, a);
         const OpsHost* ops = b->ops;
         int grid = 0;
         const int rc = tune_grid(key, grid_candidates(batch_tiles(a)), [&](int g, cudaStream_t ts) {
@@ -300,15 +306,11 @@ extern "C" int dgx_batch_rk3_step(dgx_batch* b, const double* dt, int n_steps, v
         if (rc) return rc;
         b->grid = grid;
     }
-    if (!b->graph) {
-        int rc = capture_batch(b, &b->graph, 2);
-        if (!rc) rc = capture_batch(b, &b->graph1, 1);
-        if (rc) return rc;
-    }
-    for (int i = 0; i + 1 < n_steps; i += 2)
-        if (cudaGraphLaunch(b->graph, s) != cudaSuccess)
+    return for_step_graphs(n_steps, [&](int g) {
+        if (!b->graph[g])
+            if (int rc = capture_batch(b, &b->graph[g], g)) return rc;
+        if (cudaGraphLaunch(b->graph[g], s) != cudaSuccess)
             return set_error(DGX_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(cudaGetLastError()));
-    if ((n_steps & 1) && cudaGraphLaunch(b->graph1, s) != cudaSuccess)
-        return set_error(DGX_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(cudaGetLastError()));
-    return DGX_OK;
+        return (int)DGX_OK;
+    });
 }

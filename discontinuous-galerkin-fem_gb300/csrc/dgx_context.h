@@ -33,6 +33,7 @@ struct dgx_ctx {
     int* d_flag = nullptr;
     int* d_status = nullptr;  // bit 0: an RK3 step produced a non-finite value (dgx_step_status)
     float* d_uhi[2] = {nullptr, nullptr};  // FP32 copies of u^n (mixed RK3), ping-ponged
+    float* d_ulo = nullptr;                 // low parts of the double-float state (mixed RK3)
     float* d_tr[2] = {nullptr, nullptr};    // face traces of the stage states (mixed Euler, trace form)
     // trace form with ghost blocks (every boundary face has a condition): the connectivity with
     // boundary face k pointing at block ne + k of d_tr, and each ghost block's condition slot
@@ -48,8 +49,8 @@ struct dgx_ctx {
     cudaStream_t cap = nullptr;  // capture stream
     cudaStream_t host_out = nullptr;          // host-pointer step: copies back (dgx_rk3_step_host)
     cudaEvent_t host_ev[4] = {nullptr, nullptr, nullptr, nullptr};
-    cudaGraphExec_t graph = nullptr;   // one step (FP64) or two steps (mixed)
-    cudaGraphExec_t graph1 = nullptr;  // mixed: one step
+    cudaGraphExec_t graph = nullptr;                         // FP64 / double-float: one step
+    cudaGraphExec_t mgraph[dgx::N_STEP_GRAPHS] = {};         // mixed: the StepGraph replays
     int stage_grid = 0;  // mixed: stage-kernel grid picked by the autotuner (0: not yet)
     const double* graph_u = nullptr;
     double graph_dt = 0.0;

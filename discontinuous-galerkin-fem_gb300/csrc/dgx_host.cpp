@@ -671,11 +671,13 @@ static void free_ctx(dgx_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->graph) cudaGraphExecDestroy(c->graph);
-    if (c->graph1) cudaGraphExecDestroy(c->graph1);
+    for (cudaGraphExec_t g : c->mgraph)
+        if (g) cudaGraphExecDestroy(g);
     for (double* a : c->d_adj) cudaFree(a);
     cudaFree(c->d_kin);
     cudaFree(c->d_uhi[0]);
     cudaFree(c->d_uhi[1]);
+    cudaFree(c->d_ulo);
     cudaFree(c->d_d1);
     cudaFree(c->d_d2);
     cudaFree(c->d_tr[0]);
@@ -1018,6 +1020,7 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
         (p->precision == DGX_MIXED &&
          (!alloc((void**)&c->d_uhi[0], c->nstate * sizeof(float)) ||
           !alloc((void**)&c->d_uhi[1], c->nstate * sizeof(float)) ||
+          !alloc((void**)&c->d_ulo, c->nstate * sizeof(float)) ||
           !alloc((void**)&c->d_d1, c->nstate * sizeof(float)) ||
           !alloc((void**)&c->d_d2, c->nstate * sizeof(float)))) ||
         (p->precision == DGX_MIXED && !quad && p->physics == DGX_EULER &&
@@ -1194,6 +1197,7 @@ static StageArgs mixed_stage_args(const dgx_ctx* c, double* u, double dt, int sr
     a.boundary = c->boundary;
     a.uhi = c->d_uhi[src];
     a.u64 = u;
+    a.ulo = c->d_ulo;
     a.uhi_out = c->d_uhi[1 - src];
     a.grid = c->stage_grid;
     a.status = c->d_status;
@@ -1204,9 +1208,11 @@ static StageArgs mixed_stage_args(const dgx_ctx* c, double* u, double dt, int sr
 
 // Face-trace form: the stages of a step that starts from uhi[q] read the traces in d_tr[q],
 // d_tr[1-q], d_tr[q] and write d_tr[1-q], d_tr[q], d_tr[1-q]: the next step starts from
-// uhi[1-q] with its traces in d_tr[1-q].
-static void mixed_step_args(const dgx_ctx* c, double* u, double dt, int src, StageArgs st[3]) {
-    const StageArgs a = mixed_stage_args(c, u, dt, src);
+// uhi[1-q] with its traces in d_tr[1-q].  kind: the step's place in its call (StepKind).
+static void mixed_step_args(const dgx_ctx* c, double* u, double dt, int src, StageArgs st[3],
+                            StepKind kind = STEP_ONLY) {
+    StageArgs a = mixed_stage_args(c, u, dt, src);
+    set_step_kind(a, kind);
     float* const t0 = c->d_tr[src];
     float* const t1 = c->d_tr[1 - src];
     st[0] = a; st[0].stage = 1; st[0].din = nullptr;   st[0].dout = c->d_d1;  st[0].tin = t0; st[0].tout = t1;
@@ -1220,9 +1226,9 @@ static int launch_stage(const dgx_ctx* c, const StageArgs& a, cudaStream_t s) {
     return DGX_OK;
 }
 
-static int enqueue_rk3_mixed(dgx_ctx* c, double* u, double dt, int src, cudaStream_t s) {
+static int enqueue_rk3_mixed(dgx_ctx* c, double* u, double dt, int src, StepKind kind, cudaStream_t s) {
     StageArgs st[3];
-    mixed_step_args(c, u, dt, src, st);
+    mixed_step_args(c, u, dt, src, st, kind);
     for (const StageArgs& t : st)
         if (int rc = launch_stage(c, t, s)) return rc;
     return DGX_OK;
@@ -1242,6 +1248,15 @@ static int capture(dgx_ctx* c, cudaGraphExec_t* out, const std::function<int(cud
         return fail(DGX_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
     }
     return DGX_OK;
+}
+
+static void destroy_graphs(dgx_ctx* c) {
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+    for (cudaGraphExec_t& g : c->mgraph) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+    }
 }
 
 // Mixed precision, before the first step of a call: the FP32 copy of the caller's state
@@ -1301,9 +1316,7 @@ static int mixed_prologue(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
             return launch_stage_mixed(c->prm.order, visc, t, c->ops, ts);
         }, s, &c->stage_grid);
         if (rc) return rc;
-        if (c->graph) cudaGraphExecDestroy(c->graph);
-        if (c->graph1) cudaGraphExecDestroy(c->graph1);
-        c->graph = c->graph1 = nullptr;
+        destroy_graphs(c);
     }
     if (c->d_tr[0] && (c->stage_grid & (STAGE_TRACE | STAGE_TC)))
         if (int rc = init_traces((c->stage_grid & STAGE_TC) != 0)) return rc;
@@ -1319,33 +1332,32 @@ extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void*
         return fail(DGX_ERR_INVALID, "dgx_rk3_step: a mixed-precision state must be 16-byte aligned");
     if (mixed)
         if (int rc = mixed_prologue(c, u, dt, s)) return rc;
-    if (!c->graph || c->graph_u != u || c->graph_dt != dt) {
-        if (c->graph) cudaGraphExecDestroy(c->graph);
-        if (c->graph1) cudaGraphExecDestroy(c->graph1);
-        c->graph = c->graph1 = nullptr;
-        int rc;
-        if (mixed) {
-            // two steps per replay: uhi[0] -> uhi[1] -> uhi[0]
-            rc = capture(c, &c->graph, [&](cudaStream_t cs) {
-                int r = enqueue_rk3_mixed(c, u, dt, 0, cs);
-                return r ? r : enqueue_rk3_mixed(c, u, dt, 1, cs);
-            });
-            if (!rc) rc = capture(c, &c->graph1, [&](cudaStream_t cs) { return enqueue_rk3_mixed(c, u, dt, 0, cs); });
-        } else {
-            rc = capture(c, &c->graph, [&](cudaStream_t cs) { return enqueue_rk3(c, u, dt, cs); });
-        }
-        if (rc) return rc;
+    if (c->graph_u != u || c->graph_dt != dt) {
+        destroy_graphs(c);
         c->graph_u = u;
         c->graph_dt = dt;
     }
     if (!mixed) {
+        if (!c->graph)
+            if (int rc = capture(c, &c->graph, [&](cudaStream_t cs) { return enqueue_rk3(c, u, dt, cs); })) return rc;
         for (int i = 0; i < n_steps; ++i) CUDA_OK(cudaGraphLaunch(c->graph, s));
         return DGX_OK;
     }
-    // pairs of steps and a last single step
-    for (int i = 0; i + 1 < n_steps; i += 2) CUDA_OK(cudaGraphLaunch(c->graph, s));
-    if (n_steps & 1) CUDA_OK(cudaGraphLaunch(c->graph1, s));
-    return DGX_OK;
+    // the call's steps as replays of the StepGraph graphs, each captured on first use
+    return for_step_graphs(n_steps, [&](int g) {
+        if (!c->mgraph[g]) {
+            GraphStep gs[2];
+            const int ns = graph_steps(g, gs);
+            if (int rc = capture(c, &c->mgraph[g], [&](cudaStream_t cs) {
+                    for (int k = 0; k < ns; ++k)
+                        if (int r = enqueue_rk3_mixed(c, u, dt, gs[k].src, gs[k].kind, cs)) return r;
+                    return (int)DGX_OK;
+                }))
+                return rc;
+        }
+        CUDA_OK(cudaGraphLaunch(c->mgraph[g], s));
+        return (int)DGX_OK;
+    });
 }
 
 static int monitor(dgx_ctx* c, const double* u, double dt, cudaStream_t s) {

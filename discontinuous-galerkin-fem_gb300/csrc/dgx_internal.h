@@ -206,7 +206,13 @@ struct StageArgs {
     const float* uhi;   // FP32 u^n (neighbours read it)
     const float* din;   // increment of the stage state (null in stage 1)
     float* dout;        // next increment (stages 1, 2)
-    double* u64;        // FP64 state, updated in place in stage 3
+    // The state between the steps of one call is the double-float pair uhi + ulo (both FP32,
+    // |ulo| <= ulp(uhi) / 2: a 48-bit significand); the caller's FP64 state u64 is read by the
+    // first step of a call and written by its last (stage 3 only):
+    //   u64_in:  u^n = u64 (else uhi + ulo);  u64_out: u^{n+1} -> u64 (else -> uhi_out + ulo)
+    double* u64;        // the caller's FP64 state
+    float* ulo;         // low part of the double-float state, updated in place in stage 3
+    int u64_in, u64_out;
     float* uhi_out;     // FP32 rounding of u^{n+1} (stage 3; not the buffer uhi points to)
     const ElemGeomF* geom;
     const ElemConn* conn;
@@ -228,6 +234,46 @@ struct StageArgs {
     const int* ghost_bc;
 };
 
+// The steps of one mixed-precision call: the first reads the caller's FP64 state, the last
+// writes it back, the ones between carry the double-float pair (StageArgs::u64_in / u64_out of
+// stage 3); a call of one step reads and writes FP64.
+enum StepKind { STEP_ONLY = 0, STEP_FIRST = 1, STEP_MID = 2, STEP_LAST = 3 };
+inline StepKind step_kind(int k, int n) {
+    return n == 1 ? STEP_ONLY : k == 0 ? STEP_FIRST : k == n - 1 ? STEP_LAST : STEP_MID;
+}
+inline void set_step_kind(StageArgs& a, StepKind kind) {
+    a.u64_in = kind == STEP_ONLY || kind == STEP_FIRST;
+    a.u64_out = kind == STEP_ONLY || kind == STEP_LAST;
+}
+// A call of n steps as replays of at most six captured graphs; step k reads the FP32 copy
+// uhi[k & 1]:  ONLY (src 0) | FIRST (src 0), MID2 (src 1, 0) ..., MID (src 1)?, LAST0/LAST1.
+enum StepGraph { G_ONLY = 0, G_FIRST, G_MID2, G_MID, G_LAST0, G_LAST1, N_STEP_GRAPHS };
+struct GraphStep {
+    int src;
+    StepKind kind;
+};
+inline int graph_steps(int g, GraphStep out[2]) {
+    switch (g) {
+    case G_ONLY: out[0] = {0, STEP_ONLY}; return 1;
+    case G_FIRST: out[0] = {0, STEP_FIRST}; return 1;
+    case G_MID2: out[0] = {1, STEP_MID}; out[1] = {0, STEP_MID}; return 2;
+    case G_MID: out[0] = {1, STEP_MID}; return 1;
+    case G_LAST0: out[0] = {0, STEP_LAST}; return 1;
+    default: out[0] = {1, STEP_LAST}; return 1;
+    }
+}
+template <class F>
+inline int for_step_graphs(int n, F&& f) {
+    if (n <= 0) return 0;
+    if (n == 1) return f(G_ONLY);
+    if (int rc = f(G_FIRST)) return rc;
+    const int m = n - 2;
+    for (int i = 0; i + 1 < m; i += 2)
+        if (int rc = f(G_MID2)) return rc;
+    if (m & 1)
+        if (int rc = f(G_MID)) return rc;
+    return f(((n - 1) & 1) ? G_LAST1 : G_LAST0);
+}
 
 // Launchers (one translation unit per precision).
 int launch_element_fp64(int p, bool viscous, const StepArgs& a, const OpsHost& ops, cudaStream_t s);

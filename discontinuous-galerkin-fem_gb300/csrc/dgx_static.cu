@@ -29,7 +29,9 @@
 
 using namespace dgx;
 
-static __device__ __align__(256) double g_rk3_scratch[2 * DGX_STATIC_MAX_STATE];
+// FP64 / double-float contexts: two FP64 stage states; mixed: five FP32 arrays (the two FP32
+// copies of u^n, the two increments and the low parts of the double-float state)
+static __device__ __align__(256) double g_rk3_scratch[(5 * (size_t)DGX_STATIC_MAX_STATE + 1) / 2];
 
 namespace {
 constexpr int kMaxDevices = 64;
@@ -118,6 +120,7 @@ extern "C" int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps
         float* uhi[2] = {f, f + c->nstate};
         float* d1 = f + 2 * c->nstate;
         float* d2 = f + 3 * c->nstate;
+        float* ulo = f + 4 * c->nstate;
         if (launch_f64_to_f32(c->nstate, u, uhi[0], s))
             return dgx::set_error(DGX_ERR_CUDA, std::string("dgx_rk3_step_static: conversion launch failed: ") +
                                                     launch_error_text());
@@ -134,10 +137,12 @@ extern "C" int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps
         a.sigma0 = (float)c->prm.sigma0;
         a.boundary = c->boundary;
         a.u64 = u;
+        a.ulo = ulo;
         for (int n = 0; n < n_steps && !rc; ++n) {
             const int src = n & 1;
             a.uhi = uhi[src];
             a.uhi_out = uhi[1 - src];
+            set_step_kind(a, step_kind(n, n_steps));
             a.stage = 1; a.din = nullptr; a.dout = d1;
             rc = launch_stage_mixed(c->prm.order, visc, a, c->ops, s);
             a.stage = 2; a.din = d1; a.dout = d2;

@@ -156,7 +156,11 @@ int dgx_rhs(dgx_ctx* c, const double* u, double* du, void* stream);
 /* CompressibleDGSolverBase::time_step_ssp_rk3 + SSP_RK::step_rk3,
  * include/dgfem/solver/dg_solver.hpp:239, include/dgfem/solver/time_stepping.hpp:39-55.
  * Advances u (device, in place) by n_steps SSP-RK3 steps of size dt.  The three stages
- * of a step are captured once into a CUDA graph and replayed. */
+ * of a step are captured once into a CUDA graph and replayed.  Mixed precision: the stage
+ * residuals and increments are FP32; u is read by the first step and written by the last,
+ * and between the steps of one call the state is a double-float pair (an FP32 value and
+ * its FP32 remainder, 48 significant bits) updated with exact FP32 sums, so no step but
+ * the first and the last uses the FP64 pipe (a call of one step adds in FP64). */
 int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void* stream);
 
 /* One stage of time_step_ssp_rk3 (include/dgfem/solver/time_stepping.hpp:39-55) on device
@@ -269,7 +273,7 @@ int dgx_kinetic_energy_gradient_binomial(dgx_ctx* c, const double* u0, double dt
  * device state u (in place), with the stage buffers taken from one static device array
  * of the library instead of memory the library allocates.  The call allocates nothing.
  *  - Limit: n_elements * n_basis * 4 <= DGX_STATIC_MAX_STATE; larger states are rejected
- *    with DGX_ERR_INVALID.  The array (2 * DGX_STATIC_MAX_STATE doubles, 16 MiB) is
+ *    with DGX_ERR_INVALID.  The array (5 * DGX_STATIC_MAX_STATE floats, 20 MiB) is
  *    reserved on a device when the first triangle-mesh context is created there
  *    (dgx_create loads it, looks up its device address and loads the kernels this call
  *    launches, with that device current), and it stays reserved until the process exits.

@@ -6,6 +6,7 @@ Tolerances (relative L2 over all entries):
   FP64 M_K^-1 R, projection and SSP-RK3 steps     <= 1e-11
   double-float (df64) residual                    <= 1e-11
   mixed (FP32 arithmetic) residual                <= 2e-5
+  mixed M_K^-1 R                                  <= 5e-5 (M_K^-1 lifts the high modes)
   mixed SSP-RK3, 5 steps                          <= 1e-6
 The element mass inverse is applied as D^-1 Phi^T diag(w/|J|) Phi D^-1 on the GPU and as
 dgfem's LU inverse of the assembled M_K in the oracle: equal in exact arithmetic.
@@ -120,8 +121,10 @@ def test_quad_rk3_steps_fp64(dg, order, visc):
     om, pm = make_pair(dg, v, e, b, order, True)
     oph, wf = physics(dg, visc, mu=0.01)
     u0 = vortex_state(om, noise=0.0)
-    dt = 0.1 / om.max_cfl(1.4, u0, 1.0)
+    # at CFL 0.1 the p=4 Navier-Stokes step diverges in the oracle itself (NaN within 4 steps)
+    dt = (0.05 if order == 4 else 0.1) / om.max_cfl(1.4, u0, 1.0)
     ref = om.rk3_step(oph, u0, dt, 4)
+    assert np.isfinite(ref).all()
     ctx = dg.DGContext(pm, dg.DGSpace("quad", order), wf, "fp64")
     ut = torch.tensor(u0, device="cuda")
     ctx.rk3_step(ut, dt, 2)
@@ -192,11 +195,16 @@ def test_quad_residual_mixed_and_df64(dg, order, visc):
     R_orc = om.residual(oph, u)
     ut = torch.tensor(u, device="cuda")
     mixed = dg.DGContext(pm, dg.DGSpace("quad", order), wf, "mixed")
-    assert rel(mixed.residual(ut).cpu().numpy(), R_orc) <= 2e-5
+    R_mx = mixed.residual(ut).cpu().numpy()
+    assert rel(R_mx, R_orc) <= 2e-5
     df = dg.DGContext(pm, dg.DGSpace("quad", order), wf, "df64")
     assert rel(df.residual(ut).cpu().numpy(), R_orc) <= 1e-11
-    # the rhs entry of the FP32 form applies M_K^-1 in FP64
-    assert rel(mixed.rhs(ut).cpu().numpy(), om.rhs(oph, u)) <= 2e-5
+    # the rhs entry of the FP32 form applies M_K^-1 in FP64 to its FP32 residual
+    rhs_mx = mixed.rhs(ut).cpu().numpy()
+    assert rel(rhs_mx, om.apply_mass_inv(R_mx)) <= 1e-11
+    # M_K^-1 scales Legendre mode (i, j) by about (2i+1)(2j+1)/4 (up to 20 at p=4), which lifts
+    # the FP32 residual's relative error in the high modes: 5e-5 of the oracle's M_K^-1 R
+    assert rel(rhs_mx, om.rhs(oph, u)) <= 5e-5
 
 
 @pytest.mark.parametrize("visc", [False, True])
