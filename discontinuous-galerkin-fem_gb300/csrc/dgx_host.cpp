@@ -1323,10 +1323,9 @@ static int mixed_prologue(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
     return DGX_OK;
 }
 
-extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void* stream) {
-    if (!c || (c->ne && !u) || n_steps < 0) return fail(DGX_ERR_INVALID, "dgx_rk3_step: bad argument");
-    if (c->ne == 0 || n_steps == 0) return DGX_OK;
-    cudaStream_t s = (cudaStream_t)stream;
+// dgx_rk3_step; with all_but_last (mixed precision, n_steps >= 2) the call's last step is left
+// to the caller (dgx_rk3_step_host), which runs it as STEP_LAST from uhi[(n_steps - 1) & 1].
+static int rk3_step_impl(dgx_ctx* c, double* u, double dt, int n_steps, cudaStream_t s, bool all_but_last) {
     const bool mixed = c->prm.precision == DGX_MIXED;
     if (mixed && (reinterpret_cast<uintptr_t>(u) & 15))  // the stage kernels move the state in 16-byte pieces
         return fail(DGX_ERR_INVALID, "dgx_rk3_step: a mixed-precision state must be 16-byte aligned");
@@ -1345,6 +1344,7 @@ extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void*
     }
     // the call's steps as replays of the StepGraph graphs, each captured on first use
     return for_step_graphs(n_steps, [&](int g) {
+        if (all_but_last && (g == G_LAST0 || g == G_LAST1)) return (int)DGX_OK;
         if (!c->mgraph[g]) {
             GraphStep gs[2];
             const int ns = graph_steps(g, gs);
@@ -1358,6 +1358,12 @@ extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void*
         CUDA_OK(cudaGraphLaunch(c->mgraph[g], s));
         return (int)DGX_OK;
     });
+}
+
+extern "C" int dgx_rk3_step(dgx_ctx* c, double* u, double dt, int n_steps, void* stream) {
+    if (!c || (c->ne && !u) || n_steps < 0) return fail(DGX_ERR_INVALID, "dgx_rk3_step: bad argument");
+    if (c->ne == 0 || n_steps == 0) return DGX_OK;
+    return rk3_step_impl(c, u, dt, n_steps, (cudaStream_t)stream, false);
 }
 
 static int monitor(dgx_ctx* c, const double* u, double dt, cudaStream_t s) {
@@ -1539,10 +1545,11 @@ extern "C" int dgx_rk3_step_host(dgx_ctx* c, double* u, double dt, int n_steps) 
         CUDA_OK(cudaStreamSynchronize(c->cap));
         return DGX_OK;
     }
-    if (n_steps > 1 && (rc = dgx_rk3_step(c, c->d_hu, dt, n_steps - 1, c->cap))) return rc;
-    if (!chunk_in && (rc = mixed_prologue(c, c->d_hu, dt, c->cap))) return rc;
+    // the call's steps but the last, then the last one (STEP_ONLY or STEP_LAST) by hand
+    if (n_steps > 1 && (rc = rk3_step_impl(c, c->d_hu, dt, n_steps, c->cap, true))) return rc;
+    if (n_steps == 1 && !chunk_in && (rc = mixed_prologue(c, c->d_hu, dt, c->cap))) return rc;
     StageArgs st[3];
-    mixed_step_args(c, c->d_hu, dt, 0, st);
+    mixed_step_args(c, c->d_hu, dt, (n_steps - 1) & 1, st, n_steps == 1 ? STEP_ONLY : STEP_LAST);
     if ((rc = launch_stage(c, st[0], c->cap)) || (rc = launch_stage(c, st[1], c->cap))) return rc;
     const bool chunked = ntiles >= HOST_CHUNKS;
     const int nch = chunked ? HOST_CHUNKS : 1;
