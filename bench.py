@@ -59,6 +59,11 @@ STAGE_FORMS = {
     "traces": {"kernel": "dgx::stage_trace_kernel<3, no boundary> (mixed SSP-RK3 stage, face traces)",
                "design": 1104, "traffic": 889,
                "note": "ncu dram read+write of one stage-2 launch (889 B/element, its design bytes are 944)"},
+    # the same bytes; each CTA bulk-copies its next tile's inputs while it computes a tile
+    "traces pipelined": {"kernel": "dgx::stage_trace_pipe_kernel<3, no ghost blocks> (mixed SSP-RK3 stage, face "
+                                   "traces, next tile copied while a tile is computed)",
+                         "design": 1104, "traffic": None,
+                         "note": "not captured yet"},
 }
 
 
@@ -597,7 +602,7 @@ def main():
     sf = STAGE_FORMS.get(form, STAGE_FORMS["rows"])
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_kind": peak_kind,
-            "traffic": sf["traffic"] * ne,
+            "traffic": sf["traffic"] * ne if sf["traffic"] else None,
             "kernel": sf["kernel"],
             "algorithmic_bytes_per_launch": ALGO_BYTES_PER_ELEM_STAGE * ne, "launch_ms": t_launch * 1e3,
             "design_bytes_per_launch": sf["design"] * ne,
@@ -791,7 +796,7 @@ def main():
                         "d2h_bytes_per_step": dof * 8},
                 # per timed rk3_step call: the FP32 copy of u^n, the face traces of it (trace
                 # form), then three stage launches per step
-                "gpu_launches": 3 * args.steps + (2 if form == "traces" else 1),
+                "gpu_launches": 3 * args.steps + (2 if form.startswith("traces") else 1),
                 "roofline": {k: roof[k] for k in ("bound", "achieved", "peak", "unit", "frac", "traffic",
                                                   "launch_ms", "peak_kind")},
                 "clocks": clocks,

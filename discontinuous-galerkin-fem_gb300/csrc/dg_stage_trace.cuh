@@ -21,6 +21,7 @@
 #pragma once
 
 #include "dg_stage.cuh"
+#include "tc_ptx.cuh"
 
 namespace dgx {
 
@@ -129,8 +130,26 @@ __device__ __forceinline__ void write_traces(const Ops<P, float>& o, const float
     }
 }
 
-template <int P, bool BND, bool GHOST>
-__device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, float* sU, float* sDt, int tile) {
+// the neighbours' trace blocks of element e (64-byte aligned, one line each) into L2, while the
+// volume terms are formed
+template <int P, bool BND>
+__device__ __forceinline__ void prefetch_neighbour_traces(const StageArgs& s, const ElemConn& C) {
+    constexpr int NFQ = P + 1, TRF = trace_floats<P>();
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+        const int nb = C.nbr[f];
+        if (BND && nb < 0) continue;
+        prefetch_l2_line(s.tin + (size_t)nb * TRF + ((C.flags >> (4 * f)) & 3) * NFQ * NV);
+    }
+}
+
+// One tile: `stage(G, C)` puts the stage state's rows into sU and the element's geometry and
+// connectivity into G and C (the boundary variant reads G itself, after staging, short of
+// registers) and ends with a barrier; then the residual, the stage combination and the next
+// traces.
+template <int P, bool BND, bool GHOST, class Stage>
+__device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka, float* sU, float* sDt, int tile,
+                                                      Stage&& stage) {
     constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1, NB = NP * NV, STR = stage_stride<P>();
     constexpr int TRF = trace_floats<P>();
     const StageArgs& s = ka.s;
@@ -143,27 +162,9 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
     const int el = stage_elem(tl);
     const bool active = el < nloc;
     const int e = e0 + el;
-    if (tl == 0 && s.stage == 3)  // u^n is read back in the stage combination
-        rk3_prefetch(s, (size_t)e0 * NB, nloc * NB);
-    // the element's geometry and connectivity ride in the same round trip as the tile's state
-    // (the boundary variant, short of registers, loads the geometry after staging)
     ElemGeomF G;
     ElemConn C;
-    if (active) {
-        if (!BND) G = s.geom[e];
-        C = s.conn[e];
-    }
-    stage_load_tile<NB, STR>(s.uhi, s.din, sU, e0, nloc, [](int le) { return stage_row(le); });
-    if (active) {  // the neighbours' trace blocks (64-byte aligned, one line each), into L2 while
-                   // the volume terms are formed
-#pragma unroll
-        for (int f = 0; f < 3; ++f) {
-            const int nb = C.nbr[f];
-            if (BND && nb < 0) continue;
-            prefetch_l2_line(s.tin + (size_t)nb * TRF + ((C.flags >> (4 * f)) & 3) * NFQ * NV);
-        }
-    }
-    __syncthreads();
+    stage(G, C);
 
     float R[NP][NV];
 #pragma unroll
@@ -284,6 +285,26 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
     __syncthreads();  // the next tile reuses sU / sDt
 }
 
+template <int P, bool BND, bool GHOST>
+__device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, float* sU, float* sDt, int tile) {
+    constexpr int NB = n_basis(P) * NV, STR = stage_stride<P>();
+    const StageArgs& s = ka.s;
+    stage_trace_tile_with<P, BND, GHOST>(ka, sU, sDt, tile, [&](ElemGeomF& G, ElemConn& C) {
+        const int e0 = tile * TILE, nloc = min(TILE, s.ne - e0);
+        const int tl = threadIdx.x, el = stage_elem(tl);
+        if (tl == 0 && s.stage == 3)  // u^n is read back in the stage combination
+            rk3_prefetch(s, (size_t)e0 * NB, nloc * NB);
+        // the element's geometry and connectivity ride in the same round trip as the tile's state
+        if (el < nloc) {
+            if (!BND) G = s.geom[e0 + el];
+            C = s.conn[e0 + el];
+        }
+        stage_load_tile<NB, STR>(s.uhi, s.din, sU, e0, nloc, [](int le) { return stage_row(le); });
+        if (el < nloc) prefetch_neighbour_traces<P, BND>(s, C);
+        __syncthreads();
+    });
+}
+
 // CTAs per SM the register allocation must allow.  Measured on GB300 for p=3 (512x512x2):
 // 3 CTAs (168 registers, no spills) 0.513 ms/step, 4 CTAs (128 registers) 0.544; the
 // boundary-branch kernel, with the face loop still unrolled, ran 0.743 ms/step at 2 CTAs
@@ -306,6 +327,108 @@ __global__ void __launch_bounds__(TILE, trace_min_blocks(P, BND))
     float* sU = sDt + TILE;
     const int ntiles = ka.s.ntile > 0 ? ka.s.ntile : (ka.s.ne + TILE - 1) / TILE;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) stage_trace_tile<P, BND, GHOST>(ka, sU, sDt, ka.s.tile0 + t);
+}
+
+// Pipelined persistent form (Euler, no boundary branch: periodic meshes or ghost blocks).  Each
+// CTA walks tiles blockIdx.x, + gridDim.x, ...; one thread bulk-copies (cp.async.bulk, completing
+// on an mbarrier) the next tile's uhi and din rows, geometry and connectivity into a staging
+// buffer as soon as the current tile has been staged from it, so a tile's loads run while the
+// tile before it is computed.  The staged numbers and every operation after them are those of
+// stage_trace_kernel.  Shared memory: sDt, sU, then the staging buffer and its barrier.
+template <int P>
+struct TracePipe {
+    static constexpr int NB = n_basis(P) * NV;
+    static constexpr int OFF_U = TILE * 4;
+    static constexpr int OFF_HI = OFF_U + TILE * stage_stride<P>() * 4;
+    static constexpr int OFF_DIN = OFF_HI + TILE * NB * 4;
+    static constexpr int OFF_G = OFF_DIN + TILE * NB * 4;
+    static constexpr int OFF_C = OFF_G + TILE * (int)sizeof(ElemGeomF);
+    static constexpr int OFF_BAR = OFF_C + TILE * (int)sizeof(ElemConn);
+    static constexpr int SMEM = OFF_BAR + 16;  // the barrier and the CTA's abort flag
+    static_assert(OFF_HI % 16 == 0 && OFF_DIN % 16 == 0 && OFF_G % 16 == 0 && OFF_C % 16 == 0 && OFF_BAR % 8 == 0,
+                  "bulk-copy destinations must be 16-byte aligned");
+};
+
+// bulk copies of tile `tile`'s inputs into the staging buffer (issuing thread only); every
+// source starts on a 16-byte boundary (tile offsets are multiples of 128 elements) and every
+// size is a multiple of 16 bytes
+template <int P>
+__device__ __forceinline__ void trace_pipe_issue(const StageArgs& s, unsigned char* sm, uint64_t* bar, int tile) {
+    using TP = TracePipe<P>;
+    const int e0 = tile * TILE, nloc = min(TILE, s.ne - e0);
+    const uint32_t bs = (uint32_t)nloc * TP::NB * 4u, bd = s.din ? bs : 0u;
+    const uint32_t bg = (uint32_t)nloc * (uint32_t)sizeof(ElemGeomF), bc = (uint32_t)nloc * (uint32_t)sizeof(ElemConn);
+    tc::mbar_expect_tx(bar, bs + bd + bg + bc);
+    tc::bulk_g2s(sm + TP::OFF_HI, s.uhi + (size_t)e0 * TP::NB, bs, bar);
+    if (bd) tc::bulk_g2s(sm + TP::OFF_DIN, s.din + (size_t)e0 * TP::NB, bd, bar);
+    tc::bulk_g2s(sm + TP::OFF_G, s.geom + e0, bg, bar);
+    tc::bulk_g2s(sm + TP::OFF_C, s.conn + e0, bc, bar);
+    if (s.stage == 3) rk3_prefetch(s, (size_t)e0 * TP::NB, nloc * TP::NB);
+}
+
+template <int P, bool GHOST>
+__global__ void __launch_bounds__(TILE, 3) stage_trace_pipe_kernel(const __grid_constant__ SArgs<P, false> ka) {
+    using TP = TracePipe<P>;
+    constexpr int NB = TP::NB, NB4 = NB / 4, STR = stage_stride<P>();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* sDt = reinterpret_cast<float*>(smem_raw);
+    float* sU = reinterpret_cast<float*>(smem_raw + TP::OFF_U);
+    const float4* rHi = reinterpret_cast<const float4*>(smem_raw + TP::OFF_HI);
+    const float4* rDin = reinterpret_cast<const float4*>(smem_raw + TP::OFF_DIN);
+    const ElemGeomF* rG = reinterpret_cast<const ElemGeomF*>(smem_raw + TP::OFF_G);
+    const ElemConn* rC = reinterpret_cast<const ElemConn*>(smem_raw + TP::OFF_C);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + TP::OFF_BAR);
+    volatile int* abort = reinterpret_cast<volatile int*>(smem_raw + TP::OFF_BAR + 8);
+    const StageArgs& s = ka.s;
+    const int ntiles = s.ntile > 0 ? s.ntile : (s.ne + TILE - 1) / TILE;
+    const int tl = threadIdx.x;
+    if (tl == 0) {
+        tc::mbar_init(bar, 1);
+        *abort = 0;
+    }
+    __syncthreads();
+    if (tl == 0 && (int)blockIdx.x < ntiles) trace_pipe_issue<P>(s, smem_raw, bar, s.tile0 + blockIdx.x);
+    uint32_t parity = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const bool ok = tc::mbar_wait_or_abort(bar, parity, s.wait_limit, abort, s.wait_hint_ns);
+        if (__syncthreads_or(!ok)) {
+            // a copy did not complete in time: report it, let the copy in flight land, and stop
+            if (tl == 0) {
+                if (s.status) atomicOr(s.status, 2);
+                // the copy in flight lands in this CTA's shared memory: wait for it (up to about
+                // 1.3 s, whatever the configured limit) before the CTA exits
+                for (int it = 0; it < (1 << 16) && !tc::mbar_test_sleep(bar, parity, 20000); ++it) {
+                }
+            }
+            return;
+        }
+        parity ^= 1;
+        const int tile = s.tile0 + t;
+        stage_trace_tile_with<P, false, GHOST>(ka, sU, sDt, tile, [&](ElemGeomF& G, ElemConn& C) {
+            const int e0 = tile * TILE, nloc = min(TILE, s.ne - e0);
+            // the stage state uhi + din into sU (stage_load_tile's sums), the element's records
+            for (int g = tl; g < nloc * NB4; g += TILE) {
+                float4 a = rHi[g];
+                if (s.din) {
+                    const float4 b = rDin[g];
+                    a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w;
+                }
+                const int le = g / NB4, k = 4 * (g - le * NB4);
+                *reinterpret_cast<float4*>(sU + stage_row(le) * STR + k) = a;
+            }
+            const int el = stage_elem(tl);
+            if (el < nloc) {
+                G = rG[el];
+                C = rC[el];
+                prefetch_neighbour_traces<P, false>(s, C);
+            }
+            __syncthreads();  // the staging buffer has been read: the next tile's copies may land
+            if (tl == 0 && t + (int)gridDim.x < ntiles) {
+                tc::fence_async_smem();
+                trace_pipe_issue<P>(s, smem_raw, bar, tile + gridDim.x);
+            }
+        });
+    }
 }
 
 // The traces of the state u = uhi (+ din) a step starts from: one thread per element.
@@ -343,7 +466,11 @@ inline int configure_stage_trace_t() {
                    cudaFuncSetAttribute(stage_trace_kernel<P, false, true>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, b) == cudaSuccess &&
                    cudaFuncSetAttribute(trace_init_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
-                       cudaSuccess
+                       cudaSuccess &&
+                   cudaFuncSetAttribute(stage_trace_pipe_kernel<P, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        TracePipe<P>::SMEM) == cudaSuccess &&
+                   cudaFuncSetAttribute(stage_trace_pipe_kernel<P, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        TracePipe<P>::SMEM) == cudaSuccess
                ? 0
                : -1;
 }
@@ -357,7 +484,17 @@ inline int launch_stage_trace_t(const StageArgs& a, const OpsHost& oh, int grid,
     fill_lift<P, float>(oh, ka.l);
     const int ntiles = a.ntile > 0 ? a.ntile : (a.ne + TILE - 1) / TILE;
     if (ntiles == 0) return 0;
+    const bool pipe = (grid & STAGE_PIPE) != 0 && (a.tconn || !a.boundary);
+    grid &= ~STAGE_PIPE;
+    if (ka.s.wait_limit <= 0) kernel_wait_bounds("DGX_TRACE_WAIT_LIMIT", &ka.s.wait_limit, &ka.s.wait_hint_ns);
     if (grid <= 0 || grid > ntiles) grid = ntiles;
+    if (pipe) {
+        if (a.tconn)
+            stage_trace_pipe_kernel<P, true><<<grid, TILE, TracePipe<P>::SMEM, st>>>(ka);
+        else
+            stage_trace_pipe_kernel<P, false><<<grid, TILE, TracePipe<P>::SMEM, st>>>(ka);
+        return launch_status();
+    }
     if (a.tconn)
         stage_trace_kernel<P, false, true><<<grid, TILE, stage_trace_smem_bytes<P>(), st>>>(ka);
     else if (a.boundary)

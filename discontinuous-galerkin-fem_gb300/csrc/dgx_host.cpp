@@ -1097,8 +1097,12 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
 
 extern "C" int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles, int* form) {
     if (!c) return fail(DGX_ERR_INVALID, "null context");
-    if (grid) *grid = c->stage_grid & ~(STAGE_TC | STAGE_TRACE);
-    if (form) *form = (c->stage_grid & STAGE_TC) ? 1 : (c->stage_grid & STAGE_TRACE) ? 2 : 0;
+    if (grid) *grid = c->stage_grid & ~(STAGE_TC | STAGE_TRACE | STAGE_PIPE);
+    if (form)
+        *form = (c->stage_grid & STAGE_TC)      ? 1
+                : (c->stage_grid & STAGE_PIPE)  ? 3
+                : (c->stage_grid & STAGE_TRACE) ? 2
+                                                : 0;
     if (tiles) *tiles = (c->ne + TILE - 1) / TILE;
     return DGX_OK;
 }
@@ -1280,22 +1284,31 @@ static int mixed_prologue(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
         const StageArgs a = mixed_stage_args(c, u, dt, 0);
         const bool visc = c->prm.physics == DGX_NAVIER_STOKES;
         // candidates: the neighbour-row form at each grid; for Euler the face-trace form at each
-        // grid and the tensor-core form (orders 1-3, meshes whose faces are all interior or ghost
-        // faces) at one CTA per SM.  DGX_STAGE_KERNEL=rows / =trace / =tc keeps one form.
+        // grid, its pipelined persistent kernel at 2 and 3 CTAs per SM (meshes whose faces are all
+        // interior or ghost faces) and the tensor-core form (orders 1-3, the same meshes) at one
+        // CTA per SM.  DGX_STAGE_KERNEL=rows / =trace / =pipe / =tc keeps one form (=trace: both
+        // trace kernels).
         const int ntiles = (c->ne + TILE - 1) / TILE;
         const char* mode = std::getenv("DGX_STAGE_KERNEL");
         const bool only_tc = mode && std::strcmp(mode, "tc") == 0;
-        const bool only_trace = mode && std::strcmp(mode, "trace") == 0;
+        const bool only_pipe = mode && std::strcmp(mode, "pipe") == 0;
+        const bool only_trace = (mode && std::strcmp(mode, "trace") == 0) || only_pipe;
         const bool only_rows = mode && std::strcmp(mode, "rows") == 0;
         const bool tc_ok = !visc && c->d_tr[0] && stage_tc_supported(c->prm.order) && (!c->boundary || c->d_tconn);
+        const bool pipe_ok = !visc && c->d_tr[0] && (!c->boundary || c->d_tconn);
+        int sms = 152;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
         std::vector<int> cands;
         const std::vector<int> grids = grid_candidates(ntiles);
-        if (visc || (!only_tc && !only_trace) || (only_tc && !tc_ok)) cands = grids;  // the neighbour-row form
-        if (!visc && c->d_tr[0] && !only_tc && !only_rows)
-            for (int g : grids) cands.push_back(STAGE_TRACE | g);
+        if (visc || (!only_tc && !only_trace) || (only_tc && !tc_ok) || (only_pipe && !pipe_ok))
+            cands = grids;  // the neighbour-row form
+        if (!visc && c->d_tr[0] && !only_tc && !only_rows) {
+            if (!only_pipe)
+                for (int g : grids) cands.push_back(STAGE_TRACE | g);
+            if (pipe_ok)
+                for (int k = 2; k <= 3; ++k) cands.push_back(STAGE_TRACE | STAGE_PIPE | std::min(ntiles, sms * k));
+        }
         if (tc_ok && !only_trace && !only_rows) {
-            int sms = 152;
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
             cands.push_back(STAGE_TC | std::min(ntiles, sms * stage_tc_ctas_per_sm(c->prm.order)));
         }
         // the traces the timed launches read (their rounding does not matter for the timing)
@@ -1418,8 +1431,8 @@ extern "C" int dgx_step_status(dgx_ctx* c, int* nonfinite, void* stream) {
     CUDA_OK(cudaStreamSynchronize(s));
     if (nonfinite) *nonfinite = f & 1;
     if (f & 2)
-        return fail(DGX_ERR_TIMEOUT, "a bounded wait inside the tensor-core stage kernel gave up; the step's "
-                                     "results are not valid");
+        return fail(DGX_ERR_TIMEOUT, "a bounded wait inside a stage kernel (tensor-core or pipelined trace form) "
+                                     "gave up; the step's results are not valid");
     return (f & 1) ? fail(DGX_ERR_NONFINITE, "an SSP-RK3 step produced a non-finite value") : DGX_OK;
 }
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdlib>
 
 namespace dgx {
 
@@ -27,6 +28,23 @@ inline const char* launch_error_text() {
     last_launch_error() = cudaSuccess;
     if (e == cudaSuccess) e = cudaGetLastError();
     return cudaGetErrorString(e);
+}
+
+// Bounded waits inside the kernels that wait on bulk copies or tensor-core work: by default up
+// to 2^16 polls that may each sleep up to 20 us (about 1.3 s in all, far beyond any wait in a
+// healthy launch).  The environment variable `env` = n makes it n plain polls (a test makes the
+// waits run out on purpose and checks the status the kernels report).
+inline void kernel_wait_bounds(const char* env, long long* limit, unsigned* hint_ns) {
+    *limit = 1LL << 16;
+    *hint_ns = 20000;
+    const char* v = std::getenv(env);
+    if (v && *v) {
+        const long long x = std::atoll(v);
+        if (x > 0) {
+            *limit = x;
+            *hint_ns = 0;
+        }
+    }
 }
 
 constexpr int NV = 4;      // conserved variables (rho, rho u, rho v, E), assembler.cpp:154
@@ -232,6 +250,9 @@ struct StageArgs {
     // buffers, and the condition slot of each ghost block
     const ElemConn* tconn;
     const int* ghost_bc;
+    // bounded waits of the pipelined trace kernel: polls, and the sleep hint of each poll (ns)
+    long long wait_limit;
+    unsigned wait_hint_ns;
 };
 
 // The steps of one mixed-precision call: the first reads the caller's FP64 state, the last
@@ -298,6 +319,9 @@ bool stage_tc_supported(int p);
 // STAGE_TRACE set selects it; the low bits are its grid.  launch_trace_init writes the traces
 // of uhi to tout (the state a step starts from).
 constexpr int STAGE_TRACE = 1 << 28;
+// With STAGE_TRACE: the pipelined persistent trace kernel (stage_trace_pipe_kernel), which
+// bulk-copies the next tile's inputs while a tile is computed; periodic or ghost-block meshes.
+constexpr int STAGE_PIPE = 1 << 27;
 int launch_stage_trace(int p, const StageArgs& a, const OpsHost& ops, int grid, cudaStream_t s);
 int launch_trace_init(int p, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
 int configure_stage_trace(int p);

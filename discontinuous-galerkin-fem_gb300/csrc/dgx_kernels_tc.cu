@@ -6,22 +6,8 @@
 
 namespace dgx {
 
-// Bounded waits inside the kernels: by default up to 2^16 polls that may each sleep up to 20 us
-// (about 1.3 s in all, far beyond any wait in a healthy launch).  DGX_TC_WAIT_LIMIT=n makes it n
-// plain polls (a test makes the waits run out on purpose and checks the status the kernels
-// report).
-static void tc_wait_bounds(long long* limit, unsigned* hint_ns) {
-    *limit = 1LL << 16;
-    *hint_ns = 20000;
-    const char* v = std::getenv("DGX_TC_WAIT_LIMIT");
-    if (v && *v) {
-        const long long x = std::atoll(v);
-        if (x > 0) {
-            *limit = x;
-            *hint_ns = 0;
-        }
-    }
-}
+// Bounded waits inside the kernels (kernel_wait_bounds); DGX_TC_WAIT_LIMIT=n: n plain polls.
+static void tc_wait_bounds(long long* limit, unsigned* hint_ns) { kernel_wait_bounds("DGX_TC_WAIT_LIMIT", limit, hint_ns); }
 
 template <int P>
 static int configure_tc_t() {

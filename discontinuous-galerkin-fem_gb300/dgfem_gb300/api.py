@@ -334,10 +334,11 @@ class DGContext:
 
     def stage_form(self) -> str:
         """The mixed stage kernel's form: "rows" (neighbour coefficient rows per face),
-        "traces" (face traces through HBM) or "tensor cores"."""
+        "traces" (face traces through HBM), "traces pipelined" (the same, each CTA copying its
+        next tile's inputs while it computes one) or "tensor cores"."""
         k = C.c_int()
         check(L.load().dgx_launch_shape(self._h, None, None, C.byref(k)))
-        return {0: "rows", 1: "tensor cores", 2: "traces"}[k.value]
+        return {0: "rows", 1: "tensor cores", 2: "traces", 3: "traces pipelined"}[k.value]
 
     def quad_points(self) -> np.ndarray:
         xq = np.zeros((self.n_elements, self.n_quad, 2))

@@ -186,7 +186,7 @@ int dgx_has_nan(dgx_ctx* c, const double* u, int* has_nan, void* stream);
  * a device flag as they write u^{n+1}; this call reads and clears it (synchronising with
  * `stream`).  Returns DGX_ERR_NONFINITE with *nonfinite = 1, or DGX_OK with 0.  dgfem scans
  * the state after each step and stops the run (compressible_solver_base.cpp:290-301).
- * Returns DGX_ERR_TIMEOUT when a bounded wait inside the tensor-core stage kernel gave up
+ * Returns DGX_ERR_TIMEOUT when a bounded wait inside a stage kernel (tensor-core or pipelined trace form) gave up
  * (its results are then not valid; the kernel returned and the context stays usable). */
 int dgx_step_status(dgx_ctx* c, int* nonfinite, void* stream);
 
@@ -302,13 +302,15 @@ int dgx_eval_points(dgx_ctx* c, int n_points, const double* ref_xy, const double
 /* The stage kernel the autotuner picked for a mixed-precision context: its grid (CTAs;
  * each walks the 128-element tiles with a grid stride), the number of tiles, and its form:
  * 0 = CUDA cores, neighbour coefficient rows read per face; 2 = CUDA cores, face traces
- * exchanged through HBM (Euler); 1 = the 3xTF32 tcgen05 tensor-core form (Euler, orders 1-3,
- * meshes whose boundary faces all have a condition; one CTA per SM).  grid is 0 until the
- * first dgx_rk3_step, which times the candidates on its stream: the CUDA-core forms at one
- * CTA per tile and at 1..8 CTAs per SM, and the tensor-core form.  Environment:
- * DGX_STAGE_KERNEL=rows, =trace or =tc keeps one form; DGX_AUTOTUNE=0 skips the timing (the
- * first candidate).  Quadrilateral meshes have one form (grid = tiles).  A mixed-precision
- * state passed to dgx_rk3_step must be 16-byte aligned.  No counterpart in dgfem. */
+ * exchanged through HBM (Euler); 3 = the same with each CTA bulk-copying its next tile's
+ * inputs while it computes a tile (Euler, meshes whose boundary faces all have a condition;
+ * 2 or 3 CTAs per SM); 1 = the 3xTF32 tcgen05 tensor-core form (Euler, orders 1-3, the same
+ * meshes; one CTA per SM).  grid is 0 until the first dgx_rk3_step, which times the
+ * candidates on its stream: the CUDA-core forms at one CTA per tile and at 1..8 CTAs per SM,
+ * and the others at their grids.  Environment: DGX_STAGE_KERNEL=rows, =trace (forms 2 and 3),
+ * =pipe or =tc keeps one form; DGX_AUTOTUNE=0 skips the timing (the first candidate).
+ * Quadrilateral meshes have one form (grid = tiles).  A mixed-precision state passed to
+ * dgx_rk3_step must be 16-byte aligned.  No counterpart in dgfem. */
 int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles, int* form);
 
 /* ---------------------------------------------------------------- batched solves */

@@ -1,6 +1,7 @@
-"""The two CUDA-core forms of the mixed-precision Euler stage, through the C ABI:
-DGX_STAGE_KERNEL=rows (neighbour coefficient rows per face) and =trace (face traces through
-HBM).  They perform the same FP32 operations in the same order, so their states agree bit
+"""The CUDA-core forms of the mixed-precision Euler stage, through the C ABI:
+DGX_STAGE_KERNEL=rows (neighbour coefficient rows per face), =trace (face traces through
+HBM) and =pipe (the trace kernel whose CTAs copy their next tile's inputs while computing a
+tile).  They perform the same FP32 operations in the same order, so their states agree bit
 for bit, p = 1..4, periodic and with far-field / no-slip / slip faces, over step counts that
 exercise the one-step and two-step graphs; both stay within the mixed-precision bar of the
 FP64 oracle.  With a condition on every boundary face the trace form writes ghost blocks and
@@ -47,9 +48,51 @@ def test_trace_form_equals_row_form(dg, monkeypatch, order, walls):
     ref = om.rk3_step(O.euler(1.4), u0, dt, 5)
     rows, f1 = run(dg, monkeypatch, pm, order, u0, dt, "rows")
     trace, f2 = run(dg, monkeypatch, pm, order, u0, dt, "trace")
-    assert (f1, f2) == ("rows", "traces")
+    pipe, f3 = run(dg, monkeypatch, pm, order, u0, dt, "pipe")
+    assert f1 == "rows" and f2 in ("traces", "traces pipelined")
+    # the pipelined kernel needs every boundary face to have a condition (ghost blocks)
+    assert f3 == ("rows" if walls == "skip" else "traces pipelined")
     assert np.array_equal(rows, trace)
+    assert np.array_equal(rows, pipe)
     assert rel(trace, ref) <= 1e-6
+
+
+@pytest.mark.parametrize("walls", [False, True])
+def test_pipelined_form_equals_row_form_many_tiles(dg, monkeypatch, walls):
+    """200 x 200 x 2 elements, 625 tiles: every CTA of the pipelined kernel (2 or 3 per SM)
+    walks two to four tiles, each tile's inputs copied while the tile before it is computed.
+    The states equal the row form's bit for bit after steps (3, 2) (one call's first, middle and
+    last steps, and a call of two)."""
+    _, pm, u0, dt = case(dg, 200, 3, walls)
+    rows, _ = run(dg, monkeypatch, pm, 3, u0, dt, "rows")
+    pipe, form = run(dg, monkeypatch, pm, 3, u0, dt, "pipe")
+    assert form == "traces pipelined"
+    assert np.isfinite(pipe).all() and np.abs(pipe - u0).max() > 0
+    assert np.array_equal(rows, pipe)
+
+
+def test_pipelined_form_bounded_wait_runs_out_and_reports(dg, monkeypatch):
+    """With one poll per wait, the first wait of every CTA of the pipelined kernel gives up
+    (its bulk copy cannot have landed yet): the CTA flags a timeout, waits for the copy in
+    flight and returns.  dgx_step_status reports DGX_ERR_TIMEOUT; a new context then steps
+    correctly."""
+    om, pm, u0, dt = case(dg, 8, 3, False)
+    monkeypatch.setenv("DGX_TRACE_WAIT_LIMIT", "1")
+    monkeypatch.setenv("DGX_STAGE_KERNEL", "pipe")
+    ctx = dg.DGContext(pm, dg.DGSpace("triangle", 3, "dubiner"), dg.EulerWeakFormulation(1.4), "mixed")
+    u = torch.tensor(u0, device="cuda")
+    ctx.rk3_step(u, dt, 1)
+    torch.cuda.synchronize()
+    assert ctx.stage_form() == "traces pipelined"
+    with pytest.raises(dg.DGXError) as ex:
+        ctx.step_nonfinite()
+    assert ex.value.code == dg._lib.ERR_TIMEOUT
+    monkeypatch.delenv("DGX_TRACE_WAIT_LIMIT")
+    ctx2 = dg.DGContext(pm, dg.DGSpace("triangle", 3, "dubiner"), dg.EulerWeakFormulation(1.4), "mixed")
+    u2 = torch.tensor(u0, device="cuda")
+    ctx2.rk3_step(u2, dt, 2)
+    assert not ctx2.step_nonfinite()
+    assert rel(u2.cpu().numpy(), om.rk3_step(O.euler(1.4), u0, dt, 2)) <= 1e-6
 
 
 @pytest.mark.parametrize("order", [2, 3])
@@ -72,9 +115,51 @@ def test_trace_form_equals_row_form_channel(dg, monkeypatch, order):
     ref = om.rk3_step(O.euler(1.4), u0, dt, 5)
     rows, f1 = run(dg, monkeypatch, pm, order, u0, dt, "rows")
     trace, f2 = run(dg, monkeypatch, pm, order, u0, dt, "trace")
-    assert (f1, f2) == ("rows", "traces")
+    pipe, f3 = run(dg, monkeypatch, pm, order, u0, dt, "pipe")
+    assert f1 == "rows" and f2 in ("traces", "traces pipelined")
+    # the pipelined kernel needs every boundary face to have a condition (ghost blocks)
+    assert f3 == ("rows" if walls == "skip" else "traces pipelined")
     assert np.array_equal(rows, trace)
+    assert np.array_equal(rows, pipe)
     assert rel(trace, ref) <= 1e-6
+
+
+@pytest.mark.parametrize("walls", [False, True])
+def test_pipelined_form_equals_row_form_many_tiles(dg, monkeypatch, walls):
+    """200 x 200 x 2 elements, 625 tiles: every CTA of the pipelined kernel (2 or 3 per SM)
+    walks two to four tiles, each tile's inputs copied while the tile before it is computed.
+    The states equal the row form's bit for bit after steps (3, 2) (one call's first, middle and
+    last steps, and a call of two)."""
+    _, pm, u0, dt = case(dg, 200, 3, walls)
+    rows, _ = run(dg, monkeypatch, pm, 3, u0, dt, "rows")
+    pipe, form = run(dg, monkeypatch, pm, 3, u0, dt, "pipe")
+    assert form == "traces pipelined"
+    assert np.isfinite(pipe).all() and np.abs(pipe - u0).max() > 0
+    assert np.array_equal(rows, pipe)
+
+
+def test_pipelined_form_bounded_wait_runs_out_and_reports(dg, monkeypatch):
+    """With one poll per wait, the first wait of every CTA of the pipelined kernel gives up
+    (its bulk copy cannot have landed yet): the CTA flags a timeout, waits for the copy in
+    flight and returns.  dgx_step_status reports DGX_ERR_TIMEOUT; a new context then steps
+    correctly."""
+    om, pm, u0, dt = case(dg, 8, 3, False)
+    monkeypatch.setenv("DGX_TRACE_WAIT_LIMIT", "1")
+    monkeypatch.setenv("DGX_STAGE_KERNEL", "pipe")
+    ctx = dg.DGContext(pm, dg.DGSpace("triangle", 3, "dubiner"), dg.EulerWeakFormulation(1.4), "mixed")
+    u = torch.tensor(u0, device="cuda")
+    ctx.rk3_step(u, dt, 1)
+    torch.cuda.synchronize()
+    assert ctx.stage_form() == "traces pipelined"
+    with pytest.raises(dg.DGXError) as ex:
+        ctx.step_nonfinite()
+    assert ex.value.code == dg._lib.ERR_TIMEOUT
+    monkeypatch.delenv("DGX_TRACE_WAIT_LIMIT")
+    ctx2 = dg.DGContext(pm, dg.DGSpace("triangle", 3, "dubiner"), dg.EulerWeakFormulation(1.4), "mixed")
+    u2 = torch.tensor(u0, device="cuda")
+    ctx2.rk3_step(u2, dt, 2)
+    assert not ctx2.step_nonfinite()
+    assert rel(u2.cpu().numpy(), om.rk3_step(O.euler(1.4), u0, dt, 2)) <= 1e-6
 
 
 def test_autotuner_reports_a_form(dg, monkeypatch):
@@ -85,7 +170,8 @@ def test_autotuner_reports_a_form(dg, monkeypatch):
 
 
 @pytest.mark.parametrize("walls", [False, True, "skip"])
-@pytest.mark.parametrize("kernel,n", [("rows", 1), ("trace", 1), ("trace", 3), ("tc", 1), ("tc", 3)])
+@pytest.mark.parametrize("kernel,n", [("rows", 1), ("trace", 1), ("trace", 3), ("pipe", 1), ("pipe", 3),
+                                      ("tc", 1), ("tc", 3)])
 def test_host_pointer_step_equals_device_step(dg, monkeypatch, kernel, n, walls):
     """dgx_rk3_step_host runs its last step's stage 3 in tile ranges, each copied back to the
     host while the next range computes; the state equals the device-pointer step's bit for bit."""
