@@ -1314,8 +1314,11 @@ static int mixed_prologue(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
         // the traces the timed launches read (their rounding does not matter for the timing)
         if (c->d_tr[0])
             if (int rc = init_traces(false)) return rc;
+        // the forms on offer depend on the boundary faces: none, all with ghost blocks, or some
+        // without a condition (no ghost blocks: neither the pipelined nor the tensor-core form)
         const std::string key = "stage p" + std::to_string(c->prm.order) + (visc ? " ns" : " euler") +
-                                (c->boundary ? " bnd" : "") + " ne" + std::to_string(c->ne) + " " + (mode ? mode : "");
+                                (c->d_tconn ? " ghost" : c->boundary ? " bnd" : "") + " ne" + std::to_string(c->ne) +
+                                " " + (mode ? mode : "");
         // timed as stage 2 (state uhi + d1, the increment zeroed at creation), which reads the
         // increment as stages 2 and 3 do; it writes only scratch (d2 and the traces in d_tr[1])
         int rc = tune_grid(key, cands, [&](int grid, cudaStream_t ts) {
