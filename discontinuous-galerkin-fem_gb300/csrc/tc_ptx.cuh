@@ -63,6 +63,14 @@ __device__ __forceinline__ bool mbar_test(uint64_t* mbar, uint32_t parity) {
                  : "=r"(done) : "r"(smem_u32(mbar)), "r"(parity) : "memory");
     return done != 0;
 }
+// One non-blocking poll (mbarrier.test_wait): true once the phase with the given parity has
+// completed.  try_wait above may itself wait for a system-dependent time.
+__device__ __forceinline__ bool mbar_test_now(uint64_t* mbar, uint32_t parity) {
+    uint32_t done = 0;
+    asm volatile("{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done) : "r"(smem_u32(mbar)), "r"(parity) : "memory");
+    return done != 0;
+}
 // One poll that may suspend the thread until the phase completes or about `hint_ns`
 // nanoseconds have passed (a sleeping waiter takes no issue slots).
 __device__ __forceinline__ bool mbar_test_sleep(uint64_t* mbar, uint32_t parity, uint32_t hint_ns) {
@@ -79,11 +87,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, long 
 }
 // The same, also giving up (false) as soon as *abort is set; on running out of polls it sets
 // *abort itself, so that every other waiter of the CTA gives up too.  With hint_ns > 0 each
-// poll may sleep up to that long (the wait is then bounded by limit * hint_ns).
+// poll may sleep up to that long (the wait is then bounded by limit * hint_ns); with
+// hint_ns == 0 the polls do not block (a limit of a few polls then runs out for sure).
 __device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* mbar, uint32_t parity, long limit, volatile int* abort,
                                                    uint32_t hint_ns = 0) {
     for (long it = 0; it < limit; ++it) {
-        if (hint_ns ? mbar_test_sleep(mbar, parity, hint_ns) : mbar_test(mbar, parity)) return true;
+        if (hint_ns ? mbar_test_sleep(mbar, parity, hint_ns) : mbar_test_now(mbar, parity)) return true;
         if (*abort) return false;
     }
     *abort = 1;
