@@ -125,7 +125,7 @@ def test_trace_form_equals_row_form_channel(dg, monkeypatch, order):
 def test_autotuner_reports_a_form(dg, monkeypatch):
     om, pm, u0, dt = case(dg, 24, 3, False)  # 1152 elements, 9 tiles
     u, form = run(dg, monkeypatch, pm, 3, u0, dt, None, steps=(1,))
-    assert form in ("rows", "traces")
+    assert form in ("rows", "traces", "traces pipelined", "tensor cores")
     assert rel(u, om.rk3_step(O.euler(1.4), u0, dt, 1)) <= 1e-6
 
 
