@@ -51,19 +51,23 @@ FALLBACK_HBM_GBS = 6800.0
 #  traffic: dram__bytes_read.sum + dram__bytes_write.sum per element of one stage-2 launch,
 #           from an ncu capture of that form on the 512x512x2 p=3 workload.
 STAGE_FORMS = {
-    # stage 1: 400 B, stage 2: 560 B, stage 3: 1200 B (FP32 stage state, FP64 u^n)
+    # stage 1: 400 B, stage 2: 560 B, stage 3: 880 B (FP32 stage state, the double-float state's
+    # low parts read and written in stage 3)
     "rows": {"kernel": "dgx::stage_kernel<3, Euler, no boundary> (mixed SSP-RK3 stage, neighbour rows)",
-             "design": 720, "traffic": 518,
+             "design": 613, "traffic": 518,
              "note": "ncu dram read+write of one stage-2 launch (518 B/element, its design bytes are 560)"},
-    # the rows form's bytes plus the face traces: 192 B written and 192 B read per element
+    # FP32 state rows, increments, the double-float state's low parts (stage 3), geometry and
+    # connectivity, and the face traces: 192 B written and 192 B read per element; stages 1/2/3
+    # 784/944/1264 B (a middle step of a call)
     "traces": {"kernel": "dgx::stage_trace_kernel<3, no boundary> (mixed SSP-RK3 stage, face traces)",
-               "design": 1104, "traffic": 889,
-               "note": "ncu dram read+write of one stage-2 launch (889 B/element, its design bytes are 944)"},
+               "design": 997, "traffic": 935,
+               "note": "ncu dram read+write of the three stage launches of a middle step, averaged "
+                       "(708, 885, 1212 B/element; design 784, 944, 1264)"},
     # the same bytes; each CTA bulk-copies its next tile's inputs while it computes a tile
     "traces pipelined": {"kernel": "dgx::stage_trace_pipe_kernel<3, no ghost blocks> (mixed SSP-RK3 stage, face "
                                    "traces, next tile copied while a tile is computed)",
-                         "design": 1104, "traffic": None,
-                         "note": "not captured yet"},
+                         "design": 997, "traffic": None,
+                         "note": "not captured with DRAM counters"},
 }
 
 
