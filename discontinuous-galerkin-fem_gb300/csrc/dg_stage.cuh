@@ -103,33 +103,73 @@ __device__ __forceinline__ void df_add(float hi, float lo, float d, float& oh, f
 
 __device__ __forceinline__ bool finite_f32(float x) { return (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u; }
 
-// Stage 3 of one value: u^{n+1} = u^n + d.  u^n is un64 (s.u64_in: the caller's FP64 state, first
-// step of a call) or the double-float pair hi + lo; u^{n+1} goes to r64 (s.u64_out: last step of
-// a call; written by the caller) or to the pair (returned hi, lo_out).  A call of one step adds
-// in FP64 exactly as before; the steps between the first and the last of a call add on the FP32
+// Stage 3 of one value: u^{n+1} = u^n + d.  u^n is un64 (M::in64: the caller's FP64 state, first
+// step of a call) or the double-float pair hi + lo; u^{n+1} goes to r64 (M::out64: last step of a
+// call; written by the caller) or to the pair (returned hi, lo_out).  A call of one step adds in
+// FP64 exactly as before; the steps between the first and the last of a call add on the FP32
 // pipe (GB300's FP64 pipe runs at a small fraction of its FP32 rate).  Returns the FP32 rounding
-// of u^{n+1}; the conversions run on the integer pipe (fp_bits.cuh).
-__device__ __forceinline__ float rk3_next(const StageArgs& s, double un64, float hi, float lo, float d, float& lo_out,
-                                          double& r64, bool& bad) {
-    if (s.u64_in) {
+// of u^{n+1}; the conversions run on the integer pipe (fp_bits.cuh).  M says which case: an
+// Rk3Mode fixes it at compile time (a loop per case, chosen once per tile by rk3_dispatch: the
+// row form's scalar loop ran 4-7 % faster so), Rk3Runtime reads it from s per value (the float4
+// combinations: four copies of those loops spill in the face-trace kernel).
+template <bool IN64, bool OUT64>
+struct Rk3Mode {
+    static constexpr bool stage12 = false;
+    __device__ static constexpr bool in64(const StageArgs&) { return IN64; }
+    __device__ static constexpr bool out64(const StageArgs&) { return OUT64; }
+};
+struct Rk3Runtime {
+    static constexpr bool stage12 = false;
+    __device__ static bool in64(const StageArgs& s) { return s.u64_in != 0; }
+    __device__ static bool out64(const StageArgs& s) { return s.u64_out != 0; }
+};
+struct Stage12Mode {  // stages 1 and 2 of stage_combine (no state update)
+    static constexpr bool stage12 = true;
+    __device__ static constexpr bool in64(const StageArgs&) { return false; }
+    __device__ static constexpr bool out64(const StageArgs&) { return false; }
+};
+
+template <class M>
+__device__ __forceinline__ float rk3_next_m(const StageArgs& s, double un64, float hi, float lo, float d,
+                                            float& lo_out, double& r64, bool& bad) {
+    if (M::in64(s)) {
         const double r = un64 + f32_to_f64_bits(d);
         const float h = f64_to_f32_bits(r);
-        if (s.u64_out) r64 = r;
+        if (M::out64(s)) r64 = r;
         else lo_out = f64_to_f32_bits(r - f32_to_f64_bits(h));  // the difference is exact in FP64
         bad |= !finite_bits(r);
         return h;
     }
     float h, l;
     df_add(hi, lo, d, h, l);
-    if (s.u64_out) r64 = f32_to_f64_bits(h) + f32_to_f64_bits(l);  // exact: l lies below h's last bit
+    if (M::out64(s)) r64 = f32_to_f64_bits(h) + f32_to_f64_bits(l);  // exact: l lies below h's last bit
     else lo_out = l;
     bad |= !finite_f32(h);
     return h;
 }
 
+// f(Rk3Mode<s.u64_in, s.u64_out>{})
+template <class F>
+__device__ __forceinline__ void rk3_dispatch(const StageArgs& s, F&& f) {
+    if (s.u64_in) {
+        if (s.u64_out) f(Rk3Mode<true, true>{});
+        else f(Rk3Mode<true, false>{});
+    } else {
+        if (s.u64_out) f(Rk3Mode<false, true>{});
+        else f(Rk3Mode<false, false>{});
+    }
+}
+
+// rk3_next_m with the case read from s (the tensor-core form's per-value combine)
+__device__ __forceinline__ float rk3_next(const StageArgs& s, double un64, float hi, float lo, float d, float& lo_out,
+                                          double& r64, bool& bad) {
+    return rk3_next_m<Rk3Runtime>(s, un64, hi, lo, d, lo_out, r64, bad);
+}
+
 // Stage 3 of four consecutive values at float4 index i4 of the state arrays: reads u^n (u64 or
 // the pair, loaded by the caller into un / hi / lo), writes u64 or ulo, and uhi_out; returns the
 // FP32 rounding of u^{n+1}.
+template <class M>
 __device__ __forceinline__ float4 rk3_next4(const StageArgs& s, size_t i4, const double2 (&un)[2], float4 hi,
                                             float4 lo, const float (&d)[4], bool& bad) {
     const double u0[4] = {un[0].x, un[0].y, un[1].x, un[1].y};
@@ -137,8 +177,8 @@ __device__ __forceinline__ float4 rk3_next4(const StageArgs& s, size_t i4, const
     float h[4], l[4];
     double r[4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) h[v] = rk3_next(s, u0[v], h0[v], l0[v], d[v], l[v], r[v], bad);
-    if (s.u64_out) {
+    for (int v = 0; v < 4; ++v) h[v] = rk3_next_m<M>(s, u0[v], h0[v], l0[v], d[v], l[v], r[v], bad);
+    if (M::out64(s)) {
         reinterpret_cast<double2*>(s.u64)[2 * i4] = make_double2(r[0], r[1]);
         reinterpret_cast<double2*>(s.u64)[2 * i4 + 1] = make_double2(r[2], r[3]);
     } else {
@@ -149,15 +189,25 @@ __device__ __forceinline__ float4 rk3_next4(const StageArgs& s, size_t i4, const
     return o;
 }
 
-// The stage-3 inputs of four values at float4 index i4: u64 (u64_in) or the pair uhi + ulo.
+// The stage-3 inputs of four values at float4 index i4: u64 (M::in64) or the pair uhi + ulo.
+template <class M>
 __device__ __forceinline__ void rk3_load4(const StageArgs& s, size_t i4, double2 (&un)[2], float4& hi, float4& lo) {
-    if (s.u64_in) {
+    if (M::in64(s)) {
         un[0] = reinterpret_cast<const double2*>(s.u64)[2 * i4];
         un[1] = reinterpret_cast<const double2*>(s.u64)[2 * i4 + 1];
     } else {
         hi = __ldg(reinterpret_cast<const float4*>(s.uhi) + i4);
         lo = reinterpret_cast<const float4*>(s.ulo)[i4];
     }
+}
+
+// rk3_load4 / rk3_next4 with the case read from s (the float4 stage combinations)
+__device__ __forceinline__ void rk3_load4(const StageArgs& s, size_t i4, double2 (&un)[2], float4& hi, float4& lo) {
+    rk3_load4<Rk3Runtime>(s, i4, un, hi, lo);
+}
+__device__ __forceinline__ float4 rk3_next4(const StageArgs& s, size_t i4, const double2 (&un)[2], float4 hi, float4 lo,
+                                            const float (&d)[4], bool& bad) {
+    return rk3_next4<Rk3Runtime>(s, i4, un, hi, lo, d, bad);
 }
 
 // Stage combination of one tile in the increment form, 16-byte accesses:
@@ -506,27 +556,38 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
             *reinterpret_cast<float4*>(sU + tl * STR + i * NV) = make_float4(R[i][0], R[i][1], R[i][2], R[i][3]);
     }
     __syncthreads();
+    // stage combination, one value per pass (the float4 form of stage_combine spills here); the
+    // stage-3 variants (rk3_next's four cases) each get their own loop
     const size_t base = (size_t)e0 * NB;
     bool bad = false;
-    for (int g = tl; g < nloc * NB; g += TILE) {
+    auto du_of = [&](int g, float& du, float& dt) {
         const int le = g / NB;
-        const float du = sU[stage_row(le) * STR + (g - le * NB)];
-        const float dt = s.dt_inst ? sDt[stage_row(le)] : s.dt;
-        if (s.stage == 1) {
-            s.dout[base + g] = dt * du;
-        } else if (s.stage == 2) {
-            s.dout[base + g] = 0.25f * (__ldg(s.din + base + g) + dt * du);
-        } else {
-            const float delta = (2.0f / 3.0f) * (__ldg(s.din + base + g) + dt * du);
-            const size_t i = base + g;
-            double r = 0.0;
-            float lo = 0.0f;
-            const float h = s.u64_in ? rk3_next(s, s.u64[i], 0.0f, 0.0f, delta, lo, r, bad)
-                                     : rk3_next(s, 0.0, __ldg(s.uhi + i), s.ulo[i], delta, lo, r, bad);
-            if (s.u64_out) s.u64[i] = r;
-            else s.ulo[i] = lo;
-            s.uhi_out[i] = h;
+        du = sU[stage_row(le) * STR + (g - le * NB)];
+        dt = s.dt_inst ? sDt[stage_row(le)] : s.dt;
+    };
+    if (s.stage <= 2) {
+        for (int g = tl; g < nloc * NB; g += TILE) {
+            float du, dt;
+            du_of(g, du, dt);
+            s.dout[base + g] = s.stage == 1 ? dt * du : 0.25f * (__ldg(s.din + base + g) + dt * du);
         }
+    } else {
+        rk3_dispatch(s, [&](auto m) {
+            using M = decltype(m);
+            for (int g = tl; g < nloc * NB; g += TILE) {
+                float du, dt;
+                du_of(g, du, dt);
+                const size_t i = base + g;
+                const float d = (2.0f / 3.0f) * (__ldg(s.din + i) + dt * du);
+                float l = 0.0f;
+                double r = 0.0;
+                const float h = M::in64(s) ? rk3_next_m<M>(s, s.u64[i], 0.0f, 0.0f, d, l, r, bad)
+                                           : rk3_next_m<M>(s, 0.0, __ldg(s.uhi + i), s.ulo[i], d, l, r, bad);
+                if (M::out64(s)) s.u64[i] = r;
+                else s.ulo[i] = l;
+                s.uhi_out[i] = h;
+            }
+        });
     }
     if (bad && s.status) atomicOr(s.status, 1);
     __syncthreads();  // the next tile reuses sU / sDt
