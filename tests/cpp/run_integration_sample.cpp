@@ -1,5 +1,5 @@
-// Runs the C++ integration sample of INTEGRATION.md (extracted verbatim into
-// integration_sample.inc by tests/test_gpu_cpp_layer.py) and writes its frames as raw doubles.
+// Runs the integration guide's C++ sample (extracted verbatim into integration_sample.inc by
+// tests/test_gpu_cpp_layer.py) and writes its frames as raw doubles.
 //   usage: run_integration_sample <dir> <n> <order> <T_final> <dt> <save_every>
 #include "integration_sample.inc"
 

@@ -2,8 +2,9 @@
 classes, from compiled C++ programs, checked against the oracle:
 * tests/cpp/test_dgfem_compat.cpp: DGMesh, DGSpace, DGAssembler(mesh, weak_form),
   EulerDGSolver(mesh, gamma) and the host-state methods, triangles and quadrilaterals;
-* the C++ sample of INTEGRATION.md, extracted verbatim: EulerDGSolver::solve with the state on
-  the GPU, every saved frame against the oracle's steps."""
+* the integration guide's C++ sample (the block after its `sample: run_vortex` marker), extracted
+  verbatim: EulerDGSolver::solve with the state on the GPU, every saved frame against the oracle's
+  steps."""
 
 import os
 import subprocess
@@ -17,6 +18,7 @@ from meshes import PERIODIC_PAIRS, isentropic_vortex, periodic_rectangle, quad_r
 
 pytestmark = pytest.mark.gpu
 ROOT = Path(__file__).resolve().parent.parent
+INTEGRATION_GUIDE = "INTEGRATION.md"  # the guide whose C++ sample the test compiles
 LIBDIR = ROOT / "discontinuous-galerkin-fem_gb300"
 
 
@@ -68,7 +70,7 @@ def test_integration_sample_solve(tmp_path):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no GPU")
-    doc = (ROOT / "INTEGRATION.md").read_text()
+    doc = (ROOT / INTEGRATION_GUIDE).read_text()
     block = doc.split("<!-- sample: run_vortex -->", 1)[1]
     code = block.split("```cpp\n", 1)[1].split("```", 1)[0]
     (tmp_path / "integration_sample.inc").write_text(code)
