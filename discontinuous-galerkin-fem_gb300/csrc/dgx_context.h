@@ -16,7 +16,8 @@ struct dgx_ctx {
     int ne = 0, np = 0, nq = 0, nfq = 0;
     size_t nstate = 0;  // ne*np*4
     dgx::OpsHost ops{};
-    std::vector<double> xq;  // physical volume points
+    mutable std::vector<double> xq;  // physical volume points (host copy, filled on first use)
+    double* d_xq = nullptr;          // physical volume points on the device [ne][nq][2]
     dgx::ElemGeom* d_geom = nullptr;
     dgx::ElemGeomF* d_geomf = nullptr;  // FP32 rounding of d_geom (mixed precision)
     dgx::ElemConn* d_conn = nullptr;
@@ -74,6 +75,8 @@ struct HostGeometry {
 };
 // Returns a DGX status code; on failure the message is set for dgx_last_error().
 int build_geometry(const dgx_mesh* m, const OpsHost& ops, HostGeometry& g);
+// build_geometry's connectivity and boundary slots only (nf: faces per element of the space)
+int build_topology(const dgx_mesh* m, int nf, HostGeometry& g);
 // FP32 rounding of an element's geometry; `instance` is stored in the spare slot.
 ElemGeomF geom_to_f32(const ElemGeom& g, int instance);
 // Checks that a CUDA device of compute capability 10.3 is current; returns its ordinal.

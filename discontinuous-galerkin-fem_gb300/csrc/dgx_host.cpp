@@ -385,46 +385,67 @@ static void rebuild_faces(dgx_mesh* m) {
         }
     }
 }
+// Face-slot pairing on the GPU (dgx_setup.cu) for meshes of at least this many face slots when a
+// device is present; DGX_SETUP_ON_HOST=1 keeps it on the host.  Both give the same table.
+static constexpr size_t DEVICE_PAIRING_MIN_SLOTS = 1 << 16;
+
+static bool setup_on_device(size_t work) {
+    const char* v = std::getenv("DGX_SETUP_ON_HOST");
+    if (v && std::strcmp(v, "1") == 0) return false;
+    if (work < DEVICE_PAIRING_MIN_SLOTS) return false;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return false;
+    }
+    return true;
+}
+
 static int build_connectivity(dgx_mesh* m, int nbe, const int* bedges) {
     const int ne = m->ne(), K = m->nvpe;
-    // face slots keyed by their vertex pair (min, max): a stable radix sort of the packed keys
-    // keeps equal pairs in slot order (the first two slots of a pair become neighbours)
     const size_t ns = (size_t)ne * K;
     const uint64_t nv = (uint64_t)(m->verts.size() / 2);
-    std::vector<uint64_t> key(ns), key2(ns);
-    std::vector<int> ord(ns), ord2(ns);
-    for (int e = 0; e < ne; ++e)
-        for (int f = 0; f < K; ++f) {
-            const int v1 = m->elems[(size_t)K * e + f], v2 = m->elems[(size_t)K * e + (f + 1) % K];
-            key[(size_t)K * e + f] = (uint64_t)std::min(v1, v2) * nv + (uint64_t)std::max(v1, v2);
-            ord[(size_t)K * e + f] = K * e + f;
-        }
-    uint64_t kmax = 0;
-    for (uint64_t k : key) kmax = std::max(kmax, k);
-    for (int shift = 0; shift < 64 && (kmax >> shift) != 0; shift += 16) {
-        std::vector<size_t> count(65537, 0);
-        for (uint64_t k : key) ++count[((k >> shift) & 0xFFFF) + 1];
-        for (int d = 0; d < 65536; ++d) count[d + 1] += count[d];
-        for (size_t i = 0; i < ns; ++i) {
-            const size_t pos = count[(key[i] >> shift) & 0xFFFF]++;
-            key2[pos] = key[i];
-            ord2[pos] = ord[i];
-        }
-        key.swap(key2);
-        ord.swap(ord2);
-    }
     m->nbr.assign((size_t)ne * 2 * K, -1);
-    for (size_t i = 0; i < ns;) {
-        size_t j = i;
-        while (j < ns && key[j] == key[i]) ++j;
-        if (j - i >= 2) {  // the first two faces of a vertex pair become neighbours
-            const int e1 = ord[i] / K, f1 = ord[i] % K, e2 = ord[i + 1] / K, f2 = ord[i + 1] % K;
-            m->nbr[2 * ((size_t)K * e1 + f1)] = e2;
-            m->nbr[2 * ((size_t)K * e1 + f1) + 1] = f2;
-            m->nbr[2 * ((size_t)K * e2 + f2)] = e1;
-            m->nbr[2 * ((size_t)K * e2 + f2) + 1] = f1;
+    if (setup_on_device(ns)) {
+        if (device_face_pairs(ne, K, m->elems.data(), (long long)nv, m->nbr.data()))
+            return fail(DGX_ERR_CUDA, std::string("face pairing on the device failed: ") + launch_error_text());
+    } else {
+        // face slots keyed by their vertex pair (min, max): a stable radix sort of the packed keys
+        // keeps equal pairs in slot order (the first two slots of a pair become neighbours)
+        std::vector<uint64_t> key(ns), key2(ns);
+        std::vector<int> ord(ns), ord2(ns);
+        for (int e = 0; e < ne; ++e)
+            for (int f = 0; f < K; ++f) {
+                const int v1 = m->elems[(size_t)K * e + f], v2 = m->elems[(size_t)K * e + (f + 1) % K];
+                key[(size_t)K * e + f] = (uint64_t)std::min(v1, v2) * nv + (uint64_t)std::max(v1, v2);
+                ord[(size_t)K * e + f] = K * e + f;
+            }
+        uint64_t kmax = 0;
+        for (uint64_t k : key) kmax = std::max(kmax, k);
+        for (int shift = 0; shift < 64 && (kmax >> shift) != 0; shift += 16) {
+            std::vector<size_t> count(65537, 0);
+            for (uint64_t k : key) ++count[((k >> shift) & 0xFFFF) + 1];
+            for (int d = 0; d < 65536; ++d) count[d + 1] += count[d];
+            for (size_t i = 0; i < ns; ++i) {
+                const size_t pos = count[(key[i] >> shift) & 0xFFFF]++;
+                key2[pos] = key[i];
+                ord2[pos] = ord[i];
+            }
+            key.swap(key2);
+            ord.swap(ord2);
         }
-        i = j;
+        for (size_t i = 0; i < ns;) {
+            size_t j = i;
+            while (j < ns && key[j] == key[i]) ++j;
+            if (j - i >= 2) {  // the first two faces of a vertex pair become neighbours
+                const int e1 = ord[i] / K, f1 = ord[i] % K, e2 = ord[i + 1] / K, f2 = ord[i + 1] % K;
+                m->nbr[2 * ((size_t)K * e1 + f1)] = e2;
+                m->nbr[2 * ((size_t)K * e1 + f1) + 1] = f2;
+                m->nbr[2 * ((size_t)K * e2 + f2)] = e1;
+                m->nbr[2 * ((size_t)K * e2 + f2) + 1] = f1;
+            }
+            i = j;
+        }
     }
     m->btag.assign((size_t)ne * K, -1);
     if (nbe > 0) {
@@ -678,6 +699,7 @@ static void free_ctx(dgx_ctx* c) {
     cudaFree(c->d_uhi[0]);
     cudaFree(c->d_uhi[1]);
     cudaFree(c->d_ulo);
+    cudaFree(c->d_xq);
     cudaFree(c->d_d1);
     cudaFree(c->d_d2);
     cudaFree(c->d_tr[0]);
@@ -708,10 +730,11 @@ static void free_ctx(dgx_ctx* c) {
 extern "C" void dgx_destroy(dgx_ctx* c) { free_ctx(c); }
 
 // Face slots and boundary-condition slots shared by both element shapes: fn/fl hold every
-// element's own outward normals and face lengths ([ne][NF][2], [ne][NF]).
+// element's own outward normals and face lengths ([ne][NF][2], [ne][NF]).  With geom null only
+// the connectivity and the slots are built (the device computes the geometry, dgx_setup.cu).
 template <int NF, class Geom, class Conn>
 static int face_slots(const dgx_mesh* m, const std::vector<double>& fn, const std::vector<double>& fl,
-                      std::vector<Geom>& geom, std::vector<Conn>& conn, HostGeometry& g) {
+                      std::vector<Geom>* geom_or_null, std::vector<Conn>& conn, HostGeometry& g) {
     const int ne = m->ne();
     std::vector<BCSlot>& slots = g.slots;
     for (int e = 0; e < ne; ++e) {
@@ -731,14 +754,17 @@ static int face_slots(const dgx_mesh* m, const std::vector<double>& fn, const st
         if (!take(L, fL) || !take(R, fR)) {
             return fail(DGX_ERR_RUNTIME, "unsupported mesh topology: an element face appears in two interior faces");
         }
-        const double* nL = &fn[2 * ((size_t)NF * L + fL)];
-        const double hL = fl[(size_t)NF * L + fL];
-        geom[L].n[fL][0] = nL[0];
-        geom[L].n[fL][1] = nL[1];
-        geom[L].h[fL] = hL;
-        geom[R].n[fR][0] = -nL[0];
-        geom[R].n[fR][1] = -nL[1];
-        geom[R].h[fR] = hL;
+        if (geom_or_null) {
+            std::vector<Geom>& geom = *geom_or_null;
+            const double* nL = &fn[2 * ((size_t)NF * L + fL)];
+            const double hL = fl[(size_t)NF * L + fL];
+            geom[L].n[fL][0] = nL[0];
+            geom[L].n[fL][1] = nL[1];
+            geom[L].h[fL] = hL;
+            geom[R].n[fR][0] = -nL[0];
+            geom[R].n[fR][1] = -nL[1];
+            geom[R].h[fR] = hL;
+        }
         conn[L].nbr[fL] = R;
         conn[L].flags |= (fR | (rev << 2) | (1 << 3)) << (4 * fL);
         conn[R].nbr[fR] = L;
@@ -748,9 +774,11 @@ static int face_slots(const dgx_mesh* m, const std::vector<double>& fn, const st
     const int nbf = (int)m->bfaces.size() / 3;
     for (int k = 0; k < nbf; ++k) {
         const int e = m->bfaces[3 * (size_t)k], f = m->bfaces[3 * (size_t)k + 1], tag = m->bfaces[3 * (size_t)k + 2];
-        geom[e].n[f][0] = fn[2 * ((size_t)NF * e + f)];
-        geom[e].n[f][1] = fn[2 * ((size_t)NF * e + f) + 1];
-        geom[e].h[f] = fl[(size_t)NF * e + f];
+        if (geom_or_null) {
+            (*geom_or_null)[e].n[f][0] = fn[2 * ((size_t)NF * e + f)];
+            (*geom_or_null)[e].n[f][1] = fn[2 * ((size_t)NF * e + f) + 1];
+            (*geom_or_null)[e].h[f] = fl[(size_t)NF * e + f];
+        }
         auto it = m->bcs.find(tag);
         if (tag < 0 || it == m->bcs.end()) continue;  // no BC: dgfem skips the face
         if (it->second.type == DGX_BC_PERIODIC) {
@@ -843,7 +871,7 @@ static int build_geometry_quad(const dgx_mesh* m, const OpsHost& ops, HostGeomet
             g.xq[((size_t)e * ops.nq + q) * 2 + 1] = y;
         }
     }
-    return face_slots<4>(m, fn, fl, g.qgeom, g.qconn, g);
+    return face_slots<4>(m, fn, fl, &g.qgeom, g.qconn, g);
 }
 
 // Element geometry, face slots and boundary-condition slots of a mesh:
@@ -883,7 +911,24 @@ int dgx::build_geometry(const dgx_mesh* m, const OpsHost& ops, HostGeometry& g) 
             g.xq[((size_t)e * ops.nq + q) * 2 + 1] = N0 * V[1] + xi * V[3] + eta * V[5];
         }
     }
-    return face_slots<3>(m, fn, fl, geom, g.conn, g);
+    return face_slots<3>(m, fn, fl, &geom, g.conn, g);
+}
+
+// The connectivity and boundary slots of build_geometry without the geometry (dgx_create
+// computes the geometry on the device).
+int dgx::build_topology(const dgx_mesh* m, int nf, HostGeometry& g) {
+    const int ne = m->ne();
+    g.slots.clear();
+    g.boundary = g.has_slip_wall = 0;
+    if ((m->nvpe == 4) != (nf == 4))
+        return fail(DGX_ERR_INVALID, "the space's element type does not match the mesh's");
+    const std::vector<double> none;
+    if (m->nvpe == 4) {
+        g.qconn.assign(ne, QuadConn{});
+        return face_slots<4, QuadGeom>(m, none, none, nullptr, g.qconn, g);
+    }
+    g.conn.assign(ne, ElemConn{});
+    return face_slots<3, ElemGeom>(m, none, none, nullptr, g.conn, g);
 }
 
 ElemGeomF dgx::geom_to_f32(const ElemGeom& g, int instance) {
@@ -973,15 +1018,19 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
     c->nfq = c->ops.nfq;
     c->nstate = (size_t)ne * c->np * NV;
 
+    // geometry on the device (dgx_setup.cu); DGX_SETUP_ON_HOST=1 builds it on the host instead
+    // (the same records bit for bit)
+    const char* hs = std::getenv("DGX_SETUP_ON_HOST");
+    const bool host_setup = hs && std::strcmp(hs, "1") == 0;
     HostGeometry hg;
-    if (int rc = build_geometry(m, c->ops, hg)) {
+    if (int rc = host_setup ? build_geometry(m, c->ops, hg) : build_topology(m, c->ops.nf, hg)) {
         free_ctx(c);
         return rc;
     }
     std::vector<ElemGeom>& geom = hg.geom;
     std::vector<ElemConn>& conn = hg.conn;
     std::vector<BCSlot>& slots = hg.slots;
-    c->xq = std::move(hg.xq);
+    c->xq = std::move(hg.xq);  // the host path's points; the device path fills it on first use
     c->boundary = hg.boundary;
     c->has_slip_wall = hg.has_slip_wall;
 
@@ -1015,6 +1064,9 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
     if ((quad ? !alloc((void**)&c->d_qgeom, sizeof(QuadGeom) * ne) || !alloc((void**)&c->d_qconn, sizeof(QuadConn) * ne)
               : !alloc((void**)&c->d_geom, sizeof(ElemGeom) * ne) || !alloc((void**)&c->d_conn, sizeof(ElemConn) * ne)) ||
         !alloc((void**)&c->d_bc, sizeof(BCSlot) * slots.size()) || !alloc((void**)&c->d_u1, sb) ||
+        !alloc((void**)&c->d_xq, (size_t)ne * c->nq * 2 * sizeof(double)) ||
+        (p->precision == DGX_MIXED && (quad ? !alloc((void**)&c->d_qgeomf, sizeof(QuadGeomF) * ne)
+                                            : !alloc((void**)&c->d_geomf, sizeof(ElemGeomF) * ne))) ||
         !alloc((void**)&c->d_u2, sb) || !alloc((void**)&c->d_mon, 4 * sizeof(double)) ||
         !alloc((void**)&c->d_flag, sizeof(int)) || !alloc((void**)&c->d_status, sizeof(int)) ||
         (p->precision == DGX_MIXED &&
@@ -1032,45 +1084,80 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
         free_ctx(c);
         return fail(DGX_ERR_CUDA, "cudaMalloc failed for the solver state");
     }
-    if (p->precision == DGX_MIXED && quad) {
-        std::vector<QuadGeomF> gf(ne);
-        for (int e = 0; e < ne; ++e) {
-            const QuadGeom& g = hg.qgeom[e];
-            QuadGeomF& h = gf[e];
-            std::memset(&h, 0, sizeof(h));
-            for (int k = 0; k < 3; ++k) {
-                h.jx[k] = (float)g.jx[k];
-                h.jy[k] = (float)g.jy[k];
+    bool geom_ok = true;
+    if (host_setup) {  // upload the host-built records
+        if (p->precision == DGX_MIXED && quad) {
+            std::vector<QuadGeomF> gf(ne);
+            for (int e = 0; e < ne; ++e) {
+                const QuadGeom& g = hg.qgeom[e];
+                QuadGeomF& h = gf[e];
+                std::memset(&h, 0, sizeof(h));
+                for (int k = 0; k < 3; ++k) {
+                    h.jx[k] = (float)g.jx[k];
+                    h.jy[k] = (float)g.jy[k];
+                }
+                for (int f = 0; f < 4; ++f) {
+                    h.h[f] = (float)g.h[f];
+                    h.n[f][0] = (float)g.n[f][0];
+                    h.n[f][1] = (float)g.n[f][1];
+                }
+                h.hmin = (float)g.hmin;
             }
-            for (int f = 0; f < 4; ++f) {
-                h.h[f] = (float)g.h[f];
-                h.n[f][0] = (float)g.n[f][0];
-                h.n[f][1] = (float)g.n[f][1];
-            }
-            h.hmin = (float)g.hmin;
+            geom_ok &= !ne || cudaMemcpy(c->d_qgeomf, gf.data(), sizeof(QuadGeomF) * ne, cudaMemcpyHostToDevice) ==
+                                  cudaSuccess;
         }
-        if (!alloc((void**)&c->d_qgeomf, sizeof(QuadGeomF) * (ne ? ne : 1)) ||
-            (ne && cudaMemcpy(c->d_qgeomf, gf.data(), sizeof(QuadGeomF) * ne, cudaMemcpyHostToDevice) != cudaSuccess)) {
+        if (p->precision == DGX_MIXED && !quad) {
+            std::vector<ElemGeomF> gf(ne);
+            for (int e = 0; e < ne; ++e) gf[e] = geom_to_f32(geom[e], 0);
+            geom_ok &= !ne || cudaMemcpy(c->d_geomf, gf.data(), sizeof(ElemGeomF) * ne, cudaMemcpyHostToDevice) ==
+                                  cudaSuccess;
+        }
+        geom_ok &= !ne || (quad ? cudaMemcpy(c->d_qgeom, hg.qgeom.data(), sizeof(QuadGeom) * ne,
+                                             cudaMemcpyHostToDevice) == cudaSuccess
+                                : cudaMemcpy(c->d_geom, geom.data(), sizeof(ElemGeom) * ne, cudaMemcpyHostToDevice) ==
+                                      cudaSuccess);
+        geom_ok &= c->xq.empty() || cudaMemcpy(c->d_xq, c->xq.data(), c->xq.size() * sizeof(double),
+                                               cudaMemcpyHostToDevice) == cudaSuccess;
+    }
+    geom_ok &= !ne || (quad ? cudaMemcpy(c->d_qconn, hg.qconn.data(), sizeof(QuadConn) * ne,
+                                         cudaMemcpyHostToDevice) == cudaSuccess
+                            : cudaMemcpy(c->d_conn, conn.data(), sizeof(ElemConn) * ne, cudaMemcpyHostToDevice) ==
+                                  cudaSuccess);
+    if (!host_setup && geom_ok && ne) {  // the geometry kernel, from the vertex and element arrays
+        double* d_v = nullptr;
+        int *d_e = nullptr, *d_err = nullptr;
+        int err = 0;
+        const bool ok = cudaMalloc((void**)&d_v, m->verts.size() * sizeof(double)) == cudaSuccess &&
+                        cudaMalloc((void**)&d_e, m->elems.size() * sizeof(int)) == cudaSuccess &&
+                        cudaMalloc((void**)&d_err, sizeof(int)) == cudaSuccess &&
+                        cudaMemcpy(d_v, m->verts.data(), m->verts.size() * sizeof(double), cudaMemcpyHostToDevice) ==
+                            cudaSuccess &&
+                        cudaMemcpy(d_e, m->elems.data(), m->elems.size() * sizeof(int), cudaMemcpyHostToDevice) ==
+                            cudaSuccess &&
+                        cudaMemset(d_err, 0, sizeof(int)) == cudaSuccess &&
+                        launch_device_geometry(ne, m->nvpe, c->ops, d_v, d_e,
+                                               quad ? (const void*)c->d_qconn : (const void*)c->d_conn,
+                                               quad ? (void*)c->d_qgeom : (void*)c->d_geom,
+                                               quad ? (void*)c->d_qgeomf : (void*)c->d_geomf, c->d_xq, d_err,
+                                               nullptr) == 0 &&
+                        cudaMemcpy(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess;
+        cudaFree(d_v);
+        cudaFree(d_e);
+        cudaFree(d_err);
+        if (!ok) {
             cudaGetLastError();
             free_ctx(c);
-            return fail(DGX_ERR_CUDA, "device upload failed (FP32 quadrilateral geometry)");
+            return fail(DGX_ERR_CUDA, "geometry set-up on the device failed");
         }
-    }
-    if (p->precision == DGX_MIXED && !quad) {
-        std::vector<ElemGeomF> gf(ne);
-        for (int e = 0; e < ne; ++e) gf[e] = geom_to_f32(geom[e], 0);
-        if (!alloc((void**)&c->d_geomf, sizeof(ElemGeomF) * ne) ||
-            cudaMemcpy(c->d_geomf, gf.data(), sizeof(ElemGeomF) * ne, cudaMemcpyHostToDevice) != cudaSuccess) {
-            cudaGetLastError();
+        if (err & 1) {
             free_ctx(c);
-            return fail(DGX_ERR_CUDA, "device upload failed (FP32 geometry)");
+            return fail(DGX_ERR_RUNTIME, "Singular Jacobian matrix");
+        }
+        if (err & 2) {
+            free_ctx(c);
+            return fail(DGX_ERR_RUNTIME, "Degenerate edge detected");
         }
     }
-    const bool geom_ok =
-        quad ? cudaMemcpy(c->d_qgeom, hg.qgeom.data(), sizeof(QuadGeom) * ne, cudaMemcpyHostToDevice) == cudaSuccess &&
-                   cudaMemcpy(c->d_qconn, hg.qconn.data(), sizeof(QuadConn) * ne, cudaMemcpyHostToDevice) == cudaSuccess
-             : cudaMemcpy(c->d_geom, geom.data(), sizeof(ElemGeom) * ne, cudaMemcpyHostToDevice) == cudaSuccess &&
-                   cudaMemcpy(c->d_conn, conn.data(), sizeof(ElemConn) * ne, cudaMemcpyHostToDevice) == cudaSuccess;
     if (cudaMemset(c->d_status, 0, sizeof(int)) != cudaSuccess || !geom_ok ||
         (c->d_d1 && cudaMemset(c->d_d1, 0, c->nstate * sizeof(float)) != cudaSuccess) ||
         cudaMemcpy(c->d_bc, slots.data(), sizeof(BCSlot) * slots.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -1441,15 +1528,19 @@ extern "C" int dgx_step_status(dgx_ctx* c, int* nonfinite, void* stream) {
 
 extern "C" int dgx_quad_points(const dgx_ctx* c, double* xq) {
     if (!c || !xq) return fail(DGX_ERR_INVALID, "dgx_quad_points: null argument");
+    const size_t n = (size_t)c->ne * c->nq * 2;
+    if (c->xq.size() != n) {  // the device-built points, copied once
+        c->xq.resize(n);
+        if (n) CUDA_OK(cudaMemcpy(c->xq.data(), c->d_xq, n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
     std::copy(c->xq.begin(), c->xq.end(), xq);
     return DGX_OK;
 }
 
 extern "C" int dgx_quad_points_device(const dgx_ctx* c, double* xq, void* stream) {
     if (!c || (c->ne && !xq)) return fail(DGX_ERR_INVALID, "dgx_quad_points_device: bad argument");
-    if (c->xq.empty()) return DGX_OK;
-    CUDA_OK(cudaMemcpyAsync(xq, c->xq.data(), c->xq.size() * sizeof(double), cudaMemcpyHostToDevice,
-                            (cudaStream_t)stream));
+    const size_t n = (size_t)c->ne * c->nq * 2;
+    if (n) CUDA_OK(cudaMemcpyAsync(xq, c->d_xq, n * sizeof(double), cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
     return DGX_OK;
 }
 

@@ -334,6 +334,16 @@ int launch_batch_stage(const StageArgs* per_order, const OpsHost* ops, int bound
 int batch_tiles(const StageArgs* per_order);
 int configure_batch_stage(bool visc);
 
+// Device-side set-up (dgx_setup.cu).  device_face_pairs: the face-slot pairing of a mesh's
+// connectivity, nbr[2 s], nbr[2 s + 1] = element and face paired with face slot s, -1 when none
+// (host arrays; returns nonzero on a CUDA failure).  launch_device_geometry: per-element
+// geometry (ElemGeom or QuadGeom, and their FP32 roundings when geomf is non-null) and the
+// physical volume points; err bit 0: singular Jacobian, bit 1: degenerate edge.
+int device_face_pairs(int ne, int K, const int* elems_host, long long nv, int* nbr_host);
+int launch_device_geometry(int ne, int nvpe, const OpsHost& ops, const double* d_verts, const int* d_elems,
+                           const void* d_conn, void* d_geom, void* d_geomf, double* d_xq, int* d_err,
+                           cudaStream_t s);
+
 // Small FP64 utility kernels (dgx_misc.cu).
 int launch_mass_inv(int ne, int p, const OpsHost& ops, const ElemGeom* geom, const double* in,
                     double* out, cudaStream_t s);
