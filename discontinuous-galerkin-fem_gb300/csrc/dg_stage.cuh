@@ -101,6 +101,14 @@ __device__ __forceinline__ void df_add(float hi, float lo, float d, float& oh, f
     ol = __fadd_rn(__fsub_rn(s, __fsub_rn(oh, bq)), __fsub_rn(t, bq));
 }
 
+// entry f of a three-entry array held in registers, for a face index known only at run time
+// (indexing the array itself places it, and the whole record, in local memory: 15 local loads
+// per element and stage in the face-trace kernel, whose stage went 2.5 % faster with these)
+template <class T>
+__device__ __forceinline__ T pick3(int f, T a, T b, T c) {
+    return f == 0 ? a : (f == 1 ? b : c);
+}
+
 __device__ __forceinline__ bool finite_f32(float x) { return (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u; }
 
 // Stage 3 of one value: u^{n+1} = u^n + d.  u^n is un64 (M::in64: the caller's FP64 state, first
@@ -419,6 +427,8 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
             const int nf = fl & 3;
             const bool rev = (fl >> 2) & 1;
             const float sideL = ((fl >> 3) & 1) ? 1.0f : -1.0f;
+            // indexed by the runtime face: the record goes to local memory (register selects, which
+            // the face-trace kernel uses, measured 3 % slower here: they add register pressure)
             const float nx = G.n[f][0], ny = G.n[f][1], hF = G.h[f];
             // neighbour traces at its own points k, then reordered to this face's points
             float Un[NFQ][4], Nr[VISC ? NFQ : 1][4], Ns[VISC ? NFQ : 1][4];

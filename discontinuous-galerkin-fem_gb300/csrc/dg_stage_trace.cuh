@@ -210,12 +210,14 @@ __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka,
         // larger code missed the instruction cache and its registers spilled)
 #pragma unroll 1
         for (int f = 0; f < 3; ++f) {
-            const int nb = C.nbr[f];
+            const int nb = pick3(f, C.nbr[0], C.nbr[1], C.nbr[2]);
             if (BND && nb == NBR_SKIP) continue;
             const int fl = (C.flags >> (4 * f)) & 15;
             const int nf = fl & 3;
             const bool rev = (fl >> 2) & 1;
-            const float nx = G.n[f][0], ny = G.n[f][1], hF = G.h[f];
+            const float nx = pick3(f, G.n[0][0], G.n[1][0], G.n[2][0]);
+            const float ny = pick3(f, G.n[0][1], G.n[1][1], G.n[2][1]);
+            const float hF = pick3(f, G.h[0], G.h[1], G.h[2]);
             float Uo[NFQ][4], Un[NFQ][4];
             // own traces from the staged coefficients: the same sums, in the same order, as the
             // previous stage's write_traces (the neighbours read those)
