@@ -60,9 +60,9 @@ STAGE_FORMS = {
     # connectivity, and the face traces: 192 B written and 192 B read per element; stages 1/2/3
     # 784/944/1264 B (a middle step of a call)
     "traces": {"kernel": "dgx::stage_trace_kernel<3, no boundary> (mixed SSP-RK3 stage, face traces)",
-               "design": 997, "traffic": 935,
+               "design": 997, "traffic": 927,
                "note": "ncu dram read+write of the three stage launches of a middle step, averaged "
-                       "(708, 885, 1212 B/element; design 784, 944, 1264)"},
+                       "(705, 880, 1196 B/element; design 784, 944, 1264)"},
     # the same bytes; each CTA bulk-copies its next tile's inputs while it computes a tile
     "traces pipelined": {"kernel": "dgx::stage_trace_pipe_kernel<3, no ghost blocks> (mixed SSP-RK3 stage, face "
                                    "traces, next tile copied while a tile is computed)",
