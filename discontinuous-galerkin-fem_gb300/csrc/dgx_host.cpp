@@ -386,13 +386,15 @@ static void rebuild_faces(dgx_mesh* m) {
     }
 }
 // Face-slot pairing on the GPU (dgx_setup.cu) for meshes of at least this many face slots when a
-// device is present; DGX_SETUP_ON_HOST=1 keeps it on the host.  Both give the same table.
+// device is present; DGX_SETUP_ON_HOST=1 keeps it on the host, DGX_SETUP_ON_DEVICE=1 takes every
+// mesh to the device.  Both give the same table.
 static constexpr size_t DEVICE_PAIRING_MIN_SLOTS = 1 << 16;
 
 static bool setup_on_device(size_t work) {
     const char* v = std::getenv("DGX_SETUP_ON_HOST");
     if (v && std::strcmp(v, "1") == 0) return false;
-    if (work < DEVICE_PAIRING_MIN_SLOTS) return false;
+    const char* d = std::getenv("DGX_SETUP_ON_DEVICE");
+    if (work < DEVICE_PAIRING_MIN_SLOTS && !(d && std::strcmp(d, "1") == 0)) return false;
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
         cudaGetLastError();

@@ -67,6 +67,29 @@ def test_device_connectivity_equals_host(dg, monkeypatch, kind):
     assert len(host.get_boundary_face_data()) == 0 == len(dev.get_boundary_face_data())
 
 
+def test_device_pairing_of_odd_meshes_equals_host(dg, monkeypatch):
+    """Small meshes forced to the device pairing (DGX_SETUP_ON_DEVICE=1): an edge shared by three
+    triangles (dgfem pairs the first two faces in element order; the third is a boundary face), a
+    duplicated element, a hanging vertex and an element whose two faces meet the same neighbour."""
+    V = np.array([[0.0, 0.0], [1.0, 0.0], [0.5, 1.0], [0.5, -1.0], [1.5, 0.5], [0.5, 2.0], [2.0, 2.0]])
+    cases = [
+        np.array([[0, 1, 2], [1, 0, 3], [0, 1, 4]]),            # non-manifold edge (0, 1)
+        np.array([[0, 1, 2], [0, 1, 2], [1, 4, 2]]),            # duplicated element
+        np.array([[0, 1, 2], [1, 4, 2], [2, 4, 5], [4, 6, 5]]),  # plain fan with a hanging corner
+        np.array([[0, 1, 2], [2, 1, 0]]),                        # two elements sharing all three edges
+    ]
+    for E in cases:
+        E = np.ascontiguousarray(E, dtype=np.int32)
+        monkeypatch.setenv("DGX_SETUP_ON_HOST", "1")
+        host = dg.DGMesh(V, E, None, {}, {})
+        monkeypatch.delenv("DGX_SETUP_ON_HOST")
+        monkeypatch.setenv("DGX_SETUP_ON_DEVICE", "1")
+        dev = dg.DGMesh(V, E, None, {}, {})
+        monkeypatch.delenv("DGX_SETUP_ON_DEVICE")
+        assert np.array_equal(host.get_interior_faces(), dev.get_interior_faces()), E
+        assert np.array_equal(host.get_boundary_face_data(), dev.get_boundary_face_data()), E
+
+
 @pytest.mark.parametrize("walls", [False, True])
 @pytest.mark.parametrize("kind", ["tri", "quad"])
 def test_device_geometry_equals_host(dg, monkeypatch, kind, walls):
