@@ -370,7 +370,10 @@ __device__ __forceinline__ void stage_tile(const SArgs<P, VISC>& ka, const float
 
         // ---------------- volume (EulerWeakFormulation::volume_residual :72-115,
         //                  NavierStokesWeakFormulation::viscous_volume_residual :100-140)
-#pragma unroll
+        // Navier-Stokes: two points per pass (fully unrolled, the viscous kernel's code outgrows the
+        // instruction cache: 0.89 no-instruction stalls per issue at p=4; unrolled by 2 the step went
+        // 0.490 -> 0.461 ms at 256x256x2, by 1 or 4 0.470 and 0.475)
+#pragma unroll (VISC ? 2 : NQ)
         for (int q = 0; q < NQ; ++q) {
             float U[4] = {0.f, 0.f, 0.f, 0.f};
             float gr[4] = {0.f, 0.f, 0.f, 0.f}, gs[4] = {0.f, 0.f, 0.f, 0.f};
