@@ -544,6 +544,7 @@ def main():
     t_mx = allreduce_max(t_mx, ws)
     grid, tiles, on_tc = cmx.launch_shape()
     form = cmx.stage_form()
+    tile = cmx.stage_tile()
     # the tensor-core (3xTF32 tcgen05) form of the same stage, forced, timed the same way
     os.environ["DGX_STAGE_KERNEL"] = "tc"
     ctc = dg.DGContext(mesh, space, wf, "mixed")
@@ -793,7 +794,7 @@ def main():
                 "accuracy": {k: acc[k] for k in ("steps", "mixed_vs_fp64_l2_rel", "mixed_vs_fp64_linf_rel",
                                                  "mixed_vs_exact_l2_rel", "fp64_vs_exact_l2_rel") if k in acc},
                 "adjoint_forward_ratio": None if adj is None else adj["adjoint_step_vs_forward_step"],
-                "stage_kernel": {"form": form, "grid": grid},
+                "stage_kernel": {"form": form, "grid": grid, "tile": tile},
                 "tensor_core_form": {"ms_per_step": tensor_core["ms_per_step"],
                                      "mixed_vs_fp64_l2_rel": tensor_core["mixed_vs_fp64_l2_rel"]},
                 "e2e": {"value": v_e2e, "unit": "DOF*stages/s", "h2d_bytes_per_step": dof * 8,
@@ -807,6 +808,7 @@ def main():
                 "cpu_baseline": cpu,
                 "details": args.details}
         details = {"line": line, "roofline": roof, "stage_kernel": {"form": form, "grid": grid, "tiles": tiles,
+                                                                    "elements_per_cta": tile,
                                                                     "picked_by": "autotuner (timed on the first step)"},
                    "tensor_core_form": tensor_core, "df64": df64, "accuracy": acc, "navier_stokes": ns,
                    "adjoint": adj, "batched": bat, "config1": cfg1, "quadrilaterals": quads, "setup": setup,

@@ -283,9 +283,10 @@ __device__ __forceinline__ void prefetch_l2_line(const void* p) {
 }
 
 // The stage state uhi + din of the tile starting at element e0 into shared memory, element
-// le's row at row_of(le) * STR.  In a full tile a thread issues all of its 16-byte loads
-// before it uses the first, so the tile costs one memory round trip instead of one per pass.
-template <int NB, int STR, typename RowOf>
+// le's row at row_of(le) * STR, by the T threads of a CTA of T-element tiles.  In a full tile a
+// thread issues all of its 16-byte loads before it uses the first, so the tile costs one memory
+// round trip instead of one per pass.
+template <int NB, int STR, int T = TILE, typename RowOf>
 __device__ __forceinline__ void stage_load_tile(const float* uhi, const float* din, float* sU, int e0, int nloc,
                                                 RowOf row_of) {
     constexpr int NB4 = NB / 4;
@@ -296,14 +297,14 @@ __device__ __forceinline__ void stage_load_tile(const float* uhi, const float* d
         const int le = g / NB4, k = 4 * (g - le * NB4);
         *reinterpret_cast<float4*>(sU + row_of(le) * STR + k) = a;
     };
-    if (nloc == TILE) {
+    if (nloc == T) {
         float4 a[NB4];
         if (dd) {
             float4 b[NB4];
 #pragma unroll
             for (int r = 0; r < NB4; ++r) {
-                a[r] = __ldg(uh + tl + r * TILE);
-                b[r] = __ldg(dd + tl + r * TILE);
+                a[r] = __ldg(uh + tl + r * T);
+                b[r] = __ldg(dd + tl + r * T);
             }
 #pragma unroll
             for (int r = 0; r < NB4; ++r) {
@@ -311,13 +312,13 @@ __device__ __forceinline__ void stage_load_tile(const float* uhi, const float* d
             }
         } else {
 #pragma unroll
-            for (int r = 0; r < NB4; ++r) a[r] = __ldg(uh + tl + r * TILE);
+            for (int r = 0; r < NB4; ++r) a[r] = __ldg(uh + tl + r * T);
         }
 #pragma unroll
-        for (int r = 0; r < NB4; ++r) put(tl + r * TILE, a[r]);
+        for (int r = 0; r < NB4; ++r) put(tl + r * T, a[r]);
         return;
     }
-    for (int g = tl; g < nloc * NB4; g += TILE) {
+    for (int g = tl; g < nloc * NB4; g += T) {
         float4 a = __ldg(uh + g);
         if (dd) {
             const float4 b = __ldg(dd + g);

@@ -143,11 +143,20 @@ __device__ __forceinline__ void prefetch_neighbour_traces(const StageArgs& s, co
     }
 }
 
+// Thread t of a CTA of T-element tiles works on local element tile_elem<T>(t): the even elements
+// (lower triangles of a structured mesh) on threads 0 .. T/2-1, the odd ones on the rest, so the
+// threads of a warp read their face records in one pattern; the element's row in shared memory
+// is tile_row<T>(tile_elem<T>(t)) = t.  For T = TILE these are stage_elem / stage_row.
+template <int T>
+__device__ __forceinline__ int tile_row(int el) { return (el & 1) * (T / 2) + (el >> 1); }
+template <int T>
+__device__ __forceinline__ int tile_elem(int t) { return 2 * (t & (T / 2 - 1)) + t / (T / 2); }
+
 // One tile: `stage(G, C)` puts the stage state's rows into sU and the element's geometry and
 // connectivity into G and C (the boundary variant reads G itself, after staging, short of
 // registers) and ends with a barrier; then the residual, the stage combination and the next
 // traces.
-template <int P, bool BND, bool GHOST, class Stage>
+template <int P, bool BND, bool GHOST, int T, class Stage>
 __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka, float* sU, float* sDt, int tile,
                                                       Stage&& stage) {
     constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1, NB = NP * NV, STR = stage_stride<P>();
@@ -156,10 +165,10 @@ __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka,
     const Ops<P, float>& o = ka.o;
     const LiftOps<P, float>& L = ka.l;
 
-    const int e0 = tile * TILE;
-    const int nloc = min(TILE, s.ne - e0);
+    const int e0 = tile * T;
+    const int nloc = min(T, s.ne - e0);
     const int tl = threadIdx.x;
-    const int el = stage_elem(tl);
+    const int el = tile_elem<T>(tl);
     const bool active = el < nloc;
     const int e = e0 + el;
     ElemGeomF G;
@@ -281,19 +290,19 @@ __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka,
     __syncthreads();
     // stage combination; the next stage state (uhi + dout, or uhi_out after stage 3) replaces
     // each residual slot of sU
-    stage_combine_next<NB, STR, TILE, 2>(s, sU, sDt, e0, nloc, [](int le) { return stage_row(le); });
+    stage_combine_next<NB, STR, T, 2>(s, sU, sDt, e0, nloc, [](int le) { return tile_row<T>(le); });
     __syncthreads();
     if (active) write_traces<P, GHOST>(o, sU + tl * STR, s.tout + (size_t)e * TRF, s, e);
     __syncthreads();  // the next tile reuses sU / sDt
 }
 
-template <int P, bool BND, bool GHOST>
+template <int P, bool BND, bool GHOST, int T>
 __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, float* sU, float* sDt, int tile) {
     constexpr int NB = n_basis(P) * NV, STR = stage_stride<P>();
     const StageArgs& s = ka.s;
-    stage_trace_tile_with<P, BND, GHOST>(ka, sU, sDt, tile, [&](ElemGeomF& G, ElemConn& C) {
-        const int e0 = tile * TILE, nloc = min(TILE, s.ne - e0);
-        const int tl = threadIdx.x, el = stage_elem(tl);
+    stage_trace_tile_with<P, BND, GHOST, T>(ka, sU, sDt, tile, [&](ElemGeomF& G, ElemConn& C) {
+        const int e0 = tile * T, nloc = min(T, s.ne - e0);
+        const int tl = threadIdx.x, el = tile_elem<T>(tl);
         if (tl == 0 && s.stage == 3)  // u^n is read back in the stage combination
             rk3_prefetch(s, (size_t)e0 * NB, nloc * NB);
         // the element's geometry and connectivity ride in the same round trip as the tile's state
@@ -301,7 +310,7 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
             if (!BND) G = s.geom[e0 + el];
             C = s.conn[e0 + el];
         }
-        stage_load_tile<NB, STR>(s.uhi, s.din, sU, e0, nloc, [](int le) { return stage_row(le); });
+        stage_load_tile<NB, STR, T>(s.uhi, s.din, sU, e0, nloc, [](int le) { return tile_row<T>(le); });
         if (el < nloc) prefetch_neighbour_traces<P, BND>(s, C);
         __syncthreads();
     });
@@ -321,14 +330,18 @@ __host__ __device__ constexpr int trace_min_blocks(int p, bool bnd) {
 
 // Persistent form, grid from the autotuner.  BND: some faces are boundary or skipped faces
 // (handled in the face loop); GHOST: boundary faces read ghost blocks, which this kernel writes.
-template <int P, bool BND, bool GHOST>
-__global__ void __launch_bounds__(TILE, trace_min_blocks(P, BND))
+// T: elements per tile and threads per CTA (TILE, or 64 or 32 at one CTA per tile: the same
+// registers per thread and CTAs per SM in proportion, so the SM holds as many elements, in
+// smaller groups whose barriers and load/compute phases are independent).  ka.s.tile0 and
+// ka.s.ntile count T-element tiles.
+template <int P, bool BND, bool GHOST, int T = TILE>
+__global__ void __launch_bounds__(T, trace_min_blocks(P, BND) * (TILE / T))
     stage_trace_kernel(const __grid_constant__ SArgs<P, false> ka) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* sDt = reinterpret_cast<float*>(smem_raw);
-    float* sU = sDt + TILE;
-    const int ntiles = ka.s.ntile > 0 ? ka.s.ntile : (ka.s.ne + TILE - 1) / TILE;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) stage_trace_tile<P, BND, GHOST>(ka, sU, sDt, ka.s.tile0 + t);
+    float* sU = sDt + T;
+    const int ntiles = ka.s.ntile > 0 ? ka.s.ntile : (ka.s.ne + T - 1) / T;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) stage_trace_tile<P, BND, GHOST, T>(ka, sU, sDt, ka.s.tile0 + t);
 }
 
 // Pipelined persistent form (Euler, no boundary branch: periodic meshes or ghost blocks).  Each
@@ -406,7 +419,7 @@ __global__ void __launch_bounds__(TILE, 3) stage_trace_pipe_kernel(const __grid_
         }
         parity ^= 1;
         const int tile = s.tile0 + t;
-        stage_trace_tile_with<P, false, GHOST>(ka, sU, sDt, tile, [&](ElemGeomF& G, ElemConn& C) {
+        stage_trace_tile_with<P, false, GHOST, TILE>(ka, sU, sDt, tile, [&](ElemGeomF& G, ElemConn& C) {
             const int e0 = tile * TILE, nloc = min(TILE, s.ne - e0);
             // the stage state uhi + din into sU (stage_load_tile's sums), the element's records
             for (int g = tl; g < nloc * NB4; g += TILE) {
@@ -453,9 +466,9 @@ __global__ void __launch_bounds__(TILE) trace_init_kernel(const __grid_constant_
                               s, e0 + threadIdx.x);
 }
 
-template <int P>
+template <int P, int T = TILE>
 inline size_t stage_trace_smem_bytes() {
-    return (size_t)(TILE + TILE * stage_stride<P>()) * sizeof(float);
+    return (size_t)(T + T * stage_stride<P>()) * sizeof(float);
 }
 
 template <int P>

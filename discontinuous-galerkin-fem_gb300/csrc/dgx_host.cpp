@@ -1186,13 +1186,22 @@ extern "C" int dgx_create(const dgx_mesh* m, const dgx_params* p, dgx_ctx** out)
 
 extern "C" int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles, int* form) {
     if (!c) return fail(DGX_ERR_INVALID, "null context");
-    if (grid) *grid = c->stage_grid & ~(STAGE_TC | STAGE_TRACE | STAGE_PIPE);
+    if (grid) *grid = c->stage_grid & ~STAGE_FLAGS;
     if (form)
         *form = (c->stage_grid & STAGE_TC)      ? 1
                 : (c->stage_grid & STAGE_PIPE)  ? 3
                 : (c->stage_grid & STAGE_TRACE) ? 2
                                                 : 0;
     if (tiles) *tiles = (c->ne + TILE - 1) / TILE;
+    return DGX_OK;
+}
+
+extern "C" int dgx_stage_tile(const dgx_ctx* c, int* elements) {
+    if (!c || !elements) return fail(DGX_ERR_INVALID, "null argument");
+    *elements = c->stage_grid == 0             ? 0
+                : (c->stage_grid & STAGE_T64) ? 64
+                : (c->stage_grid & STAGE_T32) ? 32
+                                              : TILE;
     return DGX_OK;
 }
 
@@ -1373,10 +1382,11 @@ static int mixed_prologue(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
         const StageArgs a = mixed_stage_args(c, u, dt, 0);
         const bool visc = c->prm.physics == DGX_NAVIER_STOKES;
         // candidates: the neighbour-row form at each grid; for Euler the face-trace form at each
-        // grid, its pipelined persistent kernel at 2 and 3 CTAs per SM (meshes whose faces are all
-        // interior or ghost faces) and the tensor-core form (orders 1-3, the same meshes) at one
-        // CTA per SM.  DGX_STAGE_KERNEL=rows / =trace / =pipe / =tc keeps one form (=trace: both
-        // trace kernels).
+        // grid and at 64- and 32-element tiles, its pipelined persistent kernel at 2 and 3 CTAs per
+        // SM (meshes whose faces are all interior or ghost faces) and the tensor-core form (orders
+        // 1-3, the same meshes) at one CTA per SM.  DGX_STAGE_KERNEL=rows / =trace / =pipe / =tc
+        // keeps one form (=trace: both trace kernels, every tile size), =trace64 / =trace32 one
+        // tile size of the face-trace kernel.
         const int ntiles = (c->ne + TILE - 1) / TILE;
         const char* mode = std::getenv("DGX_STAGE_KERNEL");
         const bool only_tc = mode && std::strcmp(mode, "tc") == 0;
@@ -1392,14 +1402,22 @@ static int mixed_prologue(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
         if (visc || (!only_tc && !only_trace) || (only_tc && !tc_ok) || (only_pipe && !pipe_ok))
             cands = grids;  // the neighbour-row form
         if (!visc && c->d_tr[0] && !only_tc && !only_rows) {
-            if (!only_pipe)
+            if (!only_pipe) {
                 for (int g : grids) cands.push_back(STAGE_TRACE | g);
+                // 64- and 32-element tiles, one CTA per tile
+                cands.push_back(STAGE_TRACE | STAGE_T64 | ntiles);
+                cands.push_back(STAGE_TRACE | STAGE_T32 | ntiles);
+            }
             if (pipe_ok)
                 for (int k = 2; k <= 3; ++k) cands.push_back(STAGE_TRACE | STAGE_PIPE | std::min(ntiles, sms * k));
         }
         if (tc_ok && !only_trace && !only_rows) {
             cands.push_back(STAGE_TC | std::min(ntiles, sms * stage_tc_ctas_per_sm(c->prm.order)));
         }
+        // =trace64 / =trace32: the face-trace kernel at that tile size only
+        const bool only_t64 = mode && std::strcmp(mode, "trace64") == 0;
+        if (!visc && c->d_tr[0] && (only_t64 || (mode && std::strcmp(mode, "trace32") == 0)))
+            cands = {STAGE_TRACE | (only_t64 ? STAGE_T64 : STAGE_T32) | ntiles};
         // the traces the timed launches read (their rounding does not matter for the timing)
         if (c->d_tr[0])
             if (int rc = init_traces(false)) return rc;

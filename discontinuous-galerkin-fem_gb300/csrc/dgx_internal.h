@@ -322,6 +322,12 @@ constexpr int STAGE_TRACE = 1 << 28;
 // With STAGE_TRACE: the pipelined persistent trace kernel (stage_trace_pipe_kernel), which
 // bulk-copies the next tile's inputs while a tile is computed; periodic or ghost-block meshes.
 constexpr int STAGE_PIPE = 1 << 27;
+// With STAGE_TRACE: the face-trace kernel at 64- or 32-element tiles, one CTA per tile (the
+// low bits are then ignored); dgx_kernels_trace_small.cu.
+constexpr int STAGE_T64 = 1 << 26;
+constexpr int STAGE_T32 = 1 << 25;
+constexpr int STAGE_FLAGS = STAGE_TC | STAGE_TRACE | STAGE_PIPE | STAGE_T64 | STAGE_T32;
+int launch_stage_trace_small(int p, int tile, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
 int launch_stage_trace(int p, const StageArgs& a, const OpsHost& ops, int grid, cudaStream_t s);
 int launch_trace_init(int p, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
 int configure_stage_trace(int p);

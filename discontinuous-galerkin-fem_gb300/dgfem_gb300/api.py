@@ -332,6 +332,13 @@ class DGContext:
         check(L.load().dgx_launch_shape(self._h, C.byref(g), C.byref(t), C.byref(k)))
         return g.value, t.value, k.value == 1
 
+    def stage_tile(self) -> int:
+        """Elements per CTA of the mixed stage kernel (128, or 64 / 32 for the face-trace form at
+        smaller tiles); 0 until the first rk3_step."""
+        k = C.c_int()
+        check(L.load().dgx_stage_tile(self._h, C.byref(k)))
+        return k.value
+
     def stage_form(self) -> str:
         """The mixed stage kernel's form: "rows" (neighbour coefficient rows per face),
         "traces" (face traces through HBM), "traces pipelined" (the same, each CTA copying its

@@ -312,6 +312,10 @@ int dgx_eval_points(dgx_ctx* c, int n_points, const double* ref_xy, const double
  * Quadrilateral meshes have one form (grid = tiles).  A mixed-precision state passed to
  * dgx_rk3_step must be 16-byte aligned.  No counterpart in dgfem. */
 int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles, int* form);
+/* Elements per CTA of the mixed stage kernel the autotuner picked: 128, or 64 or 32 for the
+ * face-trace form at smaller tiles (form 2, one CTA per tile; DGX_STAGE_KERNEL=trace64 or
+ * =trace32 keeps one of those); 0 until the first dgx_rk3_step.  No counterpart in dgfem. */
+int dgx_stage_tile(const dgx_ctx* c, int* elements);
 
 /* ---------------------------------------------------------------- batched solves */
 

@@ -1,7 +1,7 @@
 """The CUDA-core forms of the mixed-precision Euler stage, through the C ABI:
 DGX_STAGE_KERNEL=rows (neighbour coefficient rows per face), =trace (face traces through
-HBM) and =pipe (the trace kernel whose CTAs copy their next tile's inputs while computing a
-tile).  They perform the same FP32 operations in the same order, so their states agree bit
+HBM; =trace64 / =trace32 keep its kernel at 64- or 32-element tiles) and =pipe (the trace
+kernel whose CTAs copy their next tile's inputs while computing a tile).  They perform the same FP32 operations in the same order, so their states agree bit
 for bit, p = 1..4, periodic and with far-field / no-slip / slip faces, over step counts that
 exercise the one-step and two-step graphs; both stay within the mixed-precision bar of the
 FP64 oracle.  With a condition on every boundary face the trace form writes ghost blocks and
@@ -55,6 +55,33 @@ def test_trace_form_equals_row_form(dg, monkeypatch, order, walls):
     assert np.array_equal(rows, trace)
     assert np.array_equal(rows, pipe)
     assert rel(trace, ref) <= 1e-6
+    # 162 elements: 6 tiles of 32 and 3 of 64, the last one partial
+    for kernel, tile in (("trace64", 64), ("trace32", 32)):
+        small, form, t = run_tile(dg, monkeypatch, pm, order, u0, dt, kernel)
+        assert form == "traces" and t == tile
+        assert np.array_equal(rows, small)
+
+
+def run_tile(dg, monkeypatch, pm, order, u0, dt, kernel):
+    monkeypatch.setenv("DGX_STAGE_KERNEL", kernel)
+    ctx = dg.DGContext(pm, dg.DGSpace("triangle", order, "dubiner"), dg.EulerWeakFormulation(1.4), "mixed")
+    u = torch.tensor(u0, device="cuda")
+    for n in (3, 2):
+        ctx.rk3_step(u, dt, n)
+    torch.cuda.synchronize()
+    return u.cpu().numpy(), ctx.stage_form(), ctx.stage_tile()
+
+
+@pytest.mark.parametrize("walls", [False, True])
+def test_small_tiles_equal_row_form_many_tiles(dg, monkeypatch, walls):
+    """200 x 200 x 2 elements at 64- and 32-element tiles (1250 and 2500 CTAs): bit for bit the
+    row form's state after steps (3, 2)."""
+    _, pm, u0, dt = case(dg, 200, 3, walls)
+    rows, _ = run(dg, monkeypatch, pm, 3, u0, dt, "rows")
+    for kernel, tile in (("trace64", 64), ("trace32", 32)):
+        small, form, t = run_tile(dg, monkeypatch, pm, 3, u0, dt, kernel)
+        assert form == "traces" and t == tile
+        assert np.array_equal(rows, small)
 
 
 @pytest.mark.parametrize("walls", [False, True])
@@ -127,11 +154,17 @@ def test_autotuner_reports_a_form(dg, monkeypatch):
     u, form = run(dg, monkeypatch, pm, 3, u0, dt, None, steps=(1,))
     assert form in ("rows", "traces", "traces pipelined", "tensor cores")
     assert rel(u, om.rk3_step(O.euler(1.4), u0, dt, 1)) <= 1e-6
+    monkeypatch.delenv("DGX_STAGE_KERNEL", raising=False)
+    ctx = dg.DGContext(pm, dg.DGSpace("triangle", 3, "dubiner"), dg.EulerWeakFormulation(1.4), "mixed")
+    assert ctx.stage_tile() == 0
+    ctx.rk3_step(torch.tensor(u0, device="cuda"), dt, 1)
+    assert ctx.stage_tile() in (128, 64, 32)
+    assert ctx.stage_tile() == 128 or ctx.stage_form() == "traces"
 
 
 @pytest.mark.parametrize("walls", [False, True, "skip"])
 @pytest.mark.parametrize("kernel,n", [("rows", 1), ("trace", 1), ("trace", 3), ("pipe", 1), ("pipe", 3),
-                                      ("tc", 1), ("tc", 3)])
+                                      ("trace64", 1), ("trace32", 3), ("tc", 1), ("tc", 3)])
 def test_host_pointer_step_equals_device_step(dg, monkeypatch, kernel, n, walls):
     """dgx_rk3_step_host runs its last step's stage 3 in tile ranges, each copied back to the
     host while the next range computes; the state equals the device-pointer step's bit for bit."""
