@@ -152,13 +152,44 @@ __device__ __forceinline__ int tile_row(int el) { return (el & 1) * (T / 2) + (e
 template <int T>
 __device__ __forceinline__ int tile_elem(int t) { return 2 * (t & (T / 2 - 1)) + t / (T / 2); }
 
+// Shared-memory row stride (floats) of an element's three neighbour trace blocks: 16-byte
+// aligned, stride/4 odd (eight threads' 16-byte reads of their rows hit disjoint banks).
+template <int P>
+__host__ __device__ constexpr int nbr_trace_stride() {
+    return ((trace_floats<P>() / 4) & 1) ? trace_floats<P>() : trace_floats<P>() + 4;
+}
+
+// 16-byte asynchronous copy global -> shared memory, cached in L1 on the way (cp.async.ca),
+// and the wait for all of this thread's copies
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// the neighbours' trace blocks of element e (every face interior or a ghost face) into the
+// thread's row dst of shared memory, slot f holding the block the face loop reads for face f;
+// the copies land while the volume terms are formed
+template <int P>
+__device__ __forceinline__ void copy_neighbour_traces(const StageArgs& s, const ElemConn& C, float* dst) {
+    constexpr int NFQ = P + 1, TRF = trace_floats<P>();
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+        const float* src = s.tin + (size_t)C.nbr[f] * TRF + ((C.flags >> (4 * f)) & 3) * NFQ * NV;
+#pragma unroll
+        for (int k = 0; k < NFQ; ++k) cp_async16(dst + (f * NFQ + k) * NV, src + k * NV);
+    }
+}
+
 // One tile: `stage(G, C)` puts the stage state's rows into sU and the element's geometry and
 // connectivity into G and C (the boundary variant reads G itself, after staging, short of
 // registers) and ends with a barrier; then the residual, the stage combination and the next
-// traces.
-template <int P, bool BND, bool GHOST, int T, class Stage>
+// traces.  NBS: the neighbours' trace blocks were copied into the thread's row of sN by
+// cp.async during staging (no boundary branch), and the face loop reads them there.
+template <int P, bool BND, bool GHOST, int T, bool NBS = false, class Stage>
 __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka, float* sU, float* sDt, int tile,
-                                                      Stage&& stage) {
+                                                      Stage&& stage, const float* sN = nullptr) {
+    static_assert(!(NBS && BND), "neighbour traces in shared memory need every face interior or a ghost face");
     constexpr int NP = n_basis(P), NQ = n_quad(P), NFQ = P + 1, NB = NP * NV, STR = stage_stride<P>();
     constexpr int TRF = trace_floats<P>();
     const StageArgs& s = ka.s;
@@ -215,6 +246,7 @@ __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka,
 
         // ---------------- faces (interior_face_residual :117-175, boundary_face_residual :177-250)
         const float inv_j = __frcp_rn(G.detJ);
+        if (NBS) cp_async_wait_all();  // this thread's copies of its neighbours' blocks
         // one face body, walked three times (the unrolled form measured 2.7 % slower: its
         // larger code missed the instruction cache and its registers spilled)
 #pragma unroll 1
@@ -243,7 +275,10 @@ __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka,
             }
             BCSlot bc;
             bc.type = -1;
-            if (!BND || nb >= 0) {
+            // NBS: the neighbour's block in shared memory, read point by point in the loop below
+            const float* nts = sN + tl * nbr_trace_stride<P>() + f * NFQ * NV;
+            if (NBS) {
+            } else if (!BND || nb >= 0) {
                 const float* nt = s.tin + (size_t)nb * TRF + nf * NFQ * NV;
 #pragma unroll
                 for (int k = 0; k < NFQ; ++k) {
@@ -264,7 +299,13 @@ __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka,
 #pragma unroll
             for (int j = 0; j < NFQ; ++j) {
                 float H[4];
-                if (!BND || nb >= 0) {
+                if (NBS) {
+                    float un[4];
+                    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                                 : "=f"(un[0]), "=f"(un[1]), "=f"(un[2]), "=f"(un[3])
+                                 : "r"((unsigned)__cvta_generic_to_shared(nts + (rev ? NFQ - 1 - j : j) * NV)));
+                    rusanov<float>(Uo[j], un, nx, ny, gamma, H);
+                } else if (!BND || nb >= 0) {
                     rusanov<float>(Uo[j], Un[j], nx, ny, gamma, H);
                 } else {
                     float Ub[4];
@@ -296,11 +337,12 @@ __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka,
     __syncthreads();  // the next tile reuses sU / sDt
 }
 
-template <int P, bool BND, bool GHOST, int T>
-__device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, float* sU, float* sDt, int tile) {
+template <int P, bool BND, bool GHOST, int T, bool NBS>
+__device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, float* sU, float* sDt, float* sN,
+                                                 int tile) {
     constexpr int NB = n_basis(P) * NV, STR = stage_stride<P>();
     const StageArgs& s = ka.s;
-    stage_trace_tile_with<P, BND, GHOST, T>(ka, sU, sDt, tile, [&](ElemGeomF& G, ElemConn& C) {
+    stage_trace_tile_with<P, BND, GHOST, T, NBS>(ka, sU, sDt, tile, [&](ElemGeomF& G, ElemConn& C) {
         const int e0 = tile * T, nloc = min(T, s.ne - e0);
         const int tl = threadIdx.x, el = tile_elem<T>(tl);
         if (tl == 0 && s.stage == 3)  // u^n is read back in the stage combination
@@ -311,9 +353,12 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
             C = s.conn[e0 + el];
         }
         stage_load_tile<NB, STR, T>(s.uhi, s.din, sU, e0, nloc, [](int le) { return tile_row<T>(le); });
-        if (el < nloc) prefetch_neighbour_traces<P, BND>(s, C);
+        if (el < nloc) {
+            if (NBS) copy_neighbour_traces<P>(s, C, sN + tl * nbr_trace_stride<P>());
+            else prefetch_neighbour_traces<P, BND>(s, C);
+        }
         __syncthreads();
-    });
+    }, sN);
 }
 
 // CTAs per SM the register allocation must allow.  Measured on GB300 for p=3 (512x512x2):
@@ -333,15 +378,18 @@ __host__ __device__ constexpr int trace_min_blocks(int p, bool bnd) {
 // T: elements per tile and threads per CTA (TILE, or 64 or 32 at one CTA per tile: the same
 // registers per thread and CTAs per SM in proportion, so the SM holds as many elements, in
 // smaller groups whose barriers and load/compute phases are independent).  ka.s.tile0 and
-// ka.s.ntile count T-element tiles.
-template <int P, bool BND, bool GHOST, int T = TILE>
+// ka.s.ntile count T-element tiles.  NBS: neighbour trace blocks through shared memory (sN,
+// after sU; every face interior or a ghost face).
+template <int P, bool BND, bool GHOST, int T = TILE, bool NBS = false>
 __global__ void __launch_bounds__(T, trace_min_blocks(P, BND) * (TILE / T))
     stage_trace_kernel(const __grid_constant__ SArgs<P, false> ka) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* sDt = reinterpret_cast<float*>(smem_raw);
     float* sU = sDt + T;
+    float* sN = sU + T * stage_stride<P>();  // 16-byte aligned: T % 4 == 0, stride % 4 == 0
     const int ntiles = ka.s.ntile > 0 ? ka.s.ntile : (ka.s.ne + T - 1) / T;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) stage_trace_tile<P, BND, GHOST, T>(ka, sU, sDt, ka.s.tile0 + t);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
+        stage_trace_tile<P, BND, GHOST, T, NBS>(ka, sU, sDt, sN, ka.s.tile0 + t);
 }
 
 // Pipelined persistent form (Euler, no boundary branch: periodic meshes or ghost blocks).  Each
@@ -466,9 +514,9 @@ __global__ void __launch_bounds__(TILE) trace_init_kernel(const __grid_constant_
                               s, e0 + threadIdx.x);
 }
 
-template <int P, int T = TILE>
+template <int P, int T = TILE, bool NBS = false>
 inline size_t stage_trace_smem_bytes() {
-    return (size_t)(T + T * stage_stride<P>()) * sizeof(float);
+    return (size_t)(T + T * stage_stride<P>() + (NBS ? T * nbr_trace_stride<P>() : 0)) * sizeof(float);
 }
 
 template <int P>

@@ -1385,8 +1385,8 @@ static int mixed_prologue(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
         // grid and at 64- and 32-element tiles, its pipelined persistent kernel at 2 and 3 CTAs per
         // SM (meshes whose faces are all interior or ghost faces) and the tensor-core form (orders
         // 1-3, the same meshes) at one CTA per SM.  DGX_STAGE_KERNEL=rows / =trace / =pipe / =tc
-        // keeps one form (=trace: both trace kernels, every tile size), =trace64 / =trace32 one
-        // tile size of the face-trace kernel.
+        // keeps one form (=trace: both trace kernels, every tile size), =trace64 / =trace32 /
+        // =trace32s one tile size of the face-trace kernel.
         const int ntiles = (c->ne + TILE - 1) / TILE;
         const char* mode = std::getenv("DGX_STAGE_KERNEL");
         const bool only_tc = mode && std::strcmp(mode, "tc") == 0;
@@ -1407,6 +1407,7 @@ static int mixed_prologue(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
                 // 64- and 32-element tiles, one CTA per tile
                 cands.push_back(STAGE_TRACE | STAGE_T64 | ntiles);
                 cands.push_back(STAGE_TRACE | STAGE_T32 | ntiles);
+                if (pipe_ok) cands.push_back(STAGE_TRACE | STAGE_T32 | STAGE_NBS | ntiles);
             }
             if (pipe_ok)
                 for (int k = 2; k <= 3; ++k) cands.push_back(STAGE_TRACE | STAGE_PIPE | std::min(ntiles, sms * k));
@@ -1414,10 +1415,13 @@ static int mixed_prologue(dgx_ctx* c, double* u, double dt, cudaStream_t s) {
         if (tc_ok && !only_trace && !only_rows) {
             cands.push_back(STAGE_TC | std::min(ntiles, sms * stage_tc_ctas_per_sm(c->prm.order)));
         }
-        // =trace64 / =trace32: the face-trace kernel at that tile size only
+        // =trace64 / =trace32: the face-trace kernel at that tile size only; =trace32s: at 32-element
+        // tiles with the neighbours' trace blocks through shared memory where every face is an
+        // interior or ghost face (else as =trace32)
         const bool only_t64 = mode && std::strcmp(mode, "trace64") == 0;
-        if (!visc && c->d_tr[0] && (only_t64 || (mode && std::strcmp(mode, "trace32") == 0)))
-            cands = {STAGE_TRACE | (only_t64 ? STAGE_T64 : STAGE_T32) | ntiles};
+        const bool only_t32s = mode && std::strcmp(mode, "trace32s") == 0;
+        if (!visc && c->d_tr[0] && (only_t64 || only_t32s || (mode && std::strcmp(mode, "trace32") == 0)))
+            cands = {STAGE_TRACE | (only_t64 ? STAGE_T64 : STAGE_T32) | (only_t32s && pipe_ok ? STAGE_NBS : 0) | ntiles};
         // the traces the timed launches read (their rounding does not matter for the timing)
         if (c->d_tr[0])
             if (int rc = init_traces(false)) return rc;

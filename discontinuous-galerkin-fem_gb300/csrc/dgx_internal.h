@@ -326,8 +326,11 @@ constexpr int STAGE_PIPE = 1 << 27;
 // low bits are then ignored); dgx_kernels_trace_small.cu.
 constexpr int STAGE_T64 = 1 << 26;
 constexpr int STAGE_T32 = 1 << 25;
-constexpr int STAGE_FLAGS = STAGE_TC | STAGE_TRACE | STAGE_PIPE | STAGE_T64 | STAGE_T32;
-int launch_stage_trace_small(int p, int tile, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
+// With STAGE_T32: each thread copies its element's neighbour trace blocks into shared memory
+// by cp.async during staging (meshes whose faces are all interior or ghost faces).
+constexpr int STAGE_NBS = 1 << 24;
+constexpr int STAGE_FLAGS = STAGE_TC | STAGE_TRACE | STAGE_PIPE | STAGE_T64 | STAGE_T32 | STAGE_NBS;
+int launch_stage_trace_small(int p, int tile, bool nbs, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
 int launch_stage_trace(int p, const StageArgs& a, const OpsHost& ops, int grid, cudaStream_t s);
 int launch_trace_init(int p, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
 int configure_stage_trace(int p);

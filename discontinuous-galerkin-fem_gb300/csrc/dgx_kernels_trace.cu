@@ -13,7 +13,8 @@ namespace dgx {
     }
 
 int launch_stage_trace(int p, const StageArgs& a, const OpsHost& ops, int grid, cudaStream_t s) {
-    if (grid & (STAGE_T64 | STAGE_T32)) return launch_stage_trace_small(p, (grid & STAGE_T64) ? 64 : 32, a, ops, s);
+    if (grid & (STAGE_T64 | STAGE_T32))
+        return launch_stage_trace_small(p, (grid & STAGE_T64) ? 64 : 32, (grid & STAGE_NBS) != 0, a, ops, s);
     DGX_TRACE_P(launch_stage_trace_t, (a, ops, grid, s))
 }
 

@@ -1,6 +1,7 @@
 """The CUDA-core forms of the mixed-precision Euler stage, through the C ABI:
 DGX_STAGE_KERNEL=rows (neighbour coefficient rows per face), =trace (face traces through
-HBM; =trace64 / =trace32 keep its kernel at 64- or 32-element tiles) and =pipe (the trace
+HBM; =trace64 / =trace32 keep its kernel at 64- or 32-element tiles, =trace32s at 32-element
+tiles with each element's neighbour trace blocks copied into shared memory) and =pipe (the trace
 kernel whose CTAs copy their next tile's inputs while computing a tile).  They perform the same FP32 operations in the same order, so their states agree bit
 for bit, p = 1..4, periodic and with far-field / no-slip / slip faces, over step counts that
 exercise the one-step and two-step graphs; both stay within the mixed-precision bar of the
@@ -56,7 +57,7 @@ def test_trace_form_equals_row_form(dg, monkeypatch, order, walls):
     assert np.array_equal(rows, pipe)
     assert rel(trace, ref) <= 1e-6
     # 162 elements: 6 tiles of 32 and 3 of 64, the last one partial
-    for kernel, tile in (("trace64", 64), ("trace32", 32)):
+    for kernel, tile in (("trace64", 64), ("trace32", 32), ("trace32s", 32)):
         small, form, t = run_tile(dg, monkeypatch, pm, order, u0, dt, kernel)
         assert form == "traces" and t == tile
         assert np.array_equal(rows, small)
@@ -74,11 +75,12 @@ def run_tile(dg, monkeypatch, pm, order, u0, dt, kernel):
 
 @pytest.mark.parametrize("walls", [False, True])
 def test_small_tiles_equal_row_form_many_tiles(dg, monkeypatch, walls):
-    """200 x 200 x 2 elements at 64- and 32-element tiles (1250 and 2500 CTAs): bit for bit the
-    row form's state after steps (3, 2)."""
+    """200 x 200 x 2 elements at 64- and 32-element tiles (1250 and 2500 CTAs), the latter also
+    with the neighbour blocks through shared memory: bit for bit the row form's state after
+    steps (3, 2)."""
     _, pm, u0, dt = case(dg, 200, 3, walls)
     rows, _ = run(dg, monkeypatch, pm, 3, u0, dt, "rows")
-    for kernel, tile in (("trace64", 64), ("trace32", 32)):
+    for kernel, tile in (("trace64", 64), ("trace32", 32), ("trace32s", 32)):
         small, form, t = run_tile(dg, monkeypatch, pm, 3, u0, dt, kernel)
         assert form == "traces" and t == tile
         assert np.array_equal(rows, small)
@@ -147,6 +149,10 @@ def test_trace_form_equals_row_form_channel(dg, monkeypatch, order):
     assert np.array_equal(rows, trace)
     assert np.array_equal(rows, pipe)
     assert rel(trace, ref) <= 1e-6
+    small, form, tile = run_tile(dg, monkeypatch, pm, order, u0, dt, "trace32s")
+    assert form == "traces" and tile == 32
+    # run_tile makes steps (3, 2) like run
+    assert np.array_equal(rows, small)
 
 
 def test_autotuner_reports_a_form(dg, monkeypatch):
@@ -164,7 +170,8 @@ def test_autotuner_reports_a_form(dg, monkeypatch):
 
 @pytest.mark.parametrize("walls", [False, True, "skip"])
 @pytest.mark.parametrize("kernel,n", [("rows", 1), ("trace", 1), ("trace", 3), ("pipe", 1), ("pipe", 3),
-                                      ("trace64", 1), ("trace32", 3), ("tc", 1), ("tc", 3)])
+                                      ("trace64", 1), ("trace32", 3), ("trace32s", 1), ("trace32s", 3),
+                                      ("tc", 1), ("tc", 3)])
 def test_host_pointer_step_equals_device_step(dg, monkeypatch, kernel, n, walls):
     """dgx_rk3_step_host runs its last step's stage 3 in tile ranges, each copied back to the
     host while the next range computes; the state equals the device-pointer step's bit for bit."""
