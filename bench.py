@@ -63,6 +63,19 @@ STAGE_FORMS = {
                "design": 997, "traffic": 927,
                "note": "ncu dram read+write of the three stage launches of a middle step, averaged "
                        "(705, 880, 1196 B/element; design 784, 944, 1264)"},
+    # the same bytes at 64- and 32-element tiles, one CTA per tile
+    "traces, 64-element tiles": {"kernel": "dgx::stage_trace_kernel<3, no boundary, 64-element tiles>",
+                                 "design": 997, "traffic": None, "note": "not captured with DRAM counters"},
+    "traces, 32-element tiles": {"kernel": "dgx::stage_trace_kernel<3, no boundary, 32-element tiles>",
+                                 "design": 997, "traffic": 928,
+                                 "note": "ncu dram read+write of the three stage launches of a middle step, "
+                                         "averaged (704, 880, 1200 B/element; design 784, 944, 1264)"},
+    # each thread copies its neighbours' trace blocks into shared memory (cp.async) while staging
+    "traces, 32-element tiles, neighbour blocks in shared memory": {
+        "kernel": "dgx::stage_trace_kernel<3, no boundary, 32-element tiles, neighbour blocks in shared memory>",
+        "design": 997, "traffic": 919,
+        "note": "ncu dram read+write of the three stage launches of a middle step, averaged "
+                "(696, 873, 1189 B/element; design 784, 944, 1264)"},
     # the same bytes; each CTA bulk-copies its next tile's inputs while it computes a tile
     "traces pipelined": {"kernel": "dgx::stage_trace_pipe_kernel<3, no ghost blocks> (mixed SSP-RK3 stage, face "
                                    "traces, next tile copied while a tile is computed)",
@@ -545,6 +558,8 @@ def main():
     grid, tiles, on_tc = cmx.launch_shape()
     form = cmx.stage_form()
     tile = cmx.stage_tile()
+    if form == "traces" and tile != 128:
+        form += f", {tile}-element tiles" + (", neighbour blocks in shared memory" if cmx.stage_nbr_shared() else "")
     # the tensor-core (3xTF32 tcgen05) form of the same stage, forced, timed the same way
     os.environ["DGX_STAGE_KERNEL"] = "tc"
     ctc = dg.DGContext(mesh, space, wf, "mixed")

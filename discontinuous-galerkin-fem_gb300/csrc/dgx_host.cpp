@@ -1196,12 +1196,13 @@ extern "C" int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles, int* fo
     return DGX_OK;
 }
 
-extern "C" int dgx_stage_tile(const dgx_ctx* c, int* elements) {
+extern "C" int dgx_stage_tile(const dgx_ctx* c, int* elements, int* nbr_shared) {
     if (!c || !elements) return fail(DGX_ERR_INVALID, "null argument");
     *elements = c->stage_grid == 0             ? 0
                 : (c->stage_grid & STAGE_T64) ? 64
                 : (c->stage_grid & STAGE_T32) ? 32
                                               : TILE;
+    if (nbr_shared) *nbr_shared = (c->stage_grid & STAGE_NBS) ? 1 : 0;
     return DGX_OK;
 }
 

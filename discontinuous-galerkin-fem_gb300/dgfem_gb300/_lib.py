@@ -74,7 +74,7 @@ SIGNATURES = {
     "dgx_kinetic_energy_gradient_binomial": (C.c_int, [_vp, _vp, C.c_double, C.c_int, C.c_int, _dp, _vp,
                                                        C.POINTER(C.c_longlong), _vp]),
     "dgx_launch_shape": (C.c_int, [_vp, _ip, _ip, _ip]),
-    "dgx_stage_tile": (C.c_int, [_vp, _ip]),
+    "dgx_stage_tile": (C.c_int, [_vp, _ip, _ip]),
     "dgx_eval_points": (C.c_int, [_vp, C.c_int, _dp, _vp, _vp, _vp]),
     "dgx_step_status": (C.c_int, [_vp, _ip, _vp]),
     "dgx_batch_create": (C.c_int, [C.c_int, C.POINTER(_vp), _vp, C.POINTER(_vp)]),

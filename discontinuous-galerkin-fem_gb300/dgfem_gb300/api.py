@@ -336,8 +336,15 @@ class DGContext:
         """Elements per CTA of the mixed stage kernel (128, or 64 / 32 for the face-trace form at
         smaller tiles); 0 until the first rk3_step."""
         k = C.c_int()
-        check(L.load().dgx_stage_tile(self._h, C.byref(k)))
+        check(L.load().dgx_stage_tile(self._h, C.byref(k), None))
         return k.value
+
+    def stage_nbr_shared(self) -> bool:
+        """True when the mixed stage kernel copies each element's neighbour trace blocks into
+        shared memory during staging (the face-trace form at 32-element tiles)."""
+        k, n = C.c_int(), C.c_int()
+        check(L.load().dgx_stage_tile(self._h, C.byref(k), C.byref(n)))
+        return n.value == 1
 
     def stage_form(self) -> str:
         """The mixed stage kernel's form: "rows" (neighbour coefficient rows per face),

@@ -314,8 +314,11 @@ int dgx_eval_points(dgx_ctx* c, int n_points, const double* ref_xy, const double
 int dgx_launch_shape(const dgx_ctx* c, int* grid, int* tiles, int* form);
 /* Elements per CTA of the mixed stage kernel the autotuner picked: 128, or 64 or 32 for the
  * face-trace form at smaller tiles (form 2, one CTA per tile; DGX_STAGE_KERNEL=trace64 or
- * =trace32 keeps one of those); 0 until the first dgx_rk3_step.  No counterpart in dgfem. */
-int dgx_stage_tile(const dgx_ctx* c, int* elements);
+ * =trace32 keeps one of those); 0 until the first dgx_rk3_step.  nbr_shared (may be NULL) is
+ * 1 when that kernel copies each element's neighbour trace blocks into shared memory during
+ * staging (32-element tiles, meshes whose faces are all interior or ghost faces;
+ * DGX_STAGE_KERNEL=trace32s), else 0.  No counterpart in dgfem. */
+int dgx_stage_tile(const dgx_ctx* c, int* elements, int* nbr_shared);
 
 /* ---------------------------------------------------------------- batched solves */
 

@@ -58,8 +58,10 @@ def test_trace_form_equals_row_form(dg, monkeypatch, order, walls):
     assert rel(trace, ref) <= 1e-6
     # 162 elements: 6 tiles of 32 and 3 of 64, the last one partial
     for kernel, tile in (("trace64", 64), ("trace32", 32), ("trace32s", 32)):
-        small, form, t = run_tile(dg, monkeypatch, pm, order, u0, dt, kernel)
+        small, form, t, shared = run_tile(dg, monkeypatch, pm, order, u0, dt, kernel)
         assert form == "traces" and t == tile
+        # the shared-memory copies need every face to be an interior or a ghost face
+        assert shared == (kernel == "trace32s" and walls != "skip")
         assert np.array_equal(rows, small)
 
 
@@ -70,7 +72,7 @@ def run_tile(dg, monkeypatch, pm, order, u0, dt, kernel):
     for n in (3, 2):
         ctx.rk3_step(u, dt, n)
     torch.cuda.synchronize()
-    return u.cpu().numpy(), ctx.stage_form(), ctx.stage_tile()
+    return u.cpu().numpy(), ctx.stage_form(), ctx.stage_tile(), ctx.stage_nbr_shared()
 
 
 @pytest.mark.parametrize("walls", [False, True])
@@ -81,8 +83,8 @@ def test_small_tiles_equal_row_form_many_tiles(dg, monkeypatch, walls):
     _, pm, u0, dt = case(dg, 200, 3, walls)
     rows, _ = run(dg, monkeypatch, pm, 3, u0, dt, "rows")
     for kernel, tile in (("trace64", 64), ("trace32", 32), ("trace32s", 32)):
-        small, form, t = run_tile(dg, monkeypatch, pm, 3, u0, dt, kernel)
-        assert form == "traces" and t == tile
+        small, form, t, shared = run_tile(dg, monkeypatch, pm, 3, u0, dt, kernel)
+        assert form == "traces" and t == tile and shared == (kernel == "trace32s")
         assert np.array_equal(rows, small)
 
 
@@ -149,8 +151,8 @@ def test_trace_form_equals_row_form_channel(dg, monkeypatch, order):
     assert np.array_equal(rows, trace)
     assert np.array_equal(rows, pipe)
     assert rel(trace, ref) <= 1e-6
-    small, form, tile = run_tile(dg, monkeypatch, pm, order, u0, dt, "trace32s")
-    assert form == "traces" and tile == 32
+    small, form, tile, shared = run_tile(dg, monkeypatch, pm, order, u0, dt, "trace32s")
+    assert form == "traces" and tile == 32 and shared
     # run_tile makes steps (3, 2) like run
     assert np.array_equal(rows, small)
 
