@@ -19,7 +19,8 @@ OBJ = HERE / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["dgx_host.cpp", "dgx_kernels_fp64.cu", "dgx_kernels_mixed.cu", "dgx_misc.cu", "dgx_static.cu", "dgx_adjoint.cu",
            "dgx_batch.cu", "dgx_batch_host.cpp", "dgx_tune.cpp", "dgx_kernels_tc.cu",
-           "dgx_kernels_df64.cu", "dgx_quad.cu", "dgx_kernels_trace.cu", "dgx_kernels_trace_small.cu", "dgx_setup.cu"]
+           "dgx_kernels_df64.cu", "dgx_quad.cu", "dgx_kernels_trace.cu", "dgx_kernels_trace_small.cu", "dgx_kernels_trace_nbs.cu",
+           "dgx_setup.cu"]
 HEADERS = ["dgx_internal.h", "dgx_context.h", "dg_physics.cuh", "dg_element.cuh", "dg_stage.cuh", "dg_adjoint.cuh", "dg_stage_tc.cuh", "tc_ptx.cuh", "df64.cuh", "dg_quad.cuh", "dg_stage_trace.cuh", "fp_bits.cuh", "quad_tables.inc"]
 
 

@@ -20,24 +20,35 @@
 // branch).  Meshes with faces that take no part keep the boundary branch (BND kernels).
 #pragma once
 
+#include <type_traits>
+
 #include "dg_stage.cuh"
 #include "tc_ptx.cuh"
 
 namespace dgx {
+
+// Which stages a trace-kernel instantiation serves: any (the stage and, for stage 3, the state's
+// case read from StageArgs), stages 1 and 2 only, or stage 3 of a step between the first and
+// the last of a call (double-float state in and out).  The specialised kernels leave out the
+// code of the other stages, which the instruction cache then does not have to hold.
+enum StageKind { SK_ANY = 0, SK_12 = 1, SK_3DF = 2 };
 
 template <int P>
 __host__ __device__ constexpr int trace_floats() { return 3 * (P + 1) * NV; }
 
 // stage_combine (dg_stage.cuh), which in addition replaces each residual slot of sR with the
 // next stage state: uhi + dout after stages 1 and 2 (what the next stage stages as uhi + din),
-// the FP32 copy of u^{n+1} after stage 3.
-template <int NB, int STR, int THREADS, int CH, typename RowOf>
+// the FP32 copy of u^{n+1} after stage 3.  SK: the stages served (StageKind).
+template <int NB, int STR, int THREADS, int CH, int SK = SK_ANY, typename RowOf>
 __device__ __forceinline__ void stage_combine_next(const StageArgs& s, float* sR, const float* sDt, int e0, int nloc,
                                                    RowOf rowof) {
+    using M = typename std::conditional<SK == SK_3DF, Rk3Mode<false, false>, Rk3Runtime>::type;
     constexpr int NB4 = NB / 4;
     const int n4 = nloc * NB4;
     const size_t b4 = (size_t)e0 * NB4;
     const int t = threadIdx.x;
+    const bool st12 = SK == SK_12 || (SK == SK_ANY && s.stage <= 2);
+    const bool with_din = SK == SK_3DF || s.stage >= 2;
     bool bad = false;
     for (int g0 = t; g0 < n4; g0 += CH * THREADS) {
         float4 dv[CH], uh[CH], lo[CH];
@@ -46,9 +57,9 @@ __device__ __forceinline__ void stage_combine_next(const StageArgs& s, float* sR
         for (int k = 0; k < CH; ++k) {
             const int g = g0 + k * THREADS;
             if (g < n4) {
-                if (s.stage >= 2) dv[k] = __ldg(reinterpret_cast<const float4*>(s.din) + b4 + g);
-                if (s.stage <= 2) uh[k] = __ldg(reinterpret_cast<const float4*>(s.uhi) + b4 + g);
-                else rk3_load4(s, b4 + g, un[k], uh[k], lo[k]);
+                if (with_din) dv[k] = __ldg(reinterpret_cast<const float4*>(s.din) + b4 + g);
+                if (st12) uh[k] = __ldg(reinterpret_cast<const float4*>(s.uhi) + b4 + g);
+                else rk3_load4<M>(s, b4 + g, un[k], uh[k], lo[k]);
             }
         }
 #pragma unroll
@@ -60,7 +71,7 @@ __device__ __forceinline__ void stage_combine_next(const StageArgs& s, float* sR
             float4* slot = reinterpret_cast<float4*>(sR + row * STR + c);
             const float4 du = *slot;
             const float dt = s.dt_inst ? sDt[row] : s.dt;
-            if (s.stage <= 2) {
+            if (st12) {
                 const float4 o = s.stage == 1
                                      ? make_float4(dt * du.x, dt * du.y, dt * du.z, dt * du.w)
                                      : make_float4(0.25f * (dv[k].x + dt * du.x), 0.25f * (dv[k].y + dt * du.y),
@@ -72,7 +83,7 @@ __device__ __forceinline__ void stage_combine_next(const StageArgs& s, float* sR
             } else {
                 const float d[4] = {(2.0f / 3.0f) * (dv[k].x + dt * du.x), (2.0f / 3.0f) * (dv[k].y + dt * du.y),
                                     (2.0f / 3.0f) * (dv[k].z + dt * du.z), (2.0f / 3.0f) * (dv[k].w + dt * du.w)};
-                *slot = rk3_next4(s, b4 + g, un[k], uh[k], lo[k], d, bad);
+                *slot = rk3_next4<M>(s, b4 + g, un[k], uh[k], lo[k], d, bad);
             }
         }
     }
@@ -186,7 +197,7 @@ __device__ __forceinline__ void copy_neighbour_traces(const StageArgs& s, const 
 // registers) and ends with a barrier; then the residual, the stage combination and the next
 // traces.  NBS: the neighbours' trace blocks were copied into the thread's row of sN by
 // cp.async during staging (no boundary branch), and the face loop reads them there.
-template <int P, bool BND, bool GHOST, int T, bool NBS = false, class Stage>
+template <int P, bool BND, bool GHOST, int T, bool NBS = false, int SK = SK_ANY, class Stage>
 __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka, float* sU, float* sDt, int tile,
                                                       Stage&& stage, const float* sN = nullptr) {
     static_assert(!(NBS && BND), "neighbour traces in shared memory need every face interior or a ghost face");
@@ -331,21 +342,22 @@ __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka,
     __syncthreads();
     // stage combination; the next stage state (uhi + dout, or uhi_out after stage 3) replaces
     // each residual slot of sU
-    stage_combine_next<NB, STR, T, 2>(s, sU, sDt, e0, nloc, [](int le) { return tile_row<T>(le); });
+    stage_combine_next<NB, STR, T, 2, SK>(s, sU, sDt, e0, nloc, [](int le) { return tile_row<T>(le); });
     __syncthreads();
     if (active) write_traces<P, GHOST>(o, sU + tl * STR, s.tout + (size_t)e * TRF, s, e);
     __syncthreads();  // the next tile reuses sU / sDt
 }
 
-template <int P, bool BND, bool GHOST, int T, bool NBS>
+template <int P, bool BND, bool GHOST, int T, bool NBS, int SK>
 __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, float* sU, float* sDt, float* sN,
                                                  int tile) {
     constexpr int NB = n_basis(P) * NV, STR = stage_stride<P>();
     const StageArgs& s = ka.s;
-    stage_trace_tile_with<P, BND, GHOST, T, NBS>(ka, sU, sDt, tile, [&](ElemGeomF& G, ElemConn& C) {
+    stage_trace_tile_with<P, BND, GHOST, T, NBS, SK>(ka, sU, sDt, tile, [&](ElemGeomF& G, ElemConn& C) {
         const int e0 = tile * T, nloc = min(T, s.ne - e0);
         const int tl = threadIdx.x, el = tile_elem<T>(tl);
-        if (tl == 0 && s.stage == 3)  // u^n is read back in the stage combination
+        // u^n is read back in the stage combination
+        if (tl == 0 && (SK == SK_3DF || (SK == SK_ANY && s.stage == 3)))
             rk3_prefetch(s, (size_t)e0 * NB, nloc * NB);
         // the element's geometry and connectivity ride in the same round trip as the tile's state
         if (el < nloc) {
@@ -379,8 +391,8 @@ __host__ __device__ constexpr int trace_min_blocks(int p, bool bnd) {
 // registers per thread and CTAs per SM in proportion, so the SM holds as many elements, in
 // smaller groups whose barriers and load/compute phases are independent).  ka.s.tile0 and
 // ka.s.ntile count T-element tiles.  NBS: neighbour trace blocks through shared memory (sN,
-// after sU; every face interior or a ghost face).
-template <int P, bool BND, bool GHOST, int T = TILE, bool NBS = false>
+// after sU; every face interior or a ghost face).  SK: the stages served (StageKind).
+template <int P, bool BND, bool GHOST, int T = TILE, bool NBS = false, int SK = SK_ANY>
 __global__ void __launch_bounds__(T, trace_min_blocks(P, BND) * (TILE / T))
     stage_trace_kernel(const __grid_constant__ SArgs<P, false> ka) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -389,7 +401,7 @@ __global__ void __launch_bounds__(T, trace_min_blocks(P, BND) * (TILE / T))
     float* sN = sU + T * stage_stride<P>();  // 16-byte aligned: T % 4 == 0, stride % 4 == 0
     const int ntiles = ka.s.ntile > 0 ? ka.s.ntile : (ka.s.ne + T - 1) / T;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
-        stage_trace_tile<P, BND, GHOST, T, NBS>(ka, sU, sDt, sN, ka.s.tile0 + t);
+        stage_trace_tile<P, BND, GHOST, T, NBS, SK>(ka, sU, sDt, sN, ka.s.tile0 + t);
 }
 
 // Pipelined persistent form (Euler, no boundary branch: periodic meshes or ghost blocks).  Each

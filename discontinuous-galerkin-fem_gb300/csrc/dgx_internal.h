@@ -331,6 +331,7 @@ constexpr int STAGE_T32 = 1 << 25;
 constexpr int STAGE_NBS = 1 << 24;
 constexpr int STAGE_FLAGS = STAGE_TC | STAGE_TRACE | STAGE_PIPE | STAGE_T64 | STAGE_T32 | STAGE_NBS;
 int launch_stage_trace_small(int p, int tile, bool nbs, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
+int launch_stage_trace_nbs(int p, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
 int launch_stage_trace(int p, const StageArgs& a, const OpsHost& ops, int grid, cudaStream_t s);
 int launch_trace_init(int p, const StageArgs& a, const OpsHost& ops, cudaStream_t s);
 int configure_stage_trace(int p);

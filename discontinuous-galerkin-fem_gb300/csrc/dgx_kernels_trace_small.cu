@@ -1,14 +1,14 @@
 // Face-trace form of the mixed Euler stage at 64- and 32-element tiles (dg_stage_trace.cuh,
 // stage_trace_kernel<P, BND, GHOST, T>), in a translation unit of its own so that it compiles
 // beside the 128-element kernels.  One CTA per tile; the host's tile range (StageArgs::tile0,
-// ntile, counted in 128-element tiles) is converted to T-element tiles here.  NBS (32-element
-// tiles, meshes whose faces are all interior or ghost faces): the neighbours' trace blocks go
-// through shared memory.
+// ntile, counted in 128-element tiles) is converted to T-element tiles here.  The 32-element
+// kernels that copy the neighbours' trace blocks into shared memory are in
+// dgx_kernels_trace_nbs.cu.
 #include "dg_stage_trace.cuh"
 
 namespace dgx {
 
-template <int P, int T, bool NBS = false>
+template <int P, int T>
 static int launch_small_t(const StageArgs& a, const OpsHost& oh, cudaStream_t st) {
     static_assert(TILE % T == 0, "tiles of T elements split the 128-element tiles");
     constexpr int K = TILE / T;
@@ -23,15 +23,7 @@ static int launch_small_t(const StageArgs& a, const OpsHost& oh, cudaStream_t st
     if (nt <= 0) return 0;
     ka.s.tile0 = t0;
     ka.s.ntile = nt;
-    const size_t smem = stage_trace_smem_bytes<P, T, NBS>();
-    if (NBS) {
-        if (a.boundary && !a.tconn) return -1;  // faces without a condition: no neighbour block to copy
-        if (a.tconn)
-            stage_trace_kernel<P, false, true, T, NBS><<<nt, T, smem, st>>>(ka);
-        else
-            stage_trace_kernel<P, false, false, T, NBS><<<nt, T, smem, st>>>(ka);
-        return launch_status();
-    }
+    const size_t smem = stage_trace_smem_bytes<P, T>();
     if (a.tconn)
         stage_trace_kernel<P, false, true, T><<<nt, T, smem, st>>>(ka);
     else if (a.boundary)
@@ -44,16 +36,7 @@ static int launch_small_t(const StageArgs& a, const OpsHost& oh, cudaStream_t st
 int launch_stage_trace_small(int p, int tile, bool nbs, const StageArgs& a, const OpsHost& ops, cudaStream_t s) {
     const bool t64 = tile == 64;
     if (!t64 && tile != 32) return -1;
-    if (nbs) {
-        if (t64) return -1;
-        switch (p) {
-        case 1: return launch_small_t<1, 32, true>(a, ops, s);
-        case 2: return launch_small_t<2, 32, true>(a, ops, s);
-        case 3: return launch_small_t<3, 32, true>(a, ops, s);
-        case 4: return launch_small_t<4, 32, true>(a, ops, s);
-        default: return -1;
-        }
-    }
+    if (nbs) return t64 ? -1 : launch_stage_trace_nbs(p, a, ops, s);
     switch (p) {
     case 1: return t64 ? launch_small_t<1, 64>(a, ops, s) : launch_small_t<1, 32>(a, ops, s);
     case 2: return t64 ? launch_small_t<2, 64>(a, ops, s) : launch_small_t<2, 32>(a, ops, s);
