@@ -282,8 +282,9 @@ int dgx_kinetic_energy_gradient_binomial(dgx_ctx* c, const double* u0, double dt
  *    race on it.  Nothing in it needs to start at zero.
  *  - Mixed precision runs the stage kernel that reads neighbour coefficient rows, at one CTA
  *    per 128-element tile, not the form the autotuner picks for dgx_rk3_step (the face-trace
- *    form needs trace buffers): the results are the same bit for bit, the steps about 15 %
- *    slower at 524,288 elements.
+ *    form needs trace buffers): the results are the same bit for bit.  That kernel's stage
+ *    took 187 us against 132 us for the autotuner's pick on a 524,288-element mesh (stage 2,
+ *    p = 3, through dgx_rk3_step).
  *  - The context's device must be current.  Kernels are launched directly on `stream`. */
 #define DGX_STATIC_MAX_STATE (1 << 20)
 int dgx_rk3_step_static(dgx_ctx* c, double* u, double dt, int n_steps, void* stream);
