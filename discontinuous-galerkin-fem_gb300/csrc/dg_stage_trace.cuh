@@ -97,46 +97,80 @@ __device__ __forceinline__ void stage_combine_next(const StageArgs& s, float* sR
 // ghost state of each trace point (boundary_face_residual's, from the same trace value and
 // the same operations as the boundary path of the face loop), so the next stage treats the
 // face as an interior one.  GHOST = false leaves the ghost code out.
-template <int P, bool GHOST>
+// ROLL: one face per pass (the 32-element-tile kernels, whose warps each run their own phase and
+// so share less code in the instruction cache: unrolled over the faces they measured 2.4 %
+// slower); otherwise all faces' points in one pass over the coefficients.  Each point sums
+// i = 0 .. Np-1 in order either way.
+template <int P, bool GHOST, bool ROLL = false>
 __device__ __forceinline__ void write_traces(const Ops<P, float>& o, const float* c, float* tr, const StageArgs& s,
                                              int e) {
     constexpr int NP = n_basis(P), NFQ = P + 1;
-    float U[3][NFQ][4];
+    // the ghost state of each trace point of boundary face f (boundary_face_residual's, from the
+    // same trace value and the same operations as the boundary path of the face loop)
+    auto ghost = [&](int f, int nb, const float (&U)[NFQ][4]) {
+        const BCSlot bc = s.bc[s.ghost_bc[nb - s.ne]];
+        const float nx = s.geom[e].n[f][0], ny = s.geom[e].n[f][1];
+        float* g = s.tout + (size_t)nb * trace_floats<P>();
 #pragma unroll
-    for (int f = 0; f < 3; ++f)
+        for (int j = 0; j < NFQ; ++j) {
+            float Ub[4];
+            inviscid_ghost<float>(bc, U[j], nx, ny, s.gamma, Ub);
+            *reinterpret_cast<float4*>(g + j * NV) = make_float4(Ub[0], Ub[1], Ub[2], Ub[3]);
+        }
+    };
+    if constexpr (ROLL) {
+        ElemConn C;
+        if (GHOST && s.ghost_bc) C = s.conn[e];
+#pragma unroll 1
+        for (int f = 0; f < 3; ++f) {
+            float U[NFQ][4];
 #pragma unroll
-        for (int j = 0; j < NFQ; ++j)
+            for (int j = 0; j < NFQ; ++j)
 #pragma unroll
-            for (int v = 0; v < NV; ++v) U[f][j][v] = 0.0f;
+                for (int v = 0; v < NV; ++v) U[j][v] = 0.0f;
 #pragma unroll
-    for (int i = 0; i < NP; ++i) {
-        const float4 c4 = *reinterpret_cast<const float4*>(c + i * NV);
-        const float cc[4] = {c4.x, c4.y, c4.z, c4.w};
+            for (int i = 0; i < NP; ++i) {
+                const float4 c4 = *reinterpret_cast<const float4*>(c + i * NV);
+                const float cc[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+                for (int j = 0; j < NFQ; ++j) fma4(o.phif[f][j][i], cc, U[j]);
+            }
+#pragma unroll
+            for (int j = 0; j < NFQ; ++j)
+                *reinterpret_cast<float4*>(tr + (f * NFQ + j) * NV) = make_float4(U[j][0], U[j][1], U[j][2], U[j][3]);
+            if (GHOST && s.ghost_bc) {
+                const int nb = pick3(f, C.nbr[0], C.nbr[1], C.nbr[2]);
+                if (nb >= s.ne) ghost(f, nb, U);
+            }
+        }
+    } else {
+        float U[3][NFQ][4];
 #pragma unroll
         for (int f = 0; f < 3; ++f)
 #pragma unroll
-            for (int j = 0; j < NFQ; ++j) fma4(o.phif[f][j][i], cc, U[f][j]);
-    }
+            for (int j = 0; j < NFQ; ++j)
 #pragma unroll
-    for (int f = 0; f < 3; ++f)
+                for (int v = 0; v < NV; ++v) U[f][j][v] = 0.0f;
 #pragma unroll
-        for (int j = 0; j < NFQ; ++j)
-            *reinterpret_cast<float4*>(tr + (f * NFQ + j) * NV) = make_float4(U[f][j][0], U[f][j][1], U[f][j][2],
-                                                                              U[f][j][3]);
-    if (GHOST && s.ghost_bc) {
-        const ElemConn C = s.conn[e];
+        for (int i = 0; i < NP; ++i) {
+            const float4 c4 = *reinterpret_cast<const float4*>(c + i * NV);
+            const float cc[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
-        for (int f = 0; f < 3; ++f) {
-            if (C.nbr[f] < s.ne) continue;
-            const BCSlot bc = s.bc[s.ghost_bc[C.nbr[f] - s.ne]];
-            const float nx = s.geom[e].n[f][0], ny = s.geom[e].n[f][1];
-            float* g = s.tout + (size_t)C.nbr[f] * trace_floats<P>();
+            for (int f = 0; f < 3; ++f)
 #pragma unroll
-            for (int j = 0; j < NFQ; ++j) {
-                float Ub[4];
-                inviscid_ghost<float>(bc, U[f][j], nx, ny, s.gamma, Ub);
-                *reinterpret_cast<float4*>(g + j * NV) = make_float4(Ub[0], Ub[1], Ub[2], Ub[3]);
-            }
+                for (int j = 0; j < NFQ; ++j) fma4(o.phif[f][j][i], cc, U[f][j]);
+        }
+#pragma unroll
+        for (int f = 0; f < 3; ++f)
+#pragma unroll
+            for (int j = 0; j < NFQ; ++j)
+                *reinterpret_cast<float4*>(tr + (f * NFQ + j) * NV) = make_float4(U[f][j][0], U[f][j][1], U[f][j][2],
+                                                                                  U[f][j][3]);
+        if (GHOST && s.ghost_bc) {
+            const ElemConn C = s.conn[e];
+#pragma unroll
+            for (int f = 0; f < 3; ++f)
+                if (C.nbr[f] >= s.ne) ghost(f, C.nbr[f], U[f]);
         }
     }
 }
@@ -231,8 +265,7 @@ __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka,
         if (s.dt_inst) sDt[tl] = s.dt_inst[__float_as_int(G.pad)];
 
         // ---------------- volume (EulerWeakFormulation::volume_residual :72-115)
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) {
+        auto volume_point = [&](int q) {
             float U[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
             for (int i = 0; i < NP; ++i) {
@@ -253,6 +286,17 @@ __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka,
                 fma4(L.pr[q][i], Fr, R[i]);
                 fma4(L.ps[q][i], Fs, R[i]);
             }
+        };
+        if constexpr (T <= 32) {
+            // three points per pass (fully unrolled, the code outgrew the instruction cache:
+            // 0.406 -> 0.374 ms/step at 512x512x2 p=3 unrolled by 3, 0.373 by 2, 0.384 by 6)
+#pragma unroll 3
+            for (int q = 0; q < NQ; ++q) volume_point(q);
+        } else {
+            // fully unrolled (128-element tiles, whose four warps run one phase together, measured
+            // 3.6 % slower rolled by 3)
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) volume_point(q);
         }
 
         // ---------------- faces (interior_face_residual :117-175, boundary_face_residual :177-250)
@@ -344,7 +388,7 @@ __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka,
     // each residual slot of sU
     stage_combine_next<NB, STR, T, 2, SK>(s, sU, sDt, e0, nloc, [](int le) { return tile_row<T>(le); });
     __syncthreads();
-    if (active) write_traces<P, GHOST>(o, sU + tl * STR, s.tout + (size_t)e * TRF, s, e);
+    if (active) write_traces<P, GHOST, (T <= 32)>(o, sU + tl * STR, s.tout + (size_t)e * TRF, s, e);
     __syncthreads();  // the next tile reuses sU / sDt
 }
 
