@@ -7,8 +7,12 @@
 // the instances of each order are concatenated into one element range (geometry in FP32
 // with the instance number in the spare slot, connectivity and boundary slots offset into
 // the range), every RK3 stage of every instance is one launch of the batched stage kernel
-// (dgx_batch.cu), and a step is a CUDA graph of three such launches.
+// (dgx_batch.cu), and a step is a CUDA graph of three such launches.  Periodic Euler batches
+// may instead run each stage as one launch per order of the single context's face-trace kernel
+// (32-element tiles, neighbour blocks in shared memory, dg_stage_trace.cuh), on each order's
+// concatenated range with its own trace buffers; the autotuner keeps whichever is faster.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -29,6 +33,7 @@ struct Group {  // the instances of one order, concatenated
     float* ulo = nullptr;                 // low parts of the double-float state
     float* d1 = nullptr;                  // FP32 stage increments
     float* d2 = nullptr;
+    float* tr[2] = {nullptr, nullptr};    // face traces (periodic Euler batches), ping-ponged
 };
 }  // namespace
 
@@ -42,7 +47,8 @@ struct dgx_batch {
     float* d_dt = nullptr;                           // per-instance time step (FP32, as the stage arithmetic)
     std::vector<float> dt_uploaded;
     int boundary = 0;
-    int grid = 0;  // stage-kernel grid picked by the autotuner (0: not yet)
+    int grid = 0;  // stage-kernel grid picked by the autotuner (0: not yet); with STAGE_TRACE the face-trace form
+    bool trace_ok = false;  // periodic Euler: every group has trace buffers
     cudaStream_t cap = nullptr;
     cudaGraphExec_t graph[N_STEP_GRAPHS] = {};  // the StepGraph replays (dgx_internal.h)
 };
@@ -62,6 +68,8 @@ static void free_batch(dgx_batch* b) {
         cudaFree(g.ulo);
         cudaFree(g.d1);
         cudaFree(g.d2);
+        cudaFree(g.tr[0]);
+        cudaFree(g.tr[1]);
     }
     cudaFree(b->d_dt);
     if (b->cap) cudaStreamDestroy(b->cap);
@@ -177,6 +185,18 @@ extern "C" int dgx_batch_create(int n_inst, const dgx_mesh* const* meshes, const
             return set_error(DGX_ERR_CUDA, "cudaMalloc / upload failed for the batched state");
         }
     }
+    // face-trace form for periodic Euler batches: two trace buffers per order
+    b->trace_ok = !visc && !b->boundary;
+    for (int p = 0; p < MAX_P && b->trace_ok; ++p) {
+        Group& g = b->grp[p];
+        if (g.ne == 0) continue;
+        const size_t bytes = (size_t)g.ne * trace_floats_per_element(p + 1) * sizeof(float);
+        if (cudaMalloc((void**)&g.tr[0], bytes) != cudaSuccess || cudaMalloc((void**)&g.tr[1], bytes) != cudaSuccess) {
+            cudaGetLastError();
+            free_batch(b);
+            return set_error(DGX_ERR_CUDA, "cudaMalloc failed for the batched face traces");
+        }
+    }
     if (cudaMalloc((void**)&b->d_dt, n_inst * sizeof(float)) != cudaSuccess ||
         cudaMemset(b->d_dt, 0, n_inst * sizeof(float)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) != cudaSuccess) {
@@ -203,7 +223,7 @@ extern "C" int dgx_batch_launch_shape(const dgx_batch* b, int* grid, int* tiles)
     if (!b) return set_error(DGX_ERR_INVALID, "null batch");
     int t = 0;
     for (const Group& g : b->grp) t += (g.ne + TILE - 1) / TILE;
-    if (grid) *grid = b->grid;
+    if (grid) *grid = b->grid & ~STAGE_FLAGS;
     if (tiles) *tiles = t;
     return DGX_OK;
 }
@@ -240,11 +260,43 @@ static void batch_stage_args(const dgx_batch* b, int src, int stage, StepKind ki
     }
 }
 
+// The face-trace form of one stage: one launch per order.  A step starting from uhi[src] reads
+// the traces in tr[src], tr[1-src], tr[src] and writes tr[1-src], tr[src], tr[1-src] (the single
+// context's order), so the next step starts from uhi[1-src] with its traces in tr[1-src].
+static int launch_batch_trace_stage(const dgx_batch* b, StageArgs* a, int src, int grid, cudaStream_t s) {
+    for (int p = 0; p < MAX_P; ++p) {
+        const Group& g = b->grp[p];
+        if (!g.ne) continue;
+        const int stage = a[p].stage;
+        a[p].tin = g.tr[stage == 2 ? 1 - src : src];
+        a[p].tout = g.tr[stage == 2 ? src : 1 - src];
+        a[p].grid = grid;
+        if (launch_stage_trace(p + 1, a[p], b->ops[p], grid & ~STAGE_TRACE, s)) return -1;
+    }
+    return 0;
+}
+
+// the traces of the start state uhi[0] of every order into tr[0]
+static int launch_batch_trace_init(const dgx_batch* b, cudaStream_t s) {
+    StageArgs a[MAX_P];
+    batch_stage_args(b, 0, 1, STEP_ONLY, a);
+    for (int p = 0; p < MAX_P; ++p) {
+        const Group& g = b->grp[p];
+        if (!g.ne) continue;
+        a[p].tout = g.tr[0];
+        if (launch_trace_init(p + 1, a[p], b->ops[p], s)) return -1;
+    }
+    return 0;
+}
+
 static int enqueue_batch_step(dgx_batch* b, int src, StepKind kind, cudaStream_t s) {
     for (int stage = 1; stage <= 3; ++stage) {
         StageArgs a[MAX_P];
         batch_stage_args(b, src, stage, kind, a);
-        if (launch_batch_stage(a, b->ops, b->boundary, b->prm.physics == DGX_NAVIER_STOKES, b->grid, s))
+        const int rc = (b->grid & STAGE_TRACE)
+                           ? launch_batch_trace_stage(b, a, src, b->grid, s)
+                           : launch_batch_stage(a, b->ops, b->boundary, b->prm.physics == DGX_NAVIER_STOKES, b->grid, s);
+        if (rc)
             return set_error(DGX_ERR_CUDA, std::string("batched stage launch failed: ") +
                                                launch_error_text());
     }
@@ -289,18 +341,38 @@ extern "C" int dgx_batch_rk3_step(dgx_batch* b, const double* dt, int n_steps, v
     for (const Group& g : b->grp)
         if (g.ne && launch_f64_to_f32(g.nstate, g.u, g.uhi[0], s))
             return set_error(DGX_ERR_CUDA, "conversion launch failed");
+    // the face-trace form's traces of the start state (its timed launches below read them too)
+    if (b->trace_ok && (b->grid == 0 || (b->grid & STAGE_TRACE)) && launch_batch_trace_init(b, s))
+        return set_error(DGX_ERR_CUDA, std::string("batched trace launch failed: ") + launch_error_text());
     if (b->grid == 0) {
-        // launch shape: timed on stage 1, which writes only the increment scratch
+        // launch shape: timed on stage 1, which writes only the increment scratch (and, in the
+        // face-trace form, the traces in tr[1]); candidates: the batched kernel at each grid and,
+        // for periodic Euler batches, the face-trace form (DGX_STAGE_KERNEL=rows keeps the first)
         std::string key = "batch";
         for (int p = 0; p < MAX_P; ++p) key += " p" + std::to_string(p + 1) + ":" + std::to_string(b->grp[p].ne);
         if (b->boundary) key += " bnd";
         const bool visc = b->prm.physics == DGX_NAVIER_STOKES;
         if (visc) key += " ns";
+        const char* mode = std::getenv("DGX_STAGE_KERNEL");
+        const bool rows_only = mode && std::strcmp(mode, "rows") == 0;
+        const bool trace_only = mode && std::strcmp(mode, "trace32s") == 0;
         StageArgs a[MAX_P];
         batch_stage_args(b, 0, 1, STEP_ONLY, a);
         const OpsHost* ops = b->ops;
+        std::vector<int> cands;
+        if (!(trace_only && b->trace_ok)) cands = grid_candidates(batch_tiles(a));
+        if (b->trace_ok && !rows_only) {
+            cands.push_back(STAGE_TRACE | STAGE_T32 | STAGE_NBS | batch_tiles(a));
+            key += " trace";
+        }
+        if (mode) key += std::string(" ") + mode;
         int grid = 0;
-        const int rc = tune_grid(key, grid_candidates(batch_tiles(a)), [&](int g, cudaStream_t ts) {
+        const int rc = tune_grid(key, cands, [&](int g, cudaStream_t ts) {
+            if (g & STAGE_TRACE) {
+                StageArgs t[MAX_P];
+                std::memcpy(t, a, sizeof(t));
+                return launch_batch_trace_stage(b, t, 0, g, ts);
+            }
             return launch_batch_stage(a, ops, b->boundary, visc, g, ts);
         }, s, &grid);
         if (rc) return rc;

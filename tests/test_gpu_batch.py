@@ -86,6 +86,23 @@ def single(dg, om, pm, u0, dt, order, steps=(3, 2), wf=None):
     return u.cpu().numpy()
 
 
+def test_batch_face_trace_form_equals_batched_kernel(dg, monkeypatch):
+    """A periodic Euler batch run by the single context's face-trace kernel (one launch per order
+    and stage, DGX_STAGE_KERNEL=trace32s) equals the batched row-form kernel (=rows) bit for bit
+    after steps (3, 2): one call's first, middle and last steps, and a call of two.  Uneven sizes
+    and orders 1..4, so each order's range ends in a partial 32-element tile."""
+    insts, orders = build(dg, SPECS)
+    monkeypatch.setenv("DGX_STAGE_KERNEL", "rows")
+    _, rows = run_batch(dg, insts, orders)
+    monkeypatch.setenv("DGX_STAGE_KERNEL", "trace32s")
+    batch, trace = run_batch(dg, insts, orders)
+    grid, tiles = batch.launch_shape()
+    assert grid == tiles
+    for k in range(len(insts)):
+        assert np.isfinite(trace[k]).all() and np.abs(trace[k] - insts[k][2]).max() > 0
+        assert np.array_equal(rows[k], trace[k]), k
+
+
 @pytest.mark.parametrize("walls", [(), (1, 4, 6)])
 def test_batch_matches_single_solves_and_oracle(dg, monkeypatch, walls):
     # the single solves run a CUDA-core form, which the batched kernel equals bit for bit (the
