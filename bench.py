@@ -369,6 +369,8 @@ def batch_leg(dg, torch, n_inst, steps, seed):
     l2 = [float(torch.linalg.vector_norm(outs[i] - refs[i]) / torch.linalg.vector_norm(refs[i])) for i in range(n_inst)]
     linf = [float((outs[i] - refs[i]).abs().max() / refs[i].abs().max()) for i in range(n_inst)]
     grid, tiles = batch.launch_shape()
+    form = batch.stage_form()
+    n_orders = len(set(ps.tolist()))
 
     ctxs = [dg.DGContext(meshes[i], spaces[i], wf, "mixed") for i in range(n_inst)]
     us = [u0s[i].clone() for i in range(n_inst)]
@@ -392,8 +394,11 @@ def batch_leg(dg, torch, n_inst, steps, seed):
             "value": total / t_batch, "unit": "DOF*stages/s", "s": t_batch,
             "single_solve_loop": {"value": total / t_loop, "s": t_loop},
             "batched_vs_loop": t_loop / t_batch,
-            "launch_shape": {"grid": grid, "tiles": tiles},
-            "gpu_launches": 3 * steps + len(set(ps.tolist())),
+            "launch_shape": {"grid": grid, "tiles": tiles}, "stage_form": form,
+            # per call: one FP32 conversion per order (and, for the face-trace form, the traces of
+            # the start state per order); per stage: one launch, or one per order
+            "gpu_launches": (3 * steps * n_orders + 2 * n_orders if form == "traces per order"
+                             else 3 * steps + n_orders),
             "batched_vs_loop_max_rel_diff": same,
             "per_instance_vs_fp64": {"l2_rel_max": max(l2), "l2_rel_median": float(np.median(l2)),
                                      "linf_rel_max": max(linf)},

@@ -228,6 +228,12 @@ extern "C" int dgx_batch_launch_shape(const dgx_batch* b, int* grid, int* tiles)
     return DGX_OK;
 }
 
+extern "C" int dgx_batch_stage_form(const dgx_batch* b, int* form) {
+    if (!b || !form) return set_error(DGX_ERR_INVALID, "null argument");
+    *form = b->grid == 0 ? 0 : (b->grid & STAGE_TRACE) ? 2 : 1;
+    return DGX_OK;
+}
+
 // Stage arguments of every order for one step reading uhi[src], in place `kind` of its call.
 static void batch_stage_args(const dgx_batch* b, int src, int stage, StepKind kind, StageArgs* a) {
     for (int p = 0; p < MAX_P; ++p) {

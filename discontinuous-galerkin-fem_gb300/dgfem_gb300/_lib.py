@@ -82,6 +82,7 @@ SIGNATURES = {
     "dgx_batch_info": (C.c_int, [_vp, C.c_int, _ip, _ip, C.POINTER(_vp)]),
     "dgx_batch_rk3_step": (C.c_int, [_vp, _dp, C.c_int, _vp]),
     "dgx_batch_launch_shape": (C.c_int, [_vp, _ip, _ip]),
+    "dgx_batch_stage_form": (C.c_int, [_vp, _ip]),
 }
 STATIC_MAX_STATE = 1 << 20  # DGX_STATIC_MAX_STATE
 

@@ -529,6 +529,14 @@ class DGBatch:
         check(L.load().dgx_batch_launch_shape(self._h, C.byref(g), C.byref(t)))
         return g.value, t.value
 
+    def stage_form(self) -> str:
+        """The batch's stage form: "batched rows" (one launch per stage over every order's tiles)
+        or "traces per order" (the face-trace kernel, one launch per order); "" until the first
+        rk3_step."""
+        k = C.c_int()
+        check(L.load().dgx_batch_stage_form(self._h, C.byref(k)))
+        return {0: "", 1: "batched rows", 2: "traces per order"}[k.value]
+
 
 class DGAssembler:
     """DGAssembler(mesh, weak_form) with assemble_euler_residual (assembler.hpp:58-59)."""

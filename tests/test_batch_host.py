@@ -91,6 +91,7 @@ def test_batch_create_rejects_empty_and_null(dg):
     assert lib.dgx_batch_create(1, None, None, C.byref(out)) == L.ERR_INVALID
     assert lib.dgx_batch_info(None, 0, None, None, None) == L.ERR_INVALID
     assert lib.dgx_batch_launch_shape(None, None, None) == L.ERR_INVALID
+    assert lib.dgx_batch_stage_form(None, None) == L.ERR_INVALID
     assert lib.dgx_launch_shape(None, None, None, None) == L.ERR_INVALID
     assert lib.dgx_stage_tile(None, None, None) == L.ERR_INVALID
     assert lib.dgx_batch_rk3_step(None, None, 1, None) == L.ERR_INVALID

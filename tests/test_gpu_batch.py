@@ -93,9 +93,11 @@ def test_batch_face_trace_form_equals_batched_kernel(dg, monkeypatch):
     and orders 1..4, so each order's range ends in a partial 32-element tile."""
     insts, orders = build(dg, SPECS)
     monkeypatch.setenv("DGX_STAGE_KERNEL", "rows")
-    _, rows = run_batch(dg, insts, orders)
+    brows, rows = run_batch(dg, insts, orders)
+    assert brows.stage_form() == "batched rows"
     monkeypatch.setenv("DGX_STAGE_KERNEL", "trace32s")
     batch, trace = run_batch(dg, insts, orders)
+    assert batch.stage_form() == "traces per order"
     grid, tiles = batch.launch_shape()
     assert grid == tiles
     for k in range(len(insts)):
