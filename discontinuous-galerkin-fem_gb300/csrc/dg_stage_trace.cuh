@@ -105,8 +105,7 @@ template <int P, bool GHOST, bool ROLL = false>
 __device__ __forceinline__ void write_traces(const Ops<P, float>& o, const float* c, float* tr, const StageArgs& s,
                                              int e) {
     constexpr int NP = n_basis(P), NFQ = P + 1;
-    // the ghost state of each trace point of boundary face f (boundary_face_residual's, from the
-    // same trace value and the same operations as the boundary path of the face loop)
+    // ghost block nb of boundary face f from the face's trace values U
     auto ghost = [&](int f, int nb, const float (&U)[NFQ][4]) {
         const BCSlot bc = s.bc[s.ghost_bc[nb - s.ne]];
         const float nx = s.geom[e].n[f][0], ny = s.geom[e].n[f][1];
@@ -332,8 +331,7 @@ __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka,
             bc.type = -1;
             // NBS: the neighbour's block in shared memory, read point by point in the loop below
             const float* nts = sN + tl * nbr_trace_stride<P>() + f * NFQ * NV;
-            if (NBS) {
-            } else if (!BND || nb >= 0) {
+            if (!NBS && (!BND || nb >= 0)) {
                 const float* nt = s.tin + (size_t)nb * TRF + nf * NFQ * NV;
 #pragma unroll
                 for (int k = 0; k < NFQ; ++k) {
@@ -348,7 +346,7 @@ __device__ __forceinline__ void stage_trace_tile_with(const SArgs<P, false>& ka,
                         Un[j][v] = rev ? b : a;
                         Un[NFQ - 1 - j][v] = rev ? a : b;
                     }
-            } else {
+            } else if (BND && nb < 0) {
                 bc = s.bc[-1 - nb];
             }
 #pragma unroll
