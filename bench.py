@@ -45,6 +45,35 @@ REF_BUDGET_S = 90.0  # timed CPU work of the reference arm
 # per element per RK stage, p=3, FP64 state: 3*Np*V*8 + 92 bytes of geometry/connectivity
 ALGO_BYTES_PER_ELEM_STAGE = 1052
 MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
+# FMA rates of this machine's GB300, measured by a probe of independent FMA chains (1216 x 256 threads):
+# the denominators of the flop rooflines of the FP64 path (FP64 pipe) and of the Navier-Stokes leg
+MEASURED_FP64_TFLOPS, MEASURED_FP32_TFLOPS = 1.19, 72.6
+
+
+def flops_per_element_stage(p, viscous):
+    """Algorithmic flops of one element's RK stage (triangles, V = 4):
+    Euler: 2 Nq Np V (interpolation) + 30 Nq (flux) + 4 Nq Np V (x and y projection)
+           + 1.5 Nfq (8 Np V + 100) (traces, Rusanov and lift on both sides of 1.5 faces)
+           + 2 Np^2 V (M^-1) + 3 Np V (RK);
+    Navier-Stokes adds 4 Nq Np V (gradient interpolation) + 60 Nq (viscous flux) + 4 Nq Np V (its
+           projection) + 1.5 (8 Nfq Np V) (two-sided gradient interpolation at the face points)
+           + 1.5 Nfq 20 (penalty).
+    p=3 Euler: 6680; p=4 Navier-Stokes: 24960."""
+    nq = {1: 3, 2: 6, 3: 12, 4: 16}[p]
+    np_, nfq, v = (p + 1) * (p + 2) // 2, p + 1, 4
+    f = 2 * nq * np_ * v + 30 * nq + 4 * nq * np_ * v + 1.5 * nfq * (8 * np_ * v + 100) + 2 * np_ * np_ * v + 3 * np_ * v
+    if viscous:
+        f += 4 * nq * np_ * v + 60 * nq + 4 * nq * np_ * v + 1.5 * 8 * nfq * np_ * v + 1.5 * nfq * 20
+    return int(f)
+
+
+def flop_roofline(p, viscous, elements, ms_per_step, peak_tflops, pipe):
+    if not ms_per_step:
+        return None
+    fl = flops_per_element_stage(p, viscous)
+    achieved = fl * elements * 3 / (ms_per_step * 1e-3) / 1e12
+    return {"bound": pipe, "flops_per_element_stage": fl, "achieved_tflops": achieved, "peak_tflops": peak_tflops,
+            "frac": achieved / peak_tflops, "peak_kind": "measured (FMA-chain probe)"}
 FALLBACK_HBM_GBS = 6800.0
 # The two CUDA-core forms of the mixed stage (the autotuner picks one), p=3:
 #  design: bytes per element the form needs, averaged over the three stages;
@@ -691,6 +720,11 @@ def main():
                        "ms_per_step": 1e3 * tn_64 / kn_64 if kn_64 else None, "steps_timed": kn_64},
               "mixed_vs_fp64": (tn_64 / kn_64) / (tn_mx / kn_mx) if kn_mx and kn_64 else None,
               "mixed_vs_fp64_l2_rel_at_step_100": acc100,
+              "flop_roofline": {
+                  "mixed": flop_roofline(4, True, n64.n_elements, 1e3 * tn_mx / kn_mx if kn_mx else None,
+                                         MEASURED_FP32_TFLOPS, "fp32"),
+                  "fp64": flop_roofline(4, True, n64.n_elements, 1e3 * tn_64 / kn_64 if kn_64 else None,
+                                        MEASURED_FP64_TFLOPS, "fp64")},
               "first_nonfinite_step": {"fp64": bad_64, "mixed": bad_mx},
               "note": "only steps on finite states are timed (timing stops at the first 25-step chunk after "
                       "which the state is not finite).  dgfem's viscous face flux (half jump) grows without "
@@ -827,7 +861,11 @@ def main():
                 "clocks": clocks,
                 "cpu_baseline": cpu,
                 "details": args.details}
-        details = {"line": line, "roofline": roof, "stage_kernel": {"form": form, "grid": grid, "tiles": tiles,
+        details = {"line": line, "roofline": roof,
+                   "fp64_flop_roofline": flop_roofline(ORDER, False, ne, 1e3 * t_64 / k64, MEASURED_FP64_TFLOPS, "fp64"),
+                   "mixed_flop_roofline": flop_roofline(ORDER, False, ne, 1e3 * t_mx / args.steps, MEASURED_FP32_TFLOPS,
+                                                        "fp32"),
+                   "stage_kernel": {"form": form, "grid": grid, "tiles": tiles,
                                                                     "elements_per_cta": tile,
                                                                     "picked_by": "autotuner (timed on the first step)"},
                    "tensor_core_form": tensor_core, "df64": df64, "accuracy": acc, "navier_stokes": ns,
