@@ -10,7 +10,9 @@
 // (dgx_batch.cu), and a step is a CUDA graph of three such launches.  Periodic Euler batches
 // may instead run each stage as one launch per order of the single context's face-trace kernel
 // (32-element tiles, neighbour blocks in shared memory, dg_stage_trace.cuh), on each order's
-// concatenated range with its own trace buffers; the autotuner keeps whichever is faster.
+// concatenated range with its own trace buffers; the autotuner keeps whichever is faster.  Euler
+// batches with boundary faces take that form too when every boundary face has a condition: each
+// order's trace buffers then end in one ghost block per boundary face, as a single context's do.
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -33,7 +35,10 @@ struct Group {  // the instances of one order, concatenated
     float* ulo = nullptr;                 // low parts of the double-float state
     float* d1 = nullptr;                  // FP32 stage increments
     float* d2 = nullptr;
-    float* tr[2] = {nullptr, nullptr};    // face traces (periodic Euler batches), ping-ponged
+    float* tr[2] = {nullptr, nullptr};    // face traces (face-trace form), ping-ponged
+    ElemConn* tconn = nullptr;            // face-trace form with ghost blocks: boundary faces as interior
+    int* ghost_bc = nullptr;              //   faces to ghost blocks ne + k, and block k's condition slot
+    int nghost = 0;
 };
 }  // namespace
 
@@ -48,7 +53,7 @@ struct dgx_batch {
     std::vector<float> dt_uploaded;
     int boundary = 0;
     int grid = 0;  // stage-kernel grid picked by the autotuner (0: not yet); with STAGE_TRACE the face-trace form
-    bool trace_ok = false;  // periodic Euler: every group has trace buffers
+    bool trace_ok = false;  // Euler without skipped faces: every group has trace buffers (and ghost blocks)
     cudaStream_t cap = nullptr;
     cudaGraphExec_t graph[N_STEP_GRAPHS] = {};  // the StepGraph replays (dgx_internal.h)
 };
@@ -70,6 +75,8 @@ static void free_batch(dgx_batch* b) {
         cudaFree(g.d2);
         cudaFree(g.tr[0]);
         cudaFree(g.tr[1]);
+        cudaFree(g.tconn);
+        cudaFree(g.ghost_bc);
     }
     cudaFree(b->d_dt);
     if (b->cap) cudaStreamDestroy(b->cap);
@@ -185,13 +192,38 @@ extern "C" int dgx_batch_create(int n_inst, const dgx_mesh* const* meshes, const
             return set_error(DGX_ERR_CUDA, "cudaMalloc / upload failed for the batched state");
         }
     }
-    // face-trace form for periodic Euler batches: two trace buffers per order
-    b->trace_ok = !visc && !b->boundary;
+    // face-trace form for Euler batches whose faces are all interior or boundary faces with a
+    // condition: two trace buffers per order, each with one ghost block per boundary face after
+    // the order's elements (the single context's trace-form connectivity, dgx_create)
+    b->trace_ok = !visc;
+    std::vector<ElemConn> tc[MAX_P];
+    std::vector<int> gb[MAX_P];
+    for (int p = 0; p < MAX_P && b->trace_ok; ++p) {
+        const int ne = b->grp[p].ne;
+        if (ne == 0 || !b->boundary) continue;
+        tc[p] = cn[p];
+        for (int e = 0; e < ne && b->trace_ok; ++e)
+            for (int f = 0; f < 3; ++f) {
+                const int nb = cn[p][e].nbr[f];
+                if (nb == NBR_SKIP) {
+                    b->trace_ok = false;  // a face without a condition: the batched kernel only
+                    break;
+                }
+                if (nb < 0) {
+                    tc[p][e].nbr[f] = ne + (int)gb[p].size();
+                    tc[p][e].flags &= ~(7 << (4 * f));  // the block's face 0, points in this face's order
+                    gb[p].push_back(-1 - nb);
+                }
+            }
+    }
     for (int p = 0; p < MAX_P && b->trace_ok; ++p) {
         Group& g = b->grp[p];
         if (g.ne == 0) continue;
-        const size_t bytes = (size_t)g.ne * trace_floats_per_element(p + 1) * sizeof(float);
-        if (cudaMalloc((void**)&g.tr[0], bytes) != cudaSuccess || cudaMalloc((void**)&g.tr[1], bytes) != cudaSuccess) {
+        g.nghost = (int)gb[p].size();
+        const size_t bytes = ((size_t)g.ne + g.nghost) * trace_floats_per_element(p + 1) * sizeof(float);
+        if (cudaMalloc((void**)&g.tr[0], bytes) != cudaSuccess || cudaMalloc((void**)&g.tr[1], bytes) != cudaSuccess ||
+            (g.nghost && (!up((void**)&g.tconn, tc[p].data(), tc[p].size() * sizeof(ElemConn)) ||
+                          !up((void**)&g.ghost_bc, gb[p].data(), gb[p].size() * sizeof(int))))) {
             cudaGetLastError();
             free_batch(b);
             return set_error(DGX_ERR_CUDA, "cudaMalloc failed for the batched face traces");
@@ -260,7 +292,11 @@ static void batch_stage_args(const dgx_batch* b, int src, int stage, StepKind ki
             s.kappa = (float)(b->prm.mu * b->prm.gamma / (b->prm.prandtl * (b->prm.gamma - 1.0)));
             s.sigma0 = (float)b->prm.sigma0;
         }
-        s.boundary = b->boundary;
+        // the batched kernel takes the batch's boundary flag as its own argument; the face-trace form
+        // needs each order's: with ghost blocks, the order has boundary faces iff it has ghosts
+        s.boundary = b->trace_ok ? (g.nghost > 0) : b->boundary;
+        s.tconn = g.tconn;  // read by the face-trace form only
+        s.ghost_bc = g.ghost_bc;
         s.dt_inst = b->d_dt;
         s.grid = b->grid;
     }
@@ -353,7 +389,8 @@ extern "C" int dgx_batch_rk3_step(dgx_batch* b, const double* dt, int n_steps, v
     if (b->grid == 0) {
         // launch shape: timed on stage 1, which writes only the increment scratch (and, in the
         // face-trace form, the traces in tr[1]); candidates: the batched kernel at each grid and,
-        // for periodic Euler batches, the face-trace form (DGX_STAGE_KERNEL=rows keeps the first)
+        // for Euler batches without skipped faces, the face-trace form (DGX_STAGE_KERNEL=rows keeps
+        // the first)
         std::string key = "batch";
         for (int p = 0; p < MAX_P; ++p) key += " p" + std::to_string(p + 1) + ":" + std::to_string(b->grp[p].ne);
         if (b->boundary) key += " bnd";

@@ -346,8 +346,9 @@ int dgx_batch_launch_shape(const dgx_batch* b, int* grid, int* tiles);
 /* The form the autotuner picked for a batch's stages (0 until the first step): 1 = the batched
  * kernel (one launch per stage over every order's tiles, neighbour coefficient rows); 2 = the
  * face-trace kernel of dgx_rk3_step (32-element tiles, neighbour blocks in shared memory), one
- * launch per order and stage, offered for periodic Euler batches (DGX_STAGE_KERNEL=rows or
- * =trace32s keeps one).  No counterpart in dgfem. */
+ * launch per order and stage, offered for Euler batches whose boundary faces all have a condition
+ * (ghost blocks, as for a single context; DGX_STAGE_KERNEL=rows or =trace32s keeps one).  No
+ * counterpart in dgfem. */
 int dgx_batch_stage_form(const dgx_batch* b, int* form);
 
 #ifdef __cplusplus

@@ -86,12 +86,15 @@ def single(dg, om, pm, u0, dt, order, steps=(3, 2), wf=None):
     return u.cpu().numpy()
 
 
-def test_batch_face_trace_form_equals_batched_kernel(dg, monkeypatch):
-    """A periodic Euler batch run by the single context's face-trace kernel (one launch per order
-    and stage, DGX_STAGE_KERNEL=trace32s) equals the batched row-form kernel (=rows) bit for bit
-    after steps (3, 2): one call's first, middle and last steps, and a call of two.  Uneven sizes
-    and orders 1..4, so each order's range ends in a partial 32-element tile."""
-    insts, orders = build(dg, SPECS)
+@pytest.mark.parametrize("walls", [(), (1, 4, 6)])
+def test_batch_face_trace_form_equals_batched_kernel(dg, monkeypatch, walls):
+    """An Euler batch run by the single context's face-trace kernel (one launch per order and
+    stage, DGX_STAGE_KERNEL=trace32s) equals the batched row-form kernel (=rows) bit for bit after
+    steps (3, 2): one call's first, middle and last steps, and a call of two.  Uneven sizes and
+    orders 1..4, so each order's range ends in a partial 32-element tile.  With walls, instances
+    1, 4 and 6 have far-field and no-slip sides: their orders' trace buffers end in ghost blocks,
+    the other orders' do not."""
+    insts, orders = build(dg, SPECS, walls)
     monkeypatch.setenv("DGX_STAGE_KERNEL", "rows")
     brows, rows = run_batch(dg, insts, orders)
     assert brows.stage_form() == "batched rows"
