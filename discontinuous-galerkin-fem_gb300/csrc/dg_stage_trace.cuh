@@ -28,10 +28,11 @@
 namespace dgx {
 
 // Which stages a trace-kernel instantiation serves: any (the stage and, for stage 3, the state's
-// case read from StageArgs), stages 1 and 2 only, or stage 3 of a step between the first and
-// the last of a call (double-float state in and out).  The specialised kernels leave out the
-// code of the other stages, which the instruction cache then does not have to hold.
-enum StageKind { SK_ANY = 0, SK_12 = 1, SK_3DF = 2 };
+// case read from StageArgs), stages 1 and 2 (the stage read from StageArgs), stage 1 or stage 2
+// alone, or stage 3 of a step between the first and the last of a call (double-float state in
+// and out).  The specialised kernels leave out the code of the other stages, which the
+// instruction cache then does not have to hold.
+enum StageKind { SK_ANY = 0, SK_12 = 1, SK_3DF = 2, SK_1 = 3, SK_2 = 4 };
 
 template <int P>
 __host__ __device__ constexpr int trace_floats() { return 3 * (P + 1) * NV; }
@@ -47,8 +48,9 @@ __device__ __forceinline__ void stage_combine_next(const StageArgs& s, float* sR
     const int n4 = nloc * NB4;
     const size_t b4 = (size_t)e0 * NB4;
     const int t = threadIdx.x;
-    const bool st12 = SK == SK_12 || (SK == SK_ANY && s.stage <= 2);
-    const bool with_din = SK == SK_3DF || s.stage >= 2;
+    const int stage = SK == SK_1 ? 1 : SK == SK_2 ? 2 : SK == SK_3DF ? 3 : s.stage;
+    const bool st12 = SK == SK_12 || SK == SK_1 || SK == SK_2 || (SK == SK_ANY && stage <= 2);
+    const bool with_din = SK == SK_3DF || SK == SK_2 || (SK != SK_1 && stage >= 2);
     bool bad = false;
     for (int g0 = t; g0 < n4; g0 += CH * THREADS) {
         float4 dv[CH], uh[CH], lo[CH];
@@ -72,7 +74,7 @@ __device__ __forceinline__ void stage_combine_next(const StageArgs& s, float* sR
             const float4 du = *slot;
             const float dt = s.dt_inst ? sDt[row] : s.dt;
             if (st12) {
-                const float4 o = s.stage == 1
+                const float4 o = stage == 1
                                      ? make_float4(dt * du.x, dt * du.y, dt * du.z, dt * du.w)
                                      : make_float4(0.25f * (dv[k].x + dt * du.x), 0.25f * (dv[k].y + dt * du.y),
                                                    0.25f * (dv[k].z + dt * du.z), 0.25f * (dv[k].w + dt * du.w));
@@ -407,7 +409,8 @@ __device__ __forceinline__ void stage_trace_tile(const SArgs<P, false>& ka, floa
             if (!BND) G = s.geom[e0 + el];
             C = s.conn[e0 + el];
         }
-        stage_load_tile<NB, STR, T>(s.uhi, s.din, sU, e0, nloc, [](int le) { return tile_row<T>(le); });
+        stage_load_tile<NB, STR, T>(s.uhi, SK == SK_1 ? nullptr : s.din, sU, e0, nloc,
+                                    [](int le) { return tile_row<T>(le); });
         if (el < nloc) {
             if (NBS) copy_neighbour_traces<P>(s, C, sN + tl * nbr_trace_stride<P>());
             else prefetch_neighbour_traces<P, BND>(s, C);
